@@ -1,0 +1,360 @@
+#!/usr/bin/env python3
+"""Benchmark of the D2Q9 step on one GB300 (per rank), printing one JSON line.
+
+Workload: periodic Taylor-Green vortex, 4096 x 4096, u0 = 0.04, tau = 0.56
+(the large plain-method configuration). A "step" is one LBM time step over the
+whole grid. Inputs (1.2 GB of FP64 populations, 0.6 GB FP32) are far larger
+than L2, so no flush is needed between steps.
+
+  value     FP32-shifted fused step, state resident in HBM (lbm_gpu_run), MLUPS
+  fp64      the plain FP64 fused kernel (bit-identical to lbc), same workload
+  fp16      FP16-shifted storage, same workload
+  e2e       lbc's own main_lbm call through this library's C ABI with host
+            arrays (page-locked): each call uploads f, f_new, rho, u, v and
+            downloads f, f_new, rho, u, v, L, D, as lbc's API requires
+  cpu_baseline  the oracle / lbc's build on this host's cores (OpenMP)
+
+--impl reference times lbc's own CPU implementation of main_lbm on the host
+cores (oracle/_ref when lbc's sources were compiled here, else the oracle port)
+on the same workload.
+
+Multi-GPU (torchrun): every rank runs an independent replica (the path has no
+data exchange between cases); value sums over ranks, time is the max over ranks.
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "aggregate MLUPS & %HBM roofline, FP32-shifted batched vs FP64 plain at stated u error; p50/p99"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=1000)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=4096, help="grid edge (N x N)")
+    p.add_argument("--fp64-steps", type=int, default=0, help="timed FP64 steps (default steps/5)")
+    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--skip-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        import torch.distributed as td
+        td.init_process_group("gloo")
+        pg = td
+    return ws, rank, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allmax(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.p = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.t.join(timeout=2)
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            c = [x.strip() for x in ln.split(",")]
+            if len(c) < 9 or (vis.isdigit() and c[0] != vis):
+                continue
+            try:
+                sm.append(float(c[1]))
+                mx = float(c[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, c[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_per_launch(key):
+    """Per-launch DRAM bytes of the step kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "step_kernel_traffic.json")) as fh:
+            return json.load(fh).get(key)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_lib():
+    """lbc's own build (oracle/_ref) when present, else the oracle port."""
+    from lbc_gb300.abi import LbcAbi
+    ref = os.path.join(ROOT, "oracle", "_ref", "libref_lbc.so")
+    if os.path.exists(ref):
+        return LbcAbi(C.CDLL(ref), "ref_"), "reference"
+    so = os.path.join(ROOT, "oracle", "_build", "liblbm_oracle.so")
+    if not os.path.exists(so):
+        subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_oracle.sh")], check=True,
+                       capture_output=True)
+    return LbcAbi(C.CDLL(so), "orc_"), "port"
+
+
+def cpu_time(n, seconds, max_steps=None):
+    """Bounded sample of the workload on the host cores: main_lbm calls on the
+    full grid until `seconds` of CPU time (at least 2 calls)."""
+    from lbc_gb300 import cases
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    lib, kind = cpu_lib()
+    case, st = cases.taylor_green(n, n, 0.04, 0.56)
+    bnd = lib.boundaries(case.bcs)
+    lib.step(case, st, bnd)  # warm-up call
+    t0 = time.perf_counter()
+    k = 0
+    while True:
+        lib.step(case, st, bnd)
+        k += 1
+        el = time.perf_counter() - t0
+        if (k >= 2 and el >= seconds) or (max_steps and k >= max_steps):
+            break
+    mlups = case.nodes * k / el / 1e6
+    return mlups, kind, k, el
+
+
+def run_ours(a, ws, rank, pg):
+    import numpy as np
+
+    import lbc_gb300
+    from lbc_gb300 import cases
+
+    lbc_gb300.load_library()
+    n = a.n
+    case, st = cases.taylor_green(n, n, 0.04, 0.56)
+    N = case.nodes
+    hbm, peak_kind = peaks()
+    res = {}
+
+    def timed(storage, steps):
+        s = lbc_gb300.GpuSolver(case, storage)
+        s.set_state(st)
+        s.run(a.warmup)
+        s.sync()
+        barrier(pg)
+        clk = Clocks()
+        clk.start()
+        ms = s.run_timed(steps)
+        clocks = clk.stop()
+        barrier(pg)
+        ms = allmax(pg, ms)
+        info = s.info()
+        return s, ms, clocks, info
+
+    # FP32-shifted: the headline.
+    s32, ms32, clocks, info32 = timed(lbc_gb300.F32_SHIFTED, a.steps)
+    bytes32 = 2 * 9 * 4 * N
+    t_step = ms32 / a.steps / 1e3
+    res["f32"] = {"mlups": ws * N * a.steps / (ms32 / 1e3) / 1e6, "ms_per_step": ms32 / a.steps,
+                  "gbs": bytes32 / t_step / 1e9, "launches": 1 + a.steps * info32.launches_per_step}
+    del s32
+    # FP64 plain.
+    k64 = a.fp64_steps or max(20, a.steps // 5)
+    s64, ms64, _, _ = timed(lbc_gb300.F64, k64)
+    del s64
+    bytes64 = 2 * 9 * 8 * N
+    t64 = ms64 / k64 / 1e3
+    res["f64"] = {"mlups": ws * N * k64 / (ms64 / 1e3) / 1e6, "ms_per_step": ms64 / k64,
+                  "gbs": bytes64 / t64 / 1e9, "steps": k64}
+    # FP16-shifted.
+    s16, ms16, _, _ = timed(lbc_gb300.F16_SHIFTED, a.steps)
+    del s16
+    bytes16 = 2 * 9 * 2 * N
+    t16 = ms16 / a.steps / 1e3
+    res["f16"] = {"mlups": ws * N * a.steps / (ms16 / 1e3) / 1e6, "ms_per_step": ms16 / a.steps,
+                  "gbs": bytes16 / t16 / 1e9}
+
+    # Accuracy against the FP64 kernel (itself bit-identical to lbc) after E steps.
+    E = 200
+    fields = {}
+    for name, stg in (("f64", lbc_gb300.F64), ("f32", lbc_gb300.F32_SHIFTED), ("f16", lbc_gb300.F16_SHIFTED)):
+        s = lbc_gb300.GpuSolver(case, stg)
+        s.set_state(st)
+        s.run(E)
+        fields[name] = s.get_fields()
+        del s
+    r64, u64, v64 = fields["f64"]
+    m0 = float(np.sum(st.rho))
+    acc = {}
+    for name in ("f32", "f16"):
+        r, u, v = fields[name]
+        acc[name] = {
+            "u_l2_rel_vs_fp64": float(np.sqrt(np.sum((u - u64) ** 2 + (v - v64) ** 2) / np.sum(u64 ** 2 + v64 ** 2))),
+            "mass_drift": float(np.sum(r) / m0 - 1.0),
+        }
+    acc["f64_mass_drift"] = float(np.sum(r64) / m0 - 1.0)
+
+    # End to end through lbc's main_lbm with page-locked host arrays (FP64).
+    api = lbc_gb300.dropin()
+    pin = {k: lbc_gb300.PinnedArray(getattr(st, k).shape) for k in ("f", "f_new", "rho", "u", "v")}
+    for k, p in pin.items():
+        p.array[...] = getattr(st, k)
+    from lbc_gb300.cases import State
+    hst = State(*(pin[k].array for k in ("f", "f_new", "rho", "u", "v")))
+    bnd = api.boundaries(case.bcs)
+    api.step(case, hst, bnd)  # first call builds the device tables
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(a.e2e_steps):
+        api.step(case, hst, bnd)
+    el = allmax(pg, time.perf_counter() - t0)
+    e2e = {"value": ws * N * a.e2e_steps / el / 1e6, "unit": "MLUPS",
+           "h2d_bytes_per_step": (2 * 72 + 24) * N, "d2h_bytes_per_step": (2 * 72 + 24) * N + 16,
+           "steps": a.e2e_steps, "path": "main_lbm (lbc C ABI), FP64, host arrays page-locked"}
+    lib = lbc_gb300.load_library()
+    lib.lbm_gpu_dropin_release()
+
+    cpu = None
+    if rank == 0 and not a.skip_cpu:
+        mlups, kind, k, el = cpu_time(n, a.cpu_seconds)
+        cpu = {"value": round(mlups, 2), "unit": "MLUPS", "cores": os.cpu_count(), "kind": kind,
+               "sample": f"{k} main_lbm calls on the full {n}x{n} grid ({el:.1f} s), OpenMP"}
+
+    f32 = res["f32"]
+    line = {
+        "metric": METRIC, "value": round(f32["mlups"], 1), "unit": "MLUPS", "n_gpus": ws,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(f32["ms_per_step"], 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (populations stored as f - w in FP32, FP32 collision)",
+        "data": "synthetic (analytic Taylor-Green initial field)",
+        "config": {"workload": f"taylor_green_{n}x{n}", "u0": 0.04, "tau": 0.56, "nodes": N,
+                   "l2": "inputs larger than L2 (0.6-1.2 GB per buffer), no flush",
+                   "parallelism": f"replicas x{ws}"},
+        "roofline": {"bound": "hbm", "achieved": round(f32["gbs"], 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(f32["gbs"] / hbm, 4), "peak_kind": peak_kind,
+                     "traffic": traffic_per_launch(f"f32_{n}"),
+                     "algorithmic_bytes_per_launch": bytes32},
+        "fp64": {"value": round(res["f64"]["mlups"], 1), "ms_per_step": round(res["f64"]["ms_per_step"], 4),
+                 "achieved_gbs": round(res["f64"]["gbs"], 1), "frac_hbm": round(res["f64"]["gbs"] / hbm, 4),
+                 "steps": res["f64"]["steps"], "parity": "bit-identical to lbc's FP64 CPU solver"},
+        "fp16": {"value": round(res["f16"]["mlups"], 1), "achieved_gbs": round(res["f16"]["gbs"], 1),
+                 "frac_hbm": round(res["f16"]["gbs"] / hbm, 4)},
+        "speedup_f32_vs_fp64": round(f32["mlups"] / res["f64"]["mlups"], 2),
+        "accuracy_after_200_steps": acc,
+        "e2e": e2e,
+        "gpu_launches": f32["launches"],
+        "clocks": clocks,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def run_reference(a, ws, rank, pg):
+    if rank != 0:
+        return
+    n = a.n
+    N = n * n
+    # Each timed step is one main_lbm call on the full grid; the run is capped
+    # at about two minutes.
+    from lbc_gb300 import cases
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    lib, kind = cpu_lib()
+    case, st = cases.taylor_green(n, n, 0.04, 0.56)
+    bnd = lib.boundaries(case.bcs)
+    for _ in range(max(1, min(a.warmup, 3))):
+        lib.step(case, st, bnd)
+    t0 = time.perf_counter()
+    k = 0
+    while k < a.steps:
+        lib.step(case, st, bnd)
+        k += 1
+        if time.perf_counter() - t0 > 120.0:
+            break
+    el = time.perf_counter() - t0
+    mlups = N * k / el / 1e6
+    line = {"metric": METRIC, "value": round(mlups, 2), "unit": "MLUPS", "n_gpus": 0, "steps": k,
+            "warmup": a.warmup, "ms_per_step": round(el / k * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+            "data": "synthetic (analytic Taylor-Green initial field)",
+            "config": {"workload": f"taylor_green_{n}x{n}", "u0": 0.04, "tau": 0.56, "nodes": N},
+            "cpu_baseline": {"value": round(mlups, 2), "unit": "MLUPS", "cores": os.cpu_count(), "kind": kind,
+                             "sample": f"{k} main_lbm calls on the full grid ({el:.1f} s), OpenMP, "
+                                       "no I/O"},
+            "e2e": {"value": round(mlups, 2), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    a = parse()
+    ws, rank, pg = dist()
+    if a.impl == "reference":
+        run_reference(a, ws, rank, pg)
+    else:
+        run_ours(a, ws, rank, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

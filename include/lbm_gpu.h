@@ -1,0 +1,110 @@
+/* lbm_gpu.h -- extended C API of the GB300 engine (no counterpart in lbc).
+ *
+ * lbc's main_lbm moves every array between host and device on each call. This
+ * API keeps a case resident on the GPU instead: create a solver from the same
+ * inputs main_lbm takes, upload a state once, advance it n steps on the device
+ * (graph-captured step loop), and read fields, forces or the full state back
+ * when needed. lbm_gpu_run(s, n) leaves exactly what n main_lbm calls plus the
+ * caller-side f/f_new swap would leave (FP64 storage: bit for bit).
+ *
+ * Every function returns LBM_GPU_OK (0) or a negative code; the message is in
+ * lbm_gpu_last_error() (thread-local). Nothing falls back to the CPU.
+ */
+#ifndef LBM_GPU_H
+#define LBM_GPU_H
+
+#include <stddef.h>
+
+#include "lbm_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBM_GPU_OK 0
+#define LBM_GPU_ERR_ARG (-1)
+#define LBM_GPU_ERR_CUDA (-2)
+#define LBM_GPU_ERR_NOMEM (-3)
+
+/* Population storage. F64: lbc's arithmetic, bit for bit. F32/F16_SHIFTED:
+ * populations stored as f_k - w_k in FP32 / FP16, collision in FP32. */
+enum { LBM_GPU_F64 = 0, LBM_GPU_F32_SHIFTED = 1, LBM_GPU_F16_SHIFTED = 2 };
+
+typedef struct lbm_gpu_solver lbm_gpu_solver;
+
+/* The inputs of main_lbm that describe a case (lbc include/lbm_core.h:6-31),
+ * plus optional moving walls and the storage mode. Arrays are read during
+ * lbm_gpu_create only, except Boundary val1/val2, which are read again by
+ * lbm_gpu_set_bc_values. */
+typedef struct {
+    int Nx, Ny;
+    const int *cx, *cy, *opp;      /* must be lbc's D2Q9 ordering */
+    const double *w;
+    const double *omega_eff;       /* [Ny][Nx] */
+    const int *solid_mask;         /* [Ny][Nx] */
+    const double *phi;             /* [Ny][Nx] level set, used when use_IBB */
+    int use_IBB;
+    const Boundary *boundaries;    /* apply = this library's BC functions */
+    int num_boundaries;
+    int isperiodic_x, isperiodic_y;
+    double Fx, Fy;
+    const double *wall_u, *wall_v; /* [Ny][Nx] wall velocity of solid nodes, or NULL */
+    int storage;                   /* LBM_GPU_F64 / _F32_SHIFTED / _F16_SHIFTED */
+} lbm_gpu_case;
+
+typedef struct {
+    int Nx, Ny, pitch, storage;
+    int has_geometry;              /* 0: fully periodic, no solids, no edge BCs */
+    int edge_stages;               /* Boundary entries run as edge kernels */
+    int launches_per_step;         /* kernel launches per time step in the loop */
+    size_t device_bytes;
+    long long steps_done;
+} lbm_gpu_info;
+
+const char *lbm_gpu_last_error(void);
+int lbm_gpu_device_count(void);
+
+int lbm_gpu_create(const lbm_gpu_case *c, lbm_gpu_solver **out);
+int lbm_gpu_destroy(lbm_gpu_solver *s);
+
+/* f, f_new: [Ny][Nx][9] as main_lbm receives them; rho/u/v: the stored fields
+ * the next collision uses (lbc collides its first step with these arrays). */
+int lbm_gpu_set_state(lbm_gpu_solver *s, const double *f, const double *f_new, const double *rho,
+                      const double *u, const double *v);
+/* After n steps: f = newest populations (what the caller's f holds after the
+ * swap), f_new = the other buffer. Any pointer may be NULL. */
+int lbm_gpu_get_state(lbm_gpu_solver *s, double *f, double *f_new, double *rho, double *u,
+                      double *v);
+int lbm_gpu_get_fields(lbm_gpu_solver *s, double *rho, double *u, double *v);
+/* Re-read val1/val2 (length Ny or Nx) of Boundary entry `entry`. */
+int lbm_gpu_set_bc_values(lbm_gpu_solver *s, int entry, const double *val1, const double *val2);
+
+int lbm_gpu_run(lbm_gpu_solver *s, int nsteps);
+/* Same as lbm_gpu_run, timed with CUDA events on the solver's stream. */
+int lbm_gpu_run_timed(lbm_gpu_solver *s, int nsteps, double *ms);
+int lbm_gpu_sync(lbm_gpu_solver *s);
+
+/* Momentum-exchange force of the last step: *D = x, *L = y (as main_lbm). */
+int lbm_gpu_forces(lbm_gpu_solver *s, double *L, double *D);
+/* Record the force of every step in a device ring of `capacity` steps. */
+int lbm_gpu_enable_force_history(lbm_gpu_solver *s, int capacity);
+/* Copies up to max_steps records (x, y), oldest first; returns the count. */
+int lbm_gpu_force_history(lbm_gpu_solver *s, double *xy, int max_steps);
+
+int lbm_gpu_get_info(lbm_gpu_solver *s, lbm_gpu_info *info);
+/* Thread-block shape of the fused step (bx * by <= 256, bx multiple of 32). */
+int lbm_gpu_set_block(lbm_gpu_solver *s, int bx, int by);
+
+/* Page-locked host memory for fast transfers. */
+void *lbm_gpu_host_alloc(size_t bytes);
+void lbm_gpu_host_free(void *p);
+
+/* The drop-in main_lbm keeps device buffers and geometry tables keyed by the
+ * caller's array pointers. Call this after changing solid_mask, omega_eff or
+ * phi in place; it also frees those buffers. */
+void lbm_gpu_dropin_release(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,573 @@
+// engine.cpp -- host side of the GB300 D2Q9 engine.
+//
+// A Solver owns one case on the device:
+//   * two population buffers (SoA planes, FP64 or shifted FP32/FP16), swapped
+//     every step like lbc's caller swaps f/f_new (cases/nit/nit.c:309-311);
+//   * a per-node flag word and a cut-link table built once from the geometry;
+//   * the edge-BC band: pre-collision populations and previous-step moments of
+//     the nodes lbc's Boundary list writes or reads;
+//   * stored macroscopic fields rho/u/v (dense [Ny][Nx], FP64).
+// Solver::run(n) is equivalent to n calls of lbc's main_lbm plus the caller-side
+// swap: it collides the current state with the stored fields (as lbc's first
+// call does), runs n-1 fused steps from a two-step CUDA graph, and ends with a
+// step that stores pre-collision populations and the moments, so the state at
+// exit is what lbc's arrays hold after n calls.
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <set>
+
+namespace lbm {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string &msg) { g_err = msg; }
+const char *last_error() { return g_err.c_str(); }
+
+bool check_cuda(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return true;
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return false;
+}
+
+#define CK(call)                                \
+    do {                                        \
+        if (!check_cuda((call), #call)) return false; \
+    } while (0)
+
+template <class T> bool Solver::dalloc(T **p, size_t count) {
+    if (count == 0) count = 1;
+    void *q = nullptr;
+    if (!check_cuda(cudaMalloc(&q, count * sizeof(T)), "cudaMalloc")) return false;
+    allocs_.push_back(q);
+    dev_bytes_ += count * sizeof(T);
+    *p = (T *)q;
+    return true;
+}
+
+Solver::Solver(const CaseDesc &d) : d_(d) {
+    if (d_.Nx < 2 || d_.Ny < 2) {
+        set_error("grid must be at least 2 x 2");
+        return;
+    }
+    esize_ = d_.store == STORE_F64 ? 8 : (d_.store == STORE_F32 ? 4 : 2);
+    pitch_ = (d_.Nx + 63) / 64 * 64;
+    plane_ = (long long)pitch_ * d_.Ny;
+    if (!check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate")) return;
+    if (!build_geometry()) return;
+    ok_ = true;
+}
+
+Solver::~Solver() {
+    if (pair_exec_) cudaGraphExecDestroy(pair_exec_);
+    for (void *p : allocs_) cudaFree(p);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+static inline bool wrap(int &c, int n, int periodic) {
+    if (periodic) {
+        if (c < 0) c += n;
+        else if (c >= n) c -= n;
+        return true;
+    }
+    return c >= 0 && c < n;
+}
+
+// Geometry preprocessing (once per case):
+//   flags: solid bit; bit k when the pull source x - c_k is solid or off a
+//          non-periodic edge; band/BC-write bits; link bit.
+//   links: per fluid node with solid sources, one entry per such source in k
+//          order: interpolated bounce-back coefficients computed exactly as
+//          src/bc/interpolated_bounce_back.c:52-99 does, or the moving-wall term.
+//   band:  the columns/rows lbc's Boundary list writes or reads.
+bool Solver::build_geometry() {
+    const int Nx = d_.Nx, Ny = d_.Ny;
+    const size_t N = (size_t)Nx * Ny;
+    auto solid = [&](int i, int j) { return d_.mask && d_.mask[(size_t)j * Nx + i] != 0; };
+
+    // Uniform omega becomes a scalar.
+    bool uniform = true;
+    omega0_ = d_.omega ? d_.omega[0] : 1.0;
+    if (d_.omega)
+        for (size_t n = 1; n < N && uniform; n++) uniform = (d_.omega[n] == omega0_);
+
+    // Stages from the Boundary list.
+    bool nonperiodic_seen = false;
+    for (size_t e = 0; e < d_.bcs.size(); e++) {
+        const BCEntry &b = d_.bcs[e];
+        if (b.kind < 0 || b.kind >= BC_KIND_COUNT) {
+            set_error("boundary entry " + std::to_string(e) + ": unknown BC function");
+            return false;
+        }
+        const bool per = b.kind == BC_PERIODIC_X || b.kind == BC_PERIODIC_Y;
+        if (per) {
+            // A periodic entry re-copies what the wrap in streaming already wrote
+            // (src/bc/periodic_x.c vs src/core/streaming.c:24-34); it only matters
+            // when its flag is off or an earlier entry overwrote the edge.
+            const int flag = b.kind == BC_PERIODIC_X ? d_.px : d_.py;
+            if (flag && !nonperiodic_seen) continue;
+            Stage st{b.kind, 0, b.kind == BC_PERIODIC_X ? 2 * Ny : 2 * Nx, (int)e};
+            stages_.push_back(st);
+            continue;
+        }
+        nonperiodic_seen = true;
+        const bool col = bc_is_column(b.kind);
+        const int lim = col ? Nx : Ny;
+        if (b.index < 0 || b.index >= lim) {
+            set_error("boundary entry " + std::to_string(e) + ": index out of range");
+            return false;
+        }
+        Stage st{b.kind, b.index, col ? Ny : Nx, (int)e};
+        stages_.push_back(st);
+    }
+
+    // Band lines.
+    std::set<int> cols, rows, wcols, wrows;
+    for (const Stage &st : stages_) {
+        const int k = st.kind, x = st.index;
+        auto need = [&](bool col, int idx, bool write) -> bool {
+            const int lim = col ? Nx : Ny;
+            if (idx < 0 || idx >= lim) {
+                set_error("boundary entry " + std::to_string(st.entry) +
+                          ": the BC reads a line outside the grid");
+                return false;
+            }
+            (col ? cols : rows).insert(idx);
+            if (write) (col ? wcols : wrows).insert(idx);
+            return true;
+        };
+        bool okk = true;
+        switch (k) {
+        case BC_PERIODIC_X: okk = need(true, 0, true) && need(true, Nx - 1, true); break;
+        case BC_PERIODIC_Y: okk = need(false, 0, true) && need(false, Ny - 1, true); break;
+        case BC_VEL_IN_ZH: case BC_VEL_OUT_ZH: okk = need(true, x, true); break;
+        case BC_VEL_TOP_ZH: case BC_VEL_BOT_ZH: okk = need(false, x, true); break;
+        case BC_PRES_IN_ZH: case BC_CONV_IN: case BC_VEL_IN_REG: case BC_PRES_IN_REG:
+            okk = need(true, x, true) && need(true, x + 1, false); break;
+        case BC_PRES_OUT_ZH: case BC_CONV_OUT: case BC_VEL_OUT_REG: case BC_PRES_OUT_REG:
+            okk = need(true, x, true) && need(true, x - 1, false); break;
+        case BC_VEL_BOT_REG: case BC_PRES_BOT_REG: okk = need(false, x, true) && need(false, x + 1, false); break;
+        case BC_VEL_TOP_REG: case BC_PRES_TOP_REG: okk = need(false, x, true) && need(false, x - 1, false); break;
+        default: break;
+        }
+        if (!okk) return false;
+    }
+    std::vector<int> colbase(Nx, -1), rowbase(Ny, -1);
+    int ns = 0;
+    for (int c : cols) { colbase[c] = ns; ns += Ny; }
+    for (int r : rows) { rowbase[r] = ns; ns += Nx; }
+    nslots_ = ns;
+    auto slot_of = [&](int i, int j) { return colbase[i] >= 0 ? colbase[i] + j : rowbase[j] + i; };
+
+    // Flags and links.
+    std::vector<uint16_t> flags((size_t)pitch_ * Ny, 0);
+    std::vector<int> link_off;
+    std::vector<Link> links;
+    const bool moving = d_.wall_u || d_.wall_v;
+    if (moving && d_.use_ibb) {
+        set_error("moving walls and interpolated bounce-back cannot be combined");
+        return false;
+    }
+    const bool want_links = d_.use_ibb || moving;
+    if (want_links) link_off.assign((size_t)pitch_ * Ny, 0);
+    bool any_special = false, any_solid_link = false;
+    std::vector<int2> wnodes, seed_nodes;
+    std::vector<int> seed_slots;
+    for (int j = 0; j < Ny; j++) {
+        for (int i = 0; i < Nx; i++) {
+            uint16_t fl = 0;
+            const size_t node = (size_t)j * pitch_ + i;
+            const bool band = (colbase[i] >= 0) || (rowbase[j] >= 0);
+            const bool bcw = !solid(i, j) && (wcols.count(i) || wrows.count(j));
+            if (band) {
+                fl |= NF_BAND;
+                seed_nodes.push_back(make_int2(i, j));
+                seed_slots.push_back(slot_of(i, j));
+            }
+            if (solid(i, j)) {
+                fl |= NF_SOLID;
+                flags[node] = fl;
+                any_special = true;
+                continue;
+            }
+            if (bcw) {
+                fl |= NF_BCW;
+                wnodes.push_back(make_int2(i, j));
+            }
+            int first_link = (int)links.size();
+            bool has_link = false;
+            for (int k = 1; k < 9; k++) {
+                int si = i - cxk(k), sj = j - cyk(k);
+                if (!wrap(si, Nx, d_.px) || !wrap(sj, Ny, d_.py)) {
+                    fl |= (uint16_t)(1u << k);
+                    any_special = true;
+                    continue;
+                }
+                if (!solid(si, sj)) continue;
+                fl |= (uint16_t)(1u << k);
+                any_special = true;
+                any_solid_link = true;
+                if (!want_links) continue;
+                Link L;
+                std::memset(&L, 0, sizeof L);
+                L.mode = LINK_BB;
+                L.k = (uint8_t)k;
+                L.behind = -1;
+                const int kl = oppk(k);  // link direction, from x towards the solid node
+                if (d_.use_ibb) {
+                    const double eps = 1e-12;
+                    const double phx = d_.phi[(size_t)j * Nx + i];
+                    double denom = phx - d_.phi[(size_t)sj * Nx + si];
+                    if (std::fabs(denom) < eps) denom = (denom >= 0.0) ? eps : -eps;
+                    double q = phx / denom;
+                    if (q < eps) q = eps;
+                    if (q > 1.0 - eps) q = 1.0 - eps;
+                    int bi = i - cxk(kl), bj = j - cyk(kl);
+                    if (wrap(bi, Nx, d_.px) && wrap(bj, Ny, d_.py)) {
+                        if (q <= 0.5) {
+                            L.mode = LINK_IBB_LO;
+                            L.c1 = 1.0 - 2.0 * q;
+                            L.c2 = 2.0 * q;
+                            L.behind = (int64_t)bj * pitch_ + bi;
+                        } else if (!solid(bi, bj)) {
+                            L.mode = LINK_IBB_HI;
+                            L.c1 = 1.0 / (2.0 * q);
+                            L.c2 = (2.0 * q - 1.0) / (2.0 * q);
+                            L.behind = (int64_t)bj * pitch_ + bi;
+                        }
+                    }
+                } else {
+                    const size_t s = (size_t)sj * Nx + si;
+                    const double uw = d_.wall_u ? d_.wall_u[s] : 0.0;
+                    const double vw = d_.wall_v ? d_.wall_v[s] : 0.0;
+                    const double cuw = cxk(kl) * uw + cyk(kl) * vw;
+                    if (cuw != 0.0) {
+                        L.mode = LINK_MOVING;
+                        L.c2 = 6.0 * d_.w[kl] * cuw;
+                    }
+                }
+                links.push_back(L);
+                has_link = true;
+            }
+            if (has_link) {
+                fl |= NF_LINKS;
+                link_off[node] = first_link;
+            }
+            flags[node] = fl;
+        }
+    }
+    has_flags_ = any_special || !stages_.empty() || !d_.px || !d_.py;
+    has_links_ = want_links && !links.empty();
+    has_mem_ = any_solid_link;
+    nw_ = (int)wnodes.size();
+    nseed_ = (int)seed_nodes.size();
+
+    // Device allocation.
+    for (int b = 0; b < 2; b++) {
+        void *p = nullptr;
+        if (!check_cuda(cudaMalloc(&p, (size_t)plane_ * 9 * esize_), "cudaMalloc populations")) return false;
+        allocs_.push_back(p);
+        dev_bytes_ += (size_t)plane_ * 9 * esize_;
+        buf_[b] = p;
+        CK(cudaMemsetAsync(p, 0, (size_t)plane_ * 9 * esize_, stream_));
+    }
+    if (!dalloc(&d_rho_, N) || !dalloc(&d_ux_, N) || !dalloc(&d_uy_, N)) return false;
+    if (!dalloc(&d_stage_, N * 9)) return false;
+    if (has_flags_) {
+        if (!dalloc(&d_flags_, flags.size())) return false;
+        CK(cudaMemcpyAsync(d_flags_, flags.data(), flags.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, stream_));
+    }
+    if (has_links_) {
+        if (!dalloc(&d_link_off_, link_off.size()) || !dalloc(&d_links_, links.size())) return false;
+        CK(cudaMemcpyAsync(d_link_off_, link_off.data(), link_off.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
+        CK(cudaMemcpyAsync(d_links_, links.data(), links.size() * sizeof(Link), cudaMemcpyHostToDevice, stream_));
+    }
+    if (!uniform) {
+        if (!dalloc(&d_omega_, N)) return false;
+        CK(cudaMemcpyAsync(d_omega_, d_.omega, N * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    }
+    if (nslots_ > 0) {
+        if (!dalloc(&d_colbase_, (size_t)Nx) || !dalloc(&d_rowbase_, (size_t)Ny)) return false;
+        CK(cudaMemcpyAsync(d_colbase_, colbase.data(), Nx * sizeof(int), cudaMemcpyHostToDevice, stream_));
+        CK(cudaMemcpyAsync(d_rowbase_, rowbase.data(), Ny * sizeof(int), cudaMemcpyHostToDevice, stream_));
+        if (!dalloc(&d_bandf_, (size_t)nslots_ * 9) || !dalloc(&d_bandm_[0], (size_t)nslots_ * 3) ||
+            !dalloc(&d_bandm_[1], (size_t)nslots_ * 3))
+            return false;
+        if (!dalloc(&d_wnodes_, wnodes.size()) || !dalloc(&d_seed_nodes_, seed_nodes.size()) ||
+            !dalloc(&d_seed_slots_, seed_slots.size()))
+            return false;
+        if (nw_) CK(cudaMemcpyAsync(d_wnodes_, wnodes.data(), wnodes.size() * sizeof(int2), cudaMemcpyHostToDevice, stream_));
+        if (nseed_) {
+            CK(cudaMemcpyAsync(d_seed_nodes_, seed_nodes.data(), seed_nodes.size() * sizeof(int2), cudaMemcpyHostToDevice, stream_));
+            CK(cudaMemcpyAsync(d_seed_slots_, seed_slots.data(), seed_slots.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
+        }
+    }
+    for (Stage &st : stages_) {
+        if (st.kind == BC_PERIODIC_X || st.kind == BC_PERIODIC_Y) continue;
+        if (!dalloc(&st.d_val1, (size_t)st.along) || !dalloc(&st.d_val2, (size_t)st.along)) return false;
+        CK(cudaMemsetAsync(st.d_val1, 0, st.along * sizeof(double), stream_));
+        CK(cudaMemsetAsync(st.d_val2, 0, st.along * sizeof(double), stream_));
+    }
+    if (has_mem_) {
+        const unsigned nb = ((Nx + block_.x - 1) / block_.x) * ((Ny + block_.y - 1) / block_.y);
+        // Partials sized for the smallest block the autotuner may pick (32 threads).
+        const size_t cap = (size_t)((Nx + 31) / 32) * Ny;
+        if (!dalloc(&d_partials_, 2 * std::max<size_t>(cap, nb)) || !dalloc(&d_ticket_, 1) ||
+            !dalloc(&d_mem_out_, 2))
+            return false;
+        CK(cudaMemsetAsync(d_ticket_, 0, sizeof(unsigned int), stream_));
+        CK(cudaMemsetAsync(d_mem_out_, 0, 2 * sizeof(double), stream_));
+    }
+    if (!upload_all_bc_values()) return false;
+    CK(cudaStreamSynchronize(stream_));
+    return true;
+}
+
+bool Solver::upload_all_bc_values() {
+    for (const Stage &st : stages_) {
+        const BCEntry &b = d_.bcs[st.entry];
+        if (st.d_val1 && b.val1) CK(cudaMemcpyAsync(st.d_val1, b.val1, st.along * sizeof(double), cudaMemcpyHostToDevice, stream_));
+        if (st.d_val2 && b.val2) CK(cudaMemcpyAsync(st.d_val2, b.val2, st.along * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    }
+    return true;
+}
+
+bool Solver::set_bc_values(int entry, const double *val1, const double *val2) {
+    for (const Stage &st : stages_) {
+        if (st.entry != entry) continue;
+        if (st.d_val1 && val1) CK(cudaMemcpyAsync(st.d_val1, val1, st.along * sizeof(double), cudaMemcpyHostToDevice, stream_));
+        if (st.d_val2 && val2) CK(cudaMemcpyAsync(st.d_val2, val2, st.along * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    }
+    if (entry >= 0 && entry < (int)d_.bcs.size()) {
+        d_.bcs[entry].val1 = val1;
+        d_.bcs[entry].val2 = val2;
+    }
+    return true;
+}
+
+bool Solver::set_state(const double *f, const double *f_new, const double *rho, const double *u,
+                       const double *v) {
+    const int Nx = d_.Nx, Ny = d_.Ny;
+    const size_t N = (size_t)Nx * Ny;
+    cur_ = 0;
+    const double *src[2] = {f, f_new};
+    for (int b = 0; b < 2; b++) {
+        CK(cudaMemcpyAsync(d_stage_, src[b], N * 9 * sizeof(double), cudaMemcpyHostToDevice, stream_));
+        CK(launch::aos_to_soa(d_stage_, buf_[b], d_.store, Nx, Ny, pitch_, plane_, d_.w, stream_));
+    }
+    CK(cudaMemcpyAsync(d_rho_, rho, N * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemcpyAsync(d_ux_, u, N * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemcpyAsync(d_uy_, v, N * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    if (nslots_ > 0)
+        CK(launch::seed_band(d_seed_nodes_, d_seed_slots_, nseed_, Nx, d_rho_, d_ux_, d_uy_,
+                             d_bandm_[parity_], nslots_, stream_));
+    return true;
+}
+
+bool Solver::get_state(double *f, double *f_new, double *rho, double *u, double *v) {
+    const int Nx = d_.Nx, Ny = d_.Ny;
+    const size_t N = (size_t)Nx * Ny;
+    double *dst[2] = {f, f_new};
+    const int which[2] = {cur_, 1 - cur_};
+    for (int b = 0; b < 2; b++) {
+        if (!dst[b]) continue;
+        CK(launch::soa_to_aos(buf_[which[b]], d_stage_, d_.store, Nx, Ny, pitch_, plane_, d_.w, stream_));
+        CK(cudaMemcpyAsync(dst[b], d_stage_, N * 9 * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    }
+    if (!get_fields(rho, u, v)) return false;
+    CK(cudaStreamSynchronize(stream_));
+    return true;
+}
+
+bool Solver::get_fields(double *rho, double *u, double *v) {
+    const size_t N = (size_t)d_.Nx * d_.Ny;
+    if (rho) CK(cudaMemcpyAsync(rho, d_rho_, N * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    if (u) CK(cudaMemcpyAsync(u, d_ux_, N * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    if (v) CK(cudaMemcpyAsync(v, d_uy_, N * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    return true;
+}
+
+bool Solver::forces(double *Fx, double *Fy) {
+    double h[2] = {0.0, 0.0};
+    if (has_mem_) {
+        CK(cudaMemcpyAsync(h, d_mem_out_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+    }
+    if (Fx) *Fx = h[0];
+    if (Fy) *Fy = h[1];
+    return true;
+}
+
+bool Solver::enable_force_history(int capacity) {
+    if (!has_mem_) {
+        set_error("the geometry has no wall links: no force to record");
+        return false;
+    }
+    if (capacity <= 0) {
+        set_error("force history capacity must be positive");
+        return false;
+    }
+    if (!dalloc(&d_hist_, (size_t)capacity * 2)) return false;
+    unsigned long long *cnt = nullptr;
+    if (!dalloc(&cnt, 1)) return false;
+    CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), stream_));
+    hist_cap_ = capacity;
+    hist_count_ptr_ = cnt;
+    graph_valid_ = false;
+    return true;
+}
+
+int Solver::force_history(double *out, int max_steps) {
+    if (!d_hist_) return 0;
+    unsigned long long cnt = 0;
+    if (!check_cuda(cudaMemcpyAsync(&cnt, hist_count_ptr_, sizeof cnt, cudaMemcpyDeviceToHost, stream_), "history"))
+        return -1;
+    if (!check_cuda(cudaStreamSynchronize(stream_), "history")) return -1;
+    const long long avail = std::min<long long>((long long)cnt, hist_cap_);
+    const int n = (int)std::min<long long>(avail, max_steps);
+    // Oldest first.
+    std::vector<double> ring((size_t)hist_cap_ * 2);
+    if (!check_cuda(cudaMemcpy(ring.data(), d_hist_, ring.size() * sizeof(double), cudaMemcpyDeviceToHost), "history"))
+        return -1;
+    const long long first = (long long)cnt - n;
+    for (int s = 0; s < n; s++) {
+        const long long slot = (first + s) % hist_cap_;
+        out[2 * s] = ring[2 * slot];
+        out[2 * s + 1] = ring[2 * slot + 1];
+    }
+    return n;
+}
+
+bool Solver::launch_collide(int b) {
+    CollideParams c;
+    c.Nx = d_.Nx; c.Ny = d_.Ny; c.pitch = pitch_; c.plane = plane_;
+    c.f = (double *)buf_[b];
+    c.flags = d_flags_;
+    c.rho = d_rho_; c.ux = d_ux_; c.uy = d_uy_;
+    c.omega = d_omega_; c.omega0 = omega0_;
+    c.has_force = (d_.Fx != 0.0 || d_.Fy != 0.0);
+    c.Fx = d_.Fx; c.Fy = d_.Fy;
+    for (int k = 0; k < 9; k++) c.w[k] = d_.w[k];
+    if (d_.store == STORE_F64) CK(launch::collide_exact(c, stream_));
+    else CK(launch::collide_shifted(c, d_.store, stream_));
+    return true;
+}
+
+// One time step src -> dst: fused bulk kernel, then the Boundary list in order
+// and the finish kernel for BC-written nodes.
+bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int bparity) {
+    StepParams p;
+    std::memset(&p, 0, sizeof p);
+    p.Nx = d_.Nx; p.Ny = d_.Ny; p.pitch = pitch_; p.plane = plane_;
+    p.px = d_.px; p.py = d_.py;
+    p.src = buf_[src]; p.dst = buf_[dst];
+    p.flags = d_flags_; p.link_off = d_link_off_; p.links = d_links_;
+    p.omega = d_omega_; p.omega0 = omega0_;
+    p.has_force = (d_.Fx != 0.0 || d_.Fy != 0.0);
+    p.Fx = d_.Fx; p.Fy = d_.Fy; p.hFx = 0.5 * d_.Fx; p.hFy = 0.5 * d_.Fy;
+    for (int k = 0; k < 9; k++) p.w[k] = d_.w[k];
+    p.write_macro = write_macro ? 1 : 0;
+    p.rho = d_rho_; p.ux = d_ux_; p.uy = d_uy_;
+    p.colbase = d_colbase_; p.rowbase = d_rowbase_; p.nslots = nslots_;
+    p.bandf = d_bandf_;
+    p.bandm_next = nslots_ ? d_bandm_[bparity ^ 1] : nullptr;
+    if (has_mem_) {
+        p.mem_partials = d_partials_; p.mem_ticket = d_ticket_; p.mem_out = d_mem_out_;
+        p.mem_hist = d_hist_; p.mem_hist_count = hist_count_ptr_; p.mem_hist_cap = hist_cap_;
+    }
+    if (d_.store == STORE_F64) {
+        CK(launch::step_exact(p, has_flags_, collide, block_, stream_));
+    } else {
+        FastStepParams fp;
+        fp.s = p;
+        for (int k = 0; k < 9; k++) fp.wf[k] = (float)d_.w[k];
+        fp.omega0f = (float)omega0_;
+        fp.Fxf = (float)d_.Fx; fp.Fyf = (float)d_.Fy;
+        CK(launch::step_shifted(fp, d_.store, has_flags_, collide, block_, stream_));
+    }
+    if (stages_.empty()) return true;
+    for (const Stage &st : stages_) {
+        StageParams s;
+        std::memset(&s, 0, sizeof s);
+        s.Nx = d_.Nx; s.Ny = d_.Ny; s.pitch = pitch_; s.plane = plane_;
+        s.kind = st.kind; s.index = st.index; s.along = st.along;
+        s.val1 = st.d_val1; s.val2 = st.d_val2;
+        s.flags = d_flags_; s.colbase = d_colbase_; s.rowbase = d_rowbase_; s.nslots = nslots_;
+        s.bandf = d_bandf_; s.bandm_prev = d_bandm_[bparity];
+        s.src = buf_[src];
+        for (int k = 0; k < 9; k++) s.w[k] = d_.w[k];
+        CK(launch::stage(s, d_.store, stream_));
+    }
+    FinishParams f;
+    std::memset(&f, 0, sizeof f);
+    f.Nx = d_.Nx; f.Ny = d_.Ny; f.pitch = pitch_; f.plane = plane_;
+    f.nw = nw_; f.wnodes = d_wnodes_;
+    f.colbase = d_colbase_; f.rowbase = d_rowbase_; f.nslots = nslots_;
+    f.bandf = d_bandf_; f.bandm_next = d_bandm_[bparity ^ 1];
+    f.dst = buf_[dst];
+    f.omega = d_omega_; f.omega0 = omega0_;
+    f.has_force = p.has_force; f.Fx = d_.Fx; f.Fy = d_.Fy; f.hFx = p.hFx; f.hFy = p.hFy;
+    for (int k = 0; k < 9; k++) f.w[k] = d_.w[k];
+    f.write_macro = p.write_macro;
+    f.rho = d_rho_; f.ux = d_ux_; f.uy = d_uy_;
+    if (d_.store == STORE_F64) CK(launch::finish_exact(f, collide, stream_));
+    else CK(launch::finish_shifted(f, d_.store, collide, stream_));
+    return true;
+}
+
+// Two fused steps (cur -> other -> cur) captured once and replayed.
+bool Solver::capture_pair() {
+    if (graph_valid_ && pair_cur_ == cur_ && pair_parity_ == parity_) return true;
+    if (pair_exec_) {
+        cudaGraphExecDestroy(pair_exec_);
+        pair_exec_ = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    bool okk = launch_step(cur_, 1 - cur_, true, false, parity_) &&
+               launch_step(1 - cur_, cur_, true, false, parity_ ^ 1);
+    cudaError_t e = cudaStreamEndCapture(stream_, &g);
+    if (!okk) {
+        if (g) cudaGraphDestroy(g);
+        return false;
+    }
+    CK(e);
+    e = cudaGraphInstantiate(&pair_exec_, g, 0);
+    cudaGraphDestroy(g);
+    CK(e);
+    pair_cur_ = cur_;
+    pair_parity_ = parity_;
+    graph_valid_ = true;
+    return true;
+}
+
+bool Solver::run(int nsteps) {
+    if (nsteps <= 0) return true;
+    if (!launch_collide(cur_)) return false;
+    int remaining = nsteps - 1;
+    if (remaining >= 2) {
+        if (!capture_pair()) return false;
+        while (remaining >= 2) {
+            CK(cudaGraphLaunch(pair_exec_, stream_));
+            remaining -= 2;
+        }
+    }
+    if (remaining == 1) {
+        if (!launch_step(cur_, 1 - cur_, true, false, parity_)) return false;
+        cur_ ^= 1;
+        parity_ ^= 1;
+    }
+    if (!launch_step(cur_, 1 - cur_, false, true, parity_)) return false;
+    cur_ ^= 1;
+    parity_ ^= 1;
+    steps_done_ += nsteps;
+    return true;
+}
+
+}  // namespace lbm

@@ -1,0 +1,137 @@
+// engine.h -- host-side solver of the GB300 D2Q9 engine (internal header).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "lbm_device.cuh"
+
+namespace lbm {
+
+void set_error(const std::string &msg);
+const char *last_error();
+bool check_cuda(cudaError_t e, const char *what);
+
+// One entry of the Boundary list, resolved to a device BC kind.
+struct BCEntry {
+    int kind;      // BCKind
+    int index;
+    const double *val1, *val2;  // host arrays (lbc: length Ny for columns, Nx for rows)
+};
+
+// Everything a case needs besides its populations (what main_lbm receives).
+struct CaseDesc {
+    int Nx = 0, Ny = 0;
+    double w[9];
+    const int *mask = nullptr;
+    const double *omega = nullptr;
+    const double *phi = nullptr;
+    int use_ibb = 0;
+    const double *wall_u = nullptr, *wall_v = nullptr;
+    int px = 0, py = 0;
+    double Fx = 0.0, Fy = 0.0;
+    std::vector<BCEntry> bcs;
+    int store = STORE_F64;
+};
+
+struct Stage {
+    int kind, index, along;
+    int entry;                  // position in the Boundary list
+    double *d_val1 = nullptr, *d_val2 = nullptr;
+};
+
+class Solver {
+  public:
+    explicit Solver(const CaseDesc &d);
+    ~Solver();
+    bool ok() const { return ok_; }
+
+    // Host arrays in lbc's layout. set_state makes buf[cur] = f and the other
+    // buffer = f_new, and takes rho/u/v as the stored fields of the next step.
+    bool set_state(const double *f, const double *f_new, const double *rho, const double *u,
+                   const double *v);
+    bool get_state(double *f, double *f_new, double *rho, double *u, double *v);
+    bool get_fields(double *rho, double *u, double *v);
+    bool set_bc_values(int entry, const double *val1, const double *val2);
+    bool upload_all_bc_values();
+    // n time steps, each equivalent to one main_lbm call plus the caller's swap.
+    bool run(int nsteps);
+    bool forces(double *Fx, double *Fy);  // MEM force of the last step
+    // Per-step force record (lbm_gpu_force_history).
+    bool enable_force_history(int capacity);
+    int force_history(double *out, int max_steps);
+
+    int Nx() const { return d_.Nx; }
+    int Ny() const { return d_.Ny; }
+    int store() const { return d_.store; }
+    cudaStream_t stream() const { return stream_; }
+    size_t device_bytes() const { return dev_bytes_; }
+    bool has_flags() const { return has_flags_; }
+    int nstages() const { return (int)stages_.size(); }
+    int pitch() const { return pitch_; }
+    long long plane() const { return plane_; }
+    void *buffer(int b) const { return buf_[b]; }
+    int current() const { return cur_; }
+    long long steps_done() const { return steps_done_; }
+    // Kernel launches per time step inside the loop (for launch counting).
+    int launches_per_step() const { return 1 + (int)stages_.size() + (nw_ > 0 ? 1 : 0); }
+    void set_block(dim3 b) { block_ = b; graph_valid_ = false; }
+    dim3 block() const { return block_; }
+
+  private:
+    bool build_geometry();
+    bool alloc();
+    bool launch_step(int src, int dst, bool collide, bool write_macro, int bparity);
+    bool launch_collide(int b);
+    bool capture_pair();
+    template <class T> bool dalloc(T **p, size_t count);
+
+    CaseDesc d_;
+    bool ok_ = false;
+    cudaStream_t stream_ = nullptr;
+    int pitch_ = 0;
+    long long plane_ = 0;
+    size_t esize_ = 8;
+    void *buf_[2] = {nullptr, nullptr};
+    int cur_ = 0;
+    int parity_ = 0;
+    bool has_flags_ = false, has_links_ = false, has_mem_ = false;
+    uint16_t *d_flags_ = nullptr;
+    int *d_link_off_ = nullptr;
+    Link *d_links_ = nullptr;
+    double *d_omega_ = nullptr;
+    double omega0_ = 1.0;
+    int *d_colbase_ = nullptr, *d_rowbase_ = nullptr;
+    int nslots_ = 0;
+    double *d_bandf_ = nullptr;
+    double *d_bandm_[2] = {nullptr, nullptr};
+    int2 *d_wnodes_ = nullptr;
+    int nw_ = 0;
+    int2 *d_seed_nodes_ = nullptr;
+    int *d_seed_slots_ = nullptr;
+    int nseed_ = 0;
+    double *d_rho_ = nullptr, *d_ux_ = nullptr, *d_uy_ = nullptr;
+    double *d_partials_ = nullptr;
+    unsigned int *d_ticket_ = nullptr;
+    double *d_mem_out_ = nullptr;
+    double *d_hist_ = nullptr;
+    int hist_cap_ = 0;
+    unsigned long long *hist_count_ptr_ = nullptr;
+    double *d_stage_ = nullptr;  // AoS staging (FP64, 72 N bytes)
+    std::vector<Stage> stages_;
+    dim3 block_{64, 4, 1};
+    cudaGraphExec_t pair_exec_ = nullptr;
+    int pair_cur_ = -1, pair_parity_ = -1;
+    bool graph_valid_ = false;
+    size_t dev_bytes_ = 0;
+    long long steps_done_ = 0;
+    std::vector<void *> allocs_;
+};
+
+// Maps lbc BC function pointers to device kinds (dropin.cpp).
+int bc_kind_of(const void *fn);
+
+}  // namespace lbm

@@ -1,0 +1,77 @@
+// kernels.h -- host-side launchers of the device kernels (internal header).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "lbm_device.cuh"
+
+namespace lbm {
+
+enum StoreKind : int { STORE_F64 = 0, STORE_F32 = 1, STORE_F16 = 2 };
+
+struct Wt { double w[9]; };
+
+struct CollideParams {
+    int Nx, Ny, pitch;
+    long long plane;
+    double *f;                       // SoA planes (FP64, or shifted FP32/FP16 as void data)
+    const uint16_t *flags;           // solid bit, or null
+    const double *rho, *ux, *uy;     // stored fields, dense [Ny * Nx]
+    const double *omega;
+    double omega0;
+    int has_force;
+    double Fx, Fy;
+    double w[9];
+};
+
+// Arguments of lbc's standalone functions on device copies of lbc's AoS arrays.
+struct AosArgs {
+    int Nx, Ny, px, py;
+    double *f, *fnew;                // [Ny][Nx][9]
+    double *rho, *u, *v;             // [Ny][Nx]
+    const double *omega, *phi;
+    const int *mask;
+    double Fx, Fy;
+    double w[9];
+    double *partials;                // reductions
+    unsigned int *ticket;
+    double *out2;
+};
+
+enum AosOp : int { AOS_COLLISION, AOS_STREAMING, AOS_MOMENTS, AOS_BOUNCE_BACK, AOS_IBB, AOS_MEM };
+
+// Parameters of the shifted-storage (FP32 / FP16) fused step.
+struct FastStepParams {
+    StepParams s;
+    float wf[9];
+    float omega0f;
+    float Fxf, Fyf;
+};
+
+namespace launch {
+// exact FP64 (kernels_exact.cu)
+cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block, cudaStream_t s);
+cudaError_t stage(const StageParams &p, int store, cudaStream_t s);
+cudaError_t finish_exact(const FinishParams &p, bool collide, cudaStream_t s);
+cudaError_t collide_exact(const CollideParams &p, cudaStream_t s);
+cudaError_t aos_to_soa(const double *aos, void *soa, int store, int Nx, int Ny, int pitch,
+                       long long plane, const double w[9], cudaStream_t s);
+cudaError_t soa_to_aos(const void *soa, double *aos, int store, int Nx, int Ny, int pitch,
+                       long long plane, const double w[9], cudaStream_t s);
+cudaError_t seed_band(const int2 *nodes, const int *slots, int n, int Nx, const double *rho,
+                      const double *ux, const double *uy, double *bandm, int nslots,
+                      cudaStream_t s);
+cudaError_t aos_op(int op, const AosArgs &a, cudaStream_t s);
+unsigned aos_mem_blocks(int Nx, int Ny);
+cudaError_t aos_bc(const AosArgs &a, int kind, int index, int along, const double *val1,
+                   const double *val2, cudaStream_t s);
+cudaError_t mei_init(const AosArgs &a, double rho0, cudaStream_t s);
+cudaError_t mei_iter(const AosArgs &a, double rho0, unsigned long long *maxbits, cudaStream_t s);
+
+// shifted storage (kernels_shifted.cu)
+cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
+                         cudaStream_t s);
+cudaError_t finish_shifted(const FinishParams &p, int store, bool collide, cudaStream_t s);
+cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s);
+}  // namespace launch
+
+}  // namespace lbm

@@ -1,0 +1,555 @@
+// kernels_exact.cu -- FP64 kernels that reproduce lbc's arithmetic bit for bit.
+//
+// Compiled with --fmad=false: every multiply and add rounds separately, in the
+// order the reference C code evaluates them, so results match lbc's FP64 CPU
+// solver exactly (signed zeros aside) on identical inputs.
+//
+// Contents:
+//   * k_step_exact      fused pull step (stream + halfway/interpolated/moving-wall
+//                       bounce-back + stale slots + MEM force + moments + BGK/Guo
+//                       collision), one thread per node, SoA planes
+//   * k_stage           one edge BC of the Boundary list on the band buffer
+//   * k_finish_exact    moments + collision of BC-written nodes
+//   * k_collide_exact   in-place collision with stored rho/u/v (first step)
+//   * AoS kernels       lbc's standalone functions on lbc's own layout
+//   * transposes        lbc AoS <-> device SoA, with FP32/FP16 shifted storage
+#include <cmath>
+#include <cstdio>
+
+#include "kernels.h"
+#include "lbm_device.cuh"
+#include "reduce.cuh"
+
+namespace lbm {
+
+// ---------------------------------------------------------------- fused step
+
+// src/core/main_lbm.c:31-61 restructured as a pull: the state entering the
+// kernel is the post-collision f of step n (what lbc's collision leaves in f),
+// each fluid node gathers f_new from its neighbours (src/core/streaming.c:20-42),
+// takes bounce-back values where the source is solid (src/bc/bounce_back.c:42-46,
+// src/bc/interpolated_bounce_back.c:91-100), keeps the old content of its slot
+// where the source is off a non-periodic edge (src/core/streaming.c:36-37), adds
+// its momentum-exchange terms (src/core/compute_force_mem.c:51-58), computes
+// moments (src/core/compute_macroscopic_fields.c:23-46) and, unless it is written
+// by an edge BC, collides (src/core/collision.c:22-38) and stores.
+template <bool FLAGS, bool COLLIDE>
+__global__ void __launch_bounds__(256) k_step_exact(const StepParams p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    double mfx = 0.0, mfy = 0.0;
+    if (i < p.Nx && j < p.Ny) {
+        const long long node = (long long)j * p.pitch + i;
+        const uint16_t fl = FLAGS ? p.flags[node] : (uint16_t)0;
+        const size_t dn = (size_t)j * (size_t)p.Nx + (size_t)i;
+        if (FLAGS && (fl & NF_SOLID)) {
+            if (p.write_macro) { p.rho[dn] = NAN; p.ux[dn] = NAN; p.uy[dn] = NAN; }
+            if (fl & NF_BAND) {
+                // A BC may read a solid neighbour: lbc sees the untouched buffer
+                // content and NaN moments there.
+                const int slot = band_slot(p.colbase, p.rowbase, i, j);
+                const double *Dst = (const double *)p.dst;
+#pragma unroll
+                for (int k = 0; k < 9; k++) p.bandf[(size_t)k * p.nslots + slot] = Dst[k * p.plane + node];
+                p.bandm_next[slot] = NAN;
+                p.bandm_next[(size_t)p.nslots + slot] = NAN;
+                p.bandm_next[2 * (size_t)p.nslots + slot] = NAN;
+            }
+        } else {
+            const double *S = (const double *)p.src;
+            double *Dst = (double *)p.dst;
+            const long long pl = p.plane;
+            int im = i - 1, ip = i + 1, jm = j - 1, jp = j + 1;
+            if (p.px) { if (im < 0) im += p.Nx; if (ip >= p.Nx) ip -= p.Nx; }
+            if (p.py) { if (jm < 0) jm += p.Ny; if (jp >= p.Ny) jp -= p.Ny; }
+            const long long r0 = (long long)j * p.pitch, rm = (long long)jm * p.pitch,
+                            rp = (long long)jp * p.pitch;
+            const long long so[9] = {r0 + i, r0 + im, rm + i, r0 + ip, rp + i,
+                                     rm + im, rm + ip, rp + ip, rp + im};
+            double f[9];
+            if (!FLAGS) {
+#pragma unroll
+                for (int k = 0; k < 9; k++) f[k] = S[k * pl + so[k]];
+            } else {
+                const Link *lk = (fl & NF_LINKS) ? p.links + p.link_off[node] : nullptr;
+#pragma unroll
+                for (int k = 0; k < 9; k++) {
+                    if (!(fl & (1u << k))) {
+                        f[k] = S[k * pl + so[k]];
+                        continue;
+                    }
+                    const int si = i - cxk(k), sj = j - cyk(k);
+                    const bool off = (!p.px && (si < 0 || si >= p.Nx)) ||
+                                     (!p.py && (sj < 0 || sj >= p.Ny));
+                    if (off) {
+                        f[k] = Dst[k * pl + node];
+                        continue;
+                    }
+                    const int ko = oppk(k);
+                    const double own = S[ko * pl + node];
+                    double val = own;
+                    if (lk) {
+                        const Link L = *lk++;
+                        if (L.mode == LINK_IBB_LO) val = L.c1 * own + L.c2 * S[ko * pl + L.behind];
+                        else if (L.mode == LINK_IBB_HI) val = L.c1 * own + L.c2 * S[k * pl + L.behind];
+                        else if (L.mode == LINK_MOVING) val = own - L.c2;
+                    }
+                    f[k] = val;
+                    const double df = own + val;
+                    mfx -= df * cxk(k);
+                    mfy -= df * cyk(k);
+                }
+            }
+            int slot = -1;
+            if (FLAGS && (fl & NF_BAND)) {
+                slot = band_slot(p.colbase, p.rowbase, i, j);
+#pragma unroll
+                for (int k = 0; k < 9; k++) p.bandf[(size_t)k * p.nslots + slot] = f[k];
+            }
+            if (!(FLAGS && (fl & NF_BCW))) {
+                double rho, ux, uy;
+                moments_exact(f, p.hFx, p.hFy, rho, ux, uy);
+                if (p.write_macro) { p.rho[dn] = rho; p.ux[dn] = ux; p.uy[dn] = uy; }
+                if (slot >= 0) {
+                    p.bandm_next[slot] = rho;
+                    p.bandm_next[(size_t)p.nslots + slot] = ux;
+                    p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
+                }
+                if (COLLIDE) {
+                    const double om = p.omega ? p.omega[dn] : p.omega0;
+                    collide_exact(f, p.w, rho, ux, uy, om, p.has_force != 0, p.Fx, p.Fy);
+                }
+#pragma unroll
+                for (int k = 0; k < 9; k++) Dst[k * pl + node] = f[k];
+            }
+        }
+    }
+    if (FLAGS && p.mem_partials)
+        reduce2_grid(mfx, mfy, p.mem_partials, p.mem_ticket, p.mem_out, p.mem_hist, p.mem_hist_count,
+                     p.mem_hist_cap);
+}
+
+// ---------------------------------------------------------------- edge BCs
+
+template <typename T> struct BandAccessor {
+    const StageParams &p;
+    __device__ int slot(int i, int j) const { return band_slot(p.colbase, p.rowbase, i, j); }
+    __device__ double get(int i, int j, int k) const { return p.bandf[(size_t)k * p.nslots + slot(i, j)]; }
+    __device__ void set(int i, int j, int k, double v) const { p.bandf[(size_t)k * p.nslots + slot(i, j)] = v; }
+    __device__ double rho(int i, int j) const { return p.bandm_prev[slot(i, j)]; }
+    __device__ double ux(int i, int j) const { return p.bandm_prev[(size_t)p.nslots + slot(i, j)]; }
+    __device__ double uy(int i, int j) const { return p.bandm_prev[2 * (size_t)p.nslots + slot(i, j)]; }
+    __device__ double post(int i, int j, int k) const {
+        return Store<T>::to_f64(((const T *)p.src)[k * p.plane + (long long)j * p.pitch + i], p.w[k]);
+    }
+    __device__ bool solid(int i, int j) const { return (p.flags[(long long)j * p.pitch + i] & NF_SOLID) != 0; }
+};
+
+// One entry of lbc's Boundary list (src/core/main_lbm.c:49-58), applied to the
+// pre-collision f_new of the band nodes. Entries run as separate launches in list
+// order, so each sees the writes of the previous ones, as in lbc.
+template <typename T>
+__global__ void k_stage(const StageParams p) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.along) return;
+    BandAccessor<T> a{p};
+    bc_apply(a, p.w, p.kind, p.Nx, p.Ny, p.index, t, p.val1, p.val2);
+}
+
+// Moments and collision of every node an edge BC wrote.
+template <bool COLLIDE>
+__global__ void k_finish_exact(const FinishParams p) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.nw) return;
+    const int2 ij = p.wnodes[t];
+    const int slot = band_slot(p.colbase, p.rowbase, ij.x, ij.y);
+    double f[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) f[k] = p.bandf[(size_t)k * p.nslots + slot];
+    double rho, ux, uy;
+    moments_exact(f, p.hFx, p.hFy, rho, ux, uy);
+    const size_t dn = (size_t)ij.y * p.Nx + ij.x;
+    if (p.write_macro) { p.rho[dn] = rho; p.ux[dn] = ux; p.uy[dn] = uy; }
+    p.bandm_next[slot] = rho;
+    p.bandm_next[(size_t)p.nslots + slot] = ux;
+    p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
+    if (COLLIDE) {
+        const double om = p.omega ? p.omega[dn] : p.omega0;
+        collide_exact(f, p.w, rho, ux, uy, om, p.has_force != 0, p.Fx, p.Fy);
+    }
+    double *D = (double *)p.dst;
+    const long long node = (long long)ij.y * p.pitch + ij.x;
+#pragma unroll
+    for (int k = 0; k < 9; k++) D[k * p.plane + node] = f[k];
+}
+
+// In-place collision with the stored rho/u/v (src/core/collision.c:18-40); used
+// for the first step, whose stored fields are the caller's arrays.
+__global__ void k_collide_exact(const CollideParams p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= p.Nx || j >= p.Ny) return;
+    const long long node = (long long)j * p.pitch + i;
+    if (p.flags && (p.flags[node] & NF_SOLID)) return;
+    const size_t dn = (size_t)j * p.Nx + i;
+    double f[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) f[k] = p.f[k * p.plane + node];
+    const double om = p.omega ? p.omega[dn] : p.omega0;
+    collide_exact(f, p.w, p.rho[dn], p.ux[dn], p.uy[dn], om, p.has_force != 0, p.Fx, p.Fy);
+#pragma unroll
+    for (int k = 0; k < 9; k++) p.f[k * p.plane + node] = f[k];
+}
+
+// ---------------------------------------------------------------- transposes
+
+// lbc AoS [Ny][Nx][9] (dense) -> device SoA planes of type T.
+template <typename T>
+__global__ void k_aos_to_soa(const double *__restrict__ aos, T *__restrict__ soa, int Nx, int Ny,
+                             int pitch, long long plane, Wt w) {
+    __shared__ double tile[128 * 9];
+    const long long n0 = (long long)blockIdx.x * 128;
+    const long long N = (long long)Nx * Ny;
+    const int cnt = (int)min((long long)128, N - n0);
+    for (int e = threadIdx.x; e < cnt * 9; e += blockDim.x) tile[e] = aos[n0 * 9 + e];
+    __syncthreads();
+    for (int e = threadIdx.x; e < cnt * 9; e += blockDim.x) {
+        const int k = e / cnt, r = e - k * cnt;
+        const long long n = n0 + r;
+        const int j = (int)(n / Nx), i = (int)(n - (long long)j * Nx);
+        soa[k * plane + (long long)j * pitch + i] = Store<T>::from_f64(tile[r * 9 + k], w.w[k]);
+    }
+}
+
+template <typename T>
+__global__ void k_soa_to_aos(const T *__restrict__ soa, double *__restrict__ aos, int Nx, int Ny,
+                             int pitch, long long plane, Wt w) {
+    __shared__ double tile[128 * 9];
+    const long long n0 = (long long)blockIdx.x * 128;
+    const long long N = (long long)Nx * Ny;
+    const int cnt = (int)min((long long)128, N - n0);
+    for (int e = threadIdx.x; e < cnt * 9; e += blockDim.x) {
+        const int k = e / cnt, r = e - k * cnt;
+        const long long n = n0 + r;
+        const int j = (int)(n / Nx), i = (int)(n - (long long)j * Nx);
+        tile[r * 9 + k] = Store<T>::to_f64(soa[k * plane + (long long)j * pitch + i], w.w[k]);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < cnt * 9; e += blockDim.x) aos[n0 * 9 + e] = tile[e];
+}
+
+// Band moments of the first step come from the caller's stored rho/u/v.
+__global__ void k_seed_band(const int2 *nodes, const int *slots, int n, int Nx, const double *rho,
+                            const double *ux, const double *uy, double *bandm, int nslots) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const size_t dn = (size_t)nodes[t].y * Nx + nodes[t].x;
+    const int s = slots[t];
+    bandm[s] = rho[dn];
+    bandm[(size_t)nslots + s] = ux[dn];
+    bandm[2 * (size_t)nslots + s] = uy[dn];
+}
+
+// ---------------------------------------------------------------- AoS kernels
+// lbc's standalone functions on lbc's own layout, one thread per node.
+
+#define AOS_IDX(j, i, k) ((((size_t)(j)) * (size_t)Nx + (size_t)(i)) * 9 + (size_t)(k))
+
+__device__ __forceinline__ bool wrapc(int &c, int n, int periodic) {
+    if (periodic) {
+        if (c < 0) c += n;
+        else if (c >= n) c -= n;
+        return true;
+    }
+    return c >= 0 && c < n;
+}
+
+// src/core/collision.c:18-40
+__global__ void k_aos_collision(AosArgs a) {
+    const int Nx = a.Nx;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= a.Nx || j >= a.Ny) return;
+    const size_t n = (size_t)j * Nx + i;
+    if (a.mask[n]) return;
+    double f[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) f[k] = a.f[AOS_IDX(j, i, k)];
+    collide_exact(f, a.w, a.rho[n], a.u[n], a.v[n], a.omega[n], a.Fx != 0.0 || a.Fy != 0.0, a.Fx, a.Fy);
+#pragma unroll
+    for (int k = 0; k < 9; k++) a.f[AOS_IDX(j, i, k)] = f[k];
+}
+
+// src/core/streaming.c:14-45
+__global__ void k_aos_streaming(AosArgs a) {
+    const int Nx = a.Nx, Ny = a.Ny;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= Nx || j >= Ny) return;
+    if (a.mask[(size_t)j * Nx + i]) return;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        int is = i - cxk(k), js = j - cyk(k);
+        if (!wrapc(is, Nx, a.px) || !wrapc(js, Ny, a.py)) continue;
+        if (a.mask[(size_t)js * Nx + is]) continue;
+        a.fnew[AOS_IDX(j, i, k)] = a.f[AOS_IDX(js, is, k)];
+    }
+}
+
+// src/core/compute_macroscopic_fields.c:19-48
+__global__ void k_aos_moments(AosArgs a) {
+    const int Nx = a.Nx;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= a.Nx || j >= a.Ny) return;
+    const size_t n = (size_t)j * Nx + i;
+    double f[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) f[k] = a.fnew[AOS_IDX(j, i, k)];
+    double rho, ux, uy;
+    moments_exact(f, 0.5 * a.Fx, 0.5 * a.Fy, rho, ux, uy);
+    if (!a.mask[n]) { a.rho[n] = rho; a.u[n] = ux; a.v[n] = uy; }
+    else { a.rho[n] = NAN; a.u[n] = NAN; a.v[n] = NAN; }
+}
+
+// src/bc/bounce_back.c:15-49
+__global__ void k_aos_bounce_back(AosArgs a) {
+    const int Nx = a.Nx, Ny = a.Ny;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= Nx || j >= Ny) return;
+    if (a.mask[(size_t)j * Nx + i]) return;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        int in = i + cxk(k), jn = j + cyk(k);
+        if (!wrapc(in, Nx, a.px) || !wrapc(jn, Ny, a.py)) continue;
+        if (!a.mask[(size_t)jn * Nx + in]) continue;
+        a.fnew[AOS_IDX(j, i, oppk(k))] = a.f[AOS_IDX(j, i, k)];
+    }
+}
+
+// src/bc/interpolated_bounce_back.c:19-103
+__global__ void k_aos_ibb(AosArgs a) {
+    const int Nx = a.Nx, Ny = a.Ny;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= Nx || j >= Ny) return;
+    const size_t n = (size_t)j * Nx + i;
+    if (a.mask[n]) return;
+    const double eps = 1e-12;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        int in = i + cxk(k), jn = j + cyk(k);
+        if (!wrapc(in, Nx, a.px) || !wrapc(jn, Ny, a.py)) continue;
+        if (!a.mask[(size_t)jn * Nx + in]) continue;
+        double denom = a.phi[n] - a.phi[(size_t)jn * Nx + in];
+        if (fabs(denom) < eps) denom = (denom >= 0.0) ? eps : -eps;
+        double q = a.phi[n] / denom;
+        if (q < eps) q = eps;
+        if (q > 1.0 - eps) q = 1.0 - eps;
+        const size_t dst = AOS_IDX(j, i, oppk(k));
+        const double fk = a.f[AOS_IDX(j, i, k)];
+        int ib = i - cxk(k), jb = j - cyk(k);
+        if (!wrapc(ib, Nx, a.px) || !wrapc(jb, Ny, a.py)) { a.fnew[dst] = fk; continue; }
+        if (q <= 0.5) a.fnew[dst] = (1.0 - 2.0 * q) * fk + 2.0 * q * a.f[AOS_IDX(jb, ib, k)];
+        else if (a.mask[(size_t)jb * Nx + ib]) a.fnew[dst] = fk;
+        else a.fnew[dst] = (1.0 / (2.0 * q)) * fk + (2.0 * q - 1.0) / (2.0 * q) * a.f[AOS_IDX(jb, ib, oppk(k))];
+    }
+}
+
+// src/core/compute_force_mem.c:19-67, reduced deterministically.
+__global__ void k_aos_mem(AosArgs a) {
+    const int Nx = a.Nx, Ny = a.Ny;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    double fx = 0.0, fy = 0.0;
+    if (i < Nx && j < Ny && !a.mask[(size_t)j * Nx + i]) {
+#pragma unroll
+        for (int k = 1; k < 9; k++) {
+            int in = i + cxk(k), jn = j + cyk(k);
+            if (!wrapc(in, Nx, a.px) || !wrapc(jn, Ny, a.py)) continue;
+            if (!a.mask[(size_t)jn * Nx + in]) continue;
+            const double df = a.f[AOS_IDX(j, i, k)] + a.fnew[AOS_IDX(j, i, oppk(k))];
+            fx += df * cxk(k);
+            fy += df * cyk(k);
+        }
+    }
+    reduce2_grid(fx, fy, a.partials, a.ticket, a.out2);
+}
+
+struct AosAccessor {
+    const AosArgs &a;
+    __device__ double get(int i, int j, int k) const { const int Nx = a.Nx; return a.fnew[AOS_IDX(j, i, k)]; }
+    __device__ void set(int i, int j, int k, double v) const { const int Nx = a.Nx; a.fnew[AOS_IDX(j, i, k)] = v; }
+    __device__ double rho(int i, int j) const { return a.rho[(size_t)j * a.Nx + i]; }
+    __device__ double ux(int i, int j) const { return a.u[(size_t)j * a.Nx + i]; }
+    __device__ double uy(int i, int j) const { return a.v[(size_t)j * a.Nx + i]; }
+    __device__ double post(int i, int j, int k) const { const int Nx = a.Nx; return a.f[AOS_IDX(j, i, k)]; }
+    __device__ bool solid(int i, int j) const { return a.mask[(size_t)j * a.Nx + i] != 0; }
+};
+
+// Any of lbc's edge BC functions on the AoS arrays (src/bc/*.c).
+__global__ void k_aos_bc(AosArgs a, int kind, int index, int along, const double *val1,
+                         const double *val2) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= along) return;
+    AosAccessor acc{a};
+    bc_apply(acc, a.w, kind, a.Nx, a.Ny, index, t, val1, val2);
+}
+
+// ---- Mei initialisation (src/core/mei_initialization.c:50-127) on AoS arrays.
+
+// :51-63 incompressible equilibrium
+__global__ void k_mei_init(AosArgs a, double rho0) {
+    const int Nx = a.Nx;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= a.Nx || j >= a.Ny) return;
+    const size_t n = (size_t)j * Nx + i;
+    const double ux = a.u[n], uy = a.v[n];
+    const double usq = ux * ux + uy * uy;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const double cu = cxk(k) * ux + cyk(k) * uy;
+        a.f[AOS_IDX(j, i, k)] = a.w[k] * a.rho[n] + a.w[k] * rho0 * (3.0 * cu + 4.5 * cu * cu - 1.5 * usq);
+    }
+}
+
+// :76-108 density moment, then incompressible collision on every node, and the
+// max |rho - rho_prev| of :121-127 folded in.
+__global__ void k_mei_iter(AosArgs a, double rho0, unsigned long long *maxbits) {
+    const int Nx = a.Nx;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    double d = 0.0;
+    if (i < a.Nx && j < a.Ny) {
+        const size_t n = (size_t)j * Nx + i;
+        double f[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) f[k] = a.f[AOS_IDX(j, i, k)];
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < 9; k++) s += f[k];
+        d = fabs(s - a.rho[n]);
+        a.rho[n] = s;
+        const double ux = a.u[n], uy = a.v[n];
+        const double usq = ux * ux + uy * uy;
+        const double om = a.omega[n];
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const double cu = cxk(k) * ux + cyk(k) * uy;
+            const double feq = a.w[k] * s + a.w[k] * rho0 * (3.0 * cu + 4.5 * cu * cu - 1.5 * usq);
+            a.f[AOS_IDX(j, i, k)] = f[k] + -om * (f[k] - feq);
+        }
+    }
+    // d >= 0, so the IEEE bit pattern orders like the value.
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d = fmax(d, __shfl_down_sync(0xffffffffu, d, o));
+    if (((threadIdx.y * blockDim.x + threadIdx.x) & 31) == 0 && d > 0.0)
+        atomicMax(maxbits, (unsigned long long)__double_as_longlong(d));
+}
+
+// ---------------------------------------------------------------- launchers
+
+namespace launch {
+
+static dim3 grid2(int Nx, int Ny, dim3 b) { return dim3((Nx + b.x - 1) / b.x, (Ny + b.y - 1) / b.y); }
+
+cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block, cudaStream_t s) {
+    const dim3 g = grid2(p.Nx, p.Ny, block);
+    if (flags) {
+        if (collide) k_step_exact<true, true><<<g, block, 0, s>>>(p);
+        else k_step_exact<true, false><<<g, block, 0, s>>>(p);
+    } else {
+        if (collide) k_step_exact<false, true><<<g, block, 0, s>>>(p);
+        else k_step_exact<false, false><<<g, block, 0, s>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t stage(const StageParams &p, int store, cudaStream_t s) {
+    const int b = 128, g = (p.along + b - 1) / b;
+    if (store == STORE_F64) k_stage<double><<<g, b, 0, s>>>(p);
+    else if (store == STORE_F32) k_stage<float><<<g, b, 0, s>>>(p);
+    else k_stage<__half><<<g, b, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t finish_exact(const FinishParams &p, bool collide, cudaStream_t s) {
+    if (p.nw == 0) return cudaSuccess;
+    const int b = 128, g = (p.nw + b - 1) / b;
+    if (collide) k_finish_exact<true><<<g, b, 0, s>>>(p);
+    else k_finish_exact<false><<<g, b, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t collide_exact(const CollideParams &p, cudaStream_t s) {
+    const dim3 b(64, 4);
+    k_collide_exact<<<grid2(p.Nx, p.Ny, b), b, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t aos_to_soa(const double *aos, void *soa, int store, int Nx, int Ny, int pitch,
+                       long long plane, const double w[9], cudaStream_t s) {
+    Wt wt;
+    for (int k = 0; k < 9; k++) wt.w[k] = w[k];
+    const long long N = (long long)Nx * Ny;
+    const unsigned g = (unsigned)((N + 127) / 128);
+    if (store == STORE_F64) k_aos_to_soa<double><<<g, 256, 0, s>>>(aos, (double *)soa, Nx, Ny, pitch, plane, wt);
+    else if (store == STORE_F32) k_aos_to_soa<float><<<g, 256, 0, s>>>(aos, (float *)soa, Nx, Ny, pitch, plane, wt);
+    else k_aos_to_soa<__half><<<g, 256, 0, s>>>(aos, (__half *)soa, Nx, Ny, pitch, plane, wt);
+    return cudaGetLastError();
+}
+
+cudaError_t soa_to_aos(const void *soa, double *aos, int store, int Nx, int Ny, int pitch,
+                       long long plane, const double w[9], cudaStream_t s) {
+    Wt wt;
+    for (int k = 0; k < 9; k++) wt.w[k] = w[k];
+    const long long N = (long long)Nx * Ny;
+    const unsigned g = (unsigned)((N + 127) / 128);
+    if (store == STORE_F64) k_soa_to_aos<double><<<g, 256, 0, s>>>((const double *)soa, aos, Nx, Ny, pitch, plane, wt);
+    else if (store == STORE_F32) k_soa_to_aos<float><<<g, 256, 0, s>>>((const float *)soa, aos, Nx, Ny, pitch, plane, wt);
+    else k_soa_to_aos<__half><<<g, 256, 0, s>>>((const __half *)soa, aos, Nx, Ny, pitch, plane, wt);
+    return cudaGetLastError();
+}
+
+cudaError_t seed_band(const int2 *nodes, const int *slots, int n, int Nx, const double *rho,
+                      const double *ux, const double *uy, double *bandm, int nslots,
+                      cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_seed_band<<<(n + 127) / 128, 128, 0, s>>>(nodes, slots, n, Nx, rho, ux, uy, bandm, nslots);
+    return cudaGetLastError();
+}
+
+cudaError_t aos_op(int op, const AosArgs &a, cudaStream_t s) {
+    const dim3 b(64, 4);
+    const dim3 g = grid2(a.Nx, a.Ny, b);
+    switch (op) {
+    case AOS_COLLISION: k_aos_collision<<<g, b, 0, s>>>(a); break;
+    case AOS_STREAMING: k_aos_streaming<<<g, b, 0, s>>>(a); break;
+    case AOS_MOMENTS: k_aos_moments<<<g, b, 0, s>>>(a); break;
+    case AOS_BOUNCE_BACK: k_aos_bounce_back<<<g, b, 0, s>>>(a); break;
+    case AOS_IBB: k_aos_ibb<<<g, b, 0, s>>>(a); break;
+    case AOS_MEM: k_aos_mem<<<g, b, 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+unsigned aos_mem_blocks(int Nx, int Ny) {
+    const dim3 g = grid2(Nx, Ny, dim3(64, 4));
+    return g.x * g.y;
+}
+
+cudaError_t aos_bc(const AosArgs &a, int kind, int index, int along, const double *val1,
+                   const double *val2, cudaStream_t s) {
+    k_aos_bc<<<(along + 127) / 128, 128, 0, s>>>(a, kind, index, along, val1, val2);
+    return cudaGetLastError();
+}
+
+cudaError_t mei_init(const AosArgs &a, double rho0, cudaStream_t s) {
+    const dim3 b(64, 4);
+    k_mei_init<<<grid2(a.Nx, a.Ny, b), b, 0, s>>>(a, rho0);
+    return cudaGetLastError();
+}
+
+cudaError_t mei_iter(const AosArgs &a, double rho0, unsigned long long *maxbits, cudaStream_t s) {
+    const dim3 b(64, 4);
+    k_mei_iter<<<grid2(a.Nx, a.Ny, b), b, 0, s>>>(a, rho0, maxbits);
+    return cudaGetLastError();
+}
+
+}  // namespace launch
+}  // namespace lbm

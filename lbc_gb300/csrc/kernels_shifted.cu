@@ -1,0 +1,277 @@
+// kernels_shifted.cu -- fused step with populations stored as shifted deviations
+// g_k = f_k - w_k in FP32 or FP16 and the collision done in FP32.
+//
+// Same pull structure as the exact FP64 step (kernels_exact.cu): stream, halfway /
+// interpolated / moving-wall bounce-back, stale slots off non-periodic edges, MEM
+// force, moments, BGK + Guo collision. Storing g instead of f keeps the relative
+// precision of the small deviations from the rest state; FP64 is used only for the
+// force reduction and the band values handed to the edge BCs.
+#include <cmath>
+
+#include "kernels.h"
+#include "lbm_device.cuh"
+#include "reduce.cuh"
+
+namespace lbm {
+
+template <typename T> struct SV;
+template <> struct SV<float> {
+    static __device__ __forceinline__ float ld(const float *p) { return __ldg(p); }
+    static __device__ __forceinline__ float ld_plain(const float *p) { return *p; }
+    static __device__ __forceinline__ void st(float *p, float v) { *p = v; }
+};
+template <> struct SV<__half> {
+    static __device__ __forceinline__ float ld(const __half *p) { return __half2float(__ldg(p)); }
+    static __device__ __forceinline__ float ld_plain(const __half *p) { return __half2float(*p); }
+    static __device__ __forceinline__ void st(__half *p, float v) { *p = __float2half_rn(v); }
+};
+
+// Shifted moments: delta rho = sum g, j = sum c g (sum c w = 0).
+__device__ __forceinline__ void moments_shifted(const float g[9], float hFx, float hFy, float &dr,
+                                                float &rho, float &ux, float &uy) {
+    dr = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
+    const float jx = (g[1] - g[3]) + (g[5] - g[6]) + (g[8] - g[7]);
+    const float jy = (g[2] - g[4]) + (g[5] + g[6]) - (g[7] + g[8]);
+    rho = 1.0f + dr;
+    if (rho < 1e-16f) rho = 1e-16f;
+    const float inv = 1.0f / rho;
+    ux = (jx + hFx) * inv;
+    uy = (jy + hFy) * inv;
+}
+
+// BGK + Guo on shifted populations: g' = g + om (geq - g) + (1 - om/2) F_k with
+// geq_k = w_k (drho + rho (3 c.u + 4.5 (c.u)^2 - 1.5 u.u)).
+__device__ __forceinline__ void collide_shifted(float g[9], const float w[9], float dr, float rho,
+                                                float ux, float uy, float om, bool force,
+                                                float Fx, float Fy) {
+    const float t = 1.5f * (ux * ux + uy * uy);
+    float geq[9];
+    geq[0] = w[0] * (dr - rho * t);
+    {
+        const float c = ux, X = fmaf(rho, fmaf(4.5f * c, c, -t), dr), Y = rho * 3.0f * c;
+        geq[1] = w[1] * (X + Y); geq[3] = w[3] * (X - Y);
+    }
+    {
+        const float c = uy, X = fmaf(rho, fmaf(4.5f * c, c, -t), dr), Y = rho * 3.0f * c;
+        geq[2] = w[2] * (X + Y); geq[4] = w[4] * (X - Y);
+    }
+    {
+        const float c = ux + uy, X = fmaf(rho, fmaf(4.5f * c, c, -t), dr), Y = rho * 3.0f * c;
+        geq[5] = w[5] * (X + Y); geq[7] = w[7] * (X - Y);
+    }
+    {
+        const float c = uy - ux, X = fmaf(rho, fmaf(4.5f * c, c, -t), dr), Y = rho * 3.0f * c;
+        geq[6] = w[6] * (X + Y); geq[8] = w[8] * (X - Y);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) g[k] = fmaf(om, geq[k] - g[k], g[k]);
+    if (force) {
+        const float uF = ux * Fx + uy * Fy;
+        const float gf = 1.0f - 0.5f * om;
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const float cu = cxk(k) * ux + cyk(k) * uy;
+            const float cF = cxk(k) * Fx + cyk(k) * Fy;
+            g[k] = fmaf(gf, w[k] * (3.0f * cF + 9.0f * cu * cF - 3.0f * uF), g[k]);
+        }
+    }
+}
+
+template <typename T, bool FLAGS, bool COLLIDE>
+__global__ void __launch_bounds__(256) k_step_shifted(const FastStepParams fp) {
+    const StepParams &p = fp.s;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    double mfx = 0.0, mfy = 0.0;
+    if (i < p.Nx && j < p.Ny) {
+        const long long node = (long long)j * p.pitch + i;
+        const uint16_t fl = FLAGS ? p.flags[node] : (uint16_t)0;
+        const size_t dn = (size_t)j * (size_t)p.Nx + (size_t)i;
+        if (FLAGS && (fl & NF_SOLID)) {
+            if (p.write_macro) { p.rho[dn] = NAN; p.ux[dn] = NAN; p.uy[dn] = NAN; }
+            if (fl & NF_BAND) {
+                const int slot = band_slot(p.colbase, p.rowbase, i, j);
+                const T *Dst = (const T *)p.dst;
+#pragma unroll
+                for (int k = 0; k < 9; k++)
+                    p.bandf[(size_t)k * p.nslots + slot] = (double)SV<T>::ld_plain(Dst + k * p.plane + node) + p.w[k];
+                p.bandm_next[slot] = NAN;
+                p.bandm_next[(size_t)p.nslots + slot] = NAN;
+                p.bandm_next[2 * (size_t)p.nslots + slot] = NAN;
+            }
+        } else {
+            const T *S = (const T *)p.src;
+            T *Dst = (T *)p.dst;
+            const long long pl = p.plane;
+            int im = i - 1, ip = i + 1, jm = j - 1, jp = j + 1;
+            if (p.px) { if (im < 0) im += p.Nx; if (ip >= p.Nx) ip -= p.Nx; }
+            if (p.py) { if (jm < 0) jm += p.Ny; if (jp >= p.Ny) jp -= p.Ny; }
+            const long long r0 = (long long)j * p.pitch, rm = (long long)jm * p.pitch,
+                            rp = (long long)jp * p.pitch;
+            const long long so[9] = {r0 + i, r0 + im, rm + i, r0 + ip, rp + i,
+                                     rm + im, rm + ip, rp + ip, rp + im};
+            float g[9];
+            if (!FLAGS) {
+#pragma unroll
+                for (int k = 0; k < 9; k++) g[k] = SV<T>::ld(S + k * pl + so[k]);
+            } else {
+                const Link *lk = (fl & NF_LINKS) ? p.links + p.link_off[node] : nullptr;
+#pragma unroll
+                for (int k = 0; k < 9; k++) {
+                    if (!(fl & (1u << k))) {
+                        g[k] = SV<T>::ld(S + k * pl + so[k]);
+                        continue;
+                    }
+                    const int si = i - cxk(k), sj = j - cyk(k);
+                    const bool off = (!p.px && (si < 0 || si >= p.Nx)) ||
+                                     (!p.py && (sj < 0 || sj >= p.Ny));
+                    if (off) {
+                        g[k] = SV<T>::ld_plain(Dst + k * pl + node);
+                        continue;
+                    }
+                    const int ko = oppk(k);
+                    const float own = SV<T>::ld(S + ko * pl + node);
+                    float val = own;
+                    if (lk) {
+                        const Link L = *lk++;
+                        if (L.mode == LINK_IBB_LO)
+                            val = (float)L.c1 * own + (float)L.c2 * SV<T>::ld(S + ko * pl + L.behind);
+                        else if (L.mode == LINK_IBB_HI)
+                            val = (float)L.c1 * own + (float)L.c2 * SV<T>::ld(S + k * pl + L.behind);
+                        else if (L.mode == LINK_MOVING)
+                            val = own - (float)L.c2;
+                    }
+                    g[k] = val;
+                    const double df = (double)own + (double)val + 2.0 * p.w[k];
+                    mfx -= df * cxk(k);
+                    mfy -= df * cyk(k);
+                }
+            }
+            int slot = -1;
+            if (FLAGS && (fl & NF_BAND)) {
+                slot = band_slot(p.colbase, p.rowbase, i, j);
+#pragma unroll
+                for (int k = 0; k < 9; k++) p.bandf[(size_t)k * p.nslots + slot] = (double)g[k] + p.w[k];
+            }
+            if (!(FLAGS && (fl & NF_BCW))) {
+                float dr, rho, ux, uy;
+                moments_shifted(g, (float)p.hFx, (float)p.hFy, dr, rho, ux, uy);
+                if (p.write_macro) { p.rho[dn] = 1.0 + (double)dr; p.ux[dn] = ux; p.uy[dn] = uy; }
+                if (slot >= 0) {
+                    p.bandm_next[slot] = 1.0 + (double)dr;
+                    p.bandm_next[(size_t)p.nslots + slot] = ux;
+                    p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
+                }
+                if (COLLIDE) {
+                    const float om = p.omega ? (float)p.omega[dn] : fp.omega0f;
+                    collide_shifted(g, fp.wf, dr, rho, ux, uy, om, p.has_force != 0, fp.Fxf, fp.Fyf);
+                }
+#pragma unroll
+                for (int k = 0; k < 9; k++) SV<T>::st(Dst + k * pl + node, g[k]);
+            }
+        }
+    }
+    if (FLAGS && p.mem_partials) {
+        reduce2_grid(mfx, mfy, p.mem_partials, p.mem_ticket, p.mem_out, p.mem_hist,
+                     p.mem_hist_count, p.mem_hist_cap);
+    }
+}
+
+template <typename T, bool COLLIDE>
+__global__ void k_finish_shifted(const FinishParams p) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.nw) return;
+    const int2 ij = p.wnodes[t];
+    const int slot = band_slot(p.colbase, p.rowbase, ij.x, ij.y);
+    float g[9], wf[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        g[k] = (float)(p.bandf[(size_t)k * p.nslots + slot] - p.w[k]);
+        wf[k] = (float)p.w[k];
+    }
+    float dr, rho, ux, uy;
+    moments_shifted(g, (float)p.hFx, (float)p.hFy, dr, rho, ux, uy);
+    const size_t dn = (size_t)ij.y * p.Nx + ij.x;
+    if (p.write_macro) { p.rho[dn] = 1.0 + (double)dr; p.ux[dn] = ux; p.uy[dn] = uy; }
+    p.bandm_next[slot] = 1.0 + (double)dr;
+    p.bandm_next[(size_t)p.nslots + slot] = ux;
+    p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
+    if (COLLIDE) {
+        const float om = p.omega ? (float)p.omega[dn] : (float)p.omega0;
+        collide_shifted(g, wf, dr, rho, ux, uy, om, p.has_force != 0, (float)p.Fx, (float)p.Fy);
+    }
+    T *D = (T *)p.dst;
+    const long long node = (long long)ij.y * p.pitch + ij.x;
+#pragma unroll
+    for (int k = 0; k < 9; k++) SV<T>::st(D + k * p.plane + node, g[k]);
+}
+
+// In-place collision of shifted populations with the stored (FP64) rho/u/v:
+// the first step of a run (src/core/collision.c:18-40).
+template <typename T>
+__global__ void k_collide_shifted(const CollideParams p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= p.Nx || j >= p.Ny) return;
+    const long long node = (long long)j * p.pitch + i;
+    if (p.flags && (p.flags[node] & NF_SOLID)) return;
+    const size_t dn = (size_t)j * p.Nx + i;
+    T *F = (T *)p.f;
+    float g[9], wf[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) { g[k] = SV<T>::ld_plain(F + k * p.plane + node); wf[k] = (float)p.w[k]; }
+    const float rho = (float)p.rho[dn];
+    const float dr = (float)(p.rho[dn] - 1.0);
+    const float om = p.omega ? (float)p.omega[dn] : (float)p.omega0;
+    collide_shifted(g, wf, dr, rho, (float)p.ux[dn], (float)p.uy[dn], om, p.has_force != 0,
+                    (float)p.Fx, (float)p.Fy);
+#pragma unroll
+    for (int k = 0; k < 9; k++) SV<T>::st(F + k * p.plane + node, g[k]);
+}
+
+namespace launch {
+
+cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s) {
+    const dim3 b(64, 4);
+    const dim3 g((p.Nx + 63) / 64, (p.Ny + 3) / 4);
+    if (store == STORE_F32) k_collide_shifted<float><<<g, b, 0, s>>>(p);
+    else k_collide_shifted<__half><<<g, b, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+
+template <typename T>
+static void step_shifted_t(const FastStepParams &p, bool flags, bool collide, dim3 g, dim3 b,
+                           cudaStream_t s) {
+    if (flags) {
+        if (collide) k_step_shifted<T, true, true><<<g, b, 0, s>>>(p);
+        else k_step_shifted<T, true, false><<<g, b, 0, s>>>(p);
+    } else {
+        if (collide) k_step_shifted<T, false, true><<<g, b, 0, s>>>(p);
+        else k_step_shifted<T, false, false><<<g, b, 0, s>>>(p);
+    }
+}
+
+cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
+                         cudaStream_t s) {
+    const dim3 g((p.s.Nx + block.x - 1) / block.x, (p.s.Ny + block.y - 1) / block.y);
+    if (store == STORE_F32) step_shifted_t<float>(p, flags, collide, g, block, s);
+    else step_shifted_t<__half>(p, flags, collide, g, block, s);
+    return cudaGetLastError();
+}
+
+cudaError_t finish_shifted(const FinishParams &p, int store, bool collide, cudaStream_t s) {
+    if (p.nw == 0) return cudaSuccess;
+    const int b = 128, g = (p.nw + b - 1) / b;
+    if (store == STORE_F32) {
+        if (collide) k_finish_shifted<float, true><<<g, b, 0, s>>>(p);
+        else k_finish_shifted<float, false><<<g, b, 0, s>>>(p);
+    } else {
+        if (collide) k_finish_shifted<__half, true><<<g, b, 0, s>>>(p);
+        else k_finish_shifted<__half, false><<<g, b, 0, s>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace launch
+}  // namespace lbm

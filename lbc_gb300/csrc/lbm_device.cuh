@@ -1,0 +1,390 @@
+// lbm_device.cuh -- shared device-side definitions of the D2Q9 engine.
+//
+// Populations live on the device as structure-of-arrays planes: population k of
+// node (i, j) is at plane k, offset j * pitch + i. lbc's own ordering of the
+// velocity set is the canonical one (cases/nit/nit.c:195-202):
+//   c = (0,0) (1,0) (0,1) (-1,0) (0,-1) (1,1) (-1,1) (-1,-1) (1,-1), opp = 0 3 4 1 2 7 8 5 6.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+
+namespace lbm {
+
+constexpr int Q = 9;
+
+__host__ __device__ constexpr int cxk(int k) {
+    return k == 1 || k == 5 || k == 8 ? 1 : (k == 3 || k == 6 || k == 7 ? -1 : 0);
+}
+__host__ __device__ constexpr int cyk(int k) {
+    return k == 2 || k == 5 || k == 6 ? 1 : (k == 4 || k == 7 || k == 8 ? -1 : 0);
+}
+__host__ __device__ constexpr int oppk(int k) {
+    return k == 0 ? 0 : (k <= 4 ? ((k + 1) % 4) + 1 : ((k - 5 + 2) % 4) + 5);
+}
+static_assert(oppk(1) == 3 && oppk(2) == 4 && oppk(3) == 1 && oppk(4) == 2, "opp");
+static_assert(oppk(5) == 7 && oppk(6) == 8 && oppk(7) == 5 && oppk(8) == 6, "opp");
+
+// Per-node flag word (uint16), built once per geometry on the host.
+enum : uint16_t {
+    NF_SPECIAL_MASK = 0x01FF,  // bit k: the pull source x - c_k is solid or off a non-periodic edge
+    NF_SOLID = 1u << 9,        // node is solid (never written)
+    NF_BAND = 1u << 10,        // node's pre-collision populations feed the edge-BC pipeline
+    NF_BCW = 1u << 11,         // node is written by an edge BC (collided by the finish kernel)
+    NF_LINKS = 1u << 12,       // node owns entries in the cut-link table (IBB / moving wall)
+};
+
+// One wall link entry, in the order of the node's special solid sources.
+enum : uint8_t { LINK_BB = 0, LINK_IBB_LO = 1, LINK_IBB_HI = 2, LINK_MOVING = 3 };
+struct Link {
+    double c1, c2;   // interpolation weights (IBB) or wall term (moving wall: c2)
+    int64_t behind;  // plane offset of the behind node x + c_k' (IBB), else -1
+    uint8_t mode;
+    uint8_t k;       // pulled population
+    uint8_t pad[6];
+};
+static_assert(sizeof(Link) == 32, "Link layout");
+
+// Edge-BC kinds (lbc's 18 BC functions that act on populations).
+enum BCKind : int {
+    BC_VEL_IN_ZH = 0, BC_VEL_OUT_ZH, BC_VEL_TOP_ZH, BC_VEL_BOT_ZH,
+    BC_PRES_IN_ZH, BC_PRES_OUT_ZH,
+    BC_CONV_IN, BC_CONV_OUT,
+    BC_PERIODIC_X, BC_PERIODIC_Y,
+    BC_VEL_IN_REG, BC_VEL_OUT_REG, BC_VEL_TOP_REG, BC_VEL_BOT_REG,
+    BC_PRES_IN_REG, BC_PRES_OUT_REG, BC_PRES_TOP_REG, BC_PRES_BOT_REG,
+    BC_KIND_COUNT
+};
+
+__host__ __device__ inline bool bc_is_column(int kind) {
+    return kind == BC_VEL_IN_ZH || kind == BC_VEL_OUT_ZH || kind == BC_PRES_IN_ZH ||
+           kind == BC_PRES_OUT_ZH || kind == BC_CONV_IN || kind == BC_CONV_OUT ||
+           kind == BC_VEL_IN_REG || kind == BC_VEL_OUT_REG || kind == BC_PRES_IN_REG ||
+           kind == BC_PRES_OUT_REG;
+}
+
+// Storage policies: FP64 stores f as is; FP32/FP16 store the shifted deviation
+// g_k = f_k - w_k.
+template <typename T> struct Store;
+template <> struct Store<double> {
+    static __device__ __forceinline__ double to_f64(double s, double) { return s; }
+    static __device__ __forceinline__ double from_f64(double f, double) { return f; }
+};
+template <> struct Store<float> {
+    static __device__ __forceinline__ double to_f64(float s, double w) { return (double)s + w; }
+    static __device__ __forceinline__ float from_f64(double f, double w) { return (float)(f - w); }
+};
+template <> struct Store<__half> {
+    static __device__ __forceinline__ double to_f64(__half s, double w) { return (double)__half2float(s) + w; }
+    static __device__ __forceinline__ __half from_f64(double f, double w) { return __float2half_rn((float)(f - w)); }
+};
+
+// ---------------------------------------------------------------------------
+// Exact FP64 arithmetic in lbc's operation order. The translation units that use
+// these are compiled with --fmad=false, so no multiply-add is contracted.
+
+// Moments of one node, src/core/compute_macroscopic_fields.c:23-41. The k-ordered
+// sums with integer velocities reduce to these add chains (x + (+-0) == x).
+__device__ __forceinline__ void moments_exact(const double f[9], double hFx, double hFy,
+                                              double &rho, double &ux, double &uy) {
+    double s = ((((((((f[0] + f[1]) + f[2]) + f[3]) + f[4]) + f[5]) + f[6]) + f[7]) + f[8]);
+    double sx = ((((f[1] - f[3]) + f[5]) - f[6]) - f[7]) + f[8];
+    double sy = ((((f[2] - f[4]) + f[5]) + f[6]) - f[7]) - f[8];
+    if (s < 1e-16) s = 1e-16;
+    rho = s;
+    ux = (sx + hFx) / s;
+    uy = (sy + hFy) / s;
+}
+
+// f_eq for the nine directions in the order of src/core/collision.c:31-32.
+__device__ __forceinline__ void feq_exact(const double w[9], double rho, double ux, double uy,
+                                          double feq[9]) {
+    const double usq = ux * ux + uy * uy;
+    const double t = 1.5 * usq;
+    const double wr0 = w[0] * rho, wr1 = w[1] * rho, wr2 = w[2] * rho, wr3 = w[3] * rho,
+                 wr4 = w[4] * rho, wr5 = w[5] * rho, wr6 = w[6] * rho, wr7 = w[7] * rho,
+                 wr8 = w[8] * rho;
+    feq[0] = wr0 * (1.0 - t);
+    {
+        const double c = ux, B = 3.0 * c, A = (4.5 * c) * c;
+        feq[1] = wr1 * (((1.0 + B) + A) - t);
+        feq[3] = wr3 * (((1.0 - B) + A) - t);
+    }
+    {
+        const double c = uy, B = 3.0 * c, A = (4.5 * c) * c;
+        feq[2] = wr2 * (((1.0 + B) + A) - t);
+        feq[4] = wr4 * (((1.0 - B) + A) - t);
+    }
+    {
+        const double c = ux + uy, B = 3.0 * c, A = (4.5 * c) * c;
+        feq[5] = wr5 * (((1.0 + B) + A) - t);
+        feq[7] = wr7 * (((1.0 - B) + A) - t);
+    }
+    {
+        const double c = uy - ux, B = 3.0 * c, A = (4.5 * c) * c;
+        feq[6] = wr6 * (((1.0 + B) + A) - t);
+        feq[8] = wr8 * (((1.0 - B) + A) - t);
+    }
+}
+
+// BGK + Guo forcing in place, src/core/collision.c:24-38.
+__device__ __forceinline__ void collide_exact(double f[9], const double w[9], double rho, double ux,
+                                              double uy, double om, bool force, double Fx,
+                                              double Fy) {
+    double feq[9];
+    feq_exact(w, rho, ux, uy, feq);
+    if (!force) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) f[k] = f[k] + (-om * (f[k] - feq[k]));
+        return;
+    }
+    const double uF = ux * Fx + uy * Fy;
+    const double g = 1 - 0.5 * om;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const int cx = cxk(k), cy = cyk(k);
+        const double cu = cx * ux + cy * uy;
+        const double cF = cx * Fx + cy * Fy;
+        const double Fk = w[k] * (3.0 * cF + 9.0 * cu * cF - 3.0 * uF);
+        f[k] = f[k] + (-om * (f[k] - feq[k]) + g * Fk);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Edge BCs, generic over an accessor that reads/writes the current f_new of a
+// node, the previous-step moments and (periodic only) the post-collision f.
+// Accessor interface:
+//   double get(int i, int j, int k); void set(int i, int j, int k, double v);
+//   double rho(int i, int j), ux(...), uy(...);          previous-step fields
+//   double post(int i, int j, int k);                    post-collision f
+//   bool solid(int i, int j);
+
+// Regularized node update shared by the eight *_regularized files
+// (src/bc/velocity_inlet_regularized.c:26-70).
+template <class A>
+__device__ __forceinline__ void bc_regularized(A &a, const double w[9], int ib, int jb, int in,
+                                               int jn, bool pressure, double val1, double val2) {
+    const double rho_n = a.rho(in, jn), u_n = a.ux(in, jn), v_n = a.uy(in, jn);
+    double rho_b, U, V;
+    if (pressure) {
+        rho_b = val1; U = u_n; V = v_n;
+    } else {
+        rho_b = rho_n; U = val1; V = val2;
+    }
+    double feq[9];
+    feq_exact(w, rho_n, u_n, v_n, feq);
+    double fneq[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) fneq[k] = a.get(in, jn, k) - feq[k];
+    // Pi sums in k order; terms with a zero coefficient add +-0 (no effect).
+    const double Pxx = ((((fneq[1] + fneq[3]) + fneq[5]) + fneq[6]) + fneq[7]) + fneq[8];
+    const double Pxy = ((fneq[5] - fneq[6]) + fneq[7]) - fneq[8];
+    const double Pyy = ((((fneq[2] + fneq[4]) + fneq[5]) + fneq[6]) + fneq[7]) + fneq[8];
+    double fb[9];
+    feq_exact(w, rho_b, U, V, fb);
+    const double third = 1.0 / 3.0;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const int cx = cxk(k), cy = cyk(k);
+        const double Qxx = cx * cx - third;
+        const double Qxy = cx * cy;
+        const double Qyy = cy * cy - third;
+        const double fr = (3.0 / 2.0) * w[k] * (Qxx * Pxx + 2.0 * Qxy * Pxy + Qyy * Pyy);
+        a.set(ib, jb, k, fb[k] + fr);
+    }
+}
+
+template <class A>
+__device__ __forceinline__ void bc_apply(A &a, const double w[9], int kind, int Nx, int Ny,
+                                         int index, int t, const double *val1,
+                                         const double *val2) {
+    const bool col = bc_is_column(kind);
+    int ib, jb;
+    if (kind == BC_PERIODIC_X || kind == BC_PERIODIC_Y) {
+        // src/bc/periodic_x.c:19-50 / periodic_y.c:19-50: t enumerates the two
+        // edge lines (t < along: first edge, else second edge).
+        if (kind == BC_PERIODIC_X) {
+            const int j = t % Ny;
+            const bool left = t < Ny;
+            const int i = left ? 0 : Nx - 1;
+            if (a.solid(i, j)) return;
+#pragma unroll
+            for (int k = 1; k < 9; k++) {
+                const int cx = cxk(k);
+                if (left ? cx <= 0 : cx >= 0) continue;
+                const int is = left ? Nx - cx : -cx - 1;
+                const int js = j - cyk(k);
+                if (js < 0 || js >= Ny) continue;
+                if (a.solid(is, js)) continue;
+                a.set(i, j, k, a.post(is, js, k));
+            }
+        } else {
+            const int i = t % Nx;
+            const bool bottom = t < Nx;
+            const int j = bottom ? 0 : Ny - 1;
+            if (a.solid(i, j)) return;
+#pragma unroll
+            for (int k = 1; k < 9; k++) {
+                const int cy = cyk(k);
+                if (bottom ? cy <= 0 : cy >= 0) continue;
+                const int js = bottom ? Ny - cy : -cy - 1;
+                const int is = i - cxk(k);
+                if (is < 0 || is >= Nx) continue;
+                if (a.solid(is, js)) continue;
+                a.set(i, j, k, a.post(is, js, k));
+            }
+        }
+        return;
+    }
+    if (col) { ib = index; jb = t; } else { ib = t; jb = index; }
+    if (a.solid(ib, jb)) return;
+    switch (kind) {
+    case BC_VEL_IN_ZH: {  // src/bc/velocity_inlet.c:25-39
+        const double U = val1[t], V = val2[t];
+        const double f0 = a.get(ib, jb, 0), f2 = a.get(ib, jb, 2), f3 = a.get(ib, jb, 3),
+                     f4 = a.get(ib, jb, 4), f6 = a.get(ib, jb, 6), f7 = a.get(ib, jb, 7);
+        const double r = (f0 + f2 + f4 + 2.0 * (f3 + f6 + f7)) / (1.0 - U);
+        a.set(ib, jb, 1, f3 + (2.0 / 3.0) * r * U);
+        a.set(ib, jb, 5, f7 + (1.0 / 6.0) * r * U - 0.5 * (f2 - f4) + (1.0 / 2.0) * r * V);
+        a.set(ib, jb, 8, f6 + (1.0 / 6.0) * r * U + 0.5 * (f2 - f4) - (1.0 / 2.0) * r * V);
+    } break;
+    case BC_VEL_OUT_ZH: {  // src/bc/velocity_outlet.c:25-39
+        const double U = val1[t], V = val2[t];
+        const double f0 = a.get(ib, jb, 0), f2 = a.get(ib, jb, 2), f4 = a.get(ib, jb, 4),
+                     f1 = a.get(ib, jb, 1), f5 = a.get(ib, jb, 5), f8 = a.get(ib, jb, 8);
+        const double r = (f0 + f2 + f4 + 2.0 * (f1 + f5 + f8)) / (1.0 + U);
+        a.set(ib, jb, 3, f1 - (2.0 / 3.0) * r * U);
+        a.set(ib, jb, 6, f8 - 0.5 * (f2 - f4) - (1.0 / 6.0) * r * U + (1.0 / 2.0) * r * V);
+        a.set(ib, jb, 7, f5 + 0.5 * (f2 - f4) - (1.0 / 6.0) * r * U - (1.0 / 2.0) * r * V);
+    } break;
+    case BC_VEL_TOP_ZH: {  // src/bc/velocity_top.c:25-39
+        const double U = val1[t], V = val2[t];
+        const double f0 = a.get(ib, jb, 0), f1 = a.get(ib, jb, 1), f2 = a.get(ib, jb, 2),
+                     f3 = a.get(ib, jb, 3), f5 = a.get(ib, jb, 5), f6 = a.get(ib, jb, 6);
+        const double r = (f0 + f1 + f3 + 2 * (f2 + f5 + f6)) / (1 + V);
+        a.set(ib, jb, 4, f2 - 2.0 / 3.0 * r * V);
+        a.set(ib, jb, 7, f5 + (f1 - f3) / 2.0 - 0.5 * r * U - 1.0 / 6.0 * r * V);
+        a.set(ib, jb, 8, f6 - (f1 - f3) / 2.0 + 0.5 * r * U - 1.0 / 6.0 * r * V);
+    } break;
+    case BC_VEL_BOT_ZH: {  // src/bc/velocity_bottom.c:25-39 (second write to 7 kept, :39)
+        const double U = val1[t], V = val2[t];
+        const double f0 = a.get(ib, jb, 0), f1 = a.get(ib, jb, 1), f3 = a.get(ib, jb, 3),
+                     f4 = a.get(ib, jb, 4), f7 = a.get(ib, jb, 7), f8 = a.get(ib, jb, 8);
+        const double r = (f0 + f1 + f3 + 2 * (f4 + f7 + f8)) / (1 - V);
+        a.set(ib, jb, 2, f4 + 2.0 / 3.0 * r * V);
+        a.set(ib, jb, 5, f7 - (f1 - f3) / 2.0 + 0.5 * r * U + 1.0 / 6.0 * r * V);
+        a.set(ib, jb, 7, f8 + (f1 - f3) / 2.0 - 0.5 * r * U + 1.0 / 6.0 * r * V);
+    } break;
+    case BC_PRES_IN_ZH: {  // src/bc/pressure_inlet.c:25-39
+        const double R = val1[t];
+        const double f0 = a.get(ib, jb, 0), f2 = a.get(ib, jb, 2), f4 = a.get(ib, jb, 4),
+                     f3 = a.get(ib, jb, 3), f6 = a.get(ib, jb, 6), f7 = a.get(ib, jb, 7);
+        const double U = 1.0 - (f0 + f2 + f4 + 2.0 * (f3 + f6 + f7)) / R;
+        const double V = a.uy(ib + 1, jb);
+        a.set(ib, jb, 1, f3 + (2.0 / 3.0) * R * U);
+        a.set(ib, jb, 5, f7 + (1.0 / 6.0) * R * U - 0.5 * (f2 - f4) + (1.0 / 2.0) * R * V);
+        a.set(ib, jb, 8, f6 + (1.0 / 6.0) * R * U + 0.5 * (f2 - f4) - (1.0 / 2.0) * R * V);
+    } break;
+    case BC_PRES_OUT_ZH: {  // src/bc/pressure_outlet.c:25-39
+        const double R = val1[t];
+        const double f0 = a.get(ib, jb, 0), f2 = a.get(ib, jb, 2), f4 = a.get(ib, jb, 4),
+                     f1 = a.get(ib, jb, 1), f5 = a.get(ib, jb, 5), f8 = a.get(ib, jb, 8);
+        const double U = (f0 + f2 + f4 + 2.0 * (f1 + f5 + f8)) / R - 1.0;
+        const double V = a.uy(ib - 1, jb);
+        a.set(ib, jb, 3, f1 - (2.0 / 3.0) * R * U);
+        a.set(ib, jb, 6, f8 - 0.5 * (f2 - f4) - (1.0 / 6.0) * R * U + (1.0 / 2.0) * R * V);
+        a.set(ib, jb, 7, f5 + 0.5 * (f2 - f4) - (1.0 / 6.0) * R * U - (1.0 / 2.0) * R * V);
+    } break;
+    case BC_CONV_IN:  // src/bc/convective_inlet.c:20-28
+#pragma unroll
+        for (int k = 0; k < 9; k++) a.set(ib, jb, k, a.get(ib + 1, jb, k));
+        break;
+    case BC_CONV_OUT:  // src/bc/convective_outlet.c:20-28
+#pragma unroll
+        for (int k = 0; k < 9; k++) a.set(ib, jb, k, a.get(ib - 1, jb, k));
+        break;
+    case BC_VEL_IN_REG: bc_regularized(a, w, ib, jb, ib + 1, jb, false, val1[t], val2[t]); break;
+    case BC_VEL_OUT_REG: bc_regularized(a, w, ib, jb, ib - 1, jb, false, val1[t], val2[t]); break;
+    case BC_VEL_BOT_REG: bc_regularized(a, w, ib, jb, ib, jb + 1, false, val1[t], val2[t]); break;
+    case BC_VEL_TOP_REG: bc_regularized(a, w, ib, jb, ib, jb - 1, false, val1[t], val2[t]); break;
+    case BC_PRES_IN_REG: bc_regularized(a, w, ib, jb, ib + 1, jb, true, val1[t], 0.0); break;
+    case BC_PRES_OUT_REG: bc_regularized(a, w, ib, jb, ib - 1, jb, true, val1[t], 0.0); break;
+    case BC_PRES_BOT_REG: bc_regularized(a, w, ib, jb, ib, jb + 1, true, val1[t], 0.0); break;
+    case BC_PRES_TOP_REG: bc_regularized(a, w, ib, jb, ib, jb - 1, true, val1[t], 0.0); break;
+    default: break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Kernel parameter blocks (plain structs, passed by value).
+
+struct StepParams {
+    int Nx, Ny, pitch;
+    int px, py;
+    long long plane;          // pitch * Ny
+    const void *src;          // post-collision populations of step n (planes)
+    void *dst;                // output populations (also holds the stale slots)
+    const uint16_t *flags;    // [Ny * pitch] or null (fully periodic, no solids, no BCs)
+    const int *link_off;      // [Ny * pitch]
+    const Link *links;
+    const double *omega;      // [Ny * Nx] per-node omega, or null -> omega0
+    double omega0;
+    int has_force;
+    double Fx, Fy, hFx, hFy;  // hF = 0.5 F
+    double w[9];
+    // macroscopic output, dense [Ny * Nx]
+    int write_macro;
+    double *rho, *ux, *uy;
+    // edge-BC band
+    const int *colbase, *rowbase;
+    int nslots;
+    double *bandf;            // [9][nslots], pre-collision f_new of band nodes
+    double *bandm_next;       // [3][nslots], their moments (for the next step's BCs)
+    // momentum-exchange force (null when the geometry has no wall links)
+    double *mem_partials;     // [2 * gridDim.x * gridDim.y]
+    unsigned int *mem_ticket;
+    double *mem_out;          // [2]: Fx, Fy of this step
+    double *mem_hist;         // optional per-step ring [2 * mem_hist_cap]
+    unsigned long long *mem_hist_count;
+    int mem_hist_cap;
+};
+
+struct StageParams {
+    int Nx, Ny, pitch;
+    long long plane;
+    int kind, index, along;
+    const double *val1, *val2;
+    const uint16_t *flags;
+    const int *colbase, *rowbase;
+    int nslots;
+    double *bandf;
+    const double *bandm_prev;  // [3][nslots]
+    const void *src;           // post-collision populations (periodic stages)
+    double w[9];
+};
+
+struct FinishParams {
+    int Nx, Ny, pitch;
+    long long plane;
+    int nw;                    // number of BC-written nodes
+    const int2 *wnodes;        // (i, j) of every BC-written node
+    const int *colbase, *rowbase;
+    int nslots;
+    const double *bandf;
+    double *bandm_next;
+    void *dst;
+    const double *omega;
+    double omega0;
+    int has_force;
+    double Fx, Fy, hFx, hFy;
+    double w[9];
+    int write_macro;
+    double *rho, *ux, *uy;
+};
+
+__device__ __forceinline__ int band_slot(const int *colbase, const int *rowbase, int i, int j) {
+    const int c = colbase[i];
+    return c >= 0 ? c + j : rowbase[j] + i;
+}
+
+}  // namespace lbm

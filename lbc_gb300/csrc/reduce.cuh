@@ -1,0 +1,70 @@
+// reduce.cuh -- deterministic grid-wide reduction shared by the step kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace lbm {
+
+// Deterministic block + grid reduction of two doubles. Every thread of every
+// block must call it. Blocks write partials; the last block to arrive sums them
+// in block order and writes out[0..1] (and, when a history ring is given, the
+// next ring slot), then rearms the ticket.
+__device__ __forceinline__ void reduce2_grid(double a, double b, double *partials, unsigned int *ticket,
+                                             double *out, double *hist = nullptr,
+                                             unsigned long long *hist_count = nullptr,
+                                             int hist_cap = 0) {
+    __shared__ double sa[32], sb[32];
+    __shared__ bool last;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nthr = blockDim.x * blockDim.y;
+    const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) { sa[warp] = a; sb[warp] = b; }
+    __syncthreads();
+    const int nblk = gridDim.x * gridDim.y;
+    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
+    if (tid == 0) {
+        double ta = 0.0, tb = 0.0;
+        for (int w = 0; w < (nthr + 31) / 32; w++) { ta += sa[w]; tb += sb[w]; }
+        partials[2 * bid] = ta;
+        partials[2 * bid + 1] = tb;
+        __threadfence();
+        const unsigned int t = atomicAdd(ticket, 1u);
+        last = (t == (unsigned int)nblk - 1u);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double ta = 0.0, tb = 0.0;
+    for (int q = tid; q < nblk; q += nthr) {
+        ta += __ldcg(partials + 2 * q);
+        tb += __ldcg(partials + 2 * q + 1);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ta += __shfl_down_sync(0xffffffffu, ta, o);
+        tb += __shfl_down_sync(0xffffffffu, tb, o);
+    }
+    __syncthreads();
+    if (lane == 0) { sa[warp] = ta; sb[warp] = tb; }
+    __syncthreads();
+    if (tid == 0) {
+        double ra = 0.0, rb = 0.0;
+        for (int w = 0; w < (nthr + 31) / 32; w++) { ra += sa[w]; rb += sb[w]; }
+        out[0] = ra;
+        out[1] = rb;
+        if (hist) {
+            const unsigned long long c = *hist_count;
+            const int slot = (int)(c % (unsigned long long)hist_cap);
+            hist[2 * slot] = ra;
+            hist[2 * slot + 1] = rb;
+            *hist_count = c + 1ull;
+        }
+        *ticket = 0u;
+    }
+}
+
+}  // namespace lbm

@@ -1,0 +1,223 @@
+"""Python bindings of liblbm_gpu.so (lbc's C API plus the extended lbm_gpu_* API).
+
+The library is the product: every call here goes through its C ABI. There is
+no CPU path; loading fails loudly when the shared library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from .abi import Boundary, LbcAbi, dptr, iptr
+from .cases import Case, State, Q
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liblbm_gpu.so")
+
+F64, F32_SHIFTED, F16_SHIFTED = 0, 1, 2
+STORAGE = {"f64": F64, "f32": F32_SHIFTED, "f16": F16_SHIFTED}
+BYTES_PER_POP = {F64: 8, F32_SHIFTED: 4, F16_SHIFTED: 2}
+
+_lib: Optional[C.CDLL] = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load liblbm_gpu.so (built by lbc_gb300.build). Raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -m lbc_gb300.build` "
+                           "(or __graft_entry__.build())")
+    lib = C.CDLL(path)
+    _bind_ext(lib)
+    _lib = lib
+    return lib
+
+
+class CaseDesc(C.Structure):
+    """lbm_gpu_case (include/lbm_gpu.h)."""
+    _fields_ = [
+        ("Nx", C.c_int), ("Ny", C.c_int),
+        ("cx", C.POINTER(C.c_int)), ("cy", C.POINTER(C.c_int)), ("opp", C.POINTER(C.c_int)),
+        ("w", C.POINTER(C.c_double)),
+        ("omega_eff", C.POINTER(C.c_double)), ("solid_mask", C.POINTER(C.c_int)),
+        ("phi", C.POINTER(C.c_double)), ("use_IBB", C.c_int),
+        ("boundaries", C.c_void_p), ("num_boundaries", C.c_int),
+        ("isperiodic_x", C.c_int), ("isperiodic_y", C.c_int),
+        ("Fx", C.c_double), ("Fy", C.c_double),
+        ("wall_u", C.POINTER(C.c_double)), ("wall_v", C.POINTER(C.c_double)),
+        ("storage", C.c_int),
+    ]
+
+
+class Info(C.Structure):
+    """lbm_gpu_info (include/lbm_gpu.h)."""
+    _fields_ = [("Nx", C.c_int), ("Ny", C.c_int), ("pitch", C.c_int), ("storage", C.c_int),
+                ("has_geometry", C.c_int), ("edge_stages", C.c_int),
+                ("launches_per_step", C.c_int), ("device_bytes", C.c_size_t),
+                ("steps_done", C.c_longlong)]
+
+
+def _bind_ext(lib: C.CDLL) -> None:
+    vp, dp = C.c_void_p, C.POINTER(C.c_double)
+    sig = {
+        "lbm_gpu_last_error": (C.c_char_p, []),
+        "lbm_gpu_device_count": (C.c_int, []),
+        "lbm_gpu_create": (C.c_int, [C.POINTER(CaseDesc), C.POINTER(vp)]),
+        "lbm_gpu_destroy": (C.c_int, [vp]),
+        "lbm_gpu_set_state": (C.c_int, [vp, dp, dp, dp, dp, dp]),
+        "lbm_gpu_get_state": (C.c_int, [vp, dp, dp, dp, dp, dp]),
+        "lbm_gpu_get_fields": (C.c_int, [vp, dp, dp, dp]),
+        "lbm_gpu_set_bc_values": (C.c_int, [vp, C.c_int, dp, dp]),
+        "lbm_gpu_run": (C.c_int, [vp, C.c_int]),
+        "lbm_gpu_run_timed": (C.c_int, [vp, C.c_int, dp]),
+        "lbm_gpu_sync": (C.c_int, [vp]),
+        "lbm_gpu_forces": (C.c_int, [vp, dp, dp]),
+        "lbm_gpu_enable_force_history": (C.c_int, [vp, C.c_int]),
+        "lbm_gpu_force_history": (C.c_int, [vp, dp, C.c_int]),
+        "lbm_gpu_get_info": (C.c_int, [vp, C.POINTER(Info)]),
+        "lbm_gpu_set_block": (C.c_int, [vp, C.c_int, C.c_int]),
+        "lbm_gpu_host_alloc": (vp, [C.c_size_t]),
+        "lbm_gpu_host_free": (None, [vp]),
+        "lbm_gpu_dropin_release": (None, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def last_error() -> str:
+    return load_library().lbm_gpu_last_error().decode()
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise RuntimeError(f"{what} failed ({rc}): {last_error()}")
+
+
+def dropin() -> LbcAbi:
+    """lbc's own API (main_lbm, collision, BCs, ...) as exported by the GPU library."""
+    return LbcAbi(load_library())
+
+
+class PinnedArray:
+    """A numpy array over page-locked host memory (lbm_gpu_host_alloc)."""
+
+    def __init__(self, shape, dtype=np.float64):
+        lib = load_library()
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self._p = lib.lbm_gpu_host_alloc(max(n, 1))
+        if not self._p:
+            raise RuntimeError("lbm_gpu_host_alloc failed: " + last_error())
+        buf = (C.c_char * n).from_address(self._p)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def __del__(self):
+        if getattr(self, "_p", None):
+            load_library().lbm_gpu_host_free(self._p)
+            self._p = None
+
+
+class GpuSolver:
+    """A case resident on the GPU (lbm_gpu_create / run / get_state)."""
+
+    def __init__(self, case: Case, storage: int = F64):
+        self.lib = load_library()
+        self.case = case
+        self.storage = storage
+        self._abi = LbcAbi(self.lib)
+        self._bnd = self._abi.boundaries(case.bcs)
+        self._keep = [case.cx, case.cy, case.opp, case.w, case.omega_eff, case.solid_mask, case.phi]
+        d = CaseDesc()
+        d.Nx, d.Ny = case.Nx, case.Ny
+        d.cx, d.cy, d.opp = iptr(case.cx), iptr(case.cy), iptr(case.opp)
+        d.w = dptr(case.w)
+        d.omega_eff = dptr(case.omega_eff)
+        d.solid_mask = iptr(case.solid_mask)
+        d.phi = dptr(case.phi)
+        d.use_IBB = case.use_IBB
+        d.boundaries = C.cast(self._bnd[0], C.c_void_p)
+        d.num_boundaries = len(case.bcs)
+        d.isperiodic_x, d.isperiodic_y = case.isperiodic_x, case.isperiodic_y
+        d.Fx, d.Fy = case.Fx, case.Fy
+        if case.wall_u is not None:
+            wu = np.ascontiguousarray(case.wall_u, dtype=np.float64)
+            wv = np.ascontiguousarray(case.wall_v if case.wall_v is not None else np.zeros_like(wu))
+            self._keep += [wu, wv]
+            d.wall_u, d.wall_v = dptr(wu), dptr(wv)
+        d.storage = storage
+        h = C.c_void_p()
+        _check(self.lib.lbm_gpu_create(C.byref(d), C.byref(h)), "lbm_gpu_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.lbm_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_state(self, st: State):
+        _check(self.lib.lbm_gpu_set_state(self.h, dptr(st.f), dptr(st.f_new), dptr(st.rho),
+                                          dptr(st.u), dptr(st.v)), "lbm_gpu_set_state")
+
+    def get_state(self) -> State:
+        Ny, Nx = self.case.Ny, self.case.Nx
+        st = State(np.empty((Ny, Nx, Q)), np.empty((Ny, Nx, Q)), np.empty((Ny, Nx)),
+                   np.empty((Ny, Nx)), np.empty((Ny, Nx)))
+        _check(self.lib.lbm_gpu_get_state(self.h, dptr(st.f), dptr(st.f_new), dptr(st.rho),
+                                          dptr(st.u), dptr(st.v)), "lbm_gpu_get_state")
+        return st
+
+    def get_fields(self):
+        Ny, Nx = self.case.Ny, self.case.Nx
+        rho, u, v = np.empty((Ny, Nx)), np.empty((Ny, Nx)), np.empty((Ny, Nx))
+        _check(self.lib.lbm_gpu_get_fields(self.h, dptr(rho), dptr(u), dptr(v)), "lbm_gpu_get_fields")
+        return rho, u, v
+
+    def set_bc_values(self, entry: int, val1=None, val2=None):
+        a1 = None if val1 is None else np.ascontiguousarray(val1, dtype=np.float64)
+        a2 = None if val2 is None else np.ascontiguousarray(val2, dtype=np.float64)
+        _check(self.lib.lbm_gpu_set_bc_values(self.h, entry, dptr(a1) if a1 is not None else None,
+                                              dptr(a2) if a2 is not None else None),
+               "lbm_gpu_set_bc_values")
+
+    def run(self, nsteps: int):
+        _check(self.lib.lbm_gpu_run(self.h, nsteps), "lbm_gpu_run")
+
+    def run_timed(self, nsteps: int) -> float:
+        ms = C.c_double(0.0)
+        _check(self.lib.lbm_gpu_run_timed(self.h, nsteps, C.byref(ms)), "lbm_gpu_run_timed")
+        return ms.value
+
+    def sync(self):
+        _check(self.lib.lbm_gpu_sync(self.h), "lbm_gpu_sync")
+
+    def forces(self):
+        L, D = C.c_double(), C.c_double()
+        _check(self.lib.lbm_gpu_forces(self.h, C.byref(L), C.byref(D)), "lbm_gpu_forces")
+        return L.value, D.value
+
+    def enable_force_history(self, capacity: int):
+        _check(self.lib.lbm_gpu_enable_force_history(self.h, capacity), "lbm_gpu_enable_force_history")
+
+    def force_history(self, max_steps: int) -> np.ndarray:
+        out = np.empty((max_steps, 2))
+        n = self.lib.lbm_gpu_force_history(self.h, dptr(out), max_steps)
+        if n < 0:
+            raise RuntimeError(last_error())
+        return out[:n]
+
+    def info(self) -> Info:
+        inf = Info()
+        _check(self.lib.lbm_gpu_get_info(self.h, C.byref(inf)), "lbm_gpu_get_info")
+        return inf
+
+    def set_block(self, bx: int, by: int):
+        _check(self.lib.lbm_gpu_set_block(self.h, bx, by), "lbm_gpu_set_block")

@@ -1,0 +1,207 @@
+"""GPU parity: the CUDA engine (through its C ABI) against the oracle and
+against fixtures made by lbc itself. FP64 storage must match bit for bit
+(NaN at solids and signed zeros aside); forces, which lbc sums with OpenMP
+atomics in no fixed order, to 1e-12 relative."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+import casezoo
+from conftest import GOLDEN, maxrel, same
+from lbc_gb300 import cases
+from lbc_gb300.abi import dptr, iptr
+from lbc_gb300.cases import Q
+
+pytestmark = pytest.mark.gpu
+NAMES = [n for n, _, _ in casezoo.standard_cases()]
+FIELDS = ("f", "f_new", "rho", "u", "v")
+
+
+def force_close(a, b, rtol=1e-12):
+    a, b = np.asarray(a), np.asarray(b)
+    scale = max(float(np.max(np.abs(b))) if b.size else 0.0, 1e-300)
+    return float(np.max(np.abs(a - b))) <= rtol * scale if b.size else True
+
+
+def fixture(name):
+    return np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_dropin_main_lbm_matches_lbc(gpu, oracle, name):
+    """lbc's main_lbm, called step by step with host arrays, as a case main does."""
+    (case, st), steps = casezoo.build(name)
+    st_o = st.copy()
+    fg = gpu.run(case, st, steps, record_forces=True)
+    fo = oracle.run(case, st_o, steps, record_forces=True)
+    g = fixture(name)
+    for fld in FIELDS:
+        assert same(getattr(st, fld), getattr(st_o, fld)), (name, fld, maxrel(getattr(st, fld), getattr(st_o, fld)))
+        assert same(getattr(st, fld), g[fld]), (name, fld)
+    assert force_close(fg, fo) and force_close(fg, g["forces"]), name
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_resident_run_matches_lbc(oracle, name):
+    """lbm_gpu_run(n): n steps on the device (graph-captured loop) leave what n
+    main_lbm calls leave."""
+    from lbc_gb300 import F64, GpuSolver
+    (case, st), steps = casezoo.build(name)
+    s = GpuSolver(case, F64)
+    hist = s.info().has_geometry
+    try:
+        s.enable_force_history(steps)
+    except RuntimeError:
+        hist = False
+    s.set_state(st)
+    s.run(steps)
+    out = s.get_state()
+    fo = oracle.run(case, st, steps, record_forces=True)
+    for fld in FIELDS:
+        assert same(getattr(out, fld), getattr(st, fld)), (name, fld, maxrel(getattr(out, fld), getattr(st, fld)))
+    if hist:
+        h = s.force_history(steps)
+        assert h.shape[0] == steps
+        assert force_close(h[:, 0], fo[:, 1]) and force_close(h[:, 1], fo[:, 0])
+
+
+@pytest.mark.parametrize("name", ["zoo_ibb", "zoo_convective_chain", "taylor_green", "zoo_open_edges"])
+def test_chunked_runs_and_block_shapes_agree(name):
+    """run(a); run(b) == run(a + b) bit for bit, and the result does not
+    depend on the thread-block shape (no races between nodes)."""
+    from lbc_gb300 import F64, GpuSolver
+    (case, st), steps = casezoo.build(name)
+    ref = None
+    for bx, by, chunks in [(64, 4, [steps]), (32, 8, [7, steps - 7]), (128, 2, [1, 2, steps - 3]),
+                           (256, 1, [steps - 1, 1])]:
+        s = GpuSolver(case, F64)
+        s.set_block(bx, by)
+        s.set_state(st)
+        for c in chunks:
+            s.run(c)
+        out = s.get_state()
+        if ref is None:
+            ref = out
+        else:
+            for fld in FIELDS:
+                assert same(getattr(out, fld), getattr(ref, fld)), (name, bx, by, chunks, fld)
+
+
+def test_cylinder_golden_forces_on_gpu():
+    """lbc's shipped drag history (1000 x 400, IBB, Zou-He inlet, convective
+    outlet, periodic y): the first 300 steps."""
+    from lbc_gb300 import F64, GpuSolver
+    g = np.load(os.path.join(GOLDEN, "lbc_cylinder_forces_res20_first300.npy"))
+    case, st, cf = cases.cylinder_golden()
+    s = GpuSolver(case, F64)
+    s.enable_force_history(300)
+    s.set_state(st)
+    s.run(300)
+    h = s.force_history(300)
+    D, L = h[:, 0] * cf, h[:, 1] * cf
+    assert np.max(np.abs(D - g[:, 2]) / np.abs(g[:, 2])) < 1e-13
+    assert np.max(np.abs(L - g[:, 1])) < 1e-9 * np.max(np.abs(g[:, 2]))
+
+
+def _bc_call(lib, case, st, b):
+    arr, keep = lib.boundaries([b])
+    getattr(lib, b.name)(case.Nx, case.Ny, Q, b.index, arr[0].val1, arr[0].val2, dptr(st.f),
+                         dptr(st.f_new), dptr(st.rho), dptr(st.u), dptr(st.v),
+                         iptr(case.solid_mask), iptr(case.cx), iptr(case.cy), dptr(case.w))
+
+
+@pytest.mark.parametrize("name", ["zoo_zh_mixed", "zoo_pressure_reg", "zoo_reg_periodic",
+                                  "zoo_periodic_late", "zoo_ibb", "zoo_convective_chain",
+                                  "all_regularized_box", "cavity_zouhe"])
+def test_standalone_functions_match_lbc(gpu, oracle, name):
+    """Each of lbc's functions called on its own (lbm_core.h, lbm_bc.h)."""
+    (case, st0), _ = casezoo.build(name)
+    for b in case.bcs:
+        a, r = st0.copy(), st0.copy()
+        _bc_call(gpu, case, a, b)
+        _bc_call(oracle, case, r, b)
+        assert same(a.f_new, r.f_new), (name, b.name)
+    outs = []
+    for lib in (gpu, oracle):
+        st = st0.copy()
+        args = (case.Nx, case.Ny, Q)
+        lib.collision(*args, dptr(st.f), dptr(st.rho), dptr(st.u), dptr(st.v), dptr(case.omega_eff),
+                      iptr(case.solid_mask), iptr(case.cx), iptr(case.cy), dptr(case.w), 1e-5, -2e-6)
+        st2 = st.copy()
+        lib.bounce_back(*args, dptr(st.f), dptr(st.f_new), iptr(case.solid_mask), iptr(case.cx),
+                        iptr(case.cy), iptr(case.opp), case.isperiodic_x, case.isperiodic_y)
+        phi = case.phi if case.use_IBB else np.sqrt(np.abs(case.phi) + 0.3) - 0.1 * case.solid_mask
+        phi = np.ascontiguousarray(phi)
+        lib.interpolated_bounce_back(*args, dptr(st2.f), dptr(st2.f_new), iptr(case.solid_mask), dptr(phi),
+                                     iptr(case.opp), iptr(case.cx), iptr(case.cy), case.isperiodic_x,
+                                     case.isperiodic_y)
+        Fx, Fy = C.c_double(), C.c_double()
+        lib.compute_force_mem(*args, dptr(st.f), dptr(st.f_new), iptr(case.solid_mask), case.isperiodic_x,
+                              case.isperiodic_y, iptr(case.cx), iptr(case.cy), iptr(case.opp),
+                              C.byref(Fx), C.byref(Fy))
+        lib.streaming(*args, dptr(st.f), dptr(st.f_new), iptr(case.solid_mask), iptr(case.cx),
+                      iptr(case.cy), case.isperiodic_x, case.isperiodic_y)
+        lib.compute_macroscopic_fields(*args, dptr(st.f_new), iptr(case.solid_mask), iptr(case.cx),
+                                       iptr(case.cy), dptr(st.rho), dptr(st.u), dptr(st.v), 1e-5, 0.0)
+        outs.append((st, st2, Fx.value, Fy.value))
+    (a, a2, ax, ay), (b, b2, bx, by) = outs
+    for fld in FIELDS:
+        assert same(getattr(a, fld), getattr(b, fld)), (name, fld)
+    assert same(a2.f_new, b2.f_new), name
+    assert force_close([ax, ay], [bx, by])
+
+
+def test_mei_initialization_matches_lbc(gpu, oracle):
+    case, _ = cases.taylor_green(40, 24, 0.04, 0.6)
+    rng = np.random.default_rng(3)
+    rho_in = 1.0 + 1e-3 * rng.standard_normal((case.Ny, case.Nx))
+    U = 0.02 * rng.standard_normal((case.Ny, case.Nx))
+    V = 0.02 * rng.standard_normal((case.Ny, case.Nx))
+    mask = case.solid_mask.copy()
+    mask[5:9, 10:14] = 1
+    res = []
+    for lib in (gpu, oracle):
+        fn = getattr(lib.lib, lib.prefix + "mei_initialization")
+        fn.restype = None
+        f = np.zeros((case.Ny, case.Nx, Q))
+        fnew = np.full((case.Ny, case.Nx, Q), 0.1)
+        rho, u, v = (np.zeros((case.Ny, case.Nx)) for _ in range(3))
+        fn(C.c_int(case.Nx), C.c_int(case.Ny), C.c_int(Q), dptr(f), dptr(fnew), dptr(rho_in), dptr(U),
+           dptr(V), dptr(rho), dptr(u), dptr(v), iptr(case.cx), iptr(case.cy), dptr(case.w),
+           dptr(case.omega_eff), C.c_int(1), C.c_int(1), C.c_int(7), C.c_double(1e-16), iptr(mask))
+        res.append((f, fnew, rho, u, v))
+    for x, y in zip(*res):
+        assert same(x, y)
+
+
+@pytest.mark.parametrize("storage,tol", [("f32", 1e-5), ("f16", 2e-2)])
+def test_shifted_storage_error_vs_fp64(oracle, storage, tol):
+    """Taylor-Green 128 x 128, u0 = 0.04, tau = 0.56, 1000 steps: relative L2
+    error of u against the FP64 oracle (spec bound for FP32: 1e-5)."""
+    from lbc_gb300 import STORAGE, GpuSolver
+    case, st = cases.taylor_green(128, 128, 0.04, 0.56)
+    s = GpuSolver(case, STORAGE[storage])
+    s.set_state(st)
+    s.run(1000)
+    rho, u, v = s.get_fields()
+    oracle.run(case, st, 1000)
+    err = np.sqrt(np.sum((u - st.u) ** 2 + (v - st.v) ** 2) / np.sum(st.u ** 2 + st.v ** 2))
+    print(f"{storage}: u L2 rel error {err:.3e}")
+    assert err < tol
+
+
+@pytest.mark.parametrize("name", ["zoo_ibb", "zoo_convective_chain", "zoo_zh_mixed", "cylinder_wake_small"])
+def test_shifted_storage_on_edge_bcs(oracle, name):
+    """FP32-shifted storage through every edge BC path stays close to FP64."""
+    from lbc_gb300 import F32_SHIFTED, GpuSolver
+    (case, st), steps = casezoo.build(name)
+    s = GpuSolver(case, F32_SHIFTED)
+    s.set_state(st)
+    s.run(steps)
+    rho, u, v = s.get_fields()
+    oracle.run(case, st, steps)
+    fl = case.solid_mask == 0
+    assert np.max(np.abs(u[fl] - st.u[fl])) < 1e-5
+    assert np.max(np.abs(rho[fl] - st.rho[fl])) < 1e-5

@@ -1,0 +1,51 @@
+"""Run one named case on the GPU for a number of steps (device-resident).
+
+    python -m lbc_gb300.runcase --case taylor_green --n 2048 --storage f32 --steps 20
+
+Prints one line with the wall time of the run (CUDA events) and MLUPS. Used to
+profile a single kernel on a small case, and as a command-line case main.
+"""
+import argparse
+import json
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+from lbc_gb300 import STORAGE, GpuSolver, cases  # noqa: E402
+
+BUILDERS = {
+    "taylor_green": lambda n, ny: cases.taylor_green(n, ny or n, 0.04, 0.56),
+    "poiseuille": lambda n, ny: cases.poiseuille(n, ny or max(8, n // 4), 0.8, 1e-6),
+    "cavity": lambda n, ny: cases.cavity_moving_wall(n, 0.1, 1000.0),
+    "cavity_zouhe": lambda n, ny: cases.cavity_zouhe(n, 0.1, 1000.0),
+    "cylinder": lambda n, ny: cases.cylinder_wake(n, ny or n // 4, D=max(8.0, n / 32), xc=n / 4,
+                                                  yc=(ny or n // 4) / 2),
+}
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("--case", default="taylor_green", choices=sorted(BUILDERS))
+    p.add_argument("--n", type=int, default=2048)
+    p.add_argument("--ny", type=int, default=0)
+    p.add_argument("--storage", default="f32", choices=sorted(STORAGE))
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=2)
+    p.add_argument("--block", default="", help="bx,by thread block of the fused step")
+    a = p.parse_args(argv)
+    case, st = BUILDERS[a.case](a.n, a.ny)
+    s = GpuSolver(case, STORAGE[a.storage])
+    if a.block:
+        bx, by = (int(x) for x in a.block.split(","))
+        s.set_block(bx, by)
+    s.set_state(st)
+    s.run(a.warmup)
+    ms = s.run_timed(a.steps)
+    print(json.dumps({"case": a.case, "Nx": case.Nx, "Ny": case.Ny, "storage": a.storage,
+                      "steps": a.steps, "ms": round(ms, 3),
+                      "mlups": round(case.nodes * a.steps / (ms / 1e3) / 1e6, 1)}))
+
+
+if __name__ == "__main__":
+    main()

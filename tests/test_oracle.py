@@ -18,6 +18,8 @@ NAMES = [n for n, _, _ in casezoo.standard_cases()]
 
 
 def force_close(a, b, rtol=1e-12):
+    """Per-step force pairs agree to rtol of the largest force component (the
+    lift of a symmetric flow is round-off and is summed in no fixed order)."""
     a, b = np.asarray(a), np.asarray(b)
     scale = max(np.max(np.abs(b)), 1e-300)
     return np.max(np.abs(a - b)) <= rtol * scale

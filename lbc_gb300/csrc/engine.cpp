@@ -489,6 +489,7 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
         for (int k = 0; k < 9; k++) fp.wf[k] = (float)d_.w[k];
         fp.omega0f = (float)omega0_;
         fp.Fxf = (float)d_.Fx; fp.Fyf = (float)d_.Fy;
+        fp.hFxf = (float)(0.5 * d_.Fx); fp.hFyf = (float)(0.5 * d_.Fy);
         CK(launch::step_shifted(fp, d_.store, has_flags_, collide, block_, stream_));
     }
     if (stages_.empty()) return true;

@@ -44,7 +44,7 @@ struct FastStepParams {
     StepParams s;
     float wf[9];
     float omega0f;
-    float Fxf, Fyf;
+    float Fxf, Fyf, hFxf, hFyf;   // FP32 copies (no per-thread FP64 conversions)
 };
 
 namespace launch {

@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(256) k_step_shifted(const FastStepParams fp) {
             }
             if (!(FLAGS && (fl & NF_BCW))) {
                 float dr, rho, ux, uy;
-                moments_shifted(g, (float)p.hFx, (float)p.hFy, dr, rho, ux, uy);
+                moments_shifted(g, fp.hFxf, fp.hFyf, dr, rho, ux, uy);
                 if (p.write_macro) { p.rho[dn] = 1.0 + (double)dr; p.ux[dn] = ux; p.uy[dn] = uy; }
                 if (slot >= 0) {
                     p.bandm_next[slot] = 1.0 + (double)dr;

@@ -17,12 +17,14 @@ from lbc_gb300 import cases
 NAMES = [n for n, _, _ in casezoo.standard_cases()]
 
 
-def force_close(a, b, rtol=1e-12):
-    """Per-step force pairs agree to rtol of the largest force component (the
-    lift of a symmetric flow is round-off and is summed in no fixed order)."""
+def force_close(a, b, case, rtol=1e-12):
+    """Per-step forces agree to rtol of the gross link sum (0.5 per wall link):
+    lbc sums the links with OpenMP atomics in no fixed order, and the net lift
+    of a symmetric flow is pure cancellation."""
     a, b = np.asarray(a), np.asarray(b)
-    scale = max(np.max(np.abs(b)), 1e-300)
-    return np.max(np.abs(a - b)) <= rtol * scale
+    m = case.solid_mask.astype(bool)
+    n = sum(int(np.sum(~m & np.roll(np.roll(m, -int(case.cy[k]), 0), -int(case.cx[k]), 1))) for k in range(1, 9))
+    return np.max(np.abs(a - b)) <= rtol * 0.5 * max(n, 1) if b.size else True
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -32,7 +34,7 @@ def test_oracle_matches_lbc_fixture(oracle, name):
     g = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
     for fld in ("f", "f_new", "rho", "u", "v"):
         assert same(getattr(st, fld), g[fld]), (name, fld, maxrel(getattr(st, fld), g[fld]))
-    assert force_close(fr, g["forces"]), name
+    assert force_close(fr, g["forces"], case), name
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -43,7 +45,7 @@ def test_oracle_matches_lbc_build(oracle, ref, name):
     fb = ref.run(case, st2, 20, record_forces=True)
     for fld in ("f", "f_new", "rho", "u", "v"):
         assert same(getattr(st, fld), getattr(st2, fld)), (name, fld)
-    assert force_close(fa, fb)
+    assert force_close(fa, fb, case)
 
 
 def test_oracle_cylinder_golden_forces(oracle):

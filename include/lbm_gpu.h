@@ -91,9 +91,45 @@ int lbm_gpu_enable_force_history(lbm_gpu_solver *s, int capacity);
 /* Copies up to max_steps records (x, y), oldest first; returns the count. */
 int lbm_gpu_force_history(lbm_gpu_solver *s, double *xy, int max_steps);
 
+/* ---- Time-domain impedance wall (no counterpart in lbc's library; it
+ * replaces the host-side ADE coupling of lbc's cases/nit/nit.c:276-303).
+ * Boundary entry `entry` must be velocity_bottom_regularized. Each of its
+ * nodes with m[i] > 0 carries a mass-spring-damper m v' + R v + K x = p'
+ * (FP64 state, exact zero-order-hold update per step) driven by
+ * p' = (rho - rho_ref) / 3 of the interior neighbour at the previous step; the
+ * BC then imposes u_y = -v (v > 0: flow into the liner) and u_x = val1[i].
+ * Nodes with m[i] <= 0 keep the entry's own val2. Running DFTs of p' and v at
+ * nf <= 8 angular frequencies (rad / step) are kept per node. Arrays have Nx
+ * entries. */
+int lbm_gpu_set_impedance_wall(lbm_gpu_solver *s, int entry, const double *R, const double *m,
+                               const double *K, int nf, const double *omegas, double rho_ref);
+/* spectra[(i * nf + f) * 4 + q]: q = 0,1 sum p' e^{-i w n} (re, im); q = 2,3 the
+ * same for v. state[2 i + {0,1}] = (x, v). Either pointer may be NULL. */
+int lbm_gpu_impedance_readback(lbm_gpu_solver *s, int entry, double *spectra, double *state);
+/* The per-step update the wall uses: (x, v) <- A (x, v) + b p' is the exact
+ * solution of m v' + R v + K x = p' over one step with p' held constant.
+ * A row-major 2x2, b 2. Returns 0, or LBM_GPU_ERR_ARG unless m, K > 0, R >= 0. */
+int lbm_gpu_msd_zoh(double R, double m, double K, double *A, double *b);
+
 int lbm_gpu_get_info(lbm_gpu_solver *s, lbm_gpu_info *info);
 /* Thread-block shape of the fused step (bx * by <= 256, bx multiple of 32). */
 int lbm_gpu_set_block(lbm_gpu_solver *s, int bx, int by);
+
+/* ---- Batches: many independent cases of one storage type advanced together.
+ * Per step: one persistent kernel over the flattened tile list of every case
+ * (uneven grids and different geometries share the launch), the i-th Boundary
+ * entry of every case in one launch, one launch for all BC-written nodes, one
+ * per-case force reduction; the loop runs from a captured CUDA graph. Every
+ * case ends exactly as lbm_gpu_run(s, n) alone would leave it (FP64: bit for
+ * bit; forces to round-off). The solvers stay owned by the caller and must
+ * outlive the batch. */
+typedef struct lbm_gpu_batch lbm_gpu_batch;
+int lbm_gpu_batch_create(lbm_gpu_solver *const *solvers, int n, lbm_gpu_batch **out);
+int lbm_gpu_batch_run(lbm_gpu_batch *b, int nsteps);
+int lbm_gpu_batch_run_timed(lbm_gpu_batch *b, int nsteps, double *ms);
+/* Total nodes of all cases and kernel launches per batched step. */
+int lbm_gpu_batch_info(lbm_gpu_batch *b, long long *nodes, int *launches_per_step);
+int lbm_gpu_batch_destroy(lbm_gpu_batch *b);
 
 /* Page-locked host memory for fast transfers. */
 void *lbm_gpu_host_alloc(size_t bytes);

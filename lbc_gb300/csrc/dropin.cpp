@@ -666,6 +666,24 @@ int lbm_gpu_force_history(lbm_gpu_solver *s, double *xy, int max_steps) {
     return s->s->force_history(xy, max_steps);
 }
 
+int lbm_gpu_set_impedance_wall(lbm_gpu_solver *s, int entry, const double *R, const double *m,
+                               const double *K, int nf, const double *omegas, double rho_ref) {
+    SOLVER_OR_FAIL(s);
+    if (!R || !m || !K || (nf > 0 && !omegas)) { set_error("null array"); return LBM_GPU_ERR_ARG; }
+    return s->s->set_impedance(entry, R, m, K, nf, omegas, rho_ref) ? LBM_GPU_OK : LBM_GPU_ERR_ARG;
+}
+
+int lbm_gpu_impedance_readback(lbm_gpu_solver *s, int entry, double *spectra, double *state) {
+    SOLVER_OR_FAIL(s);
+    return s->s->impedance_readback(entry, spectra, state) ? LBM_GPU_OK : LBM_GPU_ERR_ARG;
+}
+
+int lbm_gpu_msd_zoh(double R, double m, double K, double *A, double *b) {
+    if (!A || !b) { set_error("null array"); return LBM_GPU_ERR_ARG; }
+    if (!msd_zoh(R, m, K, A, b)) { set_error("need m > 0, K > 0, R >= 0"); return LBM_GPU_ERR_ARG; }
+    return LBM_GPU_OK;
+}
+
 int lbm_gpu_get_info(lbm_gpu_solver *s, lbm_gpu_info *info) {
     SOLVER_OR_FAIL(s);
     info->Nx = s->s->Nx();
@@ -687,6 +705,57 @@ int lbm_gpu_set_block(lbm_gpu_solver *s, int bx, int by) {
         return LBM_GPU_ERR_ARG;
     }
     s->s->set_block(dim3(bx, by, 1));
+    return LBM_GPU_OK;
+}
+
+struct lbm_gpu_batch {
+    std::unique_ptr<Batch> b;
+};
+
+int lbm_gpu_batch_create(lbm_gpu_solver *const *solvers, int n, lbm_gpu_batch **out) {
+    if (!solvers || n <= 0 || !out) { set_error("bad arguments"); return LBM_GPU_ERR_ARG; }
+    *out = nullptr;
+    std::vector<Solver *> v;
+    for (int i = 0; i < n; i++) {
+        if (!solvers[i] || !solvers[i]->s) { set_error("null solver in batch"); return LBM_GPU_ERR_ARG; }
+        v.push_back(solvers[i]->s.get());
+    }
+    std::unique_ptr<Batch> b(new Batch(v));
+    if (!b->ok()) return LBM_GPU_ERR_CUDA;
+    *out = new lbm_gpu_batch{std::move(b)};
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_batch_run(lbm_gpu_batch *b, int nsteps) {
+    if (!b || nsteps < 0) { set_error("bad arguments"); return LBM_GPU_ERR_ARG; }
+    return b->b->run(nsteps) ? LBM_GPU_OK : LBM_GPU_ERR_CUDA;
+}
+
+int lbm_gpu_batch_run_timed(lbm_gpu_batch *b, int nsteps, double *ms) {
+    if (!b || nsteps < 0) { set_error("bad arguments"); return LBM_GPU_ERR_ARG; }
+    cudaEvent_t e0, e1;
+    if (!check_cuda(cudaEventCreate(&e0), "event") || !check_cuda(cudaEventCreate(&e1), "event"))
+        return LBM_GPU_ERR_CUDA;
+    bool okk = check_cuda(cudaEventRecord(e0, b->b->stream()), "event") && b->b->run(nsteps) &&
+               check_cuda(cudaEventRecord(e1, b->b->stream()), "event") &&
+               check_cuda(cudaEventSynchronize(e1), "event");
+    float t = 0.f;
+    if (okk) okk = check_cuda(cudaEventElapsedTime(&t, e0, e1), "event");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ms) *ms = t;
+    return okk ? LBM_GPU_OK : LBM_GPU_ERR_CUDA;
+}
+
+int lbm_gpu_batch_info(lbm_gpu_batch *b, long long *nodes, int *launches_per_step) {
+    if (!b) { set_error("null batch"); return LBM_GPU_ERR_ARG; }
+    if (nodes) *nodes = b->b->nodes();
+    if (launches_per_step) *launches_per_step = b->b->launches_per_step();
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_batch_destroy(lbm_gpu_batch *b) {
+    delete b;
     return LBM_GPU_OK;
 }
 

@@ -262,6 +262,7 @@ bool Solver::build_geometry() {
         }
     }
     has_flags_ = any_special || !stages_.empty() || !d_.px || !d_.py;
+    wnodes_host_ = wnodes;
     has_links_ = want_links && !links.empty();
     has_mem_ = any_solid_link;
     nw_ = (int)wnodes.size();
@@ -444,7 +445,8 @@ int Solver::force_history(double *out, int max_steps) {
     return n;
 }
 
-bool Solver::launch_collide(int b) {
+bool Solver::launch_collide(int b, cudaStream_t s) {
+    if (!s) s = stream_;
     CollideParams c;
     c.Nx = d_.Nx; c.Ny = d_.Ny; c.pitch = pitch_; c.plane = plane_;
     c.f = (double *)buf_[b];
@@ -454,14 +456,12 @@ bool Solver::launch_collide(int b) {
     c.has_force = (d_.Fx != 0.0 || d_.Fy != 0.0);
     c.Fx = d_.Fx; c.Fy = d_.Fy;
     for (int k = 0; k < 9; k++) c.w[k] = d_.w[k];
-    if (d_.store == STORE_F64) CK(launch::collide_exact(c, stream_));
-    else CK(launch::collide_shifted(c, d_.store, stream_));
+    if (d_.store == STORE_F64) CK(launch::collide_exact(c, s));
+    else CK(launch::collide_shifted(c, d_.store, s));
     return true;
 }
 
-// One time step src -> dst: fused bulk kernel, then the Boundary list in order
-// and the finish kernel for BC-written nodes.
-bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int bparity) {
+StepParams Solver::step_params(int src, int dst, bool write_macro, int bparity) const {
     StepParams p;
     std::memset(&p, 0, sizeof p);
     p.Nx = d_.Nx; p.Ny = d_.Ny; p.pitch = pitch_; p.plane = plane_;
@@ -481,45 +481,194 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
         p.mem_partials = d_partials_; p.mem_ticket = d_ticket_; p.mem_out = d_mem_out_;
         p.mem_hist = d_hist_; p.mem_hist_count = hist_count_ptr_; p.mem_hist_cap = hist_cap_;
     }
-    if (d_.store == STORE_F64) {
-        CK(launch::step_exact(p, has_flags_, collide, block_, stream_));
+    return p;
+}
+
+FastStepParams Solver::fast_params(const StepParams &p) const {
+    FastStepParams fp;
+    std::memset(&fp, 0, sizeof fp);
+    fp.s = p;
+    for (int k = 0; k < 9; k++) fp.wf[k] = (float)d_.w[k];
+    fp.omega0f = (float)omega0_;
+    fp.Fxf = (float)d_.Fx; fp.Fyf = (float)d_.Fy;
+    fp.hFxf = (float)(0.5 * d_.Fx); fp.hFyf = (float)(0.5 * d_.Fy);
+    return fp;
+}
+
+StageParams Solver::stage_params(const Stage &st, int src, int bparity) const {
+    StageParams s;
+    std::memset(&s, 0, sizeof s);
+    s.Nx = d_.Nx; s.Ny = d_.Ny; s.pitch = pitch_; s.plane = plane_;
+    s.kind = st.kind; s.index = st.index; s.along = st.along;
+    s.val1 = st.d_val1; s.val2 = st.d_val2;
+    s.flags = d_flags_; s.colbase = d_colbase_; s.rowbase = d_rowbase_; s.nslots = nslots_;
+    s.bandf = d_bandf_; s.bandm_prev = d_bandm_[bparity];
+    s.src = buf_[src];
+    for (int k = 0; k < 9; k++) s.w[k] = d_.w[k];
+    s.imp = st.d_imp;
+    s.imp_nf = st.imp_nf;
+    s.imp_rho_ref = st.imp_rho_ref;
+    for (int f = 0; f < 8; f++) {
+        s.imp_cos[f] = st.imp_cos[f];
+        s.imp_sin[f] = st.imp_sin[f];
+    }
+    return s;
+}
+
+bool msd_zoh(double R, double m, double K, double A[4], double b[2]) {
+    if (!(m > 0.0) || !(K > 0.0) || !(R >= 0.0)) return false;
+    // M = [[0, 1], [-K/m, -R/m]]; exp(M) = E0 I + E1 (M - a I), a = tr/2,
+    // d^2 = a^2 - det; e^a cosh d and e^a sinh(d)/d formed from e^(a +- d)
+    // so that strongly damped nodes do not overflow.
+    const double km = K / m, rm = R / m;
+    const double a = -0.5 * rm;
+    const double d2 = a * a - km;
+    double E0, E1;
+    if (d2 > 0.0) {
+        const double d = std::sqrt(d2);
+        const double ep = std::exp(a + d), em = std::exp(a - d);
+        E0 = 0.5 * (ep + em);
+        E1 = 0.5 * (ep - em) / d;
+    } else if (d2 < 0.0) {
+        const double wd = std::sqrt(-d2);
+        const double ea = std::exp(a);
+        E0 = ea * std::cos(wd);
+        E1 = ea * std::sin(wd) / wd;
     } else {
-        FastStepParams fp;
-        fp.s = p;
-        for (int k = 0; k < 9; k++) fp.wf[k] = (float)d_.w[k];
-        fp.omega0f = (float)omega0_;
-        fp.Fxf = (float)d_.Fx; fp.Fyf = (float)d_.Fy;
-        fp.hFxf = (float)(0.5 * d_.Fx); fp.hFyf = (float)(0.5 * d_.Fy);
-        CK(launch::step_shifted(fp, d_.store, has_flags_, collide, block_, stream_));
+        E0 = std::exp(a);
+        E1 = std::exp(a);
     }
-    if (stages_.empty()) return true;
-    for (const Stage &st : stages_) {
-        StageParams s;
-        std::memset(&s, 0, sizeof s);
-        s.Nx = d_.Nx; s.Ny = d_.Ny; s.pitch = pitch_; s.plane = plane_;
-        s.kind = st.kind; s.index = st.index; s.along = st.along;
-        s.val1 = st.d_val1; s.val2 = st.d_val2;
-        s.flags = d_flags_; s.colbase = d_colbase_; s.rowbase = d_rowbase_; s.nslots = nslots_;
-        s.bandf = d_bandf_; s.bandm_prev = d_bandm_[bparity];
-        s.src = buf_[src];
-        for (int k = 0; k < 9; k++) s.w[k] = d_.w[k];
-        CK(launch::stage(s, d_.store, stream_));
+    A[0] = E0 + E1 * (0.0 - a);  // A11
+    A[1] = E1 * 1.0;             // A12
+    A[2] = E1 * (-km);           // A21
+    A[3] = E0 + E1 * (-rm - a);  // A22
+    // b = M^-1 (A - I) (0, 1/m); det M = K/m.
+    const double q1 = A[1] / m, q2 = (A[3] - 1.0) / m;
+    b[0] = (-rm * q1 - q2) / km;
+    b[1] = q1;
+    return true;
+}
+
+bool Solver::set_impedance(int entry, const double *R, const double *m, const double *K, int nf,
+                           const double *omegas, double rho_ref) {
+    Stage *st = nullptr;
+    for (Stage &x : stages_)
+        if (x.entry == entry) st = &x;
+    if (!st || st->kind != BC_VEL_BOT_REG) {
+        set_error("impedance wall: entry must be a velocity_bottom_regularized Boundary entry");
+        return false;
     }
+    if (nf < 0 || nf > 8) {
+        set_error("impedance wall: at most 8 DFT frequencies");
+        return false;
+    }
+    const int n = st->along;
+    const int nfield = IMP_FIELDS + 6 * nf;
+    std::vector<double> h((size_t)nfield * n, 0.0);
+    for (int t = 0; t < n; t++) {
+        if (!(m[t] > 0.0)) continue;
+        double A[4], b[2];
+        if (!msd_zoh(R[t], m[t], K[t], A, b)) {
+            set_error("impedance wall: need m > 0, K > 0, R >= 0 at node " + std::to_string(t));
+            return false;
+        }
+        h[(size_t)IMP_ACTIVE * n + t] = 1.0;
+        h[(size_t)IMP_A11 * n + t] = A[0];
+        h[(size_t)IMP_A12 * n + t] = A[1];
+        h[(size_t)IMP_A21 * n + t] = A[2];
+        h[(size_t)IMP_A22 * n + t] = A[3];
+        h[(size_t)IMP_B1 * n + t] = b[0];
+        h[(size_t)IMP_B2 * n + t] = b[1];
+        for (int f = 0; f < nf; f++) h[(size_t)imp_field(f, 0) * n + t] = 1.0;
+    }
+    if (!st->d_imp || st->imp_nf != nf) {
+        if (!dalloc(&st->d_imp, h.size())) return false;
+    }
+    CK(cudaMemcpyAsync(st->d_imp, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    st->imp_nf = nf;
+    st->imp_rho_ref = rho_ref;
+    for (int f = 0; f < nf; f++) {
+        st->imp_cos[f] = std::cos(omegas[f]);
+        st->imp_sin[f] = std::sin(omegas[f]);
+    }
+    graph_valid_ = false;
+    return true;
+}
+
+bool Solver::impedance_readback(int entry, double *out, double *state) {
+    const Stage *st = nullptr;
+    for (const Stage &x : stages_)
+        if (x.entry == entry) st = &x;
+    if (!st || !st->d_imp) {
+        set_error("impedance wall: none on this entry");
+        return false;
+    }
+    const int n = st->along, nf = st->imp_nf;
+    std::vector<double> h((size_t)(IMP_FIELDS + 6 * nf) * n);
+    CK(cudaStreamSynchronize(stream_));
+    CK(cudaMemcpy(h.data(), st->d_imp, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int t = 0; t < n; t++) {
+        if (state) {
+            state[2 * t] = h[(size_t)IMP_X * n + t];
+            state[2 * t + 1] = h[(size_t)IMP_V * n + t];
+        }
+        if (out)
+            for (int f = 0; f < nf; f++)
+                for (int q = 0; q < 4; q++) out[((size_t)t * nf + f) * 4 + q] = h[(size_t)imp_field(f, 2 + q) * n + t];
+    }
+    return true;
+}
+
+FinishParams Solver::finish_params(int dst, bool write_macro, int bparity) const {
     FinishParams f;
     std::memset(&f, 0, sizeof f);
     f.Nx = d_.Nx; f.Ny = d_.Ny; f.pitch = pitch_; f.plane = plane_;
     f.nw = nw_; f.wnodes = d_wnodes_;
     f.colbase = d_colbase_; f.rowbase = d_rowbase_; f.nslots = nslots_;
-    f.bandf = d_bandf_; f.bandm_next = d_bandm_[bparity ^ 1];
+    f.bandf = d_bandf_; f.bandm_next = nslots_ ? d_bandm_[bparity ^ 1] : nullptr;
     f.dst = buf_[dst];
     f.omega = d_omega_; f.omega0 = omega0_;
-    f.has_force = p.has_force; f.Fx = d_.Fx; f.Fy = d_.Fy; f.hFx = p.hFx; f.hFy = p.hFy;
+    f.has_force = (d_.Fx != 0.0 || d_.Fy != 0.0);
+    f.Fx = d_.Fx; f.Fy = d_.Fy; f.hFx = 0.5 * d_.Fx; f.hFy = 0.5 * d_.Fy;
     for (int k = 0; k < 9; k++) f.w[k] = d_.w[k];
-    f.write_macro = p.write_macro;
+    f.write_macro = write_macro ? 1 : 0;
     f.rho = d_rho_; f.ux = d_ux_; f.uy = d_uy_;
-    if (d_.store == STORE_F64) CK(launch::finish_exact(f, collide, stream_));
-    else CK(launch::finish_shifted(f, d_.store, collide, stream_));
+    return f;
+}
+
+// One time step src -> dst: fused bulk kernel, then the Boundary list in order
+// and the finish kernel for BC-written nodes.
+bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int bparity,
+                         cudaStream_t s) {
+    if (!s) s = stream_;
+    const StepParams p = step_params(src, dst, write_macro, bparity);
+    if (d_.store == STORE_F64) {
+        CK(launch::step_exact(p, has_flags_, collide, block_, s));
+    } else {
+        CK(launch::step_shifted(fast_params(p), d_.store, has_flags_, collide, block_, s));
+    }
+    if (stages_.empty()) return true;
+    for (const Stage &st : stages_) CK(launch::stage(stage_params(st, src, bparity), d_.store, s));
+    const FinishParams f = finish_params(dst, write_macro, bparity);
+    if (d_.store == STORE_F64) CK(launch::finish_exact(f, collide, s));
+    else CK(launch::finish_shifted(f, d_.store, collide, s));
     return true;
+}
+
+bool Solver::begin_steps(cudaStream_t s) { return launch_collide(cur_, s); }
+
+bool Solver::end_steps(cudaStream_t s) {
+    if (!launch_step(cur_, 1 - cur_, false, true, parity_, s)) return false;
+    advance(1);
+    return true;
+}
+
+void Solver::advance(int nsteps) {
+    if (nsteps & 1) {
+        cur_ ^= 1;
+        parity_ ^= 1;
+    }
 }
 
 // Two fused steps (cur -> other -> cur) captured once and replayed.
@@ -569,6 +718,203 @@ bool Solver::run(int nsteps) {
     parity_ ^= 1;
     steps_done_ += nsteps;
     return true;
+}
+
+}  // namespace lbm
+
+// ===================================================================== Batch
+
+namespace lbm {
+
+Batch::Batch(const std::vector<Solver *> &cases) : cases_(cases) {
+    if (cases_.empty()) {
+        set_error("empty batch");
+        return;
+    }
+    store_ = cases_[0]->store();
+    for (Solver *c : cases_) {
+        if (!c || !c->ok()) {
+            set_error("batch: invalid case");
+            return;
+        }
+        if (c->store() != store_) {
+            set_error("batch: all cases must use the same storage");
+            return;
+        }
+    }
+    if (!check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate")) return;
+    ok_ = build();
+}
+
+Batch::~Batch() {
+    if (pair_exec_) cudaGraphExecDestroy(pair_exec_);
+    for (void *p : allocs_) cudaFree(p);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+template <class T> static bool balloc(std::vector<void *> &allocs, T **p, size_t n) {
+    void *q = nullptr;
+    if (!check_cuda(cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)), "cudaMalloc batch")) return false;
+    allocs.push_back(q);
+    *p = (T *)q;
+    return true;
+}
+
+// Static tables (tile list, stage entry lists, finish nodes, force slots) and
+// room for the per-direction parameter arrays, which run() refreshes.
+bool Batch::build() {
+    const int nc = (int)cases_.size();
+    std::vector<int4> tiles;
+    std::vector<ForceSlot> force;
+    std::vector<int4> fin_nodes;
+    for (int c = 0; c < nc; c++) {
+        Solver *s = cases_[c];
+        nodes_ += (long long)s->Nx() * s->Ny();
+        const int t0 = (int)tiles.size();
+        for (int y = 0; y < s->Ny(); y += 4)
+            for (int x = 0; x < s->Nx(); x += 64) tiles.push_back(make_int4(c, x, y, s->has_mem() ? 1 : 0));
+        if (s->has_mem()) {
+            ForceSlot f;
+            std::memset(&f, 0, sizeof f);
+            f.t0 = t0;
+            f.t1 = (int)tiles.size();
+            f.out = s->mem_out();
+            f.hist = s->hist();
+            f.hist_count = s->hist_count();
+            f.hist_cap = s->hist_cap();
+            force.push_back(f);
+        }
+        for (const int2 &w : s->wnodes()) fin_nodes.push_back(make_int4(c, w.x, w.y, 0));
+        max_stages_ = std::max(max_stages_, (int)s->stages().size());
+        for (const Stage &st : s->stages()) max_along_ = std::max(max_along_, st.along);
+    }
+    ntiles_ = (int)tiles.size();
+    nfin_ = (int)fin_nodes.size();
+    nforce_ = (int)force.size();
+    const size_t psize = store_ == STORE_F64 ? sizeof(StepParams) : sizeof(FastStepParams);
+    void *sp = nullptr;
+    if (!check_cuda(cudaMalloc(&sp, psize * 2 * nc), "cudaMalloc batch")) return false;
+    allocs_.push_back(sp);
+    d_sp_ = sp;
+    if (!balloc(allocs_, &d_phase_, nc) || !balloc(allocs_, &d_tiles_, tiles.size()) ||
+        !balloc(allocs_, &d_partials_, 2 * tiles.size()) || !balloc(allocs_, &d_fin_, 2 * nc) ||
+        !balloc(allocs_, &d_fin_nodes_, fin_nodes.size()) || !balloc(allocs_, &d_force_, force.size()))
+        return false;
+    CK(cudaMemsetAsync(d_phase_, 0, nc * sizeof(int), stream_));
+    CK(cudaMemcpyAsync(d_tiles_, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, stream_));
+    if (nfin_) CK(cudaMemcpyAsync(d_fin_nodes_, fin_nodes.data(), fin_nodes.size() * sizeof(int4), cudaMemcpyHostToDevice, stream_));
+    if (nforce_) CK(cudaMemcpyAsync(d_force_, force.data(), force.size() * sizeof(ForceSlot), cudaMemcpyHostToDevice, stream_));
+    for (int s = 0; s < max_stages_; s++) {
+        int cnt = 0;
+        for (Solver *c : cases_) cnt += (int)c->stages().size() > s ? 1 : 0;
+        StageParams *d = nullptr;
+        if (!balloc(allocs_, &d, 2 * cnt)) return false;
+        d_stage_lists_.push_back(d);
+        stage_counts_.push_back(cnt);
+    }
+    grid_ = std::min(ntiles_, store_ == STORE_F64 ? launch::step_batch_exact_grid()
+                                                  : launch::step_batch_shifted_grid(store_));
+    if (grid_ < 1) grid_ = 1;
+    launches_per_step_ = 1 + max_stages_ + (nfin_ ? 1 : 0) + (nforce_ ? 1 : 0);
+    CK(cudaStreamSynchronize(stream_));
+    return true;
+}
+
+bool Batch::launch_batched(int sel) {
+    if (store_ == STORE_F64)
+        CK(launch::step_batch_exact((const StepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel,
+                                    d_partials_, grid_, stream_));
+    else
+        CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel,
+                                      d_partials_, store_, grid_, stream_));
+    for (int s = 0; s < max_stages_; s++)
+        CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], max_along_, store_, sel, stream_));
+    if (nfin_) {
+        if (store_ == STORE_F64) CK(launch::finish_batch_exact(d_fin_, d_phase_, d_fin_nodes_, nfin_, sel, stream_));
+        else CK(launch::finish_batch_shifted(d_fin_, d_phase_, d_fin_nodes_, nfin_, sel, store_, stream_));
+    }
+    if (nforce_) CK(launch::force_reduce(d_partials_, d_force_, nforce_, stream_));
+    return true;
+}
+
+bool Batch::capture_pair() {
+    if (pair_exec_) return true;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    const bool okk = launch_batched(0) && launch_batched(1);
+    const cudaError_t e = cudaStreamEndCapture(stream_, &g);
+    if (!okk) {
+        if (g) cudaGraphDestroy(g);
+        return false;
+    }
+    CK(e);
+    const cudaError_t e2 = cudaGraphInstantiate(&pair_exec_, g, 0);
+    cudaGraphDestroy(g);
+    CK(e2);
+    return true;
+}
+
+bool Batch::run(int nsteps) {
+    if (!ok_) return false;
+    if (nsteps <= 0) return true;
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    bool okk = true;
+    for (Solver *c : cases_) {
+        okk = okk && check_cuda(cudaEventRecord(ev, c->stream()), "event") &&
+              check_cuda(cudaStreamWaitEvent(stream_, ev, 0), "event");
+    }
+    for (Solver *c : cases_) okk = okk && c->begin_steps(stream_);
+    const int mid = nsteps - 1;
+    if (okk && mid > 0) {
+        // Parameters of both ping-pong directions from each case's current state.
+        const int nc = (int)cases_.size();
+        std::vector<StepParams> sp(2 * nc);
+        std::vector<FastStepParams> fsp(store_ == STORE_F64 ? 0 : 2 * nc);
+        std::vector<FinishParams> fin(2 * nc);
+        std::vector<std::vector<StageParams>> lists(max_stages_);
+        for (int c = 0; c < nc; c++) {
+            Solver *s = cases_[c];
+            const int cur = s->current(), par = s->parity();
+            sp[2 * c] = s->step_params(cur, 1 - cur, false, par);
+            sp[2 * c + 1] = s->step_params(1 - cur, cur, false, par ^ 1);
+            if (!fsp.empty()) {
+                fsp[2 * c] = s->fast_params(sp[2 * c]);
+                fsp[2 * c + 1] = s->fast_params(sp[2 * c + 1]);
+            }
+            fin[2 * c] = s->finish_params(1 - cur, false, par);
+            fin[2 * c + 1] = s->finish_params(cur, false, par ^ 1);
+            for (size_t k = 0; k < s->stages().size(); k++) {
+                lists[k].push_back(s->stage_params(s->stages()[k], cur, par));
+                lists[k].push_back(s->stage_params(s->stages()[k], 1 - cur, par ^ 1));
+            }
+        }
+        if (store_ == STORE_F64)
+            okk = okk && check_cuda(cudaMemcpyAsync(d_sp_, sp.data(), sp.size() * sizeof(StepParams), cudaMemcpyHostToDevice, stream_), "H2D");
+        else
+            okk = okk && check_cuda(cudaMemcpyAsync(d_sp_, fsp.data(), fsp.size() * sizeof(FastStepParams), cudaMemcpyHostToDevice, stream_), "H2D");
+        okk = okk && check_cuda(cudaMemcpyAsync(d_fin_, fin.data(), fin.size() * sizeof(FinishParams), cudaMemcpyHostToDevice, stream_), "H2D");
+        for (int k = 0; k < max_stages_ && okk; k++)
+            okk = check_cuda(cudaMemcpyAsync(d_stage_lists_[k], lists[k].data(), lists[k].size() * sizeof(StageParams), cudaMemcpyHostToDevice, stream_), "H2D");
+        // Host vectors must outlive the copies.
+        okk = okk && check_cuda(cudaStreamSynchronize(stream_), "sync");
+        int pairs = mid / 2;
+        if (okk && pairs > 0) okk = capture_pair();
+        for (; okk && pairs > 0; pairs--) okk = check_cuda(cudaGraphLaunch(pair_exec_, stream_), "graph");
+        if (okk && (mid & 1)) okk = launch_batched(0);
+        for (Solver *c : cases_) {
+            c->advance(mid);
+            c->add_steps(mid);
+        }
+    }
+    for (Solver *c : cases_) {
+        okk = okk && c->end_steps(stream_);
+        c->add_steps(1);
+    }
+    okk = okk && check_cuda(cudaEventRecord(ev, stream_), "event");
+    for (Solver *c : cases_) okk = okk && check_cuda(cudaStreamWaitEvent(c->stream(), ev, 0), "event");
+    cudaEventDestroy(ev);
+    return okk;
 }
 
 }  // namespace lbm

@@ -41,7 +41,16 @@ struct Stage {
     int kind, index, along;
     int entry;                  // position in the Boundary list
     double *d_val1 = nullptr, *d_val2 = nullptr;
+    // impedance wall (bottom regularized entries only)
+    double *d_imp = nullptr;
+    int imp_nf = 0;
+    double imp_rho_ref = 1.0;
+    double imp_cos[8] = {1, 1, 1, 1, 1, 1, 1, 1}, imp_sin[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
+
+// Zero-order-hold update of m v' + R v + K x = p over one lattice step:
+// (x, v) <- A (x, v) + b p. Returns false unless m > 0 and K > 0.
+bool msd_zoh(double R, double m, double K, double A[4], double b[2]);
 
 class Solver {
   public:
@@ -81,11 +90,38 @@ class Solver {
     void set_block(dim3 b) { block_ = b; graph_valid_ = false; }
     dim3 block() const { return block_; }
 
+    // Pieces used by Batch: parameters of one step in a given direction, the
+    // first-step collision and the final (pre-collision, moments) step.
+    StepParams step_params(int src, int dst, bool write_macro, int bparity) const;
+    FastStepParams fast_params(const StepParams &p) const;
+    StageParams stage_params(const Stage &st, int src, int bparity) const;
+    FinishParams finish_params(int dst, bool write_macro, int bparity) const;
+    const std::vector<Stage> &stages() const { return stages_; }
+    const std::vector<int2> &wnodes() const { return wnodes_host_; }
+    bool has_mem() const { return has_mem_; }
+    int parity() const { return parity_; }
+    double *mem_out() const { return d_mem_out_; }
+    double *hist() const { return d_hist_; }
+    unsigned long long *hist_count() const { return hist_count_ptr_; }
+    int hist_cap() const { return hist_cap_; }
+    // Impedance wall on Boundary entry `entry` (velocity_bottom_regularized):
+    // per node R, m, K (m <= 0: keep the entry's own val2), nf <= 8 DFT
+    // frequencies (rad / step), reference density for p'.
+    bool set_impedance(int entry, const double *R, const double *m, const double *K, int nf,
+                       const double *omegas, double rho_ref);
+    // out[((t * nf) + f) * 4 + {0,1,2,3}] = (P re, P im, V re, V im); state[t*2+{0,1}] = (x, v)
+    bool impedance_readback(int entry, double *out, double *state);
+    bool begin_steps(cudaStream_t s);
+    bool end_steps(cudaStream_t s);
+    void advance(int nsteps);
+    void add_steps(long long n) { steps_done_ += n; }
+
   private:
     bool build_geometry();
     bool alloc();
-    bool launch_step(int src, int dst, bool collide, bool write_macro, int bparity);
-    bool launch_collide(int b);
+    bool launch_step(int src, int dst, bool collide, bool write_macro, int bparity,
+                     cudaStream_t s = nullptr);
+    bool launch_collide(int b, cudaStream_t s = nullptr);
     bool capture_pair();
     template <class T> bool dalloc(T **p, size_t count);
 
@@ -128,6 +164,49 @@ class Solver {
     bool graph_valid_ = false;
     size_t dev_bytes_ = 0;
     long long steps_done_ = 0;
+    std::vector<void *> allocs_;
+    std::vector<int2> wnodes_host_;
+};
+
+// Many independent cases of one storage type advanced together: per step one
+// persistent bulk kernel over the flattened tile list of all cases, the i-th
+// Boundary entry of every case in one launch, one finish launch for all
+// BC-written nodes and one per-case force reduction. The steps between the
+// per-case first collision and final step run from a captured two-step graph.
+// Each case ends exactly as Solver::run(n) would leave it.
+class Batch {
+  public:
+    explicit Batch(const std::vector<Solver *> &cases);
+    ~Batch();
+    bool ok() const { return ok_; }
+    bool run(int nsteps);
+    int ncases() const { return (int)cases_.size(); }
+    long long nodes() const { return nodes_; }
+    int launches_per_step() const { return launches_per_step_; }
+    cudaStream_t stream() const { return stream_; }
+
+  private:
+    bool build();
+    bool launch_batched(int sel);
+    bool capture_pair();
+
+    std::vector<Solver *> cases_;
+    int store_ = STORE_F64;
+    bool ok_ = false;
+    cudaStream_t stream_ = nullptr;
+    long long nodes_ = 0;
+    int ntiles_ = 0, grid_ = 0, max_stages_ = 0, max_along_ = 0, nfin_ = 0, nforce_ = 0;
+    int launches_per_step_ = 0;
+    void *d_sp_ = nullptr;         // StepParams or FastStepParams [2 * ncases]
+    int *d_phase_ = nullptr;       // [ncases] (and stage entries)
+    int4 *d_tiles_ = nullptr;
+    double *d_partials_ = nullptr;
+    std::vector<StageParams *> d_stage_lists_;
+    std::vector<int> stage_counts_;
+    FinishParams *d_fin_ = nullptr;
+    int4 *d_fin_nodes_ = nullptr;
+    ForceSlot *d_force_ = nullptr;
+    cudaGraphExec_t pair_exec_ = nullptr;
     std::vector<void *> allocs_;
 };
 

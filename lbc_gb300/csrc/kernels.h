@@ -37,6 +37,17 @@ struct AosArgs {
     double *out2;
 };
 
+// Where a batched step writes one case's force (k_force_reduce): the case's
+// tiles are [t0, t1) of the tile list.
+struct ForceSlot {
+    int t0, t1;
+    double *out;
+    double *hist;
+    unsigned long long *hist_count;
+    int hist_cap;
+    int pad;
+};
+
 enum AosOp : int { AOS_COLLISION, AOS_STREAMING, AOS_MOMENTS, AOS_BOUNCE_BACK, AOS_IBB, AOS_MEM };
 
 // Parameters of the shifted-storage (FP32 / FP16) fused step.
@@ -67,11 +78,27 @@ cudaError_t aos_bc(const AosArgs &a, int kind, int index, int along, const doubl
 cudaError_t mei_init(const AosArgs &a, double rho0, cudaStream_t s);
 cudaError_t mei_iter(const AosArgs &a, double rho0, unsigned long long *maxbits, cudaStream_t s);
 
+// batches of cases (tile list = int4 {case, x0, y0, case has wall links})
+cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 *tiles, int ntiles,
+                             int sel, double *partials, int grid, cudaStream_t s);
+int step_batch_exact_grid();
+cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int max_along, int store,
+                        int sel, cudaStream_t s);
+cudaError_t finish_batch_exact(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
+                               int sel, cudaStream_t s);
+cudaError_t force_reduce(const double *partials, const ForceSlot *slots, int n, cudaStream_t s);
+
 // shifted storage (kernels_shifted.cu)
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
                          cudaStream_t s);
 cudaError_t finish_shifted(const FinishParams &p, int store, bool collide, cudaStream_t s);
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s);
+cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
+                               int ntiles, int sel, double *partials, int store, int grid,
+                               cudaStream_t s);
+int step_batch_shifted_grid(int store);
+cudaError_t finish_batch_shifted(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
+                                 int sel, int store, cudaStream_t s);
 }  // namespace launch
 
 }  // namespace lbm

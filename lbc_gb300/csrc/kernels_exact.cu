@@ -34,11 +34,9 @@ namespace lbm {
 // moments (src/core/compute_macroscopic_fields.c:23-46) and, unless it is written
 // by an edge BC, collides (src/core/collision.c:22-38) and stores.
 template <bool FLAGS, bool COLLIDE>
-__global__ void __launch_bounds__(256) k_step_exact(const StepParams p) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    double mfx = 0.0, mfy = 0.0;
-    if (i < p.Nx && j < p.Ny) {
+__device__ __forceinline__ void step_node_exact(const StepParams &p, int i, int j, double &mfx,
+                                                double &mfy) {
+    {
         const long long node = (long long)j * p.pitch + i;
         const uint16_t fl = FLAGS ? p.flags[node] : (uint16_t)0;
         const size_t dn = (size_t)j * (size_t)p.Nx + (size_t)i;
@@ -124,9 +122,41 @@ __global__ void __launch_bounds__(256) k_step_exact(const StepParams p) {
             }
         }
     }
+}
+
+template <bool FLAGS, bool COLLIDE>
+__global__ void __launch_bounds__(256) k_step_exact(const StepParams p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    double mfx = 0.0, mfy = 0.0;
+    if (i < p.Nx && j < p.Ny) step_node_exact<FLAGS, COLLIDE>(p, i, j, mfx, mfy);
     if (FLAGS && p.mem_partials)
         reduce2_grid(mfx, mfy, p.mem_partials, p.mem_ticket, p.mem_out, p.mem_hist, p.mem_hist_count,
                      p.mem_hist_cap);
+}
+
+// Many cases in one launch: a persistent loop over a flattened list of
+// 2D tiles (one tile = one thread block's worth of nodes of one case). Each
+// case brings its own parameters (sp[2 * c + (sel ^ phase[c])]: the two
+// ping-pong directions), so uneven grids and different geometries share the
+// launch. Per-tile force partials are reduced per case by k_force_reduce.
+__global__ void __launch_bounds__(256) k_step_batch_exact(const StepParams *__restrict__ sp,
+                                                          const int *__restrict__ phase,
+                                                          const int4 *__restrict__ tiles, int ntiles,
+                                                          int sel, double *partials) {
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int4 td = tiles[t];
+        const StepParams &p = sp[2 * td.x + (sel ^ phase[td.x])];
+        const int i = td.y + threadIdx.x, j = td.z + threadIdx.y;
+        double mfx = 0.0, mfy = 0.0;
+        const bool in = i < p.Nx && j < p.Ny;
+        if (p.flags) {
+            if (in) step_node_exact<true, true>(p, i, j, mfx, mfy);
+        } else {
+            if (in) step_node_exact<false, true>(p, i, j, mfx, mfy);
+        }
+        if (td.w) block_reduce2_store(mfx, mfy, partials + 2 * (size_t)t);
+    }
 }
 
 // ---------------------------------------------------------------- edge BCs
@@ -149,19 +179,76 @@ template <typename T> struct BandAccessor {
 // pre-collision f_new of the band nodes. Entries run as separate launches in list
 // order, so each sees the writes of the previous ones, as in lbc.
 template <typename T>
+__device__ __forceinline__ void stage_point(const StageParams &p, int t) {
+    BandAccessor<T> a{p};
+    if (p.imp && p.kind == BC_VEL_BOT_REG && p.imp[(size_t)IMP_ACTIVE * p.along + t] != 0.0 &&
+        !a.solid(t, p.index)) {
+        // Impedance wall on this node: the regularized bottom BC with the
+        // normal velocity from the node's mass-spring-damper.
+        const double vn = impedance_step(p.imp, p.along, p.imp_nf, t, a.rho(t, p.index + 1),
+                                         p.imp_rho_ref, p.imp_cos, p.imp_sin);
+        bc_regularized(a, p.w, t, p.index, t, p.index + 1, false, p.val1[t], -vn);
+        return;
+    }
+    bc_apply(a, p.w, p.kind, p.Nx, p.Ny, p.index, t, p.val1, p.val2);
+}
+
+template <typename T>
 __global__ void k_stage(const StageParams p) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
-    BandAccessor<T> a{p};
-    bc_apply(a, p.w, p.kind, p.Nx, p.Ny, p.index, t, p.val1, p.val2);
+    stage_point<T>(p, t);
+}
+
+// Stage `s` of every case of a batch: blockIdx.y selects the case entry,
+// list[2 * e + (sel ^ phase)] its parameters for this ping-pong direction.
+template <typename T>
+__global__ void k_stage_batch(const StageParams *__restrict__ list, const int *__restrict__ ephase,
+                              int sel) {
+    const int e = blockIdx.y;
+    const StageParams &p = list[2 * e + (sel ^ ephase[e])];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.along) return;
+    stage_point<T>(p, t);
+}
+
+// Per-case deterministic sum of the per-tile force partials of a batched step.
+__global__ void k_force_reduce(const double *__restrict__ partials, const ForceSlot *__restrict__ slots,
+                               int nslots) {
+    const int c = blockIdx.x;
+    if (c >= nslots) return;
+    const ForceSlot fs = slots[c];
+    double a = 0.0, b = 0.0;
+    for (int t = fs.t0 + (int)threadIdx.x; t < fs.t1; t += blockDim.x) {
+        a += partials[2 * (size_t)t];
+        b += partials[2 * (size_t)t + 1];
+    }
+    __shared__ double sa[32], sb[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) { sa[threadIdx.x >> 5] = a; sb[threadIdx.x >> 5] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ra = 0.0, rb = 0.0;
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) { ra += sa[w]; rb += sb[w]; }
+        fs.out[0] = ra;
+        fs.out[1] = rb;
+        if (fs.hist) {
+            const unsigned long long k = *fs.hist_count;
+            const int slot = (int)(k % (unsigned long long)fs.hist_cap);
+            fs.hist[2 * slot] = ra;
+            fs.hist[2 * slot + 1] = rb;
+            *fs.hist_count = k + 1ull;
+        }
+    }
 }
 
 // Moments and collision of every node an edge BC wrote.
 template <bool COLLIDE>
-__global__ void k_finish_exact(const FinishParams p) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.nw) return;
-    const int2 ij = p.wnodes[t];
+__device__ __forceinline__ void finish_node_exact(const FinishParams &p, int2 ij) {
     const int slot = band_slot(p.colbase, p.rowbase, ij.x, ij.y);
     double f[9];
 #pragma unroll
@@ -181,6 +268,22 @@ __global__ void k_finish_exact(const FinishParams p) {
     const long long node = (long long)ij.y * p.pitch + ij.x;
 #pragma unroll
     for (int k = 0; k < 9; k++) D[k * p.plane + node] = f[k];
+}
+
+template <bool COLLIDE>
+__global__ void k_finish_exact(const FinishParams p) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.nw) return;
+    finish_node_exact<COLLIDE>(p, p.wnodes[t]);
+}
+
+// BC-written nodes of every case of a batch: nodes[t] = (case, i, j).
+__global__ void k_finish_batch_exact(const FinishParams *__restrict__ fp, const int *__restrict__ phase,
+                                     const int4 *__restrict__ nodes, int n, int sel) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int4 c = nodes[t];
+    finish_node_exact<true>(fp[2 * c.x + (sel ^ phase[c.x])], make_int2(c.y, c.z));
 }
 
 // In-place collision with the stored rho/u/v (src/core/collision.c:18-40); used
@@ -464,6 +567,44 @@ cudaError_t stage(const StageParams &p, int store, cudaStream_t s) {
     if (store == STORE_F64) k_stage<double><<<g, b, 0, s>>>(p);
     else if (store == STORE_F32) k_stage<float><<<g, b, 0, s>>>(p);
     else k_stage<__half><<<g, b, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 *tiles, int ntiles,
+                             int sel, double *partials, int grid, cudaStream_t s) {
+    if (ntiles == 0) return cudaSuccess;
+    k_step_batch_exact<<<grid, dim3(64, 4), 0, s>>>(sp, phase, tiles, ntiles, sel, partials);
+    return cudaGetLastError();
+}
+
+int step_batch_exact_grid() {
+    int nb = 0, dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_batch_exact, 256, 0);
+    return nsm * (nb > 0 ? nb : 1);
+}
+
+cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int max_along, int store,
+                        int sel, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const dim3 g((max_along + 127) / 128, n);
+    if (store == STORE_F64) k_stage_batch<double><<<g, 128, 0, s>>>(list, ephase, sel);
+    else if (store == STORE_F32) k_stage_batch<float><<<g, 128, 0, s>>>(list, ephase, sel);
+    else k_stage_batch<__half><<<g, 128, 0, s>>>(list, ephase, sel);
+    return cudaGetLastError();
+}
+
+cudaError_t finish_batch_exact(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
+                               int sel, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_finish_batch_exact<<<(n + 127) / 128, 128, 0, s>>>(fp, phase, nodes, n, sel);
+    return cudaGetLastError();
+}
+
+cudaError_t force_reduce(const double *partials, const ForceSlot *slots, int n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_force_reduce<<<n, 256, 0, s>>>(partials, slots, n);
     return cudaGetLastError();
 }
 

@@ -78,12 +78,10 @@ __device__ __forceinline__ void collide_shifted(float g[9], const float w[9], fl
 }
 
 template <typename T, bool FLAGS, bool COLLIDE>
-__global__ void __launch_bounds__(256) k_step_shifted(const FastStepParams fp) {
+__device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int i, int j,
+                                                  double &mfx, double &mfy) {
     const StepParams &p = fp.s;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    double mfx = 0.0, mfy = 0.0;
-    if (i < p.Nx && j < p.Ny) {
+    {
         const long long node = (long long)j * p.pitch + i;
         const uint16_t fl = FLAGS ? p.flags[node] : (uint16_t)0;
         const size_t dn = (size_t)j * (size_t)p.Nx + (size_t)i;
@@ -171,17 +169,44 @@ __global__ void __launch_bounds__(256) k_step_shifted(const FastStepParams fp) {
             }
         }
     }
+}
+
+template <typename T, bool FLAGS, bool COLLIDE>
+__global__ void __launch_bounds__(256) k_step_shifted(const FastStepParams fp) {
+    const StepParams &p = fp.s;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    double mfx = 0.0, mfy = 0.0;
+    if (i < p.Nx && j < p.Ny) step_node_shifted<T, FLAGS, COLLIDE>(fp, i, j, mfx, mfy);
     if (FLAGS && p.mem_partials) {
         reduce2_grid(mfx, mfy, p.mem_partials, p.mem_ticket, p.mem_out, p.mem_hist,
                      p.mem_hist_count, p.mem_hist_cap);
     }
 }
 
+// Batched form (see k_step_batch_exact in kernels_exact.cu).
+template <typename T>
+__global__ void __launch_bounds__(256) k_step_batch_shifted(const FastStepParams *__restrict__ sp,
+                                                            const int *__restrict__ phase,
+                                                            const int4 *__restrict__ tiles,
+                                                            int ntiles, int sel, double *partials) {
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int4 td = tiles[t];
+        const FastStepParams &fp = sp[2 * td.x + (sel ^ phase[td.x])];
+        const int i = td.y + threadIdx.x, j = td.z + threadIdx.y;
+        double mfx = 0.0, mfy = 0.0;
+        const bool in = i < fp.s.Nx && j < fp.s.Ny;
+        if (fp.s.flags) {
+            if (in) step_node_shifted<T, true, true>(fp, i, j, mfx, mfy);
+        } else {
+            if (in) step_node_shifted<T, false, true>(fp, i, j, mfx, mfy);
+        }
+        if (td.w) block_reduce2_store(mfx, mfy, partials + 2 * (size_t)t);
+    }
+}
+
 template <typename T, bool COLLIDE>
-__global__ void k_finish_shifted(const FinishParams p) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.nw) return;
-    const int2 ij = p.wnodes[t];
+__device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 ij) {
     const int slot = band_slot(p.colbase, p.rowbase, ij.x, ij.y);
     float g[9], wf[9];
 #pragma unroll
@@ -204,6 +229,22 @@ __global__ void k_finish_shifted(const FinishParams p) {
     const long long node = (long long)ij.y * p.pitch + ij.x;
 #pragma unroll
     for (int k = 0; k < 9; k++) SV<T>::st(D + k * p.plane + node, g[k]);
+}
+
+template <typename T, bool COLLIDE>
+__global__ void k_finish_shifted(const FinishParams p) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.nw) return;
+    finish_node_shifted<T, COLLIDE>(p, p.wnodes[t]);
+}
+
+template <typename T>
+__global__ void k_finish_batch_shifted(const FinishParams *__restrict__ fp, const int *__restrict__ phase,
+                                       const int4 *__restrict__ nodes, int n, int sel) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int4 c = nodes[t];
+    finish_node_shifted<T, true>(fp[2 * c.x + (sel ^ phase[c.x])], make_int2(c.y, c.z));
 }
 
 // In-place collision of shifted populations with the stored (FP64) rho/u/v:
@@ -257,6 +298,32 @@ cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool co
     const dim3 g((p.s.Nx + block.x - 1) / block.x, (p.s.Ny + block.y - 1) / block.y);
     if (store == STORE_F32) step_shifted_t<float>(p, flags, collide, g, block, s);
     else step_shifted_t<__half>(p, flags, collide, g, block, s);
+    return cudaGetLastError();
+}
+
+cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
+                               int ntiles, int sel, double *partials, int store, int grid,
+                               cudaStream_t s) {
+    if (ntiles == 0) return cudaSuccess;
+    if (store == STORE_F32) k_step_batch_shifted<float><<<grid, dim3(64, 4), 0, s>>>(sp, phase, tiles, ntiles, sel, partials);
+    else k_step_batch_shifted<__half><<<grid, dim3(64, 4), 0, s>>>(sp, phase, tiles, ntiles, sel, partials);
+    return cudaGetLastError();
+}
+
+int step_batch_shifted_grid(int store) {
+    int nb = 0, dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (store == STORE_F32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_batch_shifted<float>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_batch_shifted<__half>, 256, 0);
+    return nsm * (nb > 0 ? nb : 1);
+}
+
+cudaError_t finish_batch_shifted(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
+                                 int sel, int store, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    if (store == STORE_F32) k_finish_batch_shifted<float><<<(n + 127) / 128, 128, 0, s>>>(fp, phase, nodes, n, sel);
+    else k_finish_batch_shifted<__half><<<(n + 127) / 128, 128, 0, s>>>(fp, phase, nodes, n, sel);
     return cudaGetLastError();
 }
 

@@ -56,6 +56,17 @@ enum BCKind : int {
     BC_KIND_COUNT
 };
 
+// Impedance wall (time-domain impedance BC): per wall node of a bottom
+// regularized entry, a mass-spring-damper m v' + R v + K x = p' advanced once
+// per step with the exact zero-order-hold update of the 2x2 system, plus
+// running DFTs of p' and v at nf frequencies for eduction. Layout: field-major
+// [IMP_FIELDS + 6 nf][along] doubles.
+enum : int {
+    IMP_ACTIVE = 0, IMP_A11, IMP_A12, IMP_A21, IMP_A22, IMP_B1, IMP_B2, IMP_X, IMP_V, IMP_FIELDS
+};
+// per frequency f: phasor (re, im), sum p' e^{-i w n} (re, im), sum v e^{-i w n} (re, im)
+__host__ __device__ inline int imp_field(int f, int q) { return IMP_FIELDS + 6 * f + q; }
+
 __host__ __device__ inline bool bc_is_column(int kind) {
     return kind == BC_VEL_IN_ZH || kind == BC_VEL_OUT_ZH || kind == BC_PRES_IN_ZH ||
            kind == BC_PRES_OUT_ZH || kind == BC_CONV_IN || kind == BC_CONV_OUT ||
@@ -192,6 +203,34 @@ __device__ __forceinline__ void bc_regularized(A &a, const double w[9], int ib, 
         const double fr = (3.0 / 2.0) * w[k] * (Qxx * Pxx + 2.0 * Qxy * Pxy + Qyy * Pyy);
         a.set(ib, jb, k, fb[k] + fr);
     }
+}
+
+// One step of the impedance wall at position t of the line (FP64): pressure
+// p' = c_s^2 (rho_n - rho_ref) from the previous-step density of the interior
+// neighbour, state (x, v) <- A (x, v) + b p', DFT accumulation, and the wall-
+// normal velocity into the liner returned (the BC imposes u_y = -v).
+__device__ __forceinline__ double impedance_step(double *imp, int along, int nf, int t,
+                                                 double rho_n, double rho_ref,
+                                                 const double *cw, const double *sw) {
+#define IMP(f) imp[(size_t)(f) * along + t]
+    const double p = (rho_n - rho_ref) / 3.0;
+    const double x = IMP(IMP_X), v = IMP(IMP_V);
+    const double xn = IMP(IMP_A11) * x + IMP(IMP_A12) * v + IMP(IMP_B1) * p;
+    const double vn = IMP(IMP_A21) * x + IMP(IMP_A22) * v + IMP(IMP_B2) * p;
+    IMP(IMP_X) = xn;
+    IMP(IMP_V) = vn;
+    for (int f = 0; f < nf; f++) {
+        const double cr = IMP(imp_field(f, 0)), ci = IMP(imp_field(f, 1));
+        IMP(imp_field(f, 2)) += p * cr;
+        IMP(imp_field(f, 3)) += p * ci;
+        IMP(imp_field(f, 4)) += vn * cr;
+        IMP(imp_field(f, 5)) += vn * ci;
+        // advance the phasor e^{-i w n} by one step
+        IMP(imp_field(f, 0)) = cr * cw[f] + ci * sw[f];
+        IMP(imp_field(f, 1)) = ci * cw[f] - cr * sw[f];
+    }
+    return vn;
+#undef IMP
 }
 
 template <class A>
@@ -354,6 +393,10 @@ struct StageParams {
     long long plane;
     int kind, index, along;
     const double *val1, *val2;
+    double *imp;               // impedance-wall state or null
+    int imp_nf;
+    double imp_rho_ref;
+    double imp_cos[8], imp_sin[8];  // e^{-i w_f} per frequency
     const uint16_t *flags;
     const int *colbase, *rowbase;
     int nslots;

@@ -67,4 +67,25 @@ __device__ __forceinline__ void reduce2_grid(double a, double b, double *partial
     }
 }
 
+// Block reduction of two doubles, stored by thread 0 at out[0..1] (fixed order).
+__device__ __forceinline__ void block_reduce2_store(double a, double b, double *out) {
+    __shared__ double sa[32], sb[32];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nthr = blockDim.x * blockDim.y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if ((tid & 31) == 0) { sa[tid >> 5] = a; sb[tid >> 5] = b; }
+    __syncthreads();
+    if (tid == 0) {
+        double ra = 0.0, rb = 0.0;
+        for (int w = 0; w < (nthr + 31) / 32; w++) { ra += sa[w]; rb += sb[w]; }
+        out[0] = ra;
+        out[1] = rb;
+    }
+    __syncthreads();
+}
+
 }  // namespace lbm

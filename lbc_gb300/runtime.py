@@ -81,6 +81,14 @@ def _bind_ext(lib: C.CDLL) -> None:
         "lbm_gpu_force_history": (C.c_int, [vp, dp, C.c_int]),
         "lbm_gpu_get_info": (C.c_int, [vp, C.POINTER(Info)]),
         "lbm_gpu_set_block": (C.c_int, [vp, C.c_int, C.c_int]),
+        "lbm_gpu_batch_create": (C.c_int, [C.POINTER(vp), C.c_int, C.POINTER(vp)]),
+        "lbm_gpu_batch_run": (C.c_int, [vp, C.c_int]),
+        "lbm_gpu_batch_run_timed": (C.c_int, [vp, C.c_int, dp]),
+        "lbm_gpu_batch_info": (C.c_int, [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_int)]),
+        "lbm_gpu_batch_destroy": (C.c_int, [vp]),
+        "lbm_gpu_set_impedance_wall": (C.c_int, [vp, C.c_int, dp, dp, dp, C.c_int, dp, C.c_double]),
+        "lbm_gpu_impedance_readback": (C.c_int, [vp, C.c_int, dp, dp]),
+        "lbm_gpu_msd_zoh": (C.c_int, [C.c_double, C.c_double, C.c_double, dp, dp]),
         "lbm_gpu_host_alloc": (vp, [C.c_size_t]),
         "lbm_gpu_host_free": (None, [vp]),
         "lbm_gpu_dropin_release": (None, []),
@@ -214,6 +222,24 @@ class GpuSolver:
             raise RuntimeError(last_error())
         return out[:n]
 
+    def set_impedance_wall(self, entry: int, R, m, K, omegas=(), rho_ref: float = 1.0):
+        R, m, K = (np.ascontiguousarray(a, dtype=np.float64) for a in (R, m, K))
+        om = np.ascontiguousarray(omegas, dtype=np.float64)
+        self._imp = (R, m, K, om)
+        _check(self.lib.lbm_gpu_set_impedance_wall(self.h, entry, dptr(R), dptr(m), dptr(K), len(om),
+                                                   dptr(om) if len(om) else None, rho_ref),
+               "lbm_gpu_set_impedance_wall")
+
+    def impedance_readback(self, entry: int):
+        """(spectra[Nx, nf, 4], state[Nx, 2]) of the impedance wall on `entry`."""
+        nf = len(self._imp[3])
+        n = self.case.Nx
+        spec = np.zeros((n, max(nf, 1), 4))
+        state = np.zeros((n, 2))
+        _check(self.lib.lbm_gpu_impedance_readback(self.h, entry, dptr(spec), dptr(state)),
+               "lbm_gpu_impedance_readback")
+        return spec[:, :nf], state
+
     def info(self) -> Info:
         inf = Info()
         _check(self.lib.lbm_gpu_get_info(self.h, C.byref(inf)), "lbm_gpu_get_info")
@@ -221,3 +247,36 @@ class GpuSolver:
 
     def set_block(self, bx: int, by: int):
         _check(self.lib.lbm_gpu_set_block(self.h, bx, by), "lbm_gpu_set_block")
+
+
+class GpuBatch:
+    """Independent cases of one storage type advanced together (lbm_gpu_batch_*)."""
+
+    def __init__(self, solvers):
+        self.lib = load_library()
+        self.solvers = list(solvers)
+        arr = (C.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
+        h = C.c_void_p()
+        _check(self.lib.lbm_gpu_batch_create(arr, len(self.solvers), C.byref(h)), "lbm_gpu_batch_create")
+        self.h = h
+
+    def run(self, nsteps: int):
+        _check(self.lib.lbm_gpu_batch_run(self.h, nsteps), "lbm_gpu_batch_run")
+
+    def run_timed(self, nsteps: int) -> float:
+        ms = C.c_double(0.0)
+        _check(self.lib.lbm_gpu_batch_run_timed(self.h, nsteps, C.byref(ms)), "lbm_gpu_batch_run_timed")
+        return ms.value
+
+    def info(self):
+        n, l = C.c_longlong(), C.c_int()
+        _check(self.lib.lbm_gpu_batch_info(self.h, C.byref(n), C.byref(l)), "lbm_gpu_batch_info")
+        return n.value, l.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.lbm_gpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

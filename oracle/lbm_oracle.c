@@ -651,3 +651,76 @@ void orc_ext_main_lbm_moving(int Nx, int Ny, int Q, double *f, double *f_new, do
                             boundaries[b].val2, f, f_new, rho, u, v, solid_mask, cx, cy, w);
     orc_compute_macroscopic_fields(Nx, Ny, Q, f_new, solid_mask, cx, cy, rho, u, v, Fx, Fy);
 }
+
+/* ---------------------------------------------------------------- impedance wall
+ * Extension: per wall node a mass-spring-damper m v' + R v + K x = p' replaces
+ * the single host-side ADE of cases/nit/nit.c:13-47,276-303 (which drives one
+ * velocity for the whole outlet from the surface-averaged pressure). Each step,
+ * before main_lbm, the pressure p' = (rho - rho_ref)/3 of the node above the
+ * wall (previous-step density, as the regularized BC uses it) advances the
+ * node's state with the exact zero-order-hold update, and the new wall-normal
+ * velocity v (into the liner) goes to the bottom regularized BC as val2 = -v.
+ * Layout of `imp` (shared with the GPU engine): field-major, n entries per
+ * field: active, A11, A12, A21, A22, b1, b2, x, v, then per frequency
+ * (phasor re, im, sum p' e^{-iwn} re, im, sum v e^{-iwn} re, im). */
+enum { OI_ACT, OI_A11, OI_A12, OI_A21, OI_A22, OI_B1, OI_B2, OI_X, OI_V, OI_N };
+
+int orc_ext_msd_zoh(double R, double m, double K, double *A, double *b) {
+    if (!(m > 0.0) || !(K > 0.0) || !(R >= 0.0)) return 0;
+    double km = K / m, rm = R / m;
+    double a = -0.5 * rm;
+    double d2 = a * a - km;
+    double E0, E1;
+    if (d2 > 0.0) {
+        double d = sqrt(d2);
+        double ep = exp(a + d), em = exp(a - d);
+        E0 = 0.5 * (ep + em);
+        E1 = 0.5 * (ep - em) / d;
+    } else if (d2 < 0.0) {
+        double wd = sqrt(-d2), ea = exp(a);
+        E0 = ea * cos(wd);
+        E1 = ea * sin(wd) / wd;
+    } else {
+        E0 = exp(a);
+        E1 = exp(a);
+    }
+    A[0] = E0 + E1 * (0.0 - a);
+    A[1] = E1 * 1.0;
+    A[2] = E1 * (-km);
+    A[3] = E0 + E1 * (-rm - a);
+    double q1 = A[1] / m, q2 = (A[3] - 1.0) / m;
+    b[0] = (-rm * q1 - q2) / km;
+    b[1] = q1;
+    return 1;
+}
+
+/* One step of every wall node; val2_out = -v on active nodes, val2_in
+ * elsewhere. rho is the stored [Ny][Nx] density, the wall row is `index`. */
+void orc_ext_impedance_step(int Nx, int index, const double *rho, double rho_ref, double *imp,
+                            int nf, const double *cw, const double *sw, const int *solid_mask,
+                            const double *val2_in, double *val2_out) {
+    int n = Nx;
+#define OIMP(f, t) imp[(size_t)(f) * (size_t)n + (size_t)(t)]
+    for (int t = 0; t < n; t++) {
+        val2_out[t] = val2_in ? val2_in[t] : 0.0;
+        if (OIMP(OI_ACT, t) == 0.0 || solid_mask[nid(Nx, index, t)]) continue;
+        double p = (rho[nid(Nx, index + 1, t)] - rho_ref) / 3.0;
+        double x = OIMP(OI_X, t), v = OIMP(OI_V, t);
+        double xn = OIMP(OI_A11, t) * x + OIMP(OI_A12, t) * v + OIMP(OI_B1, t) * p;
+        double vn = OIMP(OI_A21, t) * x + OIMP(OI_A22, t) * v + OIMP(OI_B2, t) * p;
+        OIMP(OI_X, t) = xn;
+        OIMP(OI_V, t) = vn;
+        for (int f = 0; f < nf; f++) {
+            int b0 = OI_N + 6 * f;
+            double cr = OIMP(b0, t), ci = OIMP(b0 + 1, t);
+            OIMP(b0 + 2, t) += p * cr;
+            OIMP(b0 + 3, t) += p * ci;
+            OIMP(b0 + 4, t) += vn * cr;
+            OIMP(b0 + 5, t) += vn * ci;
+            OIMP(b0, t) = cr * cw[f] + ci * sw[f];
+            OIMP(b0 + 1, t) = ci * cw[f] - cr * sw[f];
+        }
+        val2_out[t] = -vn;
+    }
+#undef OIMP
+}

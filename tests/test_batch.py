@@ -1,0 +1,78 @@
+"""Batches: many uneven cases advanced by one persistent kernel per step must
+each end exactly as when run alone (populations bit for bit; forces, summed
+per tile instead of per block, to round-off)."""
+import numpy as np
+import pytest
+
+import casezoo
+from conftest import same
+from lbc_gb300 import cases
+
+pytestmark = pytest.mark.gpu
+FIELDS = ("f", "f_new", "rho", "u", "v")
+MIX = ["zoo_ibb", "zoo_convective_chain", "zoo_zh_mixed", "taylor_green", "poiseuille",
+       "zoo_periodic_late", "zoo_pressure_reg", "cylinder_wake_small", "zoo_open_edges", "liner"]
+
+
+def _build(n):
+    if n == "liner":
+        from lbc_gb300 import impedance as imp
+        p = imp.LinerParams(nx=200, ny=28, mach=0.2, R=1.1 * imp.CS, m=4e-3, f_res=0.06)
+        return imp.liner_duct(p), p
+    return casezoo.build(n)[0], None
+
+
+def _solvers(storage, names):
+    from lbc_gb300 import GpuSolver
+    from lbc_gb300 import impedance as imp
+    out = []
+    for n in names:
+        (case, st), lp = _build(n)
+        s = GpuSolver(case, storage)
+        if lp is not None:
+            s.set_impedance_wall(imp.LINER_ENTRY, *imp.liner_arrays(lp), imp.TRACKED_OMEGAS)
+        try:
+            s.enable_force_history(64)
+        except RuntimeError:
+            pass
+        s.set_state(st)
+        out.append((n, case, st, s))
+    return out
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32", "f16"])
+@pytest.mark.parametrize("chunks", [[37], [1, 20, 9]])
+def test_batch_equals_alone(storage, chunks):
+    from lbc_gb300 import STORAGE, GpuBatch
+    alone = _solvers(STORAGE[storage], MIX)
+    mixed = _solvers(STORAGE[storage], MIX)
+    for _, _, _, s in alone:
+        for c in chunks:
+            s.run(c)
+    b = GpuBatch([s for _, _, _, s in mixed])
+    for c in chunks:
+        b.run(c)
+    total = sum(chunks)
+    for (n, case, _, sa), (_, _, _, sb) in zip(alone, mixed):
+        a, m = sa.get_state(), sb.get_state()
+        for fld in FIELDS:
+            assert same(getattr(a, fld), getattr(m, fld)), (storage, n, fld)
+        if n == "liner":
+            from lbc_gb300 import impedance as imp
+            sa_, ta_ = sa.impedance_readback(imp.LINER_ENTRY)
+            sb_, tb_ = sb.impedance_readback(imp.LINER_ENTRY)
+            assert same(sa_, sb_) and same(ta_, tb_), (storage, n, "impedance wall")
+        ha, hb = sa.force_history(total), sb.force_history(total)
+        assert ha.shape == hb.shape
+        if ha.size:
+            assert np.max(np.abs(ha - hb)) <= 1e-12 * max(1.0, float(np.max(np.abs(ha))))
+
+
+def test_batch_info_counts_launches():
+    from lbc_gb300 import GpuBatch, F32_SHIFTED
+    mixed = _solvers(F32_SHIFTED, MIX)
+    b = GpuBatch([s for _, _, _, s in mixed])
+    nodes, lps = b.info()
+    assert nodes == sum(c.nodes for _, c, _, _ in mixed)
+    max_stages = max(s.info().edge_stages for _, _, _, s in mixed)
+    assert lps == 1 + max_stages + 2

@@ -63,6 +63,10 @@ typedef struct {
 
 const char *lbm_gpu_last_error(void);
 int lbm_gpu_device_count(void);
+/* How kernels can reach host memory at p: 1 page-locked and mapped at the
+ * same address, 2 any pageable memory (the device walks the host page tables,
+ * e.g. over NVLink-C2C), 0 neither (copies only), -1 no device. */
+int lbm_gpu_host_access(const void *p);
 
 int lbm_gpu_create(const lbm_gpu_case *c, lbm_gpu_solver **out);
 int lbm_gpu_destroy(lbm_gpu_solver *s);
@@ -95,14 +99,19 @@ int lbm_gpu_force_history(lbm_gpu_solver *s, double *xy, int max_steps);
  * replaces the host-side ADE coupling of lbc's cases/nit/nit.c:276-303).
  * Boundary entry `entry` must be velocity_bottom_regularized. Each of its
  * nodes with m[i] > 0 carries a mass-spring-damper m v' + R v + K x = p'
- * (FP64 state, exact zero-order-hold update per step) driven by
- * p' = (rho - rho_ref) / 3 of the interior neighbour at the previous step; the
- * BC then imposes u_y = -v (v > 0: flow into the liner) and u_x = val1[i].
+ * (FP64 state, exact zero-order-hold update per step) driven by the pressure
+ * fluctuation p' = (rho - rhobar) / 3 of the interior neighbour at the
+ * previous step, where rhobar starts at rho_ref and follows rho as an
+ * exponential average, rhobar += alpha (rho - rhobar) (alpha = 0: fixed
+ * reference; alpha > 0 keeps the mean-flow static pressure from loading the
+ * spring); the BC then imposes u_y = -v (v > 0: flow into the liner) and
+ * u_x = val1[i].
  * Nodes with m[i] <= 0 keep the entry's own val2. Running DFTs of p' and v at
  * nf <= 8 angular frequencies (rad / step) are kept per node. Arrays have Nx
  * entries. */
 int lbm_gpu_set_impedance_wall(lbm_gpu_solver *s, int entry, const double *R, const double *m,
-                               const double *K, int nf, const double *omegas, double rho_ref);
+                               const double *K, int nf, const double *omegas, double rho_ref,
+                               double alpha);
 /* spectra[(i * nf + f) * 4 + q]: q = 0,1 sum p' e^{-i w n} (re, im); q = 2,3 the
  * same for v. state[2 i + {0,1}] = (x, v). Either pointer may be NULL. */
 int lbm_gpu_impedance_readback(lbm_gpu_solver *s, int entry, double *spectra, double *state);
@@ -139,6 +148,10 @@ void lbm_gpu_host_free(void *p);
  * caller's array pointers. Call this after changing solid_mask, omega_eff or
  * phi in place; it also frees those buffers. */
 void lbm_gpu_dropin_release(void);
+/* main_lbm streams the caller's arrays through its kernels when the device can
+ * reach them (lbm_gpu_host_access > 0) and stages them through copies
+ * otherwise; staged = 1 forces the copies (both give identical results). */
+void lbm_gpu_dropin_set_staged(int staged);
 
 #ifdef __cplusplus
 }

@@ -112,6 +112,7 @@ struct DropinEntry {
     std::unique_ptr<Solver> solver;
 };
 std::vector<DropinEntry> g_cache;
+bool g_force_staged = false;
 
 }  // namespace
 
@@ -216,9 +217,19 @@ void main_lbm(int Nx, int Ny, int Q, double *f, double *f_new, double *rho, doub
     for (int b = 0; b < num_boundaries; b++)
         if (!s->set_bc_values(b, boundaries[b].val1, boundaries[b].val2)) return report("main_lbm");
     double fx = 0.0, fy = 0.0;
-    if (!s->set_state(f, f_new, rho, u, v) || !s->run(1) || !s->get_state(f_new, f, rho, u, v) ||
-        !s->forces(&fx, &fy))
+    // GB300: when the device can reach the caller's arrays (page-locked, or any
+    // pageable memory through the NVLink-C2C address translation), the kernels
+    // stream them directly; otherwise stage them through copies.
+    const bool direct = !g_force_staged && lbm_gpu_host_access(f) > 0 &&
+                        lbm_gpu_host_access(f_new) > 0 && lbm_gpu_host_access(rho) > 0 &&
+                        lbm_gpu_host_access(u) > 0 && lbm_gpu_host_access(v) > 0;
+    if (direct) {
+        if (!s->dropin_step_direct(f, f_new, rho, u, v) || !s->forces(&fx, &fy)) return report("main_lbm");
+    } else if (!s->set_state(f, f_new, rho, u, v, s->needs_old_dst()) || !s->run(1) ||
+               !s->get_state(f_new, f, rho, u, v) ||
+               !s->forces(&fx, &fy)) {
         return report("main_lbm");
+    }
     if (D) *D = fx;
     if (L) *L = fy;
 }
@@ -564,6 +575,21 @@ struct lbm_gpu_solver {
 
 const char *lbm_gpu_last_error(void) { return last_error(); }
 
+int lbm_gpu_host_access(const void *p) {
+    int dev = 0, pageable = 0, via_tables = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+    cudaDeviceGetAttribute(&via_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+    if (p) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+            a.devicePointer == p)
+            return 1;
+        cudaGetLastError();
+    }
+    return (pageable && via_tables) ? 2 : 0;
+}
+
 int lbm_gpu_device_count(void) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
@@ -667,10 +693,11 @@ int lbm_gpu_force_history(lbm_gpu_solver *s, double *xy, int max_steps) {
 }
 
 int lbm_gpu_set_impedance_wall(lbm_gpu_solver *s, int entry, const double *R, const double *m,
-                               const double *K, int nf, const double *omegas, double rho_ref) {
+                               const double *K, int nf, const double *omegas, double rho_ref,
+                               double alpha) {
     SOLVER_OR_FAIL(s);
     if (!R || !m || !K || (nf > 0 && !omegas)) { set_error("null array"); return LBM_GPU_ERR_ARG; }
-    return s->s->set_impedance(entry, R, m, K, nf, omegas, rho_ref) ? LBM_GPU_OK : LBM_GPU_ERR_ARG;
+    return s->s->set_impedance(entry, R, m, K, nf, omegas, rho_ref, alpha) ? LBM_GPU_OK : LBM_GPU_ERR_ARG;
 }
 
 int lbm_gpu_impedance_readback(lbm_gpu_solver *s, int entry, double *spectra, double *state) {
@@ -767,6 +794,11 @@ void *lbm_gpu_host_alloc(size_t bytes) {
 
 void lbm_gpu_host_free(void *p) {
     if (p) cudaFreeHost(p);
+}
+
+void lbm_gpu_dropin_set_staged(int staged) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_force_staged = staged != 0;
 }
 
 void lbm_gpu_dropin_release(void) {

@@ -262,6 +262,7 @@ bool Solver::build_geometry() {
         }
     }
     has_flags_ = any_special || !stages_.empty() || !d_.px || !d_.py;
+    needs_old_dst_ = any_special;  // solid nodes or off-grid pull sources
     wnodes_host_ = wnodes;
     has_links_ = want_links && !links.empty();
     has_mem_ = any_solid_link;
@@ -352,12 +353,15 @@ bool Solver::set_bc_values(int entry, const double *val1, const double *val2) {
 }
 
 bool Solver::set_state(const double *f, const double *f_new, const double *rho, const double *u,
-                       const double *v) {
+                       const double *v, bool fnew_needed) {
     const int Nx = d_.Nx, Ny = d_.Ny;
     const size_t N = (size_t)Nx * Ny;
     cur_ = 0;
     const double *src[2] = {f, f_new};
     for (int b = 0; b < 2; b++) {
+        // The drop-in skips f_new when its old content cannot reach the
+        // results (no solid nodes, no off-grid pull sources).
+        if (b == 1 && !fnew_needed) continue;
         CK(cudaMemcpyAsync(d_stage_, src[b], N * 9 * sizeof(double), cudaMemcpyHostToDevice, stream_));
         CK(launch::aos_to_soa(d_stage_, buf_[b], d_.store, Nx, Ny, pitch_, plane_, d_.w, stream_));
     }
@@ -381,6 +385,44 @@ bool Solver::get_state(double *f, double *f_new, double *rho, double *u, double 
         CK(cudaMemcpyAsync(dst[b], d_stage_, N * 9 * sizeof(double), cudaMemcpyDeviceToHost, stream_));
     }
     if (!get_fields(rho, u, v)) return false;
+    CK(cudaStreamSynchronize(stream_));
+    return true;
+}
+
+bool Solver::dropin_step_direct(double *f, double *f_new, double *rho, double *u, double *v) {
+    if (d_.store != STORE_F64) {
+        set_error("direct drop-in step needs FP64 storage");
+        return false;
+    }
+    const int Nx = d_.Nx, Ny = d_.Ny;
+    cur_ = 0;
+    if (nslots_ > 0)
+        CK(launch::seed_band(d_seed_nodes_, d_seed_slots_, nseed_, Nx, rho, u, v, d_bandm_[parity_],
+                             nslots_, stream_));
+    CollideAosParams c;
+    std::memset(&c, 0, sizeof c);
+    c.Nx = Nx; c.Ny = Ny; c.pitch = pitch_; c.plane = plane_;
+    c.f_aos = f;
+    c.soa = (double *)buf_[0];
+    c.flags = d_flags_;
+    c.rho = rho; c.ux = u; c.uy = v;
+    c.omega = d_omega_; c.omega0 = omega0_;
+    c.has_force = (d_.Fx != 0.0 || d_.Fy != 0.0);
+    c.Fx = d_.Fx; c.Fy = d_.Fy;
+    for (int k = 0; k < 9; k++) c.w[k] = d_.w[k];
+    CK(launch::collide_aos_exact(c, stream_));
+    // Without solid nodes or off-grid pull sources every slot of f_new is
+    // rewritten before it is read, so its old content is not needed.
+    if (needs_old_dst_)
+        CK(launch::aos_to_soa(f_new, buf_[1], STORE_F64, Nx, Ny, pitch_, plane_, d_.w, stream_));
+    macro_out_[0] = rho; macro_out_[1] = u; macro_out_[2] = v;
+    const bool okk = launch_step(0, 1, false, true, parity_);
+    macro_out_[0] = macro_out_[1] = macro_out_[2] = nullptr;
+    if (!okk) return false;
+    CK(launch::soa_to_aos(buf_[1], f_new, STORE_F64, Nx, Ny, pitch_, plane_, d_.w, stream_));
+    cur_ = 1;
+    parity_ ^= 1;
+    steps_done_ += 1;
     CK(cudaStreamSynchronize(stream_));
     return true;
 }
@@ -473,7 +515,9 @@ StepParams Solver::step_params(int src, int dst, bool write_macro, int bparity) 
     p.Fx = d_.Fx; p.Fy = d_.Fy; p.hFx = 0.5 * d_.Fx; p.hFy = 0.5 * d_.Fy;
     for (int k = 0; k < 9; k++) p.w[k] = d_.w[k];
     p.write_macro = write_macro ? 1 : 0;
-    p.rho = d_rho_; p.ux = d_ux_; p.uy = d_uy_;
+    p.rho = macro_out_[0] ? macro_out_[0] : d_rho_;
+    p.ux = macro_out_[1] ? macro_out_[1] : d_ux_;
+    p.uy = macro_out_[2] ? macro_out_[2] : d_uy_;
     p.colbase = d_colbase_; p.rowbase = d_rowbase_; p.nslots = nslots_;
     p.bandf = d_bandf_;
     p.bandm_next = nslots_ ? d_bandm_[bparity ^ 1] : nullptr;
@@ -507,7 +551,7 @@ StageParams Solver::stage_params(const Stage &st, int src, int bparity) const {
     for (int k = 0; k < 9; k++) s.w[k] = d_.w[k];
     s.imp = st.d_imp;
     s.imp_nf = st.imp_nf;
-    s.imp_rho_ref = st.imp_rho_ref;
+    s.imp_alpha = st.imp_alpha;
     for (int f = 0; f < 8; f++) {
         s.imp_cos[f] = st.imp_cos[f];
         s.imp_sin[f] = st.imp_sin[f];
@@ -550,12 +594,16 @@ bool msd_zoh(double R, double m, double K, double A[4], double b[2]) {
 }
 
 bool Solver::set_impedance(int entry, const double *R, const double *m, const double *K, int nf,
-                           const double *omegas, double rho_ref) {
+                           const double *omegas, double rho_ref, double alpha) {
     Stage *st = nullptr;
     for (Stage &x : stages_)
         if (x.entry == entry) st = &x;
     if (!st || st->kind != BC_VEL_BOT_REG) {
         set_error("impedance wall: entry must be a velocity_bottom_regularized Boundary entry");
+        return false;
+    }
+    if (!(alpha >= 0.0 && alpha < 1.0)) {
+        set_error("impedance wall: alpha must be in [0, 1)");
         return false;
     }
     if (nf < 0 || nf > 8) {
@@ -579,6 +627,7 @@ bool Solver::set_impedance(int entry, const double *R, const double *m, const do
         h[(size_t)IMP_A22 * n + t] = A[3];
         h[(size_t)IMP_B1 * n + t] = b[0];
         h[(size_t)IMP_B2 * n + t] = b[1];
+        h[(size_t)IMP_RHOBAR * n + t] = rho_ref;
         for (int f = 0; f < nf; f++) h[(size_t)imp_field(f, 0) * n + t] = 1.0;
     }
     if (!st->d_imp || st->imp_nf != nf) {
@@ -587,7 +636,7 @@ bool Solver::set_impedance(int entry, const double *R, const double *m, const do
     CK(cudaMemcpyAsync(st->d_imp, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, stream_));
     CK(cudaStreamSynchronize(stream_));
     st->imp_nf = nf;
-    st->imp_rho_ref = rho_ref;
+    st->imp_alpha = alpha;
     for (int f = 0; f < nf; f++) {
         st->imp_cos[f] = std::cos(omegas[f]);
         st->imp_sin[f] = std::sin(omegas[f]);
@@ -633,7 +682,9 @@ FinishParams Solver::finish_params(int dst, bool write_macro, int bparity) const
     f.Fx = d_.Fx; f.Fy = d_.Fy; f.hFx = 0.5 * d_.Fx; f.hFy = 0.5 * d_.Fy;
     for (int k = 0; k < 9; k++) f.w[k] = d_.w[k];
     f.write_macro = write_macro ? 1 : 0;
-    f.rho = d_rho_; f.ux = d_ux_; f.uy = d_uy_;
+    f.rho = macro_out_[0] ? macro_out_[0] : d_rho_;
+    f.ux = macro_out_[1] ? macro_out_[1] : d_ux_;
+    f.uy = macro_out_[2] ? macro_out_[2] : d_uy_;
     return f;
 }
 

@@ -44,7 +44,7 @@ struct Stage {
     // impedance wall (bottom regularized entries only)
     double *d_imp = nullptr;
     int imp_nf = 0;
-    double imp_rho_ref = 1.0;
+    double imp_alpha = 0.0;
     double imp_cos[8] = {1, 1, 1, 1, 1, 1, 1, 1}, imp_sin[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
@@ -61,9 +61,16 @@ class Solver {
     // Host arrays in lbc's layout. set_state makes buf[cur] = f and the other
     // buffer = f_new, and takes rho/u/v as the stored fields of the next step.
     bool set_state(const double *f, const double *f_new, const double *rho, const double *u,
-                   const double *v);
+                   const double *v, bool fnew_needed = true);
     bool get_state(double *f, double *f_new, double *rho, double *u, double *v);
     bool get_fields(double *rho, double *u, double *v);
+    // One lbc main_lbm call on the caller's arrays when the device can reach
+    // them directly (page-locked, or pageable over NVLink-C2C address
+    // translation): the kernels read and write the host arrays themselves.
+    bool dropin_step_direct(double *f, double *f_new, double *rho, double *u, double *v);
+    // Whether the old content of f_new can reach the results (solid nodes, or
+    // populations pulled from off a non-periodic edge).
+    bool needs_old_dst() const { return needs_old_dst_; }
     bool set_bc_values(int entry, const double *val1, const double *val2);
     bool upload_all_bc_values();
     // n time steps, each equivalent to one main_lbm call plus the caller's swap.
@@ -106,9 +113,10 @@ class Solver {
     int hist_cap() const { return hist_cap_; }
     // Impedance wall on Boundary entry `entry` (velocity_bottom_regularized):
     // per node R, m, K (m <= 0: keep the entry's own val2), nf <= 8 DFT
-    // frequencies (rad / step), reference density for p'.
+    // frequencies (rad / step), reference density for p' and the rate of its
+    // running average (0: fixed).
     bool set_impedance(int entry, const double *R, const double *m, const double *K, int nf,
-                       const double *omegas, double rho_ref);
+                       const double *omegas, double rho_ref, double alpha);
     // out[((t * nf) + f) * 4 + {0,1,2,3}] = (P re, P im, V re, V im); state[t*2+{0,1}] = (x, v)
     bool impedance_readback(int entry, double *out, double *state);
     bool begin_steps(cudaStream_t s);
@@ -166,6 +174,8 @@ class Solver {
     long long steps_done_ = 0;
     std::vector<void *> allocs_;
     std::vector<int2> wnodes_host_;
+    bool needs_old_dst_ = true;
+    double *macro_out_[3] = {nullptr, nullptr, nullptr};  // moments written here when set
 };
 
 // Many independent cases of one storage type advanced together: per step one

@@ -23,6 +23,23 @@ struct CollideParams {
     double w[9];
 };
 
+// Collision that reads lbc's AoS populations where they are (host memory the
+// device can reach, or device memory), writes the post-collision values back in
+// place and into the device SoA planes.
+struct CollideAosParams {
+    int Nx, Ny, pitch;
+    long long plane;
+    double *f_aos;                   // [Ny][Nx][9], read and written in place
+    double *soa;                     // device planes (FP64)
+    const uint16_t *flags;
+    const double *rho, *ux, *uy;     // stored fields [Ny][Nx] (host or device)
+    const double *omega;
+    double omega0;
+    int has_force;
+    double Fx, Fy;
+    double w[9];
+};
+
 // Arguments of lbc's standalone functions on device copies of lbc's AoS arrays.
 struct AosArgs {
     int Nx, Ny, px, py;
@@ -64,6 +81,7 @@ cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block
 cudaError_t stage(const StageParams &p, int store, cudaStream_t s);
 cudaError_t finish_exact(const FinishParams &p, bool collide, cudaStream_t s);
 cudaError_t collide_exact(const CollideParams &p, cudaStream_t s);
+cudaError_t collide_aos_exact(const CollideAosParams &p, cudaStream_t s);
 cudaError_t aos_to_soa(const double *aos, void *soa, int store, int Nx, int Ny, int pitch,
                        long long plane, const double w[9], cudaStream_t s);
 cudaError_t soa_to_aos(const void *soa, double *aos, int store, int Nx, int Ny, int pitch,

@@ -186,7 +186,7 @@ __device__ __forceinline__ void stage_point(const StageParams &p, int t) {
         // Impedance wall on this node: the regularized bottom BC with the
         // normal velocity from the node's mass-spring-damper.
         const double vn = impedance_step(p.imp, p.along, p.imp_nf, t, a.rho(t, p.index + 1),
-                                         p.imp_rho_ref, p.imp_cos, p.imp_sin);
+                                         p.imp_alpha, p.imp_cos, p.imp_sin);
         bc_regularized(a, p.w, t, p.index, t, p.index + 1, false, p.val1[t], -vn);
         return;
     }
@@ -302,6 +302,38 @@ __global__ void k_collide_exact(const CollideParams p) {
     collide_exact(f, p.w, p.rho[dn], p.ux[dn], p.uy[dn], om, p.has_force != 0, p.Fx, p.Fy);
 #pragma unroll
     for (int k = 0; k < 9; k++) p.f[k * p.plane + node] = f[k];
+}
+
+// Collision over lbc's AoS array in place (src/core/collision.c:18-40), with the
+// result also stored in the device SoA planes. Blocks stage 128 consecutive
+// nodes through shared memory so the AoS traffic (over NVLink-C2C when the
+// array is host memory) is one contiguous run per block.
+__global__ void __launch_bounds__(128) k_collide_aos_exact(const CollideAosParams p) {
+    __shared__ double tile[128 * 9];
+    const long long n0 = (long long)blockIdx.x * 128;
+    const long long N = (long long)p.Nx * p.Ny;
+    const int cnt = (int)min((long long)128, N - n0);
+    for (int e = threadIdx.x; e < cnt * 9; e += blockDim.x) tile[e] = p.f_aos[n0 * 9 + e];
+    __syncthreads();
+    const int r = threadIdx.x;
+    if (r < cnt) {
+        const long long n = n0 + r;
+        const int j = (int)(n / p.Nx), i = (int)(n - (long long)j * p.Nx);
+        const long long node = (long long)j * p.pitch + i;
+        double f[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) f[k] = tile[r * 9 + k];
+        if (!(p.flags && (p.flags[node] & NF_SOLID))) {
+            const double om = p.omega ? p.omega[n] : p.omega0;
+            collide_exact(f, p.w, p.rho[n], p.ux[n], p.uy[n], om, p.has_force != 0, p.Fx, p.Fy);
+#pragma unroll
+            for (int k = 0; k < 9; k++) tile[r * 9 + k] = f[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 9; k++) p.soa[k * p.plane + node] = f[k];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < cnt * 9; e += blockDim.x) p.f_aos[n0 * 9 + e] = tile[e];
 }
 
 // ---------------------------------------------------------------- transposes
@@ -619,6 +651,12 @@ cudaError_t finish_exact(const FinishParams &p, bool collide, cudaStream_t s) {
 cudaError_t collide_exact(const CollideParams &p, cudaStream_t s) {
     const dim3 b(64, 4);
     k_collide_exact<<<grid2(p.Nx, p.Ny, b), b, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t collide_aos_exact(const CollideAosParams &p, cudaStream_t s) {
+    const long long N = (long long)p.Nx * p.Ny;
+    k_collide_aos_exact<<<(unsigned)((N + 127) / 128), 128, 0, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -62,7 +62,8 @@ enum BCKind : int {
 // running DFTs of p' and v at nf frequencies for eduction. Layout: field-major
 // [IMP_FIELDS + 6 nf][along] doubles.
 enum : int {
-    IMP_ACTIVE = 0, IMP_A11, IMP_A12, IMP_A21, IMP_A22, IMP_B1, IMP_B2, IMP_X, IMP_V, IMP_FIELDS
+    IMP_ACTIVE = 0, IMP_A11, IMP_A12, IMP_A21, IMP_A22, IMP_B1, IMP_B2, IMP_X, IMP_V, IMP_RHOBAR,
+    IMP_FIELDS
 };
 // per frequency f: phasor (re, im), sum p' e^{-i w n} (re, im), sum v e^{-i w n} (re, im)
 __host__ __device__ inline int imp_field(int f, int q) { return IMP_FIELDS + 6 * f + q; }
@@ -206,14 +207,19 @@ __device__ __forceinline__ void bc_regularized(A &a, const double w[9], int ib, 
 }
 
 // One step of the impedance wall at position t of the line (FP64): pressure
-// p' = c_s^2 (rho_n - rho_ref) from the previous-step density of the interior
-// neighbour, state (x, v) <- A (x, v) + b p', DFT accumulation, and the wall-
-// normal velocity into the liner returned (the BC imposes u_y = -v).
+// fluctuation p' = c_s^2 (rho_n - rhobar) from the previous-step density of the
+// interior neighbour and the node's running mean density rhobar (an
+// exponential average with rate alpha; alpha = 0 keeps the fixed reference the
+// wall was set up with), state (x, v) <- A (x, v) + b p', DFT accumulation,
+// and the wall-normal velocity into the liner returned (the BC imposes
+// u_y = -v).
 __device__ __forceinline__ double impedance_step(double *imp, int along, int nf, int t,
-                                                 double rho_n, double rho_ref,
+                                                 double rho_n, double alpha,
                                                  const double *cw, const double *sw) {
 #define IMP(f) imp[(size_t)(f) * along + t]
-    const double p = (rho_n - rho_ref) / 3.0;
+    const double rb = IMP(IMP_RHOBAR);
+    const double p = (rho_n - rb) / 3.0;
+    IMP(IMP_RHOBAR) = rb + alpha * (rho_n - rb);
     const double x = IMP(IMP_X), v = IMP(IMP_V);
     const double xn = IMP(IMP_A11) * x + IMP(IMP_A12) * v + IMP(IMP_B1) * p;
     const double vn = IMP(IMP_A21) * x + IMP(IMP_A22) * v + IMP(IMP_B2) * p;
@@ -395,7 +401,7 @@ struct StageParams {
     const double *val1, *val2;
     double *imp;               // impedance-wall state or null
     int imp_nf;
-    double imp_rho_ref;
+    double imp_alpha;
     double imp_cos[8], imp_sin[8];  // e^{-i w_f} per frequency
     const uint16_t *flags;
     const int *colbase, *rowbase;

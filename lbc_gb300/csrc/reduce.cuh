@@ -4,6 +4,17 @@
 
 namespace lbm {
 
+// Warp sum of two doubles into lane 0. Warps where every lane holds zero (no
+// wall link: most of the grid) skip the FP64 shuffles, which are slow on GB300.
+__device__ __forceinline__ void warp_reduce2(double &a, double &b) {
+    if (!__any_sync(0xffffffffu, a != 0.0 || b != 0.0)) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+}
+
 // Deterministic block + grid reduction of two doubles. Every thread of every
 // block must call it. Blocks write partials; the last block to arrive sums them
 // in block order and writes out[0..1] (and, when a history ring is given, the
@@ -17,11 +28,7 @@ __device__ __forceinline__ void reduce2_grid(double a, double b, double *partial
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const int nthr = blockDim.x * blockDim.y;
     const int lane = tid & 31, warp = tid >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, o);
-        b += __shfl_down_sync(0xffffffffu, b, o);
-    }
+    warp_reduce2(a, b);
     if (lane == 0) { sa[warp] = a; sb[warp] = b; }
     __syncthreads();
     const int nblk = gridDim.x * gridDim.y;
@@ -72,11 +79,7 @@ __device__ __forceinline__ void block_reduce2_store(double a, double b, double *
     __shared__ double sa[32], sb[32];
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const int nthr = blockDim.x * blockDim.y;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, o);
-        b += __shfl_down_sync(0xffffffffu, b, o);
-    }
+    warp_reduce2(a, b);
     if ((tid & 31) == 0) { sa[tid >> 5] = a; sb[tid >> 5] = b; }
     __syncthreads();
     if (tid == 0) {

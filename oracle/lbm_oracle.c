@@ -661,9 +661,11 @@ void orc_ext_main_lbm_moving(int Nx, int Ny, int Q, double *f, double *f_new, do
  * node's state with the exact zero-order-hold update, and the new wall-normal
  * velocity v (into the liner) goes to the bottom regularized BC as val2 = -v.
  * Layout of `imp` (shared with the GPU engine): field-major, n entries per
- * field: active, A11, A12, A21, A22, b1, b2, x, v, then per frequency
- * (phasor re, im, sum p' e^{-iwn} re, im, sum v e^{-iwn} re, im). */
-enum { OI_ACT, OI_A11, OI_A12, OI_A21, OI_A22, OI_B1, OI_B2, OI_X, OI_V, OI_N };
+ * field: active, A11, A12, A21, A22, b1, b2, x, v, mean density, then per
+ * frequency (phasor re, im, sum p' e^{-iwn} re, im, sum v e^{-iwn} re, im).
+ * p' is taken about the node's running mean density, rhobar += alpha (rho -
+ * rhobar) (alpha = 0: fixed reference). */
+enum { OI_ACT, OI_A11, OI_A12, OI_A21, OI_A22, OI_B1, OI_B2, OI_X, OI_V, OI_RHOBAR, OI_N };
 
 int orc_ext_msd_zoh(double R, double m, double K, double *A, double *b) {
     if (!(m > 0.0) || !(K > 0.0) || !(R >= 0.0)) return 0;
@@ -696,7 +698,7 @@ int orc_ext_msd_zoh(double R, double m, double K, double *A, double *b) {
 
 /* One step of every wall node; val2_out = -v on active nodes, val2_in
  * elsewhere. rho is the stored [Ny][Nx] density, the wall row is `index`. */
-void orc_ext_impedance_step(int Nx, int index, const double *rho, double rho_ref, double *imp,
+void orc_ext_impedance_step(int Nx, int index, const double *rho, double alpha, double *imp,
                             int nf, const double *cw, const double *sw, const int *solid_mask,
                             const double *val2_in, double *val2_out) {
     int n = Nx;
@@ -704,7 +706,10 @@ void orc_ext_impedance_step(int Nx, int index, const double *rho, double rho_ref
     for (int t = 0; t < n; t++) {
         val2_out[t] = val2_in ? val2_in[t] : 0.0;
         if (OIMP(OI_ACT, t) == 0.0 || solid_mask[nid(Nx, index, t)]) continue;
-        double p = (rho[nid(Nx, index + 1, t)] - rho_ref) / 3.0;
+        double rn = rho[nid(Nx, index + 1, t)];
+        double rb = OIMP(OI_RHOBAR, t);
+        double p = (rn - rb) / 3.0;
+        OIMP(OI_RHOBAR, t) = rb + alpha * (rn - rb);
         double x = OIMP(OI_X, t), v = OIMP(OI_V, t);
         double xn = OIMP(OI_A11, t) * x + OIMP(OI_A12, t) * v + OIMP(OI_B1, t) * p;
         double vn = OIMP(OI_A21, t) * x + OIMP(OI_A22, t) * v + OIMP(OI_B2, t) * p;

@@ -47,12 +47,20 @@ def fixture(name):
     return np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
 
 
+@pytest.mark.parametrize("staged", [False, True])
 @pytest.mark.parametrize("name", NAMES)
-def test_dropin_main_lbm_matches_lbc(gpu, oracle, name):
-    """lbc's main_lbm, called step by step with host arrays, as a case main does."""
+def test_dropin_main_lbm_matches_lbc(gpu, oracle, name, staged):
+    """lbc's main_lbm, called step by step with host arrays, as a case main does;
+    both the direct path (kernels read and write the host arrays) and the
+    staged path (copies)."""
+    import lbc_gb300
+    lib = lbc_gb300.load_library()
+    lib.lbm_gpu_dropin_set_staged(1 if staged else 0)
+    lib.lbm_gpu_dropin_release()
     (case, st), steps = casezoo.build(name)
     st_o = st.copy()
     fg = gpu.run(case, st, steps, record_forces=True)
+    lib.lbm_gpu_dropin_set_staged(0)
     fo = oracle.run(case, st_o, steps, record_forces=True)
     g = fixture(name)
     for fld in FIELDS:

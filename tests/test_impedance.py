@@ -10,7 +10,7 @@ from conftest import same
 from lbc_gb300 import impedance as imp
 from lbc_gb300.abi import dptr, iptr
 
-OI_N = 9  # fields before the per-frequency block (shared layout)
+OI_N = 10  # fields before the per-frequency block (shared layout)
 
 
 def _zoh_oracle(oracle, R, m, K):
@@ -59,12 +59,13 @@ def _imp_array(p, omegas, Nx):
         a[0, t] = 1.0
         a[1:5, t] = A
         a[5:7, t] = b
+        a[9, t] = 1.0  # mean density starts at rho_ref
         for f in range(nf):
             a[OI_N + 6 * f, t] = 1.0
     return a
 
 
-def oracle_liner_run(oracle, p, case, st, steps, omegas):
+def oracle_liner_run(oracle, p, case, st, steps, omegas, alpha=0.0):
     """The host coupling of cases/nit/nit.c:276-306, per node: impedance step
     from the stored density, then main_lbm with val2 = -v."""
     impa = _imp_array(p, omegas, case.Nx)
@@ -74,7 +75,7 @@ def oracle_liner_run(oracle, p, case, st, steps, omegas):
     step_fn = oracle.lib.orc_ext_impedance_step
     step_fn.restype = None
     for _ in range(steps):
-        step_fn(C.c_int(case.Nx), C.c_int(0), dptr(st.rho), C.c_double(1.0), dptr(impa), C.c_int(len(omegas)),
+        step_fn(C.c_int(case.Nx), C.c_int(0), dptr(st.rho), C.c_double(alpha), dptr(impa), C.c_int(len(omegas)),
                 dptr(cw), dptr(sw), iptr(case.solid_mask), None, dptr(v2))
         bcs[imp.LINER_ENTRY] = imp.BC("velocity_bottom_regularized", 0, bcs[imp.LINER_ENTRY].val1, v2.copy())
         case2 = imp.Case(case.name, case.Nx, case.Ny, case.solid_mask, case.omega_eff, case.phi, bcs)
@@ -97,7 +98,7 @@ def test_eduction_recovers_the_model(oracle):
     n_steps = 20000
     for n in range(n_steps):
         rho[1, :] = 1.0 + 3.0e-4 * math.exp(-((n - 200.0) ** 2) / (2 * 12.0 ** 2))
-        fn(C.c_int(p.nx), C.c_int(0), dptr(rho), C.c_double(1.0), dptr(impa), C.c_int(len(om)), dptr(cw),
+        fn(C.c_int(p.nx), C.c_int(0), dptr(rho), C.c_double(0.0), dptr(impa), C.c_int(len(om)), dptr(cw),
            dptr(sw), iptr(mask), None, dptr(v2))
     spec = np.stack([impa[OI_N + 6 * f + 2: OI_N + 6 * f + 6].T for f in range(len(om))], axis=1)
     Z = imp.educe(spec, om)[0]
@@ -119,13 +120,13 @@ def test_liner_duct_matches_oracle(oracle, storage):
     om = imp.EDUCTION_OMEGAS
     s = GpuSolver(case, STORAGE[storage])
     R, m, K = imp.liner_arrays(p)
-    s.set_impedance_wall(imp.LINER_ENTRY, R, m, K, om)  # no zero bin: compared raw
+    s.set_impedance_wall(imp.LINER_ENTRY, R, m, K, om, 1.0, 2e-3)  # no zero bin: compared raw
     s.set_state(st)
     steps = 150
     s.run(steps)
     out = s.get_state()
     spec, state = s.impedance_readback(imp.LINER_ENTRY)
-    impa = oracle_liner_run(oracle, p, case, st, steps, om)
+    impa = oracle_liner_run(oracle, p, case, st, steps, om, alpha=2e-3)
     ospec = np.stack([impa[OI_N + 6 * f + 2: OI_N + 6 * f + 6].T for f in range(len(om))], axis=1)
     ostate = impa[7:9].T
     if storage == "f64":
@@ -135,7 +136,7 @@ def test_liner_duct_matches_oracle(oracle, storage):
     else:
         fl = case.solid_mask == 0
         assert np.max(np.abs(out.rho[fl] - st.rho[fl])) < 1e-6
-        assert np.max(np.abs(state[:, 1] - ostate[:, 1])) < 1e-6 * max(1e-12, np.max(np.abs(ostate[:, 1]))) + 1e-12
+        assert np.max(np.abs(state[:, 1] - ostate[:, 1])) < 1e-3 * np.max(np.abs(ostate[:, 1])) + 1e-12
 
 
 @pytest.mark.gpu

@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--skip-cpu", action="store_true")
+    p.add_argument("--skip-liners", action="store_true")
+    p.add_argument("--liner-steps", type=int, default=20000)
     return p.parse_args()
 
 
@@ -201,17 +203,17 @@ def run_ours(a, ws, rank, pg):
         s.run(a.warmup)
         s.sync()
         barrier(pg)
-        clk = Clocks()
-        clk.start()
         ms = s.run_timed(steps)
-        clocks = clk.stop()
         barrier(pg)
         ms = allmax(pg, ms)
         info = s.info()
-        return s, ms, clocks, info
+        return s, ms, None, info
 
+    # Clocks are sampled over all timed regions (nvidia-smi samples every 200 ms).
+    clk = Clocks()
+    clk.start()
     # FP32-shifted: the headline.
-    s32, ms32, clocks, info32 = timed(lbc_gb300.F32_SHIFTED, a.steps)
+    s32, ms32, _, info32 = timed(lbc_gb300.F32_SHIFTED, a.steps)
     bytes32 = 2 * 9 * 4 * N
     t_step = ms32 / a.steps / 1e3
     res["f32"] = {"mlups": ws * N * a.steps / (ms32 / 1e3) / 1e6, "ms_per_step": ms32 / a.steps,
@@ -230,6 +232,21 @@ def run_ours(a, ws, rank, pg):
     del s16
     bytes16 = 2 * 9 * 2 * N
     t16 = ms16 / a.steps / 1e3
+    # Batched acoustic liner ducts (64 seeded ducts, one persistent launch per step).
+    liners = None
+    if not a.skip_liners:
+        from lbc_gb300 import impedance as imp
+        r32 = imp.run_liner_batch(64, a.liner_steps, lbc_gb300.F32_SHIFTED)
+        r64 = imp.run_liner_batch(64, max(2, a.liner_steps // 20), lbc_gb300.F64)
+        liners = {"ducts": 64, "nodes": r32["nodes"], "f32_mlups": round(ws * r32["mlups"], 1),
+                  "f32_steps": r32["steps"], "fp64_mlups": round(ws * r64["mlups"], 1), "fp64_steps": r64["steps"],
+                  "ratio_f32_vs_fp64": round(r32["mlups"] / r64["mlups"], 2),
+                  "launches_per_step": r32["launches_per_step"],
+                  "eduction_omegas": r32["omegas"],
+                  "eduction_err_median_f32": [round(x, 5) for x in r32["eduction_err_median"]],
+                  "eduction_err_max_f32": [round(x, 5) for x in r32["eduction_err_max"]],
+                  "finite": r32["finite"] and r64["finite"]}
+    clocks = clk.stop()
     res["f16"] = {"mlups": ws * N * a.steps / (ms16 / 1e3) / 1e6, "ms_per_step": ms16 / a.steps,
                   "gbs": bytes16 / t16 / 1e9}
 
@@ -267,9 +284,22 @@ def run_ours(a, ws, rank, pg):
     for _ in range(a.e2e_steps):
         api.step(case, hst, bnd)
     el = allmax(pg, time.perf_counter() - t0)
-    e2e = {"value": ws * N * a.e2e_steps / el / 1e6, "unit": "MLUPS",
-           "h2d_bytes_per_step": (2 * 72 + 24) * N, "d2h_bytes_per_step": (2 * 72 + 24) * N + 16,
-           "steps": a.e2e_steps, "path": "main_lbm (lbc C ABI), FP64, host arrays page-locked"}
+    # Pageable (plain numpy) arrays, as an lbc case main's malloc gives.
+    pst = st.copy()
+    api.step(case, pst, bnd)
+    t0 = time.perf_counter()
+    for _ in range(a.e2e_steps):
+        api.step(case, pst, bnd)
+    el_pageable = allmax(pg, time.perf_counter() - t0)
+    # Bytes that cross between host and device per call: f, rho, u, v in (the
+    # old f_new is not needed without solids or open edges); f, f_new, rho, u,
+    # v and the two forces out.
+    e2e = {"value": round(ws * N * a.e2e_steps / el / 1e6, 1), "unit": "MLUPS",
+           "h2d_bytes_per_step": (72 + 24) * N, "d2h_bytes_per_step": (2 * 72 + 24) * N + 16,
+           "steps": a.e2e_steps,
+           "path": "main_lbm (lbc C ABI), FP64, host arrays page-locked; the kernels read and write "
+                   "them over NVLink-C2C",
+           "pageable_value": round(ws * N * a.e2e_steps / el_pageable / 1e6, 1)}
     lib = lbc_gb300.load_library()
     lib.lbm_gpu_dropin_release()
 
@@ -301,6 +331,7 @@ def run_ours(a, ws, rank, pg):
         "speedup_f32_vs_fp64": round(f32["mlups"] / res["f64"]["mlups"], 2),
         "accuracy_after_200_steps": acc,
         "e2e": e2e,
+        "liner_batch": liners,
         "gpu_launches": f32["launches"],
         "clocks": clocks,
     }

@@ -107,11 +107,12 @@ int lbm_gpu_force_history(lbm_gpu_solver *s, double *xy, int max_steps);
  * spring); the BC then imposes u_y = -v (v > 0: flow into the liner) and
  * u_x = val1[i].
  * Nodes with m[i] <= 0 keep the entry's own val2. Running DFTs of p' and v at
- * nf <= 8 angular frequencies (rad / step) are kept per node. Arrays have Nx
+ * nf <= 8 angular frequencies (rad / step) are kept per node, weighted by a
+ * Hann window over window_steps steps (0: unweighted). Arrays have Nx
  * entries. */
 int lbm_gpu_set_impedance_wall(lbm_gpu_solver *s, int entry, const double *R, const double *m,
                                const double *K, int nf, const double *omegas, double rho_ref,
-                               double alpha);
+                               double alpha, int window_steps);
 /* spectra[(i * nf + f) * 4 + q]: q = 0,1 sum p' e^{-i w n} (re, im); q = 2,3 the
  * same for v. state[2 i + {0,1}] = (x, v). Either pointer may be NULL. */
 int lbm_gpu_impedance_readback(lbm_gpu_solver *s, int entry, double *spectra, double *state);

@@ -694,10 +694,11 @@ int lbm_gpu_force_history(lbm_gpu_solver *s, double *xy, int max_steps) {
 
 int lbm_gpu_set_impedance_wall(lbm_gpu_solver *s, int entry, const double *R, const double *m,
                                const double *K, int nf, const double *omegas, double rho_ref,
-                               double alpha) {
+                               double alpha, int window_steps) {
     SOLVER_OR_FAIL(s);
     if (!R || !m || !K || (nf > 0 && !omegas)) { set_error("null array"); return LBM_GPU_ERR_ARG; }
-    return s->s->set_impedance(entry, R, m, K, nf, omegas, rho_ref, alpha) ? LBM_GPU_OK : LBM_GPU_ERR_ARG;
+    return s->s->set_impedance(entry, R, m, K, nf, omegas, rho_ref, alpha, window_steps) ? LBM_GPU_OK
+                                                                                        : LBM_GPU_ERR_ARG;
 }
 
 int lbm_gpu_impedance_readback(lbm_gpu_solver *s, int entry, double *spectra, double *state) {

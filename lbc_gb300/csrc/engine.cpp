@@ -552,6 +552,9 @@ StageParams Solver::stage_params(const Stage &st, int src, int bparity) const {
     s.imp = st.d_imp;
     s.imp_nf = st.imp_nf;
     s.imp_alpha = st.imp_alpha;
+    s.imp_wcos = st.imp_wcos;
+    s.imp_wsin = st.imp_wsin;
+    s.imp_windowed = st.imp_windowed;
     for (int f = 0; f < 8; f++) {
         s.imp_cos[f] = st.imp_cos[f];
         s.imp_sin[f] = st.imp_sin[f];
@@ -594,7 +597,7 @@ bool msd_zoh(double R, double m, double K, double A[4], double b[2]) {
 }
 
 bool Solver::set_impedance(int entry, const double *R, const double *m, const double *K, int nf,
-                           const double *omegas, double rho_ref, double alpha) {
+                           const double *omegas, double rho_ref, double alpha, int window) {
     Stage *st = nullptr;
     for (Stage &x : stages_)
         if (x.entry == entry) st = &x;
@@ -628,6 +631,7 @@ bool Solver::set_impedance(int entry, const double *R, const double *m, const do
         h[(size_t)IMP_B1 * n + t] = b[0];
         h[(size_t)IMP_B2 * n + t] = b[1];
         h[(size_t)IMP_RHOBAR * n + t] = rho_ref;
+        h[(size_t)IMP_WC * n + t] = 1.0;
         for (int f = 0; f < nf; f++) h[(size_t)imp_field(f, 0) * n + t] = 1.0;
     }
     if (!st->d_imp || st->imp_nf != nf) {
@@ -637,6 +641,9 @@ bool Solver::set_impedance(int entry, const double *R, const double *m, const do
     CK(cudaStreamSynchronize(stream_));
     st->imp_nf = nf;
     st->imp_alpha = alpha;
+    st->imp_windowed = window > 0 ? 1 : 0;
+    st->imp_wcos = window > 0 ? std::cos(2.0 * M_PI / window) : 1.0;
+    st->imp_wsin = window > 0 ? std::sin(2.0 * M_PI / window) : 0.0;
     for (int f = 0; f < nf; f++) {
         st->imp_cos[f] = std::cos(omegas[f]);
         st->imp_sin[f] = std::sin(omegas[f]);

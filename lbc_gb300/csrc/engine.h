@@ -45,6 +45,8 @@ struct Stage {
     double *d_imp = nullptr;
     int imp_nf = 0;
     double imp_alpha = 0.0;
+    double imp_wcos = 1.0, imp_wsin = 0.0;
+    int imp_windowed = 0;
     double imp_cos[8] = {1, 1, 1, 1, 1, 1, 1, 1}, imp_sin[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
@@ -116,7 +118,7 @@ class Solver {
     // frequencies (rad / step), reference density for p' and the rate of its
     // running average (0: fixed).
     bool set_impedance(int entry, const double *R, const double *m, const double *K, int nf,
-                       const double *omegas, double rho_ref, double alpha);
+                       const double *omegas, double rho_ref, double alpha, int window);
     // out[((t * nf) + f) * 4 + {0,1,2,3}] = (P re, P im, V re, V im); state[t*2+{0,1}] = (x, v)
     bool impedance_readback(int entry, double *out, double *state);
     bool begin_steps(cudaStream_t s);

@@ -186,7 +186,8 @@ __device__ __forceinline__ void stage_point(const StageParams &p, int t) {
         // Impedance wall on this node: the regularized bottom BC with the
         // normal velocity from the node's mass-spring-damper.
         const double vn = impedance_step(p.imp, p.along, p.imp_nf, t, a.rho(t, p.index + 1),
-                                         p.imp_alpha, p.imp_cos, p.imp_sin);
+                                         p.imp_alpha, p.imp_cos, p.imp_sin, p.imp_wcos,
+                                         p.imp_wsin, p.imp_windowed);
         bc_regularized(a, p.w, t, p.index, t, p.index + 1, false, p.val1[t], -vn);
         return;
     }

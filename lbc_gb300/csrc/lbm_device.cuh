@@ -63,6 +63,7 @@ enum BCKind : int {
 // [IMP_FIELDS + 6 nf][along] doubles.
 enum : int {
     IMP_ACTIVE = 0, IMP_A11, IMP_A12, IMP_A21, IMP_A22, IMP_B1, IMP_B2, IMP_X, IMP_V, IMP_RHOBAR,
+    IMP_WC, IMP_WS,  // window phasor (cos, sin of 2 pi n / window length)
     IMP_FIELDS
 };
 // per frequency f: phasor (re, im), sum p' e^{-i w n} (re, im), sum v e^{-i w n} (re, im)
@@ -213,13 +214,24 @@ __device__ __forceinline__ void bc_regularized(A &a, const double w[9], int ib, 
 // wall was set up with), state (x, v) <- A (x, v) + b p', DFT accumulation,
 // and the wall-normal velocity into the liner returned (the BC imposes
 // u_y = -v).
+// The DFT sums are weighted by a Hann window over the eduction length
+// (weight 0.5 (1 - cos(2 pi n / L)), from a rotating phasor; no window when
+// the wall was set up without a length: wcos = 1, wsin = 0 keeps weight 1).
 __device__ __forceinline__ double impedance_step(double *imp, int along, int nf, int t,
                                                  double rho_n, double alpha,
-                                                 const double *cw, const double *sw) {
+                                                 const double *cw, const double *sw,
+                                                 double wcos, double wsin, int windowed) {
 #define IMP(f) imp[(size_t)(f) * along + t]
     const double rb = IMP(IMP_RHOBAR);
     const double p = (rho_n - rb) / 3.0;
     IMP(IMP_RHOBAR) = rb + alpha * (rho_n - rb);
+    double win = 1.0;
+    if (windowed) {
+        const double c = IMP(IMP_WC), s = IMP(IMP_WS);
+        win = 0.5 * (1.0 - c);
+        IMP(IMP_WC) = c * wcos - s * wsin;
+        IMP(IMP_WS) = s * wcos + c * wsin;
+    }
     const double x = IMP(IMP_X), v = IMP(IMP_V);
     const double xn = IMP(IMP_A11) * x + IMP(IMP_A12) * v + IMP(IMP_B1) * p;
     const double vn = IMP(IMP_A21) * x + IMP(IMP_A22) * v + IMP(IMP_B2) * p;
@@ -227,10 +239,11 @@ __device__ __forceinline__ double impedance_step(double *imp, int along, int nf,
     IMP(IMP_V) = vn;
     for (int f = 0; f < nf; f++) {
         const double cr = IMP(imp_field(f, 0)), ci = IMP(imp_field(f, 1));
-        IMP(imp_field(f, 2)) += p * cr;
-        IMP(imp_field(f, 3)) += p * ci;
-        IMP(imp_field(f, 4)) += vn * cr;
-        IMP(imp_field(f, 5)) += vn * ci;
+        const double wp = win * p, wv = win * vn;
+        IMP(imp_field(f, 2)) += wp * cr;
+        IMP(imp_field(f, 3)) += wp * ci;
+        IMP(imp_field(f, 4)) += wv * cr;
+        IMP(imp_field(f, 5)) += wv * ci;
         // advance the phasor e^{-i w n} by one step
         IMP(imp_field(f, 0)) = cr * cw[f] + ci * sw[f];
         IMP(imp_field(f, 1)) = ci * cw[f] - cr * sw[f];
@@ -402,6 +415,8 @@ struct StageParams {
     double *imp;               // impedance-wall state or null
     int imp_nf;
     double imp_alpha;
+    double imp_wcos, imp_wsin;     // window phasor rotation (2 pi / length)
+    int imp_windowed;
     double imp_cos[8], imp_sin[8];  // e^{-i w_f} per frequency
     const uint16_t *flags;
     const int *colbase, *rowbase;

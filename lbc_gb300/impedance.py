@@ -9,8 +9,10 @@ attached, include/lbm_gpu.h). A Gaussian acoustic pulse starts near the inlet.
 lbc drives one impedance model from the outlet-averaged pressure on the host
 every step (cases/nit/nit.c:276-303) and educes the impedance offline with an
 external toolkit (cases/nit/process.py:22-27). Here every liner node carries its
-own model on the device and keeps running DFTs of its pressure and velocity, so
-the impedance is educed per node as Z(w) = P(w) / V(w), with P the DFT of the
+own model on the device and keeps running, Hann-windowed DFTs of its pressure
+and velocity (the window suppresses the end-of-run state of the slow spring
+mode, which an unweighted finite sum would fold into every bin), so the
+impedance is educed per node as Z(w) = P(w) / V(w), with P the DFT of the
 pressure p'_n the wall sees at step n and V the DFT of the velocity v_{n+1} it
 imposes in response (the pair the lattice sees at the same step), and compared
 with the imposed model Z = R + i (w m - K / w). The difference is the time
@@ -120,32 +122,34 @@ def model_impedance(R, m, K, omegas):
     return R + 1j * (w * m - K / w)
 
 
-def educe(spectra: np.ndarray, omegas, nsteps: int = 0) -> np.ndarray:
-    """spectra[node, f, 4] (P re, P im, V re, V im) -> Z[node, f].
+def educe(spectra: np.ndarray, omegas, demean_steps: int = 0) -> np.ndarray:
+    """spectra[node, f, 4] (P re, P im, V re, V im) -> Z[node, f] = P / V.
 
-    When omegas[0] == 0 and nsteps is given, the first bin holds the plain sums
-    of p' and v; their means are removed from the other bins (the mean flow
-    gives the wall a steady pressure offset whose finite-window DFT would
-    otherwise leak into every bin). The zero bin itself is dropped from the
-    result."""
+    When omegas[0] == 0 the first bin holds the plain (window-weighted) sums of
+    p' and v and is dropped from the result. For an unwindowed run of
+    demean_steps steps, those sums first give the means of p' and v, which are
+    removed from the other bins."""
     w = np.asarray(omegas, dtype=np.float64)
     P = spectra[..., 0] + 1j * spectra[..., 1]
     V = spectra[..., 2] + 1j * spectra[..., 3]
-    if w.size and w[0] == 0.0 and nsteps > 0:
-        mp, mv = P[..., :1] / nsteps, V[..., :1] / nsteps
-        ww = w[1:]
-        D = (1.0 - np.exp(-1j * ww * nsteps)) / (1.0 - np.exp(-1j * ww))
-        P = P[..., 1:] - mp * D
-        V = V[..., 1:] - mv * D
+    if w.size and w[0] == 0.0:
+        if demean_steps > 0:
+            n = demean_steps
+            ww = w[1:]
+            D = (1.0 - np.exp(-1j * ww * n)) / (1.0 - np.exp(-1j * ww))
+            P = P[..., 1:] - P[..., :1] / n * D
+            V = V[..., 1:] - V[..., :1] / n * D
+        else:
+            P, V = P[..., 1:], V[..., 1:]
     with np.errstate(divide="ignore", invalid="ignore"):
         return P / V
 
 
-def eduction_error(p: LinerParams, spectra: np.ndarray, nsteps: int, omegas=TRACKED_OMEGAS):
+def eduction_error(p: LinerParams, spectra: np.ndarray, omegas=TRACKED_OMEGAS):
     """Relative error |Z_educed - Z_model| / |Z_model| over the liner nodes at
-    each eduction frequency: (median, max) per frequency."""
+    each eduction frequency (windowed run): (median, max) per frequency."""
     i0, i1 = p.liner_span
-    Z = educe(spectra[i0:i1], omegas, nsteps)
+    Z = educe(spectra[i0:i1], omegas)
     w = np.asarray(omegas)[1:] if np.asarray(omegas)[0] == 0.0 else np.asarray(omegas)
     Zm = model_impedance(p.R, p.m, p.K, w)[None, :]
     err = np.abs(Z - Zm) / np.abs(Zm)
@@ -164,7 +168,7 @@ def run_liner_batch(n: int = 64, steps: int = 20000, storage: int = 1, seed: int
         case, st = liner_duct(p)
         s = GpuSolver(case, storage)
         R, m, K = liner_arrays(p)
-        s.set_impedance_wall(LINER_ENTRY, R, m, K, TRACKED_OMEGAS, 1.0, MEAN_RATE)
+        s.set_impedance_wall(LINER_ENTRY, R, m, K, TRACKED_OMEGAS, 1.0, MEAN_RATE, steps)
         s.set_state(st)
         solvers.append(s)
     batch = GpuBatch(solvers)
@@ -173,7 +177,7 @@ def run_liner_batch(n: int = 64, steps: int = 20000, storage: int = 1, seed: int
     med, mx, finite = [], [], True
     for p, s in zip(params, solvers):
         spec, _ = s.impedance_readback(LINER_ENTRY)
-        a, b = eduction_error(p, spec, steps)
+        a, b = eduction_error(p, spec)
         med.append(a)
         mx.append(b)
         rho, _, _ = s.get_fields()

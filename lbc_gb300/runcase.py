@@ -33,7 +33,13 @@ def main(argv=None):
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=2)
     p.add_argument("--block", default="", help="bx,by thread block of the fused step")
+    p.add_argument("--ducts", type=int, default=0, help="run this many seeded liner ducts as one batch")
     a = p.parse_args(argv)
+    if a.ducts:
+        from lbc_gb300 import impedance as imp
+        r = imp.run_liner_batch(a.ducts, a.steps, STORAGE[a.storage])
+        print(json.dumps({k: v for k, v in r.items()}))
+        return
     case, st = BUILDERS[a.case](a.n, a.ny)
     s = GpuSolver(case, STORAGE[a.storage])
     if a.block:

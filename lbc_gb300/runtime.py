@@ -87,7 +87,8 @@ def _bind_ext(lib: C.CDLL) -> None:
         "lbm_gpu_batch_run_timed": (C.c_int, [vp, C.c_int, dp]),
         "lbm_gpu_batch_info": (C.c_int, [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_int)]),
         "lbm_gpu_batch_destroy": (C.c_int, [vp]),
-        "lbm_gpu_set_impedance_wall": (C.c_int, [vp, C.c_int, dp, dp, dp, C.c_int, dp, C.c_double, C.c_double]),
+        "lbm_gpu_set_impedance_wall": (C.c_int, [vp, C.c_int, dp, dp, dp, C.c_int, dp, C.c_double, C.c_double,
+                                                 C.c_int]),
         "lbm_gpu_impedance_readback": (C.c_int, [vp, C.c_int, dp, dp]),
         "lbm_gpu_msd_zoh": (C.c_int, [C.c_double, C.c_double, C.c_double, dp, dp]),
         "lbm_gpu_host_alloc": (vp, [C.c_size_t]),
@@ -224,12 +225,13 @@ class GpuSolver:
             raise RuntimeError(last_error())
         return out[:n]
 
-    def set_impedance_wall(self, entry: int, R, m, K, omegas=(), rho_ref: float = 1.0, alpha: float = 0.0):
+    def set_impedance_wall(self, entry: int, R, m, K, omegas=(), rho_ref: float = 1.0, alpha: float = 0.0,
+                           window: int = 0):
         R, m, K = (np.ascontiguousarray(a, dtype=np.float64) for a in (R, m, K))
         om = np.ascontiguousarray(omegas, dtype=np.float64)
         self._imp = (R, m, K, om)
         _check(self.lib.lbm_gpu_set_impedance_wall(self.h, entry, dptr(R), dptr(m), dptr(K), len(om),
-                                                   dptr(om) if len(om) else None, rho_ref, alpha),
+                                                   dptr(om) if len(om) else None, rho_ref, alpha, window),
                "lbm_gpu_set_impedance_wall")
 
     def impedance_readback(self, entry: int):

@@ -664,8 +664,10 @@ void orc_ext_main_lbm_moving(int Nx, int Ny, int Q, double *f, double *f_new, do
  * field: active, A11, A12, A21, A22, b1, b2, x, v, mean density, then per
  * frequency (phasor re, im, sum p' e^{-iwn} re, im, sum v e^{-iwn} re, im).
  * p' is taken about the node's running mean density, rhobar += alpha (rho -
- * rhobar) (alpha = 0: fixed reference). */
-enum { OI_ACT, OI_A11, OI_A12, OI_A21, OI_A22, OI_B1, OI_B2, OI_X, OI_V, OI_RHOBAR, OI_N };
+ * rhobar) (alpha = 0: fixed reference). The DFT terms are weighted by a Hann
+ * window 0.5 (1 - cos(2 pi n / L)) kept as a rotating phasor (wc, ws) turned
+ * by (wcos, wsin) = (cos, sin)(2 pi / L) each step when windowed. */
+enum { OI_ACT, OI_A11, OI_A12, OI_A21, OI_A22, OI_B1, OI_B2, OI_X, OI_V, OI_RHOBAR, OI_WC, OI_WS, OI_N };
 
 int orc_ext_msd_zoh(double R, double m, double K, double *A, double *b) {
     if (!(m > 0.0) || !(K > 0.0) || !(R >= 0.0)) return 0;
@@ -699,8 +701,9 @@ int orc_ext_msd_zoh(double R, double m, double K, double *A, double *b) {
 /* One step of every wall node; val2_out = -v on active nodes, val2_in
  * elsewhere. rho is the stored [Ny][Nx] density, the wall row is `index`. */
 void orc_ext_impedance_step(int Nx, int index, const double *rho, double alpha, double *imp,
-                            int nf, const double *cw, const double *sw, const int *solid_mask,
-                            const double *val2_in, double *val2_out) {
+                            int nf, const double *cw, const double *sw, double wcos, double wsin,
+                            int windowed, const int *solid_mask, const double *val2_in,
+                            double *val2_out) {
     int n = Nx;
 #define OIMP(f, t) imp[(size_t)(f) * (size_t)n + (size_t)(t)]
     for (int t = 0; t < n; t++) {
@@ -710,6 +713,13 @@ void orc_ext_impedance_step(int Nx, int index, const double *rho, double alpha, 
         double rb = OIMP(OI_RHOBAR, t);
         double p = (rn - rb) / 3.0;
         OIMP(OI_RHOBAR, t) = rb + alpha * (rn - rb);
+        double win = 1.0;
+        if (windowed) {
+            double c = OIMP(OI_WC, t), s = OIMP(OI_WS, t);
+            win = 0.5 * (1.0 - c);
+            OIMP(OI_WC, t) = c * wcos - s * wsin;
+            OIMP(OI_WS, t) = s * wcos + c * wsin;
+        }
         double x = OIMP(OI_X, t), v = OIMP(OI_V, t);
         double xn = OIMP(OI_A11, t) * x + OIMP(OI_A12, t) * v + OIMP(OI_B1, t) * p;
         double vn = OIMP(OI_A21, t) * x + OIMP(OI_A22, t) * v + OIMP(OI_B2, t) * p;
@@ -718,10 +728,11 @@ void orc_ext_impedance_step(int Nx, int index, const double *rho, double alpha, 
         for (int f = 0; f < nf; f++) {
             int b0 = OI_N + 6 * f;
             double cr = OIMP(b0, t), ci = OIMP(b0 + 1, t);
-            OIMP(b0 + 2, t) += p * cr;
-            OIMP(b0 + 3, t) += p * ci;
-            OIMP(b0 + 4, t) += vn * cr;
-            OIMP(b0 + 5, t) += vn * ci;
+            double wp = win * p, wv = win * vn;
+            OIMP(b0 + 2, t) += wp * cr;
+            OIMP(b0 + 3, t) += wp * ci;
+            OIMP(b0 + 4, t) += wv * cr;
+            OIMP(b0 + 5, t) += wv * ci;
             OIMP(b0, t) = cr * cw[f] + ci * sw[f];
             OIMP(b0 + 1, t) = ci * cw[f] - cr * sw[f];
         }

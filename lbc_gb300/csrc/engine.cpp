@@ -175,6 +175,7 @@ bool Solver::build_geometry() {
     }
     const bool want_links = d_.use_ibb || moving;
     if (want_links) link_off.assign((size_t)pitch_ * Ny, 0);
+    link_node_.assign((size_t)Nx * Ny, 0);
     bool any_special = false, any_solid_link = false;
     std::vector<int2> wnodes, seed_nodes;
     std::vector<int> seed_slots;
@@ -212,6 +213,7 @@ bool Solver::build_geometry() {
                 fl |= (uint16_t)(1u << k);
                 any_special = true;
                 any_solid_link = true;
+                link_node_[(size_t)j * Nx + i] = 1;
                 if (!want_links) continue;
                 Link L;
                 std::memset(&L, 0, sizeof L);
@@ -316,17 +318,61 @@ bool Solver::build_geometry() {
         CK(cudaMemsetAsync(st.d_val2, 0, st.along * sizeof(double), stream_));
     }
     if (has_mem_) {
-        const unsigned nb = ((Nx + block_.x - 1) / block_.x) * ((Ny + block_.y - 1) / block_.y);
-        // Partials sized for the smallest block the autotuner may pick (32 threads).
-        const size_t cap = (size_t)((Nx + 31) / 32) * Ny;
-        if (!dalloc(&d_partials_, 2 * std::max<size_t>(cap, nb)) || !dalloc(&d_ticket_, 1) ||
-            !dalloc(&d_mem_out_, 2))
-            return false;
-        CK(cudaMemsetAsync(d_ticket_, 0, sizeof(unsigned int), stream_));
+        if (!dalloc(&d_mem_out_, 2) || !dalloc(&d_force_slot_, 1)) return false;
         CK(cudaMemsetAsync(d_mem_out_, 0, 2 * sizeof(double), stream_));
+        if (!compute_block_slots()) return false;
     }
     if (!upload_all_bc_values()) return false;
     CK(cudaStreamSynchronize(stream_));
+    return true;
+}
+
+// Which blocks of the 2D launch grid contain wall links: they (only) reduce
+// and store a force partial, at a compact slot.
+bool Solver::compute_block_slots() {
+    const int Nx = d_.Nx, Ny = d_.Ny;
+    const int gx = (Nx + block_.x - 1) / block_.x, gy = (Ny + block_.y - 1) / block_.y;
+    std::vector<int> slot((size_t)gx * gy, -1);
+    int n = 0;
+    for (int by = 0; by < gy; by++)
+        for (int bx = 0; bx < gx; bx++) {
+            bool any = false;
+            for (int j = by * (int)block_.y; j < std::min(Ny, (by + 1) * (int)block_.y) && !any; j++)
+                for (int i = bx * (int)block_.x; i < std::min(Nx, (bx + 1) * (int)block_.x); i++)
+                    if (link_node_[(size_t)j * Nx + i]) { any = true; break; }
+            if (any) slot[(size_t)by * gx + bx] = n++;
+        }
+    nlink_blocks_ = n;
+    int *d = nullptr;
+    if (!dalloc(&d, slot.size())) return false;
+    CK(cudaMemcpyAsync(d, slot.data(), slot.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
+    d_blk_slot_ = d;
+    if ((size_t)std::max(n, 1) > partial_cap_) {
+        if (!dalloc(&d_partials_, 2 * (size_t)std::max(n, 1))) return false;
+        partial_cap_ = std::max(n, 1);
+    }
+    return upload_force_slot();
+}
+
+bool Solver::upload_force_slot() {
+    if (!d_force_slot_) return true;
+    ForceSlot f;
+    std::memset(&f, 0, sizeof f);
+    f.t0 = 0;
+    f.t1 = nlink_blocks_;
+    f.out = d_mem_out_;
+    f.hist = d_hist_;
+    f.hist_count = hist_count_ptr_;
+    f.hist_cap = hist_cap_;
+    CK(cudaMemcpyAsync(d_force_slot_, &f, sizeof f, cudaMemcpyHostToDevice, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    return true;
+}
+
+bool Solver::set_block(dim3 b) {
+    block_ = b;
+    graph_valid_ = false;
+    if (has_mem_) return compute_block_slots();
     return true;
 }
 
@@ -463,7 +509,7 @@ bool Solver::enable_force_history(int capacity) {
     hist_cap_ = capacity;
     hist_count_ptr_ = cnt;
     graph_valid_ = false;
-    return true;
+    return upload_force_slot();
 }
 
 int Solver::force_history(double *out, int max_steps) {
@@ -522,8 +568,8 @@ StepParams Solver::step_params(int src, int dst, bool write_macro, int bparity) 
     p.bandf = d_bandf_;
     p.bandm_next = nslots_ ? d_bandm_[bparity ^ 1] : nullptr;
     if (has_mem_) {
-        p.mem_partials = d_partials_; p.mem_ticket = d_ticket_; p.mem_out = d_mem_out_;
-        p.mem_hist = d_hist_; p.mem_hist_count = hist_count_ptr_; p.mem_hist_cap = hist_cap_;
+        p.mem_partials = d_partials_;
+        p.blk_slot = d_blk_slot_;
     }
     return p;
 }
@@ -706,6 +752,7 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
     } else {
         CK(launch::step_shifted(fast_params(p), d_.store, has_flags_, collide, block_, s));
     }
+    if (has_mem_) CK(launch::force_reduce(d_partials_, d_force_slot_, 1, s));
     if (stages_.empty()) return true;
     for (const Stage &st : stages_) CK(launch::stage(stage_params(st, src, bparity), d_.store, s));
     const FinishParams f = finish_params(dst, write_macro, bparity);
@@ -828,14 +875,27 @@ bool Batch::build() {
     for (int c = 0; c < nc; c++) {
         Solver *s = cases_[c];
         nodes_ += (long long)s->Nx() * s->Ny();
-        const int t0 = (int)tiles.size();
+        // Tiles of 64 x 4 nodes; those containing wall links get a force
+        // partial slot (w = slot + 1), consecutive per case.
+        const int s0 = nlink_tiles_;
+        const std::vector<uint8_t> &ln = s->link_nodes();
         for (int y = 0; y < s->Ny(); y += 4)
-            for (int x = 0; x < s->Nx(); x += 64) tiles.push_back(make_int4(c, x, y, s->has_mem() ? 1 : 0));
+            for (int x = 0; x < s->Nx(); x += 64) {
+                int w = 0;
+                if (s->has_mem()) {
+                    bool any = false;
+                    for (int j = y; j < std::min(s->Ny(), y + 4) && !any; j++)
+                        for (int i = x; i < std::min(s->Nx(), x + 64); i++)
+                            if (ln[(size_t)j * s->Nx() + i]) { any = true; break; }
+                    if (any) w = 1 + nlink_tiles_++;
+                }
+                tiles.push_back(make_int4(c, x, y, w));
+            }
         if (s->has_mem()) {
             ForceSlot f;
             std::memset(&f, 0, sizeof f);
-            f.t0 = t0;
-            f.t1 = (int)tiles.size();
+            f.t0 = s0;
+            f.t1 = nlink_tiles_;
             f.out = s->mem_out();
             f.hist = s->hist();
             f.hist_count = s->hist_count();
@@ -855,7 +915,7 @@ bool Batch::build() {
     allocs_.push_back(sp);
     d_sp_ = sp;
     if (!balloc(allocs_, &d_phase_, nc) || !balloc(allocs_, &d_tiles_, tiles.size()) ||
-        !balloc(allocs_, &d_partials_, 2 * tiles.size()) || !balloc(allocs_, &d_fin_, 2 * nc) ||
+        !balloc(allocs_, &d_partials_, 2 * (size_t)std::max(nlink_tiles_, 1)) || !balloc(allocs_, &d_fin_, 2 * nc) ||
         !balloc(allocs_, &d_fin_nodes_, fin_nodes.size()) || !balloc(allocs_, &d_force_, force.size()))
         return false;
     CK(cudaMemsetAsync(d_phase_, 0, nc * sizeof(int), stream_));

@@ -96,7 +96,7 @@ class Solver {
     long long steps_done() const { return steps_done_; }
     // Kernel launches per time step inside the loop (for launch counting).
     int launches_per_step() const { return 1 + (int)stages_.size() + (nw_ > 0 ? 1 : 0); }
-    void set_block(dim3 b) { block_ = b; graph_valid_ = false; }
+    bool set_block(dim3 b);
     dim3 block() const { return block_; }
 
     // Pieces used by Batch: parameters of one step in a given direction, the
@@ -108,6 +108,8 @@ class Solver {
     const std::vector<Stage> &stages() const { return stages_; }
     const std::vector<int2> &wnodes() const { return wnodes_host_; }
     bool has_mem() const { return has_mem_; }
+    // 1 for fluid nodes with at least one solid pull source (wall link), [Ny][Nx].
+    const std::vector<uint8_t> &link_nodes() const { return link_node_; }
     int parity() const { return parity_; }
     double *mem_out() const { return d_mem_out_; }
     double *hist() const { return d_hist_; }
@@ -161,7 +163,6 @@ class Solver {
     int nseed_ = 0;
     double *d_rho_ = nullptr, *d_ux_ = nullptr, *d_uy_ = nullptr;
     double *d_partials_ = nullptr;
-    unsigned int *d_ticket_ = nullptr;
     double *d_mem_out_ = nullptr;
     double *d_hist_ = nullptr;
     int hist_cap_ = 0;
@@ -177,6 +178,13 @@ class Solver {
     std::vector<void *> allocs_;
     std::vector<int2> wnodes_host_;
     bool needs_old_dst_ = true;
+    std::vector<uint8_t> link_node_;
+    int *d_blk_slot_ = nullptr;     // per block of the 2D grid: force partial slot or -1
+    int nlink_blocks_ = 0;
+    size_t partial_cap_ = 0;
+    ForceSlot *d_force_slot_ = nullptr;
+    bool compute_block_slots();
+    bool upload_force_slot();
     double *macro_out_[3] = {nullptr, nullptr, nullptr};  // moments written here when set
 };
 
@@ -208,6 +216,7 @@ class Batch {
     cudaStream_t stream_ = nullptr;
     long long nodes_ = 0;
     int ntiles_ = 0, grid_ = 0, max_stages_ = 0, max_along_ = 0, nfin_ = 0, nforce_ = 0;
+    int nlink_tiles_ = 0;
     int launches_per_step_ = 0;
     void *d_sp_ = nullptr;         // StepParams or FastStepParams [2 * ncases]
     int *d_phase_ = nullptr;       // [ncases] (and stage entries)

@@ -35,7 +35,7 @@ namespace lbm {
 // by an edge BC, collides (src/core/collision.c:22-38) and stores.
 template <bool FLAGS, bool COLLIDE>
 __device__ __forceinline__ void step_node_exact(const StepParams &p, int i, int j, double &mfx,
-                                                double &mfy) {
+                                                double &mfy, bool &link) {
     {
         const long long node = (long long)j * p.pitch + i;
         const uint16_t fl = FLAGS ? p.flags[node] : (uint16_t)0;
@@ -96,6 +96,7 @@ __device__ __forceinline__ void step_node_exact(const StepParams &p, int i, int 
                     const double df = own + val;
                     mfx -= df * cxk(k);
                     mfy -= df * cyk(k);
+                    link = true;
                 }
             }
             int slot = -1;
@@ -129,10 +130,12 @@ __global__ void __launch_bounds__(256) k_step_exact(const StepParams p) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     double mfx = 0.0, mfy = 0.0;
-    if (i < p.Nx && j < p.Ny) step_node_exact<FLAGS, COLLIDE>(p, i, j, mfx, mfy);
-    if (FLAGS && p.mem_partials)
-        reduce2_grid(mfx, mfy, p.mem_partials, p.mem_ticket, p.mem_out, p.mem_hist, p.mem_hist_count,
-                     p.mem_hist_cap);
+    bool link = false;
+    if (i < p.Nx && j < p.Ny) step_node_exact<FLAGS, COLLIDE>(p, i, j, mfx, mfy, link);
+    if (FLAGS && p.mem_partials) {
+        const int slot = p.blk_slot[blockIdx.y * gridDim.x + blockIdx.x];
+        if (slot >= 0) block_reduce2_store(mfx, mfy, link, p.mem_partials + 2 * (size_t)slot);
+    }
 }
 
 // Many cases in one launch: a persistent loop over a flattened list of
@@ -149,13 +152,15 @@ __global__ void __launch_bounds__(256) k_step_batch_exact(const StepParams *__re
         const StepParams &p = sp[2 * td.x + (sel ^ phase[td.x])];
         const int i = td.y + threadIdx.x, j = td.z + threadIdx.y;
         double mfx = 0.0, mfy = 0.0;
+        bool link = false;
         const bool in = i < p.Nx && j < p.Ny;
         if (p.flags) {
-            if (in) step_node_exact<true, true>(p, i, j, mfx, mfy);
+            if (in) step_node_exact<true, true>(p, i, j, mfx, mfy, link);
         } else {
-            if (in) step_node_exact<false, true>(p, i, j, mfx, mfy);
+            if (in) step_node_exact<false, true>(p, i, j, mfx, mfy, link);
         }
-        if (td.w) block_reduce2_store(mfx, mfy, partials + 2 * (size_t)t);
+        // td.w = 1 + partial slot of a tile that contains wall links, else 0.
+        if (td.w) block_reduce2_store(mfx, mfy, link, partials + 2 * (size_t)(td.w - 1));
     }
 }
 

@@ -79,7 +79,7 @@ __device__ __forceinline__ void collide_shifted(float g[9], const float w[9], fl
 
 template <typename T, bool FLAGS, bool COLLIDE>
 __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int i, int j,
-                                                  double &mfx, double &mfy) {
+                                                  float &mfx, float &mfy, bool &link) {
     const StepParams &p = fp.s;
     {
         const long long node = (long long)j * p.pitch + i;
@@ -140,9 +140,12 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
                             val = own - (float)L.c2;
                     }
                     g[k] = val;
-                    const double df = (double)own + (double)val + 2.0 * p.w[k];
+                    // Per-node link sum in FP32 (a few terms); the block and
+                    // case sums are FP64.
+                    const float df = (own + val) + 2.0f * fp.wf[k];
                     mfx -= df * cxk(k);
                     mfy -= df * cyk(k);
+                    link = true;
                 }
             }
             int slot = -1;
@@ -171,22 +174,35 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
     }
 }
 
-template <typename T, bool FLAGS, bool COLLIDE>
-__global__ void __launch_bounds__(256) k_step_shifted(const FastStepParams fp) {
+// Fully periodic grid without solids or edge BCs: no flag word, 32 registers.
+template <typename T, bool COLLIDE>
+__global__ void __launch_bounds__(256) k_step_shifted_plain(const FastStepParams fp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    float mfx = 0.f, mfy = 0.f;
+    bool link = false;
+    if (i < fp.s.Nx && j < fp.s.Ny) step_node_shifted<T, false, COLLIDE>(fp, i, j, mfx, mfy, link);
+}
+
+// General geometry (flag word per node). The occupancy hint keeps it at five
+// resident blocks per SM (48 registers) without spills.
+template <typename T, bool COLLIDE>
+__global__ void __launch_bounds__(256, 5) k_step_shifted_geo(const FastStepParams fp) {
     const StepParams &p = fp.s;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    double mfx = 0.0, mfy = 0.0;
-    if (i < p.Nx && j < p.Ny) step_node_shifted<T, FLAGS, COLLIDE>(fp, i, j, mfx, mfy);
-    if (FLAGS && p.mem_partials) {
-        reduce2_grid(mfx, mfy, p.mem_partials, p.mem_ticket, p.mem_out, p.mem_hist,
-                     p.mem_hist_count, p.mem_hist_cap);
+    float mfx = 0.f, mfy = 0.f;
+    bool link = false;
+    if (i < p.Nx && j < p.Ny) step_node_shifted<T, true, COLLIDE>(fp, i, j, mfx, mfy, link);
+    if (p.mem_partials) {
+        const int slot = p.blk_slot[blockIdx.y * gridDim.x + blockIdx.x];
+        if (slot >= 0) block_reduce2_store(mfx, mfy, link, p.mem_partials + 2 * (size_t)slot);
     }
 }
 
 // Batched form (see k_step_batch_exact in kernels_exact.cu).
 template <typename T>
-__global__ void __launch_bounds__(256) k_step_batch_shifted(const FastStepParams *__restrict__ sp,
+__global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepParams *__restrict__ sp,
                                                             const int *__restrict__ phase,
                                                             const int4 *__restrict__ tiles,
                                                             int ntiles, int sel, double *partials) {
@@ -194,14 +210,15 @@ __global__ void __launch_bounds__(256) k_step_batch_shifted(const FastStepParams
         const int4 td = tiles[t];
         const FastStepParams &fp = sp[2 * td.x + (sel ^ phase[td.x])];
         const int i = td.y + threadIdx.x, j = td.z + threadIdx.y;
-        double mfx = 0.0, mfy = 0.0;
+        float mfx = 0.f, mfy = 0.f;
+        bool link = false;
         const bool in = i < fp.s.Nx && j < fp.s.Ny;
         if (fp.s.flags) {
-            if (in) step_node_shifted<T, true, true>(fp, i, j, mfx, mfy);
+            if (in) step_node_shifted<T, true, true>(fp, i, j, mfx, mfy, link);
         } else {
-            if (in) step_node_shifted<T, false, true>(fp, i, j, mfx, mfy);
+            if (in) step_node_shifted<T, false, true>(fp, i, j, mfx, mfy, link);
         }
-        if (td.w) block_reduce2_store(mfx, mfy, partials + 2 * (size_t)t);
+        if (td.w) block_reduce2_store(mfx, mfy, link, partials + 2 * (size_t)(td.w - 1));
     }
 }
 
@@ -285,11 +302,11 @@ template <typename T>
 static void step_shifted_t(const FastStepParams &p, bool flags, bool collide, dim3 g, dim3 b,
                            cudaStream_t s) {
     if (flags) {
-        if (collide) k_step_shifted<T, true, true><<<g, b, 0, s>>>(p);
-        else k_step_shifted<T, true, false><<<g, b, 0, s>>>(p);
+        if (collide) k_step_shifted_geo<T, true><<<g, b, 0, s>>>(p);
+        else k_step_shifted_geo<T, false><<<g, b, 0, s>>>(p);
     } else {
-        if (collide) k_step_shifted<T, false, true><<<g, b, 0, s>>>(p);
-        else k_step_shifted<T, false, false><<<g, b, 0, s>>>(p);
+        if (collide) k_step_shifted_plain<T, true><<<g, b, 0, s>>>(p);
+        else k_step_shifted_plain<T, false><<<g, b, 0, s>>>(p);
     }
 }
 

@@ -398,13 +398,11 @@ struct StepParams {
     int nslots;
     double *bandf;            // [9][nslots], pre-collision f_new of band nodes
     double *bandm_next;       // [3][nslots], their moments (for the next step's BCs)
-    // momentum-exchange force (null when the geometry has no wall links)
-    double *mem_partials;     // [2 * gridDim.x * gridDim.y]
-    unsigned int *mem_ticket;
-    double *mem_out;          // [2]: Fx, Fy of this step
-    double *mem_hist;         // optional per-step ring [2 * mem_hist_cap]
-    unsigned long long *mem_hist_count;
-    int mem_hist_cap;
+    // momentum-exchange force (null when the geometry has no wall links):
+    // blocks that contain wall links (blk_slot >= 0, known from the geometry)
+    // store their sum at mem_partials[2 * slot]; k_force_reduce adds them up.
+    double *mem_partials;
+    const int *blk_slot;      // [gridDim.x * gridDim.y]
 };
 
 struct StageParams {

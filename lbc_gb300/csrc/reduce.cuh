@@ -4,10 +4,10 @@
 
 namespace lbm {
 
-// Warp sum of two doubles into lane 0. Warps where every lane holds zero (no
-// wall link: most of the grid) skip the FP64 shuffles, which are slow on GB300.
-__device__ __forceinline__ void warp_reduce2(double &a, double &b) {
-    if (!__any_sync(0xffffffffu, a != 0.0 || b != 0.0)) return;
+// Warp sum of two doubles into lane 0. Warps where no lane has a wall link
+// (most of the grid) skip the FP64 shuffles, which are slow on GB300.
+__device__ __forceinline__ void warp_reduce2(double &a, double &b, bool link) {
+    if (!__any_sync(0xffffffffu, link)) return;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_down_sync(0xffffffffu, a, o);
@@ -28,7 +28,7 @@ __device__ __forceinline__ void reduce2_grid(double a, double b, double *partial
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const int nthr = blockDim.x * blockDim.y;
     const int lane = tid & 31, warp = tid >> 5;
-    warp_reduce2(a, b);
+    warp_reduce2(a, b, a != 0.0 || b != 0.0);
     if (lane == 0) { sa[warp] = a; sb[warp] = b; }
     __syncthreads();
     const int nblk = gridDim.x * gridDim.y;
@@ -74,12 +74,13 @@ __device__ __forceinline__ void reduce2_grid(double a, double b, double *partial
     }
 }
 
-// Block reduction of two doubles, stored by thread 0 at out[0..1] (fixed order).
-__device__ __forceinline__ void block_reduce2_store(double a, double b, double *out) {
+// Block reduction of two doubles, stored by thread 0 at out[0..1] (fixed
+// order). `link`: this thread's node has wall links (its terms are nonzero).
+__device__ __forceinline__ void block_reduce2_store(double a, double b, bool link, double *out) {
     __shared__ double sa[32], sb[32];
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const int nthr = blockDim.x * blockDim.y;
-    warp_reduce2(a, b);
+    warp_reduce2(a, b, link);
     if ((tid & 31) == 0) { sa[tid >> 5] = a; sb[tid >> 5] = b; }
     __syncthreads();
     if (tid == 0) {

@@ -141,6 +141,43 @@ int lbm_gpu_batch_run_timed(lbm_gpu_batch *b, int nsteps, double *ms);
 int lbm_gpu_batch_info(lbm_gpu_batch *b, long long *nodes, int *launches_per_step);
 int lbm_gpu_batch_destroy(lbm_gpu_batch *b);
 
+/* ---- Serving: a continuous-batching request loop.
+ * Any thread prepares a request (case, initial state, step count; all inputs
+ * are copied), optionally attaches an impedance wall, and enqueues it. Each
+ * scheduling round (lbm_gpu_server_poll, or the server's own thread after
+ * lbm_gpu_server_start) admits queued requests in arrival order while the
+ * device-memory budget and the slot limit allow, advances all active requests
+ * by one chunk (one graph-captured persistent batch per storage type, the
+ * batches running concurrently), and retires finished ones: their fields (and
+ * populations when asked for) are copied to host memory and their device
+ * memory is freed. Results are identical to running each request alone
+ * (lbm_gpu_run). budget_bytes = 0: 85 % of the free device memory. */
+typedef struct lbm_gpu_server lbm_gpu_server;
+int lbm_gpu_server_create(size_t budget_bytes, int max_active, int chunk_steps, lbm_gpu_server **out);
+/* Returns the request id (> 0) or a negative code. */
+int lbm_gpu_server_prepare(lbm_gpu_server *srv, const lbm_gpu_case *c, const double *f,
+                           const double *f_new, const double *rho, const double *u, const double *v,
+                           int nsteps, int keep_populations);
+int lbm_gpu_server_set_impedance(lbm_gpu_server *srv, int id, int entry, const double *R,
+                                 const double *m, const double *K, int nf, const double *omegas,
+                                 double rho_ref, double alpha, int window_steps);
+int lbm_gpu_server_enqueue(lbm_gpu_server *srv, int id);
+/* One scheduling round; returns the number of requests still queued or active. */
+int lbm_gpu_server_poll(lbm_gpu_server *srv);
+int lbm_gpu_server_start(lbm_gpu_server *srv);
+int lbm_gpu_server_stop(lbm_gpu_server *srv);
+/* Returns 0 prepared, 1 queued, 2 running, 3 done, 4 failed (message in
+ * lbm_gpu_last_error); times in seconds on a monotonic clock. */
+int lbm_gpu_server_status(lbm_gpu_server *srv, int id, double *t_submit, double *t_admit,
+                          double *t_done);
+/* Copies a finished request's results; spectra as lbm_gpu_impedance_readback. */
+int lbm_gpu_server_fetch(lbm_gpu_server *srv, int id, double *f, double *f_new, double *rho,
+                         double *u, double *v, double *spectra);
+int lbm_gpu_server_release(lbm_gpu_server *srv, int id);
+int lbm_gpu_server_stats(lbm_gpu_server *srv, long long *lups_done, double *busy_s, int *queued,
+                         int *active, size_t *bytes_in_use);
+int lbm_gpu_server_destroy(lbm_gpu_server *srv);
+
 /* Page-locked host memory for fast transfers. */
 void *lbm_gpu_host_alloc(size_t bytes);
 void lbm_gpu_host_free(void *p);

@@ -25,6 +25,7 @@ UNITS = [
     ("kernels_shifted.cu", ["-O3", "-lineinfo"] + ARCH),
     ("engine.cpp", ["-O2"]),
     ("dropin.cpp", ["-O2"]),
+    ("server.cpp", ["-O2"]),
 ]
 
 

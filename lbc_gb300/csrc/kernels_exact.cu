@@ -57,25 +57,25 @@ __device__ __forceinline__ void step_node_exact(const StepParams &p, int i, int 
             const double *S = (const double *)p.src;
             double *Dst = (double *)p.dst;
             const long long pl = p.plane;
+            // Wrapped on periodic axes, clamped otherwise (all loads in bounds,
+            // issued together); the flag word says which ones to replace.
             int im = i - 1, ip = i + 1, jm = j - 1, jp = j + 1;
             if (p.px) { if (im < 0) im += p.Nx; if (ip >= p.Nx) ip -= p.Nx; }
+            else { im = max(im, 0); ip = min(ip, p.Nx - 1); }
             if (p.py) { if (jm < 0) jm += p.Ny; if (jp >= p.Ny) jp -= p.Ny; }
+            else { jm = max(jm, 0); jp = min(jp, p.Ny - 1); }
             const long long r0 = (long long)j * p.pitch, rm = (long long)jm * p.pitch,
                             rp = (long long)jp * p.pitch;
             const long long so[9] = {r0 + i, r0 + im, rm + i, r0 + ip, rp + i,
                                      rm + im, rm + ip, rp + ip, rp + im};
             double f[9];
-            if (!FLAGS) {
 #pragma unroll
-                for (int k = 0; k < 9; k++) f[k] = S[k * pl + so[k]];
-            } else {
+            for (int k = 0; k < 9; k++) f[k] = S[k * pl + so[k]];
+            if (FLAGS && (fl & NF_SPECIAL_MASK)) {
                 const Link *lk = (fl & NF_LINKS) ? p.links + p.link_off[node] : nullptr;
 #pragma unroll
                 for (int k = 0; k < 9; k++) {
-                    if (!(fl & (1u << k))) {
-                        f[k] = S[k * pl + so[k]];
-                        continue;
-                    }
+                    if (!(fl & (1u << k))) continue;
                     const int si = i - cxk(k), sj = j - cyk(k);
                     const bool off = (!p.px && (si < 0 || si >= p.Nx)) ||
                                      (!p.py && (sj < 0 || sj >= p.Ny));
@@ -600,8 +600,9 @@ cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block
     return cudaGetLastError();
 }
 
+// Edge kernels are FP64 and short: 32-thread blocks spread a line over many SMs.
 cudaError_t stage(const StageParams &p, int store, cudaStream_t s) {
-    const int b = 128, g = (p.along + b - 1) / b;
+    const int b = 32, g = (p.along + b - 1) / b;
     if (store == STORE_F64) k_stage<double><<<g, b, 0, s>>>(p);
     else if (store == STORE_F32) k_stage<float><<<g, b, 0, s>>>(p);
     else k_stage<__half><<<g, b, 0, s>>>(p);
@@ -626,17 +627,17 @@ int step_batch_exact_grid() {
 cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int max_along, int store,
                         int sel, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    const dim3 g((max_along + 127) / 128, n);
-    if (store == STORE_F64) k_stage_batch<double><<<g, 128, 0, s>>>(list, ephase, sel);
-    else if (store == STORE_F32) k_stage_batch<float><<<g, 128, 0, s>>>(list, ephase, sel);
-    else k_stage_batch<__half><<<g, 128, 0, s>>>(list, ephase, sel);
+    const dim3 g((max_along + 31) / 32, n);
+    if (store == STORE_F64) k_stage_batch<double><<<g, 32, 0, s>>>(list, ephase, sel);
+    else if (store == STORE_F32) k_stage_batch<float><<<g, 32, 0, s>>>(list, ephase, sel);
+    else k_stage_batch<__half><<<g, 32, 0, s>>>(list, ephase, sel);
     return cudaGetLastError();
 }
 
 cudaError_t finish_batch_exact(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
                                int sel, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_finish_batch_exact<<<(n + 127) / 128, 128, 0, s>>>(fp, phase, nodes, n, sel);
+    k_finish_batch_exact<<<(n + 31) / 32, 32, 0, s>>>(fp, phase, nodes, n, sel);
     return cudaGetLastError();
 }
 
@@ -648,7 +649,7 @@ cudaError_t force_reduce(const double *partials, const ForceSlot *slots, int n, 
 
 cudaError_t finish_exact(const FinishParams &p, bool collide, cudaStream_t s) {
     if (p.nw == 0) return cudaSuccess;
-    const int b = 128, g = (p.nw + b - 1) / b;
+    const int b = 32, g = (p.nw + b - 1) / b;
     if (collide) k_finish_exact<true><<<g, b, 0, s>>>(p);
     else k_finish_exact<false><<<g, b, 0, s>>>(p);
     return cudaGetLastError();

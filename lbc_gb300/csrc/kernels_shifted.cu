@@ -101,25 +101,26 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
             const T *S = (const T *)p.src;
             T *Dst = (T *)p.dst;
             const long long pl = p.plane;
+            // Source neighbours: wrapped on periodic axes, clamped otherwise so
+            // that all nine loads are in bounds and can be issued at once; the
+            // flag word then says which of them to replace.
             int im = i - 1, ip = i + 1, jm = j - 1, jp = j + 1;
             if (p.px) { if (im < 0) im += p.Nx; if (ip >= p.Nx) ip -= p.Nx; }
+            else { im = max(im, 0); ip = min(ip, p.Nx - 1); }
             if (p.py) { if (jm < 0) jm += p.Ny; if (jp >= p.Ny) jp -= p.Ny; }
+            else { jm = max(jm, 0); jp = min(jp, p.Ny - 1); }
             const long long r0 = (long long)j * p.pitch, rm = (long long)jm * p.pitch,
                             rp = (long long)jp * p.pitch;
             const long long so[9] = {r0 + i, r0 + im, rm + i, r0 + ip, rp + i,
                                      rm + im, rm + ip, rp + ip, rp + im};
             float g[9];
-            if (!FLAGS) {
 #pragma unroll
-                for (int k = 0; k < 9; k++) g[k] = SV<T>::ld(S + k * pl + so[k]);
-            } else {
+            for (int k = 0; k < 9; k++) g[k] = SV<T>::ld(S + k * pl + so[k]);
+            if (FLAGS && (fl & NF_SPECIAL_MASK)) {
                 const Link *lk = (fl & NF_LINKS) ? p.links + p.link_off[node] : nullptr;
 #pragma unroll
                 for (int k = 0; k < 9; k++) {
-                    if (!(fl & (1u << k))) {
-                        g[k] = SV<T>::ld(S + k * pl + so[k]);
-                        continue;
-                    }
+                    if (!(fl & (1u << k))) continue;
                     const int si = i - cxk(k), sj = j - cyk(k);
                     const bool off = (!p.px && (si < 0 || si >= p.Nx)) ||
                                      (!p.py && (sj < 0 || sj >= p.Ny));

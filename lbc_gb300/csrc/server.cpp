@@ -1,0 +1,445 @@
+// server.cpp -- continuous-batching request loop over the GPU engine.
+//
+// Requests (a case, its initial state and a number of steps) are submitted by
+// any thread into a lock-protected queue. Each scheduling round:
+//   1. admits queued requests in arrival order while the device-memory budget
+//      and the slot limit allow (the state then lives on the device until the
+//      request finishes);
+//   2. advances every active request by one chunk: requests of one storage type
+//      form one Batch (one persistent kernel per step over all their tiles,
+//      graph-captured), the FP32/FP16 and FP64 batches run concurrently on
+//      their own streams; a chunk is the smallest remaining step count of the
+//      batch, capped at the chunk size, so requests join and leave between
+//      chunks;
+//   3. retires finished requests: their fields (and, on request, populations
+//      and impedance spectra) are copied to host memory and their device
+//      memory is freed for the next admissions.
+// Because Solver::run(a) followed by run(b) equals run(a + b) and every case's
+// arithmetic is independent of the others in a batch, a request's result is
+// the same alone and in any mix.
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <atomic>
+#include <vector>
+
+#include "../../include/lbm_gpu.h"
+#include "engine.h"
+
+using namespace lbm;
+
+namespace {
+
+double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct ImpSpec {
+    int entry = -1;
+    std::vector<double> R, m, K, omegas;
+    double rho_ref = 1.0, alpha = 0.0;
+    int window = 0;
+};
+
+struct Request {
+    int id = 0;
+    int state = 0;  // 0 prepared, 1 queued, 2 active, 3 done, 4 failed
+    // owned copies of the case description
+    int Nx = 0, Ny = 0, storage = 0;
+    double w[9];
+    std::vector<int> mask;
+    std::vector<double> omega, phi, wall_u, wall_v;
+    int use_ibb = 0, px = 0, py = 0;
+    double Fx = 0, Fy = 0;
+    std::vector<BCEntry> bcs;
+    std::vector<std::vector<double>> bc_vals;  // 2 per entry
+    std::vector<double> f, f_new, rho, u, v;    // inputs, then results
+    int nsteps = 0, remaining = 0;
+    bool keep_populations = false;
+    ImpSpec imp;
+    std::vector<double> spectra;
+    std::unique_ptr<Solver> solver;
+    size_t est_bytes = 0;
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    std::string error;
+};
+
+size_t estimate_bytes(const Request &r) {
+    const size_t N = (size_t)r.Nx * r.Ny;
+    const size_t pitchN = (size_t)((r.Nx + 63) / 64 * 64) * r.Ny;
+    const size_t es = r.storage == LBM_GPU_F64 ? 8 : (r.storage == LBM_GPU_F32_SHIFTED ? 4 : 2);
+    return 2 * 9 * es * pitchN + 72 * N + 24 * N + 2 * pitchN + (r.use_ibb ? 4 * pitchN : 0) +
+           8 * N + (1u << 20);
+}
+
+}  // namespace
+
+struct lbm_gpu_server {
+    std::mutex mu;
+    std::map<int, std::unique_ptr<Request>> reqs;
+    std::deque<Request *> queue;
+    std::vector<Request *> active;
+    size_t budget = 0, in_use = 0;
+    int max_active = 64;
+    int chunk = 1000;
+    int next_id = 1;
+    long long lups_done = 0;
+    double busy_s = 0;
+    std::thread worker;
+    std::atomic<bool> running{false};
+    std::string err;
+};
+
+static bool admit(lbm_gpu_server *S, Request *r) {
+    CaseDesc d;
+    d.Nx = r->Nx;
+    d.Ny = r->Ny;
+    for (int k = 0; k < 9; k++) d.w[k] = r->w[k];
+    d.mask = r->mask.data();
+    d.omega = r->omega.data();
+    d.phi = r->phi.empty() ? nullptr : r->phi.data();
+    d.use_ibb = r->use_ibb;
+    d.wall_u = r->wall_u.empty() ? nullptr : r->wall_u.data();
+    d.wall_v = r->wall_v.empty() ? nullptr : r->wall_v.data();
+    d.px = r->px;
+    d.py = r->py;
+    d.Fx = r->Fx;
+    d.Fy = r->Fy;
+    d.bcs = r->bcs;
+    for (size_t e = 0; e < d.bcs.size(); e++) {
+        d.bcs[e].val1 = r->bc_vals[2 * e].empty() ? nullptr : r->bc_vals[2 * e].data();
+        d.bcs[e].val2 = r->bc_vals[2 * e + 1].empty() ? nullptr : r->bc_vals[2 * e + 1].data();
+    }
+    d.store = r->storage;
+    std::unique_ptr<Solver> s(new Solver(d));
+    if (!s->ok()) {
+        r->error = last_error();
+        return false;
+    }
+    if (r->imp.entry >= 0 &&
+        !s->set_impedance(r->imp.entry, r->imp.R.data(), r->imp.m.data(), r->imp.K.data(),
+                          (int)r->imp.omegas.size(), r->imp.omegas.data(), r->imp.rho_ref,
+                          r->imp.alpha, r->imp.window)) {
+        r->error = last_error();
+        return false;
+    }
+    if (!s->set_state(r->f.data(), r->f_new.data(), r->rho.data(), r->u.data(), r->v.data()) ||
+        !check_cuda(cudaStreamSynchronize(s->stream()), "admit")) {
+        r->error = last_error();
+        return false;
+    }
+    // Inputs are on the device now.
+    std::vector<double>().swap(r->f);
+    std::vector<double>().swap(r->f_new);
+    r->solver = std::move(s);
+    return true;
+}
+
+static bool retire(Request *r) {
+    Solver *s = r->solver.get();
+    const size_t N = (size_t)r->Nx * r->Ny;
+    r->rho.assign(N, 0.0);
+    r->u.assign(N, 0.0);
+    r->v.assign(N, 0.0);
+    bool okk;
+    if (r->keep_populations) {
+        r->f.assign(N * 9, 0.0);
+        r->f_new.assign(N * 9, 0.0);
+        okk = s->get_state(r->f.data(), r->f_new.data(), r->rho.data(), r->u.data(), r->v.data());
+    } else {
+        okk = s->get_fields(r->rho.data(), r->u.data(), r->v.data());
+    }
+    if (okk && r->imp.entry >= 0) {
+        r->spectra.assign((size_t)r->Nx * r->imp.omegas.size() * 4, 0.0);
+        okk = s->impedance_readback(r->imp.entry, r->spectra.data(), nullptr);
+    }
+    if (!okk) r->error = last_error();
+    r->solver.reset();
+    return okk;
+}
+
+// One scheduling round; returns the number of requests still queued or active.
+static int server_round(lbm_gpu_server *S) {
+    std::vector<Request *> admitted;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        while (!S->queue.empty() && (int)S->active.size() + (int)admitted.size() < S->max_active) {
+            Request *r = S->queue.front();
+            if (S->in_use + r->est_bytes > S->budget && !(S->active.empty() && admitted.empty())) break;
+            S->queue.pop_front();
+            admitted.push_back(r);
+            S->in_use += r->est_bytes;
+        }
+    }
+    for (Request *r : admitted) {
+        const double ta = now_s();
+        const bool okk = admit(S, r);
+        std::lock_guard<std::mutex> lk(S->mu);
+        r->t_admit = ta;
+        if (okk) {
+            r->state = 2;
+            S->active.push_back(r);
+        } else {
+            r->state = 4;
+            r->t_done = now_s();
+            S->in_use -= r->est_bytes;
+        }
+    }
+    if (!S->active.empty()) {
+        const double t0 = now_s();
+        // One batch per storage type, each advanced by its own chunk length.
+        std::vector<std::unique_ptr<Batch>> batches;
+        std::vector<std::vector<Request *>> groups(3);
+        for (Request *r : S->active) groups[r->storage].push_back(r);
+        std::vector<int> steps(3, 0);
+        bool okk = true;
+        for (int g = 0; g < 3; g++) {
+            if (groups[g].empty()) continue;
+            int n = S->chunk;
+            for (Request *r : groups[g]) n = std::min(n, r->remaining);
+            steps[g] = n;
+            std::vector<Solver *> sv;
+            for (Request *r : groups[g]) sv.push_back(r->solver.get());
+            std::unique_ptr<Batch> b(new Batch(sv));
+            okk = okk && b->ok() && b->run(n);
+            batches.push_back(std::move(b));
+        }
+        for (auto &b : batches) okk = okk && check_cuda(cudaStreamSynchronize(b->stream()), "server");
+        for (int g = 0; g < 3; g++)
+            for (Request *r : groups[g]) {
+                r->remaining -= steps[g];
+                S->lups_done += (long long)r->Nx * r->Ny * steps[g];
+            }
+        batches.clear();
+        std::vector<Request *> keep;
+        for (Request *r : S->active) {
+            int st;
+            if (!okk) {
+                r->error = last_error();
+                r->solver.reset();
+                st = 4;
+            } else if (r->remaining <= 0) {
+                st = retire(r) ? 3 : 4;
+            } else {
+                keep.push_back(r);
+                continue;
+            }
+            std::lock_guard<std::mutex> lk(S->mu);
+            r->t_done = now_s();
+            r->state = st;
+            S->in_use -= r->est_bytes;
+        }
+        S->active.swap(keep);
+        S->busy_s += now_s() - t0;
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    return (int)(S->queue.size() + S->active.size());
+}
+
+extern "C" {
+
+int lbm_gpu_server_create(size_t budget_bytes, int max_active, int chunk_steps, lbm_gpu_server **out) {
+    if (!out || max_active < 1 || chunk_steps < 1) {
+        set_error("bad arguments");
+        return LBM_GPU_ERR_ARG;
+    }
+    lbm_gpu_server *S = new lbm_gpu_server();
+    if (budget_bytes == 0) {
+        size_t fr = 0, tot = 0;
+        if (!check_cuda(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo")) {
+            delete S;
+            return LBM_GPU_ERR_CUDA;
+        }
+        budget_bytes = (size_t)(0.85 * (double)fr);
+    }
+    S->budget = budget_bytes;
+    S->max_active = max_active;
+    S->chunk = chunk_steps;
+    *out = S;
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_server_prepare(lbm_gpu_server *S, const lbm_gpu_case *c, const double *f,
+                           const double *f_new, const double *rho, const double *u, const double *v,
+                           int nsteps, int keep_populations) {
+    if (!S || !c || !f || !f_new || !rho || !u || !v || nsteps < 1) {
+        set_error("bad arguments");
+        return LBM_GPU_ERR_ARG;
+    }
+    std::unique_ptr<Request> r(new Request());
+    r->Nx = c->Nx;
+    r->Ny = c->Ny;
+    r->storage = c->storage;
+    const size_t N = (size_t)c->Nx * c->Ny;
+    for (int k = 0; k < 9; k++) r->w[k] = c->w[k];
+    r->mask.assign(c->solid_mask, c->solid_mask + N);
+    r->omega.assign(c->omega_eff, c->omega_eff + N);
+    if (c->phi) r->phi.assign(c->phi, c->phi + N);
+    if (c->wall_u) r->wall_u.assign(c->wall_u, c->wall_u + N);
+    if (c->wall_v) r->wall_v.assign(c->wall_v, c->wall_v + N);
+    r->use_ibb = c->use_IBB;
+    r->px = c->isperiodic_x;
+    r->py = c->isperiodic_y;
+    r->Fx = c->Fx;
+    r->Fy = c->Fy;
+    for (int b = 0; b < c->num_boundaries; b++) {
+        const int kind = bc_kind_of((const void *)c->boundaries[b].apply);
+        if (kind < 0) {
+            set_error("boundary entry " + std::to_string(b) + ": not one of lbc's BC functions");
+            return LBM_GPU_ERR_ARG;
+        }
+        const bool col = bc_is_column(kind);
+        const size_t along = col ? c->Ny : c->Nx;
+        r->bcs.push_back(BCEntry{kind, c->boundaries[b].index, nullptr, nullptr});
+        const double *v1 = c->boundaries[b].val1, *v2 = c->boundaries[b].val2;
+        r->bc_vals.push_back(v1 ? std::vector<double>(v1, v1 + along) : std::vector<double>());
+        r->bc_vals.push_back(v2 ? std::vector<double>(v2, v2 + along) : std::vector<double>());
+    }
+    r->f.assign(f, f + 9 * N);
+    r->f_new.assign(f_new, f_new + 9 * N);
+    r->rho.assign(rho, rho + N);
+    r->u.assign(u, u + N);
+    r->v.assign(v, v + N);
+    r->nsteps = r->remaining = nsteps;
+    r->keep_populations = keep_populations != 0;
+    r->est_bytes = estimate_bytes(*r);
+    std::lock_guard<std::mutex> lk(S->mu);
+    r->id = S->next_id++;
+    const int id = r->id;
+    S->reqs[id] = std::move(r);
+    return id;
+}
+
+int lbm_gpu_server_set_impedance(lbm_gpu_server *S, int id, int entry, const double *R,
+                                 const double *m, const double *K, int nf, const double *omegas,
+                                 double rho_ref, double alpha, int window_steps) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(id);
+    if (it == S->reqs.end() || it->second->state != 0) {
+        set_error("request not found or already queued");
+        return LBM_GPU_ERR_ARG;
+    }
+    Request *r = it->second.get();
+    r->imp.entry = entry;
+    r->imp.R.assign(R, R + r->Nx);
+    r->imp.m.assign(m, m + r->Nx);
+    r->imp.K.assign(K, K + r->Nx);
+    r->imp.omegas.assign(omegas, omegas + nf);
+    r->imp.rho_ref = rho_ref;
+    r->imp.alpha = alpha;
+    r->imp.window = window_steps;
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_server_enqueue(lbm_gpu_server *S, int id) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(id);
+    if (it == S->reqs.end() || it->second->state != 0) {
+        set_error("request not found or already queued");
+        return LBM_GPU_ERR_ARG;
+    }
+    it->second->state = 1;
+    it->second->t_submit = now_s();
+    S->queue.push_back(it->second.get());
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_server_poll(lbm_gpu_server *S) {
+    if (!S) return LBM_GPU_ERR_ARG;
+    return server_round(S);
+}
+
+int lbm_gpu_server_start(lbm_gpu_server *S) {
+    if (!S || S->running) return LBM_GPU_ERR_ARG;
+    S->running = true;
+    S->worker = std::thread([S] {
+        while (S->running) {
+            const int left = server_round(S);
+            if (left == 0) std::this_thread::sleep_for(std::chrono::microseconds(200));
+        }
+    });
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_server_stop(lbm_gpu_server *S) {
+    if (!S) return LBM_GPU_ERR_ARG;
+    S->running = false;
+    if (S->worker.joinable()) S->worker.join();
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_server_status(lbm_gpu_server *S, int id, double *t_submit, double *t_admit,
+                          double *t_done) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(id);
+    if (it == S->reqs.end()) {
+        set_error("request not found");
+        return LBM_GPU_ERR_ARG;
+    }
+    Request *r = it->second.get();
+    if (t_submit) *t_submit = r->t_submit;
+    if (t_admit) *t_admit = r->t_admit;
+    if (t_done) *t_done = r->t_done;
+    if (r->state == 4) set_error(r->error);
+    return r->state;
+}
+
+int lbm_gpu_server_fetch(lbm_gpu_server *S, int id, double *f, double *f_new, double *rho,
+                         double *u, double *v, double *spectra) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(id);
+    if (it == S->reqs.end() || it->second->state != 3) {
+        set_error("request not finished");
+        return LBM_GPU_ERR_ARG;
+    }
+    Request *r = it->second.get();
+    const size_t N = (size_t)r->Nx * r->Ny;
+    if ((f || f_new) && !r->keep_populations) {
+        set_error("populations were not kept (keep_populations = 0)");
+        return LBM_GPU_ERR_ARG;
+    }
+    if (f) std::memcpy(f, r->f.data(), N * 9 * sizeof(double));
+    if (f_new) std::memcpy(f_new, r->f_new.data(), N * 9 * sizeof(double));
+    if (rho) std::memcpy(rho, r->rho.data(), N * sizeof(double));
+    if (u) std::memcpy(u, r->u.data(), N * sizeof(double));
+    if (v) std::memcpy(v, r->v.data(), N * sizeof(double));
+    if (spectra && !r->spectra.empty()) std::memcpy(spectra, r->spectra.data(), r->spectra.size() * sizeof(double));
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_server_release(lbm_gpu_server *S, int id) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(id);
+    if (it == S->reqs.end() || it->second->state == 1 || it->second->state == 2) {
+        set_error("request not found or still running");
+        return LBM_GPU_ERR_ARG;
+    }
+    S->reqs.erase(it);
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_server_stats(lbm_gpu_server *S, long long *lups_done, double *busy_s, int *queued,
+                         int *active, size_t *bytes_in_use) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (lups_done) *lups_done = S->lups_done;
+    if (busy_s) *busy_s = S->busy_s;
+    if (queued) *queued = (int)S->queue.size();
+    if (active) *active = (int)S->active.size();
+    if (bytes_in_use) *bytes_in_use = S->in_use;
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_server_destroy(lbm_gpu_server *S) {
+    if (!S) return LBM_GPU_OK;
+    lbm_gpu_server_stop(S);
+    for (Request *r : S->active) r->solver.reset();
+    delete S;
+    return LBM_GPU_OK;
+}
+
+}  // extern "C"

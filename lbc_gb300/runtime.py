@@ -91,6 +91,20 @@ def _bind_ext(lib: C.CDLL) -> None:
                                                  C.c_int]),
         "lbm_gpu_impedance_readback": (C.c_int, [vp, C.c_int, dp, dp]),
         "lbm_gpu_msd_zoh": (C.c_int, [C.c_double, C.c_double, C.c_double, dp, dp]),
+        "lbm_gpu_server_create": (C.c_int, [C.c_size_t, C.c_int, C.c_int, C.POINTER(vp)]),
+        "lbm_gpu_server_prepare": (C.c_int, [vp, C.POINTER(CaseDesc), dp, dp, dp, dp, dp, C.c_int, C.c_int]),
+        "lbm_gpu_server_set_impedance": (C.c_int, [vp, C.c_int, C.c_int, dp, dp, dp, C.c_int, dp, C.c_double,
+                                                   C.c_double, C.c_int]),
+        "lbm_gpu_server_enqueue": (C.c_int, [vp, C.c_int]),
+        "lbm_gpu_server_poll": (C.c_int, [vp]),
+        "lbm_gpu_server_start": (C.c_int, [vp]),
+        "lbm_gpu_server_stop": (C.c_int, [vp]),
+        "lbm_gpu_server_status": (C.c_int, [vp, C.c_int, dp, dp, dp]),
+        "lbm_gpu_server_fetch": (C.c_int, [vp, C.c_int, dp, dp, dp, dp, dp, dp]),
+        "lbm_gpu_server_release": (C.c_int, [vp, C.c_int]),
+        "lbm_gpu_server_stats": (C.c_int, [vp, C.POINTER(C.c_longlong), dp, C.POINTER(C.c_int),
+                                           C.POINTER(C.c_int), C.POINTER(C.c_size_t)]),
+        "lbm_gpu_server_destroy": (C.c_int, [vp]),
         "lbm_gpu_host_alloc": (vp, [C.c_size_t]),
         "lbm_gpu_host_free": (None, [vp]),
         "lbm_gpu_dropin_release": (None, []),
@@ -132,6 +146,32 @@ class PinnedArray:
         if getattr(self, "_p", None):
             load_library().lbm_gpu_host_free(self._p)
             self._p = None
+
+
+def case_desc(lib, case: Case, storage: int):
+    """lbm_gpu_case for a Case; returns (desc, keep-alive list)."""
+    abi = LbcAbi(lib)
+    bnd = abi.boundaries(case.bcs)
+    keep = [bnd, case.cx, case.cy, case.opp, case.w, case.omega_eff, case.solid_mask, case.phi]
+    d = CaseDesc()
+    d.Nx, d.Ny = case.Nx, case.Ny
+    d.cx, d.cy, d.opp = iptr(case.cx), iptr(case.cy), iptr(case.opp)
+    d.w = dptr(case.w)
+    d.omega_eff = dptr(case.omega_eff)
+    d.solid_mask = iptr(case.solid_mask)
+    d.phi = dptr(case.phi)
+    d.use_IBB = case.use_IBB
+    d.boundaries = C.cast(bnd[0], C.c_void_p)
+    d.num_boundaries = len(case.bcs)
+    d.isperiodic_x, d.isperiodic_y = case.isperiodic_x, case.isperiodic_y
+    d.Fx, d.Fy = case.Fx, case.Fy
+    if case.wall_u is not None:
+        wu = np.ascontiguousarray(case.wall_u, dtype=np.float64)
+        wv = np.ascontiguousarray(case.wall_v if case.wall_v is not None else np.zeros_like(wu))
+        keep += [wu, wv]
+        d.wall_u, d.wall_v = dptr(wu), dptr(wv)
+    d.storage = storage
+    return d, keep
 
 
 class GpuSolver:
@@ -280,6 +320,79 @@ class GpuBatch:
     def close(self):
         if getattr(self, "h", None):
             self.lib.lbm_gpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class GpuServer:
+    """Continuous-batching request loop (lbm_gpu_server_*)."""
+
+    def __init__(self, budget_bytes: int = 0, max_active: int = 64, chunk_steps: int = 1000):
+        self.lib = load_library()
+        h = C.c_void_p()
+        _check(self.lib.lbm_gpu_server_create(budget_bytes, max_active, chunk_steps, C.byref(h)),
+               "lbm_gpu_server_create")
+        self.h = h
+        self.meta = {}
+
+    def submit(self, case: Case, st: State, nsteps: int, storage: int, keep_populations=False,
+               impedance=None) -> int:
+        """impedance: (entry, R, m, K, omegas, rho_ref, alpha, window) or None."""
+        d, keep = case_desc(self.lib, case, storage)
+        rid = self.lib.lbm_gpu_server_prepare(self.h, C.byref(d), dptr(st.f), dptr(st.f_new), dptr(st.rho),
+                                              dptr(st.u), dptr(st.v), nsteps, 1 if keep_populations else 0)
+        if rid <= 0:
+            raise RuntimeError("lbm_gpu_server_prepare failed: " + last_error())
+        if impedance is not None:
+            entry, R, m, K, om, rho_ref, alpha, window = impedance
+            R, m, K, om = (np.ascontiguousarray(a, dtype=np.float64) for a in (R, m, K, om))
+            _check(self.lib.lbm_gpu_server_set_impedance(self.h, rid, entry, dptr(R), dptr(m), dptr(K), len(om),
+                                                         dptr(om), rho_ref, alpha, window),
+                   "lbm_gpu_server_set_impedance")
+        self.meta[rid] = (case.Nx, case.Ny, nsteps, len(impedance[4]) if impedance else 0)
+        _check(self.lib.lbm_gpu_server_enqueue(self.h, rid), "lbm_gpu_server_enqueue")
+        return rid
+
+    def poll(self) -> int:
+        return self.lib.lbm_gpu_server_poll(self.h)
+
+    def start(self):
+        _check(self.lib.lbm_gpu_server_start(self.h), "lbm_gpu_server_start")
+
+    def stop(self):
+        self.lib.lbm_gpu_server_stop(self.h)
+
+    def status(self, rid: int):
+        ts, ta, td = C.c_double(), C.c_double(), C.c_double()
+        st = self.lib.lbm_gpu_server_status(self.h, rid, C.byref(ts), C.byref(ta), C.byref(td))
+        return st, ts.value, ta.value, td.value
+
+    def fetch(self, rid: int, populations=False):
+        Nx, Ny, _, nf = self.meta[rid]
+        rho, u, v = np.empty((Ny, Nx)), np.empty((Ny, Nx)), np.empty((Ny, Nx))
+        f = np.empty((Ny, Nx, Q)) if populations else None
+        fn = np.empty((Ny, Nx, Q)) if populations else None
+        spec = np.zeros((Nx, max(nf, 1), 4))
+        _check(self.lib.lbm_gpu_server_fetch(self.h, rid, dptr(f) if populations else None,
+                                             dptr(fn) if populations else None, dptr(rho), dptr(u), dptr(v),
+                                             dptr(spec)), "lbm_gpu_server_fetch")
+        return {"rho": rho, "u": u, "v": v, "f": f, "f_new": fn, "spectra": spec[:, :nf]}
+
+    def release(self, rid: int):
+        self.lib.lbm_gpu_server_release(self.h, rid)
+        self.meta.pop(rid, None)
+
+    def stats(self):
+        l, b, q, a, m = C.c_longlong(), C.c_double(), C.c_int(), C.c_int(), C.c_size_t()
+        _check(self.lib.lbm_gpu_server_stats(self.h, C.byref(l), C.byref(b), C.byref(q), C.byref(a), C.byref(m)),
+               "lbm_gpu_server_stats")
+        return {"lups": l.value, "busy_s": b.value, "queued": q.value, "active": a.value, "bytes": m.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.lbm_gpu_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

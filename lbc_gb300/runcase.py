@@ -34,7 +34,19 @@ def main(argv=None):
     p.add_argument("--warmup", type=int, default=2)
     p.add_argument("--block", default="", help="bx,by thread block of the fused step")
     p.add_argument("--ducts", type=int, default=0, help="run this many seeded liner ducts as one batch")
+    p.add_argument("--serve", type=int, default=0, help="serve a seeded stream of this many requests")
+    p.add_argument("--scale", type=float, default=1.0, help="step-count scale of the served stream")
+    p.add_argument("--rate", type=float, default=200.0, help="arrival rate of the served stream (1/s)")
+    p.add_argument("--max-active", type=int, default=64)
+    p.add_argument("--chunk", type=int, default=1000)
     a = p.parse_args(argv)
+    if a.serve:
+        from lbc_gb300 import serving
+        stream = serving.make_stream(a.serve, rate=a.rate, scale=a.scale)
+        r = serving.serve(stream, a.max_active, a.chunk)
+        r["serial_fp64"] = serving.serial_fp64_estimate(stream)
+        print(json.dumps(r))
+        return
     if a.ducts:
         from lbc_gb300 import impedance as imp
         r = imp.run_liner_batch(a.ducts, a.steps, STORAGE[a.storage])

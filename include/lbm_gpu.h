@@ -178,6 +178,26 @@ int lbm_gpu_server_stats(lbm_gpu_server *srv, long long *lups_done, double *busy
                          int *active, size_t *bytes_in_use);
 int lbm_gpu_server_destroy(lbm_gpu_server *srv);
 
+/* ---- Force on caller-owned device memory, allocating nothing (no counterpart
+ * in lbc; it is compute_force_mem of lbm_core.h on device arrays).
+ * For callers that cannot let a library allocate device memory: processes
+ * whose device memory is already held by their own pool (a framework's caching
+ * allocator, a server that reserves memory up front) and loops that must not
+ * stall the device, which cudaMalloc / cudaFree would do. f, f_new
+ * ([Ny][Nx][9], lbc's layout) and solid_mask ([Ny][Nx]) are device arrays;
+ * cx, cy, opp are host arrays (NULL: lbc's ordering); out is a device array of
+ * two doubles that receives (x, y), asynchronously on `stream` (a
+ * cudaStream_t, NULL for the default stream). Limit: at most 65536 blocks of
+ * 64 x 4 nodes (4096 x 4096); larger grids are rejected with LBM_GPU_ERR_ARG.
+ * Its scratch is a fixed 1 MiB device array inside the library, held on every
+ * GPU that loads it until exit. The first call on a device looks up that
+ * array's address (make it before any stream capture); calls share the array,
+ * so calls that overlap on the GPU race: order them. */
+int lbm_gpu_compute_force_mem_noalloc(int Nx, int Ny, int Q, const double *f, const double *f_new,
+                                      const int *solid_mask, int isperiodic_x, int isperiodic_y,
+                                      const int *cx, const int *cy, const int *opp, double *out,
+                                      void *stream);
+
 /* Page-locked host memory for fast transfers. */
 void *lbm_gpu_host_alloc(size_t bytes);
 void lbm_gpu_host_free(void *p);

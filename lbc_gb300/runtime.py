@@ -105,6 +105,9 @@ def _bind_ext(lib: C.CDLL) -> None:
         "lbm_gpu_server_stats": (C.c_int, [vp, C.POINTER(C.c_longlong), dp, C.POINTER(C.c_int),
                                            C.POINTER(C.c_int), C.POINTER(C.c_size_t)]),
         "lbm_gpu_server_destroy": (C.c_int, [vp]),
+        "lbm_gpu_compute_force_mem_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_int, C.c_int,
+                                                        C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                                        C.POINTER(C.c_int), vp, vp]),
         "lbm_gpu_host_alloc": (vp, [C.c_size_t]),
         "lbm_gpu_host_free": (None, [vp]),
         "lbm_gpu_dropin_release": (None, []),

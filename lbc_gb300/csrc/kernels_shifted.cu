@@ -77,124 +77,147 @@ __device__ __forceinline__ void collide_shifted(float g[9], const float w[9], fl
     }
 }
 
-template <typename T, bool FLAGS, bool COLLIDE>
-__device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int i, int j,
-                                                  float &mfx, float &mfy, bool &link) {
-    const StepParams &p = fp.s;
-    {
-        const long long node = (long long)j * p.pitch + i;
-        const uint16_t fl = FLAGS ? p.flags[node] : (uint16_t)0;
-        const size_t dn = (size_t)j * (size_t)p.Nx + (size_t)i;
-        if (FLAGS && (fl & NF_SOLID)) {
-            if (p.write_macro) { p.rho[dn] = NAN; p.ux[dn] = NAN; p.uy[dn] = NAN; }
-            if (fl & NF_BAND) {
-                const int slot = band_slot(p.colbase, p.rowbase, i, j);
-                const T *Dst = (const T *)p.dst;
+// Rare per-node outputs, kept out of line so the compiler cannot hoist their
+// FP64 conversions into every thread's path (FP64 issue is slow on GB300).
+template <typename T>
+__device__ __noinline__ void solid_node_outputs(const StepParams &p, int i, int j, long long node,
+                                                size_t dn, uint16_t fl) {
+    if (p.write_macro) { p.rho[dn] = NAN; p.ux[dn] = NAN; p.uy[dn] = NAN; }
+    if (fl & NF_BAND) {
+        // A BC may read a solid neighbour: lbc sees the untouched buffer
+        // content and NaN moments there.
+        const int slot = band_slot(p.colbase, p.rowbase, i, j);
+        const T *Dst = (const T *)p.dst;
 #pragma unroll
-                for (int k = 0; k < 9; k++)
-                    p.bandf[(size_t)k * p.nslots + slot] = (double)SV<T>::ld_plain(Dst + k * p.plane + node) + p.w[k];
-                p.bandm_next[slot] = NAN;
-                p.bandm_next[(size_t)p.nslots + slot] = NAN;
-                p.bandm_next[2 * (size_t)p.nslots + slot] = NAN;
-            }
-        } else {
-            const T *S = (const T *)p.src;
-            T *Dst = (T *)p.dst;
-            const long long pl = p.plane;
-            // Source neighbours: wrapped on periodic axes, clamped otherwise so
-            // that all nine loads are in bounds and can be issued at once; the
-            // flag word then says which of them to replace.
-            int im = i - 1, ip = i + 1, jm = j - 1, jp = j + 1;
-            if (p.px) { if (im < 0) im += p.Nx; if (ip >= p.Nx) ip -= p.Nx; }
-            else { im = max(im, 0); ip = min(ip, p.Nx - 1); }
-            if (p.py) { if (jm < 0) jm += p.Ny; if (jp >= p.Ny) jp -= p.Ny; }
-            else { jm = max(jm, 0); jp = min(jp, p.Ny - 1); }
-            const long long r0 = (long long)j * p.pitch, rm = (long long)jm * p.pitch,
-                            rp = (long long)jp * p.pitch;
-            const long long so[9] = {r0 + i, r0 + im, rm + i, r0 + ip, rp + i,
-                                     rm + im, rm + ip, rp + ip, rp + im};
-            float g[9];
-#pragma unroll
-            for (int k = 0; k < 9; k++) g[k] = SV<T>::ld(S + k * pl + so[k]);
-            if (FLAGS && (fl & NF_SPECIAL_MASK)) {
-                const Link *lk = (fl & NF_LINKS) ? p.links + p.link_off[node] : nullptr;
-#pragma unroll
-                for (int k = 0; k < 9; k++) {
-                    if (!(fl & (1u << k))) continue;
-                    const int si = i - cxk(k), sj = j - cyk(k);
-                    const bool off = (!p.px && (si < 0 || si >= p.Nx)) ||
-                                     (!p.py && (sj < 0 || sj >= p.Ny));
-                    if (off) {
-                        g[k] = SV<T>::ld_plain(Dst + k * pl + node);
-                        continue;
-                    }
-                    const int ko = oppk(k);
-                    const float own = SV<T>::ld(S + ko * pl + node);
-                    float val = own;
-                    if (lk) {
-                        const Link L = *lk++;
-                        if (L.mode == LINK_IBB_LO)
-                            val = (float)L.c1 * own + (float)L.c2 * SV<T>::ld(S + ko * pl + L.behind);
-                        else if (L.mode == LINK_IBB_HI)
-                            val = (float)L.c1 * own + (float)L.c2 * SV<T>::ld(S + k * pl + L.behind);
-                        else if (L.mode == LINK_MOVING)
-                            val = own - (float)L.c2;
-                    }
-                    g[k] = val;
-                    // Per-node link sum in FP32 (a few terms); the block and
-                    // case sums are FP64.
-                    const float df = (own + val) + 2.0f * fp.wf[k];
-                    mfx -= df * cxk(k);
-                    mfy -= df * cyk(k);
-                    link = true;
-                }
-            }
-            int slot = -1;
-            if (FLAGS && (fl & NF_BAND)) {
-                slot = band_slot(p.colbase, p.rowbase, i, j);
-#pragma unroll
-                for (int k = 0; k < 9; k++) p.bandf[(size_t)k * p.nslots + slot] = (double)g[k] + p.w[k];
-            }
-            if (!(FLAGS && (fl & NF_BCW))) {
-                float dr, rho, ux, uy;
-                moments_shifted(g, fp.hFxf, fp.hFyf, dr, rho, ux, uy);
-                if (p.write_macro) { p.rho[dn] = 1.0 + (double)dr; p.ux[dn] = ux; p.uy[dn] = uy; }
-                if (slot >= 0) {
-                    p.bandm_next[slot] = 1.0 + (double)dr;
-                    p.bandm_next[(size_t)p.nslots + slot] = ux;
-                    p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
-                }
-                if (COLLIDE) {
-                    const float om = p.omega ? (float)p.omega[dn] : fp.omega0f;
-                    collide_shifted(g, fp.wf, dr, rho, ux, uy, om, p.has_force != 0, fp.Fxf, fp.Fyf);
-                }
-#pragma unroll
-                for (int k = 0; k < 9; k++) SV<T>::st(Dst + k * pl + node, g[k]);
-            }
-        }
+        for (int k = 0; k < 9; k++)
+            p.bandf[(size_t)k * p.nslots + slot] = (double)SV<T>::ld_plain(Dst + k * p.plane + node) + p.w[k];
+        p.bandm_next[slot] = NAN;
+        p.bandm_next[(size_t)p.nslots + slot] = NAN;
+        p.bandm_next[2 * (size_t)p.nslots + slot] = NAN;
     }
 }
 
+__device__ __noinline__ void band_store_f(const StepParams &p, int slot, float g0, float g1, float g2,
+                                          float g3, float g4, float g5, float g6, float g7, float g8) {
+    const float g[9] = {g0, g1, g2, g3, g4, g5, g6, g7, g8};
+#pragma unroll
+    for (int k = 0; k < 9; k++) p.bandf[(size_t)k * p.nslots + slot] = (double)g[k] + p.w[k];
+}
+
+__device__ __noinline__ void macro_store(const StepParams &p, size_t dn, int slot, float dr, float ux,
+                                         float uy) {
+    if (p.write_macro) { p.rho[dn] = 1.0 + (double)dr; p.ux[dn] = ux; p.uy[dn] = uy; }
+    if (slot >= 0) {
+        p.bandm_next[slot] = 1.0 + (double)dr;
+        p.bandm_next[(size_t)p.nslots + slot] = ux;
+        p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
+    }
+}
+
+// One node of the fused step in shifted storage. I is the element-offset type:
+// int whenever all nine planes fit in 2^31 elements (fewer address
+// instructions), long long otherwise.
+template <typename T, typename I, bool FLAGS, bool COLLIDE>
+__device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int i, int j,
+                                                  float &mfx, float &mfy, bool &link) {
+    const StepParams &p = fp.s;
+    const I node = (I)j * (I)p.pitch + (I)i;
+    const uint16_t fl = FLAGS ? p.flags[node] : (uint16_t)0;
+    const size_t dn = (size_t)j * (size_t)p.Nx + (size_t)i;
+    if (FLAGS && (fl & NF_SOLID)) {
+        solid_node_outputs<T>(p, i, j, (long long)node, dn, fl);
+        return;
+    }
+    const T *S = (const T *)p.src;
+    T *Dst = (T *)p.dst;
+    const I pl = (I)p.plane;
+    // Source neighbours: wrapped on periodic axes, clamped otherwise so that
+    // all nine loads are in bounds and can be issued at once; the flag word
+    // then says which of them to replace.
+    int im = i - 1, ip = i + 1, jm = j - 1, jp = j + 1;
+    if (p.px) { if (im < 0) im += p.Nx; if (ip >= p.Nx) ip -= p.Nx; }
+    else { im = max(im, 0); ip = min(ip, p.Nx - 1); }
+    if (p.py) { if (jm < 0) jm += p.Ny; if (jp >= p.Ny) jp -= p.Ny; }
+    else { jm = max(jm, 0); jp = min(jp, p.Ny - 1); }
+    const I r0 = (I)j * (I)p.pitch, rm = (I)jm * (I)p.pitch, rp = (I)jp * (I)p.pitch;
+    const I so[9] = {r0 + i, r0 + im, rm + i, r0 + ip, rp + i, rm + im, rm + ip, rp + ip, rp + im};
+    float g[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) g[k] = SV<T>::ld(S + (I)k * pl + so[k]);
+    if (FLAGS && (fl & NF_SPECIAL_MASK)) {
+        const Link *lk = (fl & NF_LINKS) ? p.links + p.link_off[node] : nullptr;
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            if (!(fl & (1u << k))) continue;
+            const int si = i - cxk(k), sj = j - cyk(k);
+            const bool off = (!p.px && (si < 0 || si >= p.Nx)) || (!p.py && (sj < 0 || sj >= p.Ny));
+            if (off) {
+                g[k] = SV<T>::ld_plain(Dst + (I)k * pl + node);
+                continue;
+            }
+            const int ko = oppk(k);
+            const float own = SV<T>::ld(S + (I)ko * pl + node);
+            float val = own;
+            if (lk) {
+                const Link L = *lk++;
+                if (L.mode == LINK_IBB_LO)
+                    val = (float)L.c1 * own + (float)L.c2 * SV<T>::ld(S + (I)ko * pl + (I)L.behind);
+                else if (L.mode == LINK_IBB_HI)
+                    val = (float)L.c1 * own + (float)L.c2 * SV<T>::ld(S + (I)k * pl + (I)L.behind);
+                else if (L.mode == LINK_MOVING)
+                    val = own - (float)L.c2;
+            }
+            g[k] = val;
+            // Per-node link sum in FP32 (a few terms); block and case sums are FP64.
+            const float df = (own + val) + 2.0f * fp.wf[k];
+            mfx -= df * cxk(k);
+            mfy -= df * cyk(k);
+            link = true;
+        }
+    }
+    int slot = -1;
+    if (FLAGS && (fl & NF_BAND)) {
+        slot = band_slot(p.colbase, p.rowbase, i, j);
+        band_store_f(p, slot, g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7], g[8]);
+    }
+    if (FLAGS && (fl & NF_BCW)) return;
+    float dr, rho, ux, uy;
+    moments_shifted(g, fp.hFxf, fp.hFyf, dr, rho, ux, uy);
+    if (FLAGS) {
+        if (p.write_macro || slot >= 0) macro_store(p, dn, slot, dr, ux, uy);
+    } else if (p.write_macro) {
+        p.rho[dn] = 1.0 + (double)dr;
+        p.ux[dn] = ux;
+        p.uy[dn] = uy;
+    }
+    if (COLLIDE) {
+        const float om = p.omega ? (float)p.omega[dn] : fp.omega0f;
+        collide_shifted(g, fp.wf, dr, rho, ux, uy, om, p.has_force != 0, fp.Fxf, fp.Fyf);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) SV<T>::st(Dst + (I)k * pl + node, g[k]);
+}
+
 // Fully periodic grid without solids or edge BCs: no flag word, 32 registers.
-template <typename T, bool COLLIDE>
+template <typename T, typename I, bool COLLIDE>
 __global__ void __launch_bounds__(256) k_step_shifted_plain(const FastStepParams fp) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     float mfx = 0.f, mfy = 0.f;
     bool link = false;
-    if (i < fp.s.Nx && j < fp.s.Ny) step_node_shifted<T, false, COLLIDE>(fp, i, j, mfx, mfy, link);
+    if (i < fp.s.Nx && j < fp.s.Ny) step_node_shifted<T, I, false, COLLIDE>(fp, i, j, mfx, mfy, link);
 }
 
 // General geometry (flag word per node). The occupancy hint keeps it at five
 // resident blocks per SM (48 registers) without spills.
-template <typename T, bool COLLIDE>
+template <typename T, typename I, bool COLLIDE>
 __global__ void __launch_bounds__(256, 5) k_step_shifted_geo(const FastStepParams fp) {
     const StepParams &p = fp.s;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     float mfx = 0.f, mfy = 0.f;
     bool link = false;
-    if (i < p.Nx && j < p.Ny) step_node_shifted<T, true, COLLIDE>(fp, i, j, mfx, mfy, link);
+    if (i < p.Nx && j < p.Ny) step_node_shifted<T, I, true, COLLIDE>(fp, i, j, mfx, mfy, link);
     if (p.mem_partials) {
         const int slot = p.blk_slot[blockIdx.y * gridDim.x + blockIdx.x];
         if (slot >= 0) block_reduce2_store(mfx, mfy, link, p.mem_partials + 2 * (size_t)slot);
@@ -215,9 +238,9 @@ __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepPar
         bool link = false;
         const bool in = i < fp.s.Nx && j < fp.s.Ny;
         if (fp.s.flags) {
-            if (in) step_node_shifted<T, true, true>(fp, i, j, mfx, mfy, link);
+            if (in) step_node_shifted<T, long long, true, true>(fp, i, j, mfx, mfy, link);
         } else {
-            if (in) step_node_shifted<T, false, true>(fp, i, j, mfx, mfy, link);
+            if (in) step_node_shifted<T, long long, false, true>(fp, i, j, mfx, mfy, link);
         }
         if (td.w) block_reduce2_store(mfx, mfy, link, partials + 2 * (size_t)(td.w - 1));
     }
@@ -299,16 +322,24 @@ cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s) {
 }
 
 
+template <typename T, typename I>
+static void step_shifted_ti(const FastStepParams &p, bool flags, bool collide, dim3 g, dim3 b,
+                            cudaStream_t s) {
+    if (flags) {
+        if (collide) k_step_shifted_geo<T, I, true><<<g, b, 0, s>>>(p);
+        else k_step_shifted_geo<T, I, false><<<g, b, 0, s>>>(p);
+    } else {
+        if (collide) k_step_shifted_plain<T, I, true><<<g, b, 0, s>>>(p);
+        else k_step_shifted_plain<T, I, false><<<g, b, 0, s>>>(p);
+    }
+}
+
 template <typename T>
 static void step_shifted_t(const FastStepParams &p, bool flags, bool collide, dim3 g, dim3 b,
                            cudaStream_t s) {
-    if (flags) {
-        if (collide) k_step_shifted_geo<T, true><<<g, b, 0, s>>>(p);
-        else k_step_shifted_geo<T, false><<<g, b, 0, s>>>(p);
-    } else {
-        if (collide) k_step_shifted_plain<T, true><<<g, b, 0, s>>>(p);
-        else k_step_shifted_plain<T, false><<<g, b, 0, s>>>(p);
-    }
+    // 32-bit element offsets whenever all nine planes fit.
+    if (9LL * p.s.plane < (1LL << 31)) step_shifted_ti<T, int>(p, flags, collide, g, b, s);
+    else step_shifted_ti<T, long long>(p, flags, collide, g, b, s);
 }
 
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,

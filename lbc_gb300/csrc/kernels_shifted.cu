@@ -26,43 +26,55 @@ template <> struct SV<__half> {
     static __device__ __forceinline__ void st(__half *p, float v) { *p = __float2half_rn(v); }
 };
 
-// Shifted moments: delta rho = sum g, j = sum c g (sum c w = 0).
+// Shifted moments: delta rho = sum g, j = sum c g (sum c w = 0). Jx, Jy are the
+// momentum including half the body force (rho u of lbc).
 __device__ __forceinline__ void moments_shifted(const float g[9], float hFx, float hFy, float &dr,
-                                                float &rho, float &ux, float &uy) {
+                                                float &rho, float &ux, float &uy, float &Jx,
+                                                float &Jy) {
     dr = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
     const float jx = (g[1] - g[3]) + (g[5] - g[6]) + (g[8] - g[7]);
     const float jy = (g[2] - g[4]) + (g[5] + g[6]) - (g[7] + g[8]);
     rho = 1.0f + dr;
     if (rho < 1e-16f) rho = 1e-16f;
     const float inv = 1.0f / rho;
-    ux = (jx + hFx) * inv;
-    uy = (jy + hFy) * inv;
+    Jx = jx + hFx;
+    Jy = jy + hFy;
+    ux = Jx * inv;
+    uy = Jy * inv;
 }
 
-// BGK + Guo on shifted populations: g' = g + om (geq - g) + (1 - om/2) F_k with
-// geq_k = w_k (drho + rho (3 c.u + 4.5 (c.u)^2 - 1.5 u.u)).
+// BGK + Guo on shifted populations, g' = g + om (geq - g) + (1 - om/2) F_k,
+// with geq_k = w_k (drho + rho (3 c.u + 4.5 (c.u)^2 - 1.5 u.u)) built so that
+// its mass and momentum are the node's own by construction: the odd part of
+// each pair is h (c.J) with FP32 coefficients h1 = fl(3 w1) and
+// h5 = (1 - 2 h1) / 4 whose sum rule 2 h1 + 4 h5 = 1 holds exactly, the linear
+// term uses J = rho u directly (no division), and the rest population closes
+// the mass. Rounded weights would otherwise bias every collision's momentum by
+// ~1e-8 in the same direction, an error that grows linearly with the steps.
 __device__ __forceinline__ void collide_shifted(float g[9], const float w[9], float dr, float rho,
-                                                float ux, float uy, float om, bool force,
-                                                float Fx, float Fy) {
-    const float t = 1.5f * (ux * ux + uy * uy);
+                                                float ux, float uy, float Jx, float Jy, float om,
+                                                bool force, float Fx, float Fy) {
+    const float h1 = 3.0f * w[1];
+    const float h5 = (1.0f - 2.0f * h1) * 0.25f;
+    const float rt = 1.5f * (Jx * ux + Jy * uy);  // rho * 1.5 u.u
     float geq[9];
-    geq[0] = w[0] * (dr - rho * t);
     {
-        const float c = ux, X = fmaf(rho, fmaf(4.5f * c, c, -t), dr), Y = rho * 3.0f * c;
-        geq[1] = w[1] * (X + Y); geq[3] = w[3] * (X - Y);
+        const float c = ux, J = Jx, X = w[1] * (dr + fmaf(4.5f * J, c, -rt)), Y = h1 * J;
+        geq[1] = X + Y; geq[3] = X - Y;
     }
     {
-        const float c = uy, X = fmaf(rho, fmaf(4.5f * c, c, -t), dr), Y = rho * 3.0f * c;
-        geq[2] = w[2] * (X + Y); geq[4] = w[4] * (X - Y);
+        const float c = uy, J = Jy, X = w[2] * (dr + fmaf(4.5f * J, c, -rt)), Y = h1 * J;
+        geq[2] = X + Y; geq[4] = X - Y;
     }
     {
-        const float c = ux + uy, X = fmaf(rho, fmaf(4.5f * c, c, -t), dr), Y = rho * 3.0f * c;
-        geq[5] = w[5] * (X + Y); geq[7] = w[7] * (X - Y);
+        const float c = ux + uy, J = Jx + Jy, X = w[5] * (dr + fmaf(4.5f * J, c, -rt)), Y = h5 * J;
+        geq[5] = X + Y; geq[7] = X - Y;
     }
     {
-        const float c = uy - ux, X = fmaf(rho, fmaf(4.5f * c, c, -t), dr), Y = rho * 3.0f * c;
-        geq[6] = w[6] * (X + Y); geq[8] = w[8] * (X - Y);
+        const float c = uy - ux, J = Jy - Jx, X = w[6] * (dr + fmaf(4.5f * J, c, -rt)), Y = h5 * J;
+        geq[6] = X + Y; geq[8] = X - Y;
     }
+    geq[0] = dr - (((geq[1] + geq[3]) + (geq[2] + geq[4])) + ((geq[5] + geq[7]) + (geq[6] + geq[8])));
 #pragma unroll
     for (int k = 0; k < 9; k++) g[k] = fmaf(om, geq[k] - g[k], g[k]);
     if (force) {
@@ -181,8 +193,8 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
         band_store_f(p, slot, g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7], g[8]);
     }
     if (FLAGS && (fl & NF_BCW)) return;
-    float dr, rho, ux, uy;
-    moments_shifted(g, fp.hFxf, fp.hFyf, dr, rho, ux, uy);
+    float dr, rho, ux, uy, Jx, Jy;
+    moments_shifted(g, fp.hFxf, fp.hFyf, dr, rho, ux, uy, Jx, Jy);
     if (FLAGS) {
         if (p.write_macro || slot >= 0) macro_store(p, dn, slot, dr, ux, uy);
     } else if (p.write_macro) {
@@ -192,7 +204,7 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
     }
     if (COLLIDE) {
         const float om = p.omega ? (float)p.omega[dn] : fp.omega0f;
-        collide_shifted(g, fp.wf, dr, rho, ux, uy, om, p.has_force != 0, fp.Fxf, fp.Fyf);
+        collide_shifted(g, fp.wf, dr, rho, ux, uy, Jx, Jy, om, p.has_force != 0, fp.Fxf, fp.Fyf);
     }
 #pragma unroll
     for (int k = 0; k < 9; k++) SV<T>::st(Dst + (I)k * pl + node, g[k]);
@@ -255,8 +267,8 @@ __device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 
         g[k] = (float)(p.bandf[(size_t)k * p.nslots + slot] - p.w[k]);
         wf[k] = (float)p.w[k];
     }
-    float dr, rho, ux, uy;
-    moments_shifted(g, (float)p.hFx, (float)p.hFy, dr, rho, ux, uy);
+    float dr, rho, ux, uy, Jx, Jy;
+    moments_shifted(g, (float)p.hFx, (float)p.hFy, dr, rho, ux, uy, Jx, Jy);
     const size_t dn = (size_t)ij.y * p.Nx + ij.x;
     if (p.write_macro) { p.rho[dn] = 1.0 + (double)dr; p.ux[dn] = ux; p.uy[dn] = uy; }
     p.bandm_next[slot] = 1.0 + (double)dr;
@@ -264,7 +276,7 @@ __device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 
     p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
     if (COLLIDE) {
         const float om = p.omega ? (float)p.omega[dn] : (float)p.omega0;
-        collide_shifted(g, wf, dr, rho, ux, uy, om, p.has_force != 0, (float)p.Fx, (float)p.Fy);
+        collide_shifted(g, wf, dr, rho, ux, uy, Jx, Jy, om, p.has_force != 0, (float)p.Fx, (float)p.Fy);
     }
     T *D = (T *)p.dst;
     const long long node = (long long)ij.y * p.pitch + ij.x;
@@ -305,8 +317,9 @@ __global__ void k_collide_shifted(const CollideParams p) {
     const float rho = (float)p.rho[dn];
     const float dr = (float)(p.rho[dn] - 1.0);
     const float om = p.omega ? (float)p.omega[dn] : (float)p.omega0;
-    collide_shifted(g, wf, dr, rho, (float)p.ux[dn], (float)p.uy[dn], om, p.has_force != 0,
-                    (float)p.Fx, (float)p.Fy);
+    const float ux = (float)p.ux[dn], uy = (float)p.uy[dn];
+    collide_shifted(g, wf, dr, rho, ux, uy, (float)(p.rho[dn] * p.ux[dn]), (float)(p.rho[dn] * p.uy[dn]), om,
+                    p.has_force != 0, (float)p.Fx, (float)p.Fy);
 #pragma unroll
     for (int k = 0; k < 9; k++) SV<T>::st(F + k * p.plane + node, g[k]);
 }

@@ -403,6 +403,7 @@ bool Solver::set_state(const double *f, const double *f_new, const double *rho, 
     const int Nx = d_.Nx, Ny = d_.Ny;
     const size_t N = (size_t)Nx * Ny;
     cur_ = 0;
+    fields_are_moments_ = false;  // the caller's fields: lbc collides with them as given
     const double *src[2] = {f, f_new};
     for (int b = 0; b < 2; b++) {
         // The drop-in skips f_new when its old content cannot reach the
@@ -544,6 +545,7 @@ bool Solver::launch_collide(int b, cudaStream_t s) {
     c.has_force = (d_.Fx != 0.0 || d_.Fy != 0.0);
     c.Fx = d_.Fx; c.Fy = d_.Fy;
     for (int k = 0; k < 9; k++) c.w[k] = d_.w[k];
+    c.from_pops = fields_are_moments_ ? 1 : 0;
     if (d_.store == STORE_F64) CK(launch::collide_exact(c, s));
     else CK(launch::collide_shifted(c, d_.store, s));
     return true;
@@ -766,6 +768,7 @@ bool Solver::begin_steps(cudaStream_t s) { return launch_collide(cur_, s); }
 bool Solver::end_steps(cudaStream_t s) {
     if (!launch_step(cur_, 1 - cur_, false, true, parity_, s)) return false;
     advance(1);
+    fields_are_moments_ = true;
     return true;
 }
 
@@ -822,6 +825,7 @@ bool Solver::run(int nsteps) {
     cur_ ^= 1;
     parity_ ^= 1;
     steps_done_ += nsteps;
+    fields_are_moments_ = true;
     return true;
 }
 

@@ -21,6 +21,10 @@ struct CollideParams {
     int has_force;
     double Fx, Fy;
     double w[9];
+    // Shifted storage only: the stored fields are the moments of the
+    // populations (state left by a previous run), so recompute them from the
+    // populations in the fused step's own arithmetic.
+    int from_pops;
 };
 
 // Collision that reads lbc's AoS populations where they are (host memory the

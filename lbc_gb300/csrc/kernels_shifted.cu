@@ -314,12 +314,19 @@ __global__ void k_collide_shifted(const CollideParams p) {
     float g[9], wf[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) { g[k] = SV<T>::ld_plain(F + k * p.plane + node); wf[k] = (float)p.w[k]; }
-    const float rho = (float)p.rho[dn];
-    const float dr = (float)(p.rho[dn] - 1.0);
     const float om = p.omega ? (float)p.omega[dn] : (float)p.omega0;
-    const float ux = (float)p.ux[dn], uy = (float)p.uy[dn];
-    collide_shifted(g, wf, dr, rho, ux, uy, (float)(p.rho[dn] * p.ux[dn]), (float)(p.rho[dn] * p.uy[dn]), om,
-                    p.has_force != 0, (float)p.Fx, (float)p.Fy);
+    float dr, rho, ux, uy, Jx, Jy;
+    if (p.from_pops) {
+        moments_shifted(g, (float)(0.5 * p.Fx), (float)(0.5 * p.Fy), dr, rho, ux, uy, Jx, Jy);
+    } else {
+        rho = (float)p.rho[dn];
+        dr = (float)(p.rho[dn] - 1.0);
+        ux = (float)p.ux[dn];
+        uy = (float)p.uy[dn];
+        Jx = (float)(p.rho[dn] * p.ux[dn]);
+        Jy = (float)(p.rho[dn] * p.uy[dn]);
+    }
+    collide_shifted(g, wf, dr, rho, ux, uy, Jx, Jy, om, p.has_force != 0, (float)p.Fx, (float)p.Fy);
 #pragma unroll
     for (int k = 0; k < 9; k++) SV<T>::st(F + k * p.plane + node, g[k]);
 }

@@ -95,16 +95,17 @@ def test_resident_run_matches_lbc(oracle, name):
         assert force_close(h[:, 0], fo[:, 1], scale=mag) and force_close(h[:, 1], fo[:, 0], scale=mag)
 
 
+@pytest.mark.parametrize("storage", ["f64", "f32", "f16"])
 @pytest.mark.parametrize("name", ["zoo_ibb", "zoo_convective_chain", "taylor_green", "zoo_open_edges"])
-def test_chunked_runs_and_block_shapes_agree(name):
+def test_chunked_runs_and_block_shapes_agree(name, storage):
     """run(a); run(b) == run(a + b) bit for bit, and the result does not
     depend on the thread-block shape (no races between nodes)."""
-    from lbc_gb300 import F64, GpuSolver
+    from lbc_gb300 import STORAGE, GpuSolver
     (case, st), steps = casezoo.build(name)
     ref = None
     for bx, by, chunks in [(64, 4, [steps]), (32, 8, [7, steps - 7]), (128, 2, [1, 2, steps - 3]),
                            (256, 1, [steps - 1, 1])]:
-        s = GpuSolver(case, F64)
+        s = GpuSolver(case, STORAGE[storage])
         s.set_block(bx, by)
         s.set_state(st)
         for c in chunks:
@@ -114,7 +115,7 @@ def test_chunked_runs_and_block_shapes_agree(name):
             ref = out
         else:
             for fld in FIELDS:
-                assert same(getattr(out, fld), getattr(ref, fld)), (name, bx, by, chunks, fld)
+                assert same(getattr(out, fld), getattr(ref, fld)), (name, storage, bx, by, chunks, fld)
 
 
 def test_cylinder_golden_forces_on_gpu():

@@ -15,15 +15,21 @@
 namespace lbm {
 
 template <typename T> struct SV;
+// rnd: the value as the storage type would hold it. Pre-collision values that
+// are computed rather than loaded (bounce-back interpolation, edge BCs) are
+// rounded to the storage type before the collision, so a run split into
+// chunks (whose boundaries store and reload them) gives the same bits.
 template <> struct SV<float> {
     static __device__ __forceinline__ float ld(const float *p) { return __ldg(p); }
     static __device__ __forceinline__ float ld_plain(const float *p) { return *p; }
     static __device__ __forceinline__ void st(float *p, float v) { *p = v; }
+    static __device__ __forceinline__ float rnd(float v) { return v; }
 };
 template <> struct SV<__half> {
     static __device__ __forceinline__ float ld(const __half *p) { return __half2float(__ldg(p)); }
     static __device__ __forceinline__ float ld_plain(const __half *p) { return __half2float(*p); }
     static __device__ __forceinline__ void st(__half *p, float v) { *p = __float2half_rn(v); }
+    static __device__ __forceinline__ float rnd(float v) { return __half2float(__float2half_rn(v)); }
 };
 
 // Shifted moments: delta rho = sum g, j = sum c g (sum c w = 0). Jx, Jy are the
@@ -179,7 +185,7 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
                 else if (L.mode == LINK_MOVING)
                     val = own - (float)L.c2;
             }
-            g[k] = val;
+            g[k] = SV<T>::rnd(val);
             // Per-node link sum in FP32 (a few terms); block and case sums are FP64.
             const float df = (own + val) + 2.0f * fp.wf[k];
             mfx -= df * cxk(k);
@@ -264,7 +270,7 @@ __device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 
     float g[9], wf[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) {
-        g[k] = (float)(p.bandf[(size_t)k * p.nslots + slot] - p.w[k]);
+        g[k] = SV<T>::rnd((float)(p.bandf[(size_t)k * p.nslots + slot] - p.w[k]));
         wf[k] = (float)p.w[k];
     }
     float dr, rho, ux, uy, Jx, Jy;

@@ -33,8 +33,9 @@ struct CollideParams {
 struct CollideAosParams {
     int Nx, Ny, pitch;
     long long plane;
-    double *f_aos;                   // [Ny][Nx][9], read and written in place
+    double *f_aos;                   // [Ny][Nx][9], read (and written in place when write_aos)
     double *soa;                     // device planes (FP64)
+    int write_aos;
     const uint16_t *flags;
     const double *rho, *ux, *uy;     // stored fields [Ny][Nx] (host or device)
     const double *omega;

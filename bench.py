@@ -10,8 +10,11 @@ than L2, so no flush is needed between steps.
   fp64      the plain FP64 fused kernel (bit-identical to lbc), same workload
   fp16      FP16-shifted storage, same workload
   e2e       lbc's own main_lbm call through this library's C ABI with host
-            arrays (page-locked): each call uploads f, f_new, rho, u, v and
-            downloads f, f_new, rho, u, v, L, D, as lbc's API requires
+            arrays (page-locked): each call reads f, rho, u, v and writes f,
+            f_new, rho, u, v, L, D in host memory, as lbc's API requires
+  liner_batch  64 seeded acoustic-liner ducts in one batch (FP32 vs FP64)
+  serving   a seeded stream of solve requests with continuous batching:
+            aggregate MLUPS, p50/p99 latency, vs serial plain FP64
   cpu_baseline  the oracle / lbc's build on this host's cores (OpenMP)
 
 --impl reference times lbc's own CPU implementation of main_lbm on the host
@@ -51,6 +54,10 @@ def parse():
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--skip-liners", action="store_true")
     p.add_argument("--liner-steps", type=int, default=20000)
+    p.add_argument("--skip-serve", action="store_true")
+    p.add_argument("--serve-requests", type=int, default=200)
+    p.add_argument("--serve-scale", type=float, default=0.05)
+    p.add_argument("--serve-rate", type=float, default=400.0)
     return p.parse_args()
 
 
@@ -246,6 +253,21 @@ def run_ours(a, ws, rank, pg):
                   "eduction_err_median_f32": [round(x, 5) for x in r32["eduction_err_median"]],
                   "eduction_err_max_f32": [round(x, 5) for x in r32["eduction_err_max"]],
                   "finite": r32["finite"] and r64["finite"]}
+    # Serving: a seeded Poisson stream of channel / cylinder / liner requests
+    # (steps scaled down so the bench stays short), continuous batching.
+    serve_res = None
+    if not a.skip_serve:
+        from lbc_gb300 import serving
+        stream = serving.make_stream(a.serve_requests, rate=a.serve_rate, scale=a.serve_scale)
+        r = serving.serve(stream, max_active=64, chunk=500)
+        ser = serving.serial_fp64_estimate(stream)
+        serve_res = {"requests": r["requests"], "failed": r["failed"], "mlups": round(r["mlups"], 1),
+                     "p50_s": round(r["p50_s"], 3), "p99_s": round(r["p99_s"], 3),
+                     "makespan_s": round(r["makespan_s"], 2),
+                     "serial_fp64_mlups": round(ser["mlups"], 1),
+                     "vs_serial_fp64": round(r["mlups"] / ser["mlups"], 2),
+                     "stream": f"{a.serve_requests} requests, rate {a.serve_rate}/s, steps x{a.serve_scale} "
+                               "of U_log[5000, 50000], 80/20 FP32-shifted/FP64"}
     clocks = clk.stop()
     res["f16"] = {"mlups": ws * N * a.steps / (ms16 / 1e3) / 1e6, "ms_per_step": ms16 / a.steps,
                   "gbs": bytes16 / t16 / 1e9}
@@ -332,6 +354,7 @@ def run_ours(a, ws, rank, pg):
         "accuracy_after_200_steps": acc,
         "e2e": e2e,
         "liner_batch": liners,
+        "serving": serve_res,
         "gpu_launches": f32["launches"],
         "clocks": clocks,
     }

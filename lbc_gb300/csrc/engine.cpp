@@ -65,9 +65,6 @@ Solver::Solver(const CaseDesc &d) : d_(d) {
 
 Solver::~Solver() {
     if (pair_exec_) cudaGraphExecDestroy(pair_exec_);
-    for (cudaEvent_t e : ev_)
-        if (e) cudaEventDestroy(e);
-    if (stream2_) cudaStreamDestroy(stream2_);
     for (void *p : allocs_) cudaFree(p);
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -444,19 +441,8 @@ bool Solver::dropin_step_direct(double *f, double *f_new, double *rho, double *u
         set_error("direct drop-in step needs FP64 storage");
         return false;
     }
-    if (!stream2_) {
-        CK(cudaStreamCreateWithFlags(&stream2_, cudaStreamNonBlocking));
-        for (cudaEvent_t &e : ev_) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    }
     const int Nx = d_.Nx, Ny = d_.Ny;
     cur_ = 0;
-    // stream2_: the old f_new into buffer 1 when it can reach the results.
-    // Without solid nodes or off-grid pull sources every slot of f_new is
-    // rewritten before it is read, so its old content is not needed.
-    if (needs_old_dst_) {
-        CK(launch::aos_to_soa(f_new, buf_[1], STORE_F64, Nx, Ny, pitch_, plane_, d_.w, stream2_));
-        CK(cudaEventRecord(ev_[1], stream2_));
-    }
     if (nslots_ > 0)
         CK(launch::seed_band(d_seed_nodes_, d_seed_slots_, nseed_, Nx, rho, u, v, d_bandm_[parity_],
                              nslots_, stream_));
@@ -465,7 +451,6 @@ bool Solver::dropin_step_direct(double *f, double *f_new, double *rho, double *u
     c.Nx = Nx; c.Ny = Ny; c.pitch = pitch_; c.plane = plane_;
     c.f_aos = f;
     c.soa = (double *)buf_[0];
-    c.write_aos = 0;
     c.flags = d_flags_;
     c.rho = rho; c.ux = u; c.uy = v;
     c.omega = d_omega_; c.omega0 = omega0_;
@@ -473,19 +458,15 @@ bool Solver::dropin_step_direct(double *f, double *f_new, double *rho, double *u
     c.Fx = d_.Fx; c.Fy = d_.Fy;
     for (int k = 0; k < 9; k++) c.w[k] = d_.w[k];
     CK(launch::collide_aos_exact(c, stream_));
-    CK(cudaEventRecord(ev_[0], stream_));
-    // stream2_: the post-collision f back to the caller's array while the
-    // step (which only reads buffer 0) runs.
-    CK(cudaStreamWaitEvent(stream2_, ev_[0], 0));
-    CK(launch::soa_to_aos(buf_[0], f, STORE_F64, Nx, Ny, pitch_, plane_, d_.w, stream2_));
-    CK(cudaEventRecord(ev_[2], stream2_));
-    if (needs_old_dst_) CK(cudaStreamWaitEvent(stream_, ev_[1], 0));
+    // Without solid nodes or off-grid pull sources every slot of f_new is
+    // rewritten before it is read, so its old content is not needed.
+    if (needs_old_dst_)
+        CK(launch::aos_to_soa(f_new, buf_[1], STORE_F64, Nx, Ny, pitch_, plane_, d_.w, stream_));
     macro_out_[0] = rho; macro_out_[1] = u; macro_out_[2] = v;
     const bool okk = launch_step(0, 1, false, true, parity_);
     macro_out_[0] = macro_out_[1] = macro_out_[2] = nullptr;
     if (!okk) return false;
     CK(launch::soa_to_aos(buf_[1], f_new, STORE_F64, Nx, Ny, pitch_, plane_, d_.w, stream_));
-    CK(cudaStreamWaitEvent(stream_, ev_[2], 0));
     cur_ = 1;
     parity_ ^= 1;
     steps_done_ += 1;

@@ -178,9 +178,7 @@ class Solver {
     std::vector<void *> allocs_;
     std::vector<int2> wnodes_host_;
     bool needs_old_dst_ = true;
-    bool fields_are_moments_ = false;
-    cudaStream_t stream2_ = nullptr;          // drop-in: host write-back beside the step
-    cudaEvent_t ev_[3] = {nullptr, nullptr, nullptr};  // stored rho/u/v are the moments of the current populations
+    bool fields_are_moments_ = false;  // stored rho/u/v are the moments of the current populations
     std::vector<uint8_t> link_node_;
     int *d_blk_slot_ = nullptr;     // per block of the 2D grid: force partial slot or -1
     int nlink_blocks_ = 0;

@@ -33,9 +33,8 @@ struct CollideParams {
 struct CollideAosParams {
     int Nx, Ny, pitch;
     long long plane;
-    double *f_aos;                   // [Ny][Nx][9], read (and written in place when write_aos)
+    double *f_aos;                   // [Ny][Nx][9], read and written in place
     double *soa;                     // device planes (FP64)
-    int write_aos;
     const uint16_t *flags;
     const double *rho, *ux, *uy;     // stored fields [Ny][Nx] (host or device)
     const double *omega;

@@ -310,8 +310,8 @@ __global__ void k_collide_exact(const CollideParams p) {
     for (int k = 0; k < 9; k++) p.f[k * p.plane + node] = f[k];
 }
 
-// Collision over lbc's AoS array (src/core/collision.c:18-40) into the device
-// SoA planes, and back into the AoS array in place when write_aos. Blocks stage 128 consecutive
+// Collision over lbc's AoS array in place (src/core/collision.c:18-40), with the
+// result also stored in the device SoA planes. Blocks stage 128 consecutive
 // nodes through shared memory so the AoS traffic (over NVLink-C2C when the
 // array is host memory) is one contiguous run per block.
 __global__ void __launch_bounds__(128) k_collide_aos_exact(const CollideAosParams p) {
@@ -338,7 +338,6 @@ __global__ void __launch_bounds__(128) k_collide_aos_exact(const CollideAosParam
 #pragma unroll
         for (int k = 0; k < 9; k++) p.soa[k * p.plane + node] = f[k];
     }
-    if (!p.write_aos) return;
     __syncthreads();
     for (int e = threadIdx.x; e < cnt * 9; e += blockDim.x) p.f_aos[n0 * 9 + e] = tile[e];
 }

@@ -122,8 +122,28 @@ int lbm_gpu_impedance_readback(lbm_gpu_solver *s, int entry, double *spectra, do
 int lbm_gpu_msd_zoh(double R, double m, double K, double *A, double *b);
 
 int lbm_gpu_get_info(lbm_gpu_solver *s, lbm_gpu_info *info);
-/* Thread-block shape of the fused step (bx * by <= 256, bx multiple of 32). */
+/* Thread-block shape of the fused step (bx * by <= 256, bx multiple of 32).
+ * No result depends on it: populations, fields and the momentum-exchange force
+ * (summed per 32-node row segment in a fixed order) are bit-identical for
+ * every shape. */
 int lbm_gpu_set_block(lbm_gpu_solver *s, int bx, int by);
+int lbm_gpu_get_block(lbm_gpu_solver *s, int *bx, int *by);
+
+/* ---- Launch-shape autotuner (no counterpart in lbc).
+ * mode 1: use the shape cached for this solver's key (device, storage, grid,
+ * geometry class); without one, the next lbm_gpu_run with at least 17 steps
+ * times the candidate blocks (64x4, 32x8, 128x2, 256x1, 32x4, 64x2, 128x1)
+ * over interleaved windows of its own first steps, keeps the fastest for the
+ * rest of the run and caches it. The trial steps are steps of the run, so
+ * tuning costs no memory and changes no result. mode 0: off (the default,
+ * unless the environment variable LBM_GPU_AUTOTUNE is a nonzero integer when
+ * the solver is created). The cache lives in the process; when
+ * LBM_GPU_TUNE_CACHE names a file it is also read from and appended to that
+ * file. tuned: 1 once a shape was chosen; us_per_step: the chosen shape's time
+ * per step in its trial windows (0 when it came from the cache). */
+int lbm_gpu_set_autotune(lbm_gpu_solver *s, int mode);
+int lbm_gpu_autotune_status(lbm_gpu_solver *s, int *tuned, int *bx, int *by, double *us_per_step);
+void lbm_gpu_tune_cache_clear(void);
 
 /* ---- Batches: many independent cases of one storage type advanced together.
  * Per step: one persistent kernel over the flattened tile list of every case
@@ -131,7 +151,7 @@ int lbm_gpu_set_block(lbm_gpu_solver *s, int bx, int by);
  * entry of every case in one launch, one launch for all BC-written nodes, one
  * per-case force reduction; the loop runs from a captured CUDA graph. Every
  * case ends exactly as lbm_gpu_run(s, n) alone would leave it (FP64: bit for
- * bit; forces to round-off). The solvers stay owned by the caller and must
+ * bit, forces included). The solvers stay owned by the caller and must
  * outlive the batch. */
 typedef struct lbm_gpu_batch lbm_gpu_batch;
 int lbm_gpu_batch_create(lbm_gpu_solver *const *solvers, int n, lbm_gpu_batch **out);
@@ -139,6 +159,15 @@ int lbm_gpu_batch_run(lbm_gpu_batch *b, int nsteps);
 int lbm_gpu_batch_run_timed(lbm_gpu_batch *b, int nsteps, double *ms);
 /* Total nodes of all cases and kernel launches per batched step. */
 int lbm_gpu_batch_info(lbm_gpu_batch *b, long long *nodes, int *launches_per_step);
+/* Tile shape of the batched bulk kernel: tw x th = 256 nodes, tw in
+ * {32, 64, 128, 256} (default 64 x 4). No result depends on it. */
+int lbm_gpu_batch_set_tile(lbm_gpu_batch *b, int tw, int th);
+/* Tile-shape tuning, as lbm_gpu_set_autotune: candidates 64x4, 32x8, 128x2,
+ * 256x1 timed over step pairs of the next lbm_gpu_batch_run with at least 19
+ * steps; the cache key is the batch's composition (every case's grid and
+ * geometry class, in order). */
+int lbm_gpu_batch_set_autotune(lbm_gpu_batch *b, int mode);
+int lbm_gpu_batch_autotune_status(lbm_gpu_batch *b, int *tuned, int *tw, int *th, double *us_per_step);
 int lbm_gpu_batch_destroy(lbm_gpu_batch *b);
 
 /* ---- Serving: a continuous-batching request loop.

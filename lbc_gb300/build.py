@@ -26,6 +26,7 @@ UNITS = [
     ("engine.cpp", ["-O2"]),
     ("dropin.cpp", ["-O2"]),
     ("server.cpp", ["-O2"]),
+    ("tune.cpp", ["-O2"]),
     ("noalloc.cu", ["-O3", "-lineinfo", "--fmad=false"] + ARCH),
 ]
 

@@ -23,6 +23,7 @@
 #include "../../include/lbm.h"
 #include "../../include/lbm_gpu.h"
 #include "engine.h"
+#include "tune.h"
 
 using namespace lbm;
 
@@ -735,6 +736,30 @@ int lbm_gpu_set_block(lbm_gpu_solver *s, int bx, int by) {
     return s->s->set_block(dim3(bx, by, 1)) ? LBM_GPU_OK : LBM_GPU_ERR_CUDA;
 }
 
+int lbm_gpu_get_block(lbm_gpu_solver *s, int *bx, int *by) {
+    SOLVER_OR_FAIL(s);
+    if (bx) *bx = (int)s->s->block().x;
+    if (by) *by = (int)s->s->block().y;
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_set_autotune(lbm_gpu_solver *s, int mode) {
+    SOLVER_OR_FAIL(s);
+    s->s->set_autotune(mode);
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_autotune_status(lbm_gpu_solver *s, int *tuned, int *bx, int *by, double *us_per_step) {
+    SOLVER_OR_FAIL(s);
+    if (tuned) *tuned = s->s->tuned() ? 1 : 0;
+    if (bx) *bx = (int)s->s->block().x;
+    if (by) *by = (int)s->s->block().y;
+    if (us_per_step) *us_per_step = s->s->tuned_us();
+    return LBM_GPU_OK;
+}
+
+void lbm_gpu_tune_cache_clear(void) { tune_clear(); }
+
 struct lbm_gpu_batch {
     std::unique_ptr<Batch> b;
 };
@@ -778,6 +803,34 @@ int lbm_gpu_batch_info(lbm_gpu_batch *b, long long *nodes, int *launches_per_ste
     if (!b) { set_error("null batch"); return LBM_GPU_ERR_ARG; }
     if (nodes) *nodes = b->b->nodes();
     if (launches_per_step) *launches_per_step = b->b->launches_per_step();
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_batch_set_tile(lbm_gpu_batch *b, int tw, int th) {
+    if (!b) { set_error("null batch"); return LBM_GPU_ERR_ARG; }
+    int tws = -1;
+    for (int q = 5; q <= 8; q++)
+        if (tw == (1 << q) && th == (256 >> q)) tws = q;
+    if (tws < 0) {
+        set_error("batch tile must be tw x th = 256 with tw in {32, 64, 128, 256}");
+        return LBM_GPU_ERR_ARG;
+    }
+    return b->b->set_tile_shift(tws) ? LBM_GPU_OK : LBM_GPU_ERR_CUDA;
+}
+
+int lbm_gpu_batch_set_autotune(lbm_gpu_batch *b, int mode) {
+    if (!b) { set_error("null batch"); return LBM_GPU_ERR_ARG; }
+    b->b->set_autotune(mode);
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_batch_autotune_status(lbm_gpu_batch *b, int *tuned, int *tw, int *th, double *us_per_step) {
+    if (!b) { set_error("null batch"); return LBM_GPU_ERR_ARG; }
+    const int tws = b->b->tile_shift();
+    if (tuned) *tuned = b->b->tuned() ? 1 : 0;
+    if (tw) *tw = 1 << tws;
+    if (th) *th = 256 >> tws;
+    if (us_per_step) *us_per_step = b->b->tuned_us();
     return LBM_GPU_OK;
 }
 

@@ -13,6 +13,7 @@
 // step that stores pre-collision populations and the moments, so the state at
 // exit is what lbc's arrays hold after n calls.
 #include "engine.h"
+#include "tune.h"
 
 #include <algorithm>
 #include <cmath>
@@ -61,6 +62,7 @@ Solver::Solver(const CaseDesc &d) : d_(d) {
     if (!check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate")) return;
     if (!build_geometry()) return;
     ok_ = true;
+    set_autotune(tune_default_mode());
 }
 
 Solver::~Solver() {
@@ -320,50 +322,51 @@ bool Solver::build_geometry() {
     if (has_mem_) {
         if (!dalloc(&d_mem_out_, 2) || !dalloc(&d_force_slot_, 1)) return false;
         CK(cudaMemsetAsync(d_mem_out_, 0, 2 * sizeof(double), stream_));
-        if (!compute_block_slots()) return false;
+        if (!compute_segment_slots()) return false;
     }
     if (!upload_all_bc_values()) return false;
     CK(cudaStreamSynchronize(stream_));
     return true;
 }
 
-// Which blocks of the 2D launch grid contain wall links: they (only) reduce
-// and store a force partial, at a compact slot.
-bool Solver::compute_block_slots() {
+// Which 32-node row segments (j, i / 32) contain wall links: the warp that
+// steps such a segment stores its force sum at a slot, numbered in row-major
+// order. The table does not depend on the launch shape.
+bool Solver::compute_segment_slots() {
     const int Nx = d_.Nx, Ny = d_.Ny;
-    const int gx = (Nx + block_.x - 1) / block_.x, gy = (Ny + block_.y - 1) / block_.y;
-    std::vector<int> slot((size_t)gx * gy, -1);
+    const int nseg = (Nx + 31) / 32;
+    std::vector<int> slot((size_t)nseg * Ny, -1);
     int n = 0;
-    for (int by = 0; by < gy; by++)
-        for (int bx = 0; bx < gx; bx++) {
+    for (int j = 0; j < Ny; j++)
+        for (int g = 0; g < nseg; g++) {
             bool any = false;
-            for (int j = by * (int)block_.y; j < std::min(Ny, (by + 1) * (int)block_.y) && !any; j++)
-                for (int i = bx * (int)block_.x; i < std::min(Nx, (bx + 1) * (int)block_.x); i++)
-                    if (link_node_[(size_t)j * Nx + i]) { any = true; break; }
-            if (any) slot[(size_t)by * gx + bx] = n++;
+            for (int i = 32 * g; i < std::min(Nx, 32 * g + 32); i++)
+                if (link_node_[(size_t)j * Nx + i]) { any = true; break; }
+            if (any) slot[(size_t)j * nseg + g] = n++;
         }
-    nlink_blocks_ = n;
-    int *d = nullptr;
-    if (!dalloc(&d, slot.size())) return false;
-    CK(cudaMemcpyAsync(d, slot.data(), slot.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
-    d_blk_slot_ = d;
-    if ((size_t)std::max(n, 1) > partial_cap_) {
-        if (!dalloc(&d_partials_, 2 * (size_t)std::max(n, 1))) return false;
-        partial_cap_ = std::max(n, 1);
-    }
+    nlink_segs_ = n;
+    if (!dalloc(&d_seg_slot_, slot.size()) || !dalloc(&d_partials_, 2 * (size_t)std::max(n, 1))) return false;
+    CK(cudaMemcpyAsync(d_seg_slot_, slot.data(), slot.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemsetAsync(d_partials_, 0, 2 * (size_t)std::max(n, 1) * sizeof(double), stream_));
     return upload_force_slot();
 }
 
-bool Solver::upload_force_slot() {
-    if (!d_force_slot_) return true;
+ForceSlot Solver::force_slot() const {
     ForceSlot f;
     std::memset(&f, 0, sizeof f);
     f.t0 = 0;
-    f.t1 = nlink_blocks_;
+    f.t1 = nlink_segs_;
+    f.partials = d_partials_;
     f.out = d_mem_out_;
     f.hist = d_hist_;
     f.hist_count = hist_count_ptr_;
     f.hist_cap = hist_cap_;
+    return f;
+}
+
+bool Solver::upload_force_slot() {
+    if (!d_force_slot_) return true;
+    const ForceSlot f = force_slot();
     CK(cudaMemcpyAsync(d_force_slot_, &f, sizeof f, cudaMemcpyHostToDevice, stream_));
     CK(cudaStreamSynchronize(stream_));
     return true;
@@ -372,7 +375,6 @@ bool Solver::upload_force_slot() {
 bool Solver::set_block(dim3 b) {
     block_ = b;
     graph_valid_ = false;
-    if (has_mem_) return compute_block_slots();
     return true;
 }
 
@@ -571,7 +573,7 @@ StepParams Solver::step_params(int src, int dst, bool write_macro, int bparity) 
     p.bandm_next = nslots_ ? d_bandm_[bparity ^ 1] : nullptr;
     if (has_mem_) {
         p.mem_partials = d_partials_;
-        p.blk_slot = d_blk_slot_;
+        p.seg_slot = d_seg_slot_;
     }
     return p;
 }
@@ -754,7 +756,7 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
     } else {
         CK(launch::step_shifted(fast_params(p), d_.store, has_flags_, collide, block_, s));
     }
-    if (has_mem_) CK(launch::force_reduce(d_partials_, d_force_slot_, 1, s));
+    if (has_mem_) CK(launch::force_reduce(d_force_slot_, 1, s));
     if (stages_.empty()) return true;
     for (const Stage &st : stages_) CK(launch::stage(stage_params(st, src, bparity), d_.store, s));
     const FinishParams f = finish_params(dst, write_macro, bparity);
@@ -805,10 +807,82 @@ bool Solver::capture_pair() {
     return true;
 }
 
+std::string Solver::tune_key() const {
+    return device_tag() + "/step/s" + std::to_string(d_.store) + "/" + std::to_string(d_.Nx) + "x" +
+           std::to_string(d_.Ny) + (has_flags_ ? "/geo" : "/plain") + (has_mem_ ? "/mem" : "");
+}
+
+void Solver::set_autotune(int mode) {
+    tune_mode_ = mode ? 1 : 0;
+    tuned_ = false;
+    tuned_us_ = 0.f;
+    if (!tune_mode_) return;
+    int bx = 0, by = 0;
+    if (tune_lookup(tune_key(), bx, by) && bx >= 32 && bx % 32 == 0 && by >= 1 && bx * by <= 256) {
+        set_block(dim3(bx, by, 1));
+        tuned_ = true;
+    }
+}
+
+// One fused step cur -> other, as inside run().
+bool Solver::trial_step() {
+    if (!launch_step(cur_, 1 - cur_, true, false, parity_)) return false;
+    cur_ ^= 1;
+    parity_ ^= 1;
+    return true;
+}
+
+// Candidate blocks of the fused step: warp-wide rows (bx a multiple of 32),
+// 64 to 256 threads.
+static const int kBlockCand[][2] = {{64, 4}, {32, 8}, {128, 2}, {256, 1}, {32, 4}, {64, 2}, {128, 1}};
+static const int kNBlockCand = 7;
+
+// Times each candidate block over two interleaved windows of K real steps
+// (after two steps that estimate K) and keeps the fastest. Returns the number
+// of steps taken (all of them steps of the run), or -1 on a CUDA error.
+int Solver::tune_online(int avail) {
+    const int nc = kNBlockCand;
+    WindowTimer est(1);
+    if (!est.ok()) return -1;
+    if (!est.mark(0, stream_) || !trial_step() || !trial_step() || !est.mark(1, stream_) || !est.wait()) return -1;
+    int used = 2;
+    int K = window_steps(est.elapsed(0) / 2.f, 0.25f, 2, 64);
+    K = std::min(K, (avail - used) / (2 * nc));
+    if (K < 1) return used;
+    WindowTimer wt(2 * nc);
+    if (!wt.ok()) return -1;
+    for (int r = 0; r < 2; r++)
+        for (int c = 0; c < nc; c++) {
+            if (!wt.mark(r * nc + c, stream_)) return -1;
+            set_block(dim3(kBlockCand[c][0], kBlockCand[c][1], 1));
+            for (int k = 0; k < K; k++)
+                if (!trial_step()) return -1;
+        }
+    if (!wt.mark(2 * nc, stream_) || !wt.wait()) return -1;
+    used += 2 * nc * K;
+    int best = -1;
+    float best_ms = 0.f;
+    for (int c = 0; c < nc; c++) {
+        const float ms = std::min(wt.elapsed(c), wt.elapsed(nc + c));
+        if (best < 0 || ms < best_ms) { best = c; best_ms = ms; }
+    }
+    set_block(dim3(kBlockCand[best][0], kBlockCand[best][1], 1));
+    tuned_ = true;
+    tuned_us_ = best_ms * 1e3f / K;
+    tune_store(tune_key(), kBlockCand[best][0], kBlockCand[best][1], tuned_us_);
+    return used;
+}
+
 bool Solver::run(int nsteps) {
     if (nsteps <= 0) return true;
     if (!launch_collide(cur_)) return false;
     int remaining = nsteps - 1;
+    // Tuning takes its trial windows from the steps of this run.
+    if (tune_mode_ && !tuned_ && remaining >= 2 + 2 * kNBlockCand) {
+        const int used = tune_online(remaining);
+        if (used < 0) return false;
+        remaining -= used;
+    }
     if (remaining >= 2) {
         if (!capture_pair()) return false;
         while (remaining >= 2) {
@@ -853,10 +927,12 @@ Batch::Batch(const std::vector<Solver *> &cases) : cases_(cases) {
     }
     if (!check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate")) return;
     ok_ = build();
+    if (ok_) set_autotune(tune_default_mode());
 }
 
 Batch::~Batch() {
     if (pair_exec_) cudaGraphExecDestroy(pair_exec_);
+    if (d_tiles_) cudaFree(d_tiles_);
     for (void *p : allocs_) cudaFree(p);
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -871,46 +947,159 @@ template <class T> static bool balloc(std::vector<void *> &allocs, T **p, size_t
 
 // Static tables (tile list, stage entry lists, finish nodes, force slots) and
 // room for the per-direction parameter arrays, which run() refreshes.
+// Tiles of 2^tws x 2^(8 - tws) nodes over every case; w = 1 for tiles that
+// contain wall links (their warps store force partials).
+std::vector<int4> Batch::make_tiles(int tws) const {
+    std::vector<int4> tiles;
+    const int tw = 1 << tws, th = 256 >> tws;
+    for (int c = 0; c < (int)cases_.size(); c++) {
+        Solver *s = cases_[c];
+        const std::vector<uint8_t> &ln = s->link_nodes();
+        for (int y = 0; y < s->Ny(); y += th)
+            for (int x = 0; x < s->Nx(); x += tw) {
+                int w = 0;
+                if (s->has_mem()) {
+                    for (int j = y; j < std::min(s->Ny(), y + th) && !w; j++)
+                        for (int i = x; i < std::min(s->Nx(), x + tw); i++)
+                            if (ln[(size_t)j * s->Nx() + i]) { w = 1; break; }
+                }
+                tiles.push_back(make_int4(c, x, y, w));
+            }
+    }
+    return tiles;
+}
+
+bool Batch::upload_tiles(const std::vector<int4> &tiles, int4 **d) {
+    *d = nullptr;
+    CK(cudaMalloc(d, std::max<size_t>(tiles.size(), 1) * sizeof(int4)));
+    CK(cudaMemcpyAsync(*d, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, stream_));
+    return true;
+}
+
+// Makes (d, n, tws) the tile list of the bulk kernel, freeing the previous
+// list when free_old is set (the caller has synchronized the stream).
+void Batch::install_tiles(int4 *d, int n, int tws, bool free_old) {
+    if (free_old && d_tiles_ && d_tiles_ != d) cudaFree(d_tiles_);
+    d_tiles_ = d;
+    ntiles_ = n;
+    tws_ = tws;
+    grid_ = std::min(ntiles_, store_ == STORE_F64 ? launch::step_batch_exact_grid()
+                                                  : launch::step_batch_shifted_grid(store_));
+    if (grid_ < 1) grid_ = 1;
+    if (pair_exec_) {
+        cudaGraphExecDestroy(pair_exec_);
+        pair_exec_ = nullptr;
+    }
+}
+
+bool Batch::build_tiles(int tws) {
+    const std::vector<int4> tiles = make_tiles(tws);
+    int4 *d = nullptr;
+    CK(cudaStreamSynchronize(stream_));
+    if (!upload_tiles(tiles, &d)) return false;
+    CK(cudaStreamSynchronize(stream_));
+    install_tiles(d, (int)tiles.size(), tws, true);
+    return true;
+}
+
+std::string Batch::tune_key() const {
+    // The composition: each case's grid and geometry class, in order.
+    std::string comp;
+    for (Solver *c : cases_)
+        comp += std::to_string(c->Nx()) + "x" + std::to_string(c->Ny()) + (c->has_flags() ? "g" : "p") +
+                (c->has_mem() ? "m" : "") + ",";
+    const size_t h = std::hash<std::string>{}(comp);
+    char hex[32];
+    std::snprintf(hex, sizeof hex, "%016zx", h);
+    return device_tag() + "/batch/s" + std::to_string(store_) + "/n" + std::to_string(cases_.size()) + "/" + hex;
+}
+
+void Batch::set_autotune(int mode) {
+    tune_mode_ = mode ? 1 : 0;
+    tuned_ = false;
+    tuned_us_ = 0.f;
+    if (!tune_mode_) return;
+    int tw = 0, th = 0;
+    if (tune_lookup(tune_key(), tw, th) && tw * th == 256 && tw >= 32 && (tw & (tw - 1)) == 0) {
+        int tws = 0;
+        while ((1 << tws) < tw) tws++;
+        if (set_tile_shift(tws)) tuned_ = true;
+    }
+}
+
+static const int kTileCand[] = {6, 5, 7, 8};
+static const int kNTileCand = 4;
+
+// As Solver::tune_online, over step pairs of the batched loop (the directions
+// of a pair are sel 0 then 1, as in the captured graph). Returns the pairs taken.
+int Batch::tune_online(int avail_pairs) {
+    const int nc = kNTileCand;
+    std::vector<int4 *> d(nc, nullptr);
+    std::vector<int> n(nc, 0);
+    bool okk = true;
+    for (int c = 0; c < nc && okk; c++) {
+        const std::vector<int4> t = make_tiles(kTileCand[c]);
+        n[c] = (int)t.size();
+        okk = upload_tiles(t, &d[c]);
+        if (okk) okk = check_cuda(cudaStreamSynchronize(stream_), "sync");
+    }
+    int4 *const orig = d_tiles_;
+    const int orig_n = ntiles_, orig_tws = tws_;
+    int used = 0, best = -1;
+    float best_ms = 0.f;
+    auto pair = [&]() { return launch_batched(0) && launch_batched(1); };
+    if (okk) {
+        WindowTimer est(1);
+        okk = est.ok() && est.mark(0, stream_) && pair() && est.mark(1, stream_) && est.wait();
+        used = 1;
+        int K = okk ? window_steps(est.elapsed(0), 0.5f, 1, 32) : 0;
+        K = std::min(K, (avail_pairs - used) / (2 * nc));
+        if (okk && K >= 1) {
+            WindowTimer wt(2 * nc);
+            okk = wt.ok();
+            for (int r = 0; r < 2 && okk; r++)
+                for (int c = 0; c < nc && okk; c++) {
+                    okk = wt.mark(r * nc + c, stream_);
+                    install_tiles(d[c], n[c], kTileCand[c], false);
+                    for (int k = 0; k < K && okk; k++) okk = pair();
+                }
+            okk = okk && wt.mark(2 * nc, stream_) && wt.wait();
+            used += 2 * nc * K;
+            for (int c = 0; c < nc && okk; c++) {
+                const float ms = std::min(wt.elapsed(c), wt.elapsed(nc + c));
+                if (best < 0 || ms < best_ms) { best = c; best_ms = ms; }
+            }
+            if (okk) tuned_us_ = best_ms * 1e3f / (2 * K);
+        }
+    }
+    // Wait for every launch that used a list before freeing the lists not kept.
+    cudaStreamSynchronize(stream_);
+    if (best >= 0) {
+        install_tiles(d[best], n[best], kTileCand[best], false);
+        if (orig) cudaFree(orig);
+        tuned_ = true;
+        tune_store(tune_key(), 1 << kTileCand[best], 256 >> kTileCand[best], tuned_us_);
+    } else {
+        install_tiles(orig, orig_n, orig_tws, false);
+    }
+    for (int c = 0; c < nc; c++)
+        if (d[c] && d[c] != d_tiles_) cudaFree(d[c]);
+    return okk ? used : -1;
+}
+
 bool Batch::build() {
     const int nc = (int)cases_.size();
-    std::vector<int4> tiles;
     std::vector<ForceSlot> force;
     std::vector<int4> fin_nodes;
     for (int c = 0; c < nc; c++) {
         Solver *s = cases_[c];
         nodes_ += (long long)s->Nx() * s->Ny();
-        // Tiles of 64 x 4 nodes; those containing wall links get a force
-        // partial slot (w = slot + 1), consecutive per case.
-        const int s0 = nlink_tiles_;
-        const std::vector<uint8_t> &ln = s->link_nodes();
-        for (int y = 0; y < s->Ny(); y += 4)
-            for (int x = 0; x < s->Nx(); x += 64) {
-                int w = 0;
-                if (s->has_mem()) {
-                    bool any = false;
-                    for (int j = y; j < std::min(s->Ny(), y + 4) && !any; j++)
-                        for (int i = x; i < std::min(s->Nx(), x + 64); i++)
-                            if (ln[(size_t)j * s->Nx() + i]) { any = true; break; }
-                    if (any) w = 1 + nlink_tiles_++;
-                }
-                tiles.push_back(make_int4(c, x, y, w));
-            }
-        if (s->has_mem()) {
-            ForceSlot f;
-            std::memset(&f, 0, sizeof f);
-            f.t0 = s0;
-            f.t1 = nlink_tiles_;
-            f.out = s->mem_out();
-            f.hist = s->hist();
-            f.hist_count = s->hist_count();
-            f.hist_cap = s->hist_cap();
-            force.push_back(f);
-        }
+        if (s->has_mem()) force.push_back(s->force_slot());
         for (const int2 &w : s->wnodes()) fin_nodes.push_back(make_int4(c, w.x, w.y, 0));
         max_stages_ = std::max(max_stages_, (int)s->stages().size());
         for (const Stage &st : s->stages()) max_along_ = std::max(max_along_, st.along);
     }
-    ntiles_ = (int)tiles.size();
+    if (!build_tiles(tws_)) return false;
     nfin_ = (int)fin_nodes.size();
     nforce_ = (int)force.size();
     const size_t psize = store_ == STORE_F64 ? sizeof(StepParams) : sizeof(FastStepParams);
@@ -918,12 +1107,10 @@ bool Batch::build() {
     if (!check_cuda(cudaMalloc(&sp, psize * 2 * nc), "cudaMalloc batch")) return false;
     allocs_.push_back(sp);
     d_sp_ = sp;
-    if (!balloc(allocs_, &d_phase_, nc) || !balloc(allocs_, &d_tiles_, tiles.size()) ||
-        !balloc(allocs_, &d_partials_, 2 * (size_t)std::max(nlink_tiles_, 1)) || !balloc(allocs_, &d_fin_, 2 * nc) ||
+    if (!balloc(allocs_, &d_phase_, nc) || !balloc(allocs_, &d_fin_, 2 * nc) ||
         !balloc(allocs_, &d_fin_nodes_, fin_nodes.size()) || !balloc(allocs_, &d_force_, force.size()))
         return false;
     CK(cudaMemsetAsync(d_phase_, 0, nc * sizeof(int), stream_));
-    CK(cudaMemcpyAsync(d_tiles_, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, stream_));
     if (nfin_) CK(cudaMemcpyAsync(d_fin_nodes_, fin_nodes.data(), fin_nodes.size() * sizeof(int4), cudaMemcpyHostToDevice, stream_));
     if (nforce_) CK(cudaMemcpyAsync(d_force_, force.data(), force.size() * sizeof(ForceSlot), cudaMemcpyHostToDevice, stream_));
     for (int s = 0; s < max_stages_; s++) {
@@ -934,9 +1121,6 @@ bool Batch::build() {
         d_stage_lists_.push_back(d);
         stage_counts_.push_back(cnt);
     }
-    grid_ = std::min(ntiles_, store_ == STORE_F64 ? launch::step_batch_exact_grid()
-                                                  : launch::step_batch_shifted_grid(store_));
-    if (grid_ < 1) grid_ = 1;
     launches_per_step_ = 1 + max_stages_ + (nfin_ ? 1 : 0) + (nforce_ ? 1 : 0);
     CK(cudaStreamSynchronize(stream_));
     return true;
@@ -944,18 +1128,18 @@ bool Batch::build() {
 
 bool Batch::launch_batched(int sel) {
     if (store_ == STORE_F64)
-        CK(launch::step_batch_exact((const StepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel,
-                                    d_partials_, grid_, stream_));
+        CK(launch::step_batch_exact((const StepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
+                                    grid_, stream_));
     else
-        CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel,
-                                      d_partials_, store_, grid_, stream_));
+        CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
+                                      store_, grid_, stream_));
     for (int s = 0; s < max_stages_; s++)
         CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], max_along_, store_, sel, stream_));
     if (nfin_) {
         if (store_ == STORE_F64) CK(launch::finish_batch_exact(d_fin_, d_phase_, d_fin_nodes_, nfin_, sel, stream_));
         else CK(launch::finish_batch_shifted(d_fin_, d_phase_, d_fin_nodes_, nfin_, sel, store_, stream_));
     }
-    if (nforce_) CK(launch::force_reduce(d_partials_, d_force_, nforce_, stream_));
+    if (nforce_) CK(launch::force_reduce(d_force_, nforce_, stream_));
     return true;
 }
 
@@ -1021,6 +1205,12 @@ bool Batch::run(int nsteps) {
         // Host vectors must outlive the copies.
         okk = okk && check_cuda(cudaStreamSynchronize(stream_), "sync");
         int pairs = mid / 2;
+        // Tuning takes its trial windows from the step pairs of this run.
+        if (okk && tune_mode_ && !tuned_ && pairs >= 1 + 2 * kNTileCand) {
+            const int used = tune_online(pairs);
+            okk = used >= 0;
+            pairs -= std::max(used, 0);
+        }
         if (okk && pairs > 0) okk = capture_pair();
         for (; okk && pairs > 0; pairs--) okk = check_cuda(cudaGraphLaunch(pair_exec_, stream_), "graph");
         if (okk && (mid & 1)) okk = launch_batched(0);

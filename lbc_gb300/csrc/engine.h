@@ -98,6 +98,14 @@ class Solver {
     int launches_per_step() const { return 1 + (int)stages_.size() + (nw_ > 0 ? 1 : 0); }
     bool set_block(dim3 b);
     dim3 block() const { return block_; }
+    // Launch-shape tuning (tune.h). mode 1: take the cached block for this
+    // case's key, else time the candidate blocks on the first steps of the
+    // next run that has enough of them and keep the fastest. mode 0: off.
+    void set_autotune(int mode);
+    int autotune_mode() const { return tune_mode_; }
+    bool tuned() const { return tuned_; }
+    float tuned_us() const { return tuned_us_; }
+    std::string tune_key() const;
 
     // Pieces used by Batch: parameters of one step in a given direction, the
     // first-step collision and the final (pre-collision, moments) step.
@@ -115,6 +123,8 @@ class Solver {
     double *hist() const { return d_hist_; }
     unsigned long long *hist_count() const { return hist_count_ptr_; }
     int hist_cap() const { return hist_cap_; }
+    // Where this case's force is reduced from and written to.
+    ForceSlot force_slot() const;
     // Impedance wall on Boundary entry `entry` (velocity_bottom_regularized):
     // per node R, m, K (m <= 0: keep the entry's own val2), nf <= 8 DFT
     // frequencies (rad / step), reference density for p' and the rate of its
@@ -135,6 +145,11 @@ class Solver {
                      cudaStream_t s = nullptr);
     bool launch_collide(int b, cudaStream_t s = nullptr);
     bool capture_pair();
+    bool trial_step();
+    int tune_online(int avail);
+    int tune_mode_ = 0;
+    bool tuned_ = false;
+    float tuned_us_ = 0.f;
     template <class T> bool dalloc(T **p, size_t count);
 
     CaseDesc d_;
@@ -180,11 +195,10 @@ class Solver {
     bool needs_old_dst_ = true;
     bool fields_are_moments_ = false;  // stored rho/u/v are the moments of the current populations
     std::vector<uint8_t> link_node_;
-    int *d_blk_slot_ = nullptr;     // per block of the 2D grid: force partial slot or -1
-    int nlink_blocks_ = 0;
-    size_t partial_cap_ = 0;
+    int *d_seg_slot_ = nullptr;     // per 32-node row segment: force partial slot or -1
+    int nlink_segs_ = 0;
     ForceSlot *d_force_slot_ = nullptr;
-    bool compute_block_slots();
+    bool compute_segment_slots();
     bool upload_force_slot();
     double *macro_out_[3] = {nullptr, nullptr, nullptr};  // moments written here when set
 };
@@ -206,8 +220,26 @@ class Batch {
     int launches_per_step() const { return launches_per_step_; }
     cudaStream_t stream() const { return stream_; }
 
+    // Tile shape of the bulk kernel: 2^tws x 2^(8 - tws) nodes, tws in [5, 8].
+    int tile_shift() const { return tws_; }
+    bool set_tile_shift(int tws) { return tws == tws_ || build_tiles(tws); }
+    // Tile-shape tuning, as Solver::set_autotune (the key is the batch's
+    // composition: every case's grid and geometry class).
+    void set_autotune(int mode);
+    bool tuned() const { return tuned_; }
+    float tuned_us() const { return tuned_us_; }
+    std::string tune_key() const;
+
   private:
     bool build();
+    bool build_tiles(int tws);
+    std::vector<int4> make_tiles(int tws) const;
+    bool upload_tiles(const std::vector<int4> &tiles, int4 **d);
+    void install_tiles(int4 *d, int n, int tws, bool free_old);
+    int tune_online(int avail_pairs);
+    int tune_mode_ = 0;
+    bool tuned_ = false;
+    float tuned_us_ = 0.f;
     bool launch_batched(int sel);
     bool capture_pair();
 
@@ -217,12 +249,11 @@ class Batch {
     cudaStream_t stream_ = nullptr;
     long long nodes_ = 0;
     int ntiles_ = 0, grid_ = 0, max_stages_ = 0, max_along_ = 0, nfin_ = 0, nforce_ = 0;
-    int nlink_tiles_ = 0;
+    int tws_ = 6;
     int launches_per_step_ = 0;
     void *d_sp_ = nullptr;         // StepParams or FastStepParams [2 * ncases]
     int *d_phase_ = nullptr;       // [ncases] (and stage entries)
     int4 *d_tiles_ = nullptr;
-    double *d_partials_ = nullptr;
     std::vector<StageParams *> d_stage_lists_;
     std::vector<int> stage_counts_;
     FinishParams *d_fin_ = nullptr;

@@ -58,10 +58,12 @@ struct AosArgs {
     double *out2;
 };
 
-// Where a batched step writes one case's force (k_force_reduce): the case's
-// tiles are [t0, t1) of the tile list.
+// One case's force (k_force_reduce): the sum of its segment partials
+// partials[2 t .. 2 t + 1], t in [t0, t1), in that order, into out[0..1] (and
+// the next slot of the history ring, when there is one).
 struct ForceSlot {
     int t0, t1;
+    const double *partials;
     double *out;
     double *hist;
     unsigned long long *hist_count;
@@ -101,14 +103,15 @@ cudaError_t mei_init(const AosArgs &a, double rho0, cudaStream_t s);
 cudaError_t mei_iter(const AosArgs &a, double rho0, unsigned long long *maxbits, cudaStream_t s);
 
 // batches of cases (tile list = int4 {case, x0, y0, case has wall links})
+// Tiles of 2^tws x 2^(8 - tws) nodes, tws in [5, 8].
 cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 *tiles, int ntiles,
-                             int sel, double *partials, int grid, cudaStream_t s);
+                             int sel, int tws, int grid, cudaStream_t s);
 int step_batch_exact_grid();
 cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int max_along, int store,
                         int sel, cudaStream_t s);
 cudaError_t finish_batch_exact(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
                                int sel, cudaStream_t s);
-cudaError_t force_reduce(const double *partials, const ForceSlot *slots, int n, cudaStream_t s);
+cudaError_t force_reduce(const ForceSlot *slots, int n, cudaStream_t s);
 
 // shifted storage (kernels_shifted.cu)
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
@@ -116,7 +119,7 @@ cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool co
 cudaError_t finish_shifted(const FinishParams &p, int store, bool collide, cudaStream_t s);
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s);
 cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
-                               int ntiles, int sel, double *partials, int store, int grid,
+                               int ntiles, int sel, int tws, int store, int grid,
                                cudaStream_t s);
 int step_batch_shifted_grid(int store);
 cudaError_t finish_batch_shifted(const FinishParams *fp, const int *phase, const int4 *nodes, int n,

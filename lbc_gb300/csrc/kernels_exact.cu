@@ -132,25 +132,25 @@ __global__ void __launch_bounds__(256) k_step_exact(const StepParams p) {
     double mfx = 0.0, mfy = 0.0;
     bool link = false;
     if (i < p.Nx && j < p.Ny) step_node_exact<FLAGS, COLLIDE>(p, i, j, mfx, mfy, link);
-    if (FLAGS && p.mem_partials) {
-        const int slot = p.blk_slot[blockIdx.y * gridDim.x + blockIdx.x];
-        if (slot >= 0) block_reduce2_store(mfx, mfy, link, p.mem_partials + 2 * (size_t)slot);
-    }
+    if (FLAGS && p.mem_partials) segment_reduce2_store(mfx, mfy, link, i, j, p.Nx, p.seg_slot, p.mem_partials);
 }
 
 // Many cases in one launch: a persistent loop over a flattened list of
-// 2D tiles (one tile = one thread block's worth of nodes of one case). Each
-// case brings its own parameters (sp[2 * c + (sel ^ phase[c])]: the two
-// ping-pong directions), so uneven grids and different geometries share the
-// launch. Per-tile force partials are reduced per case by k_force_reduce.
+// 2D tiles (one tile = one thread block's worth of nodes of one case: 256
+// threads as 2^tws x 2^(8 - tws) nodes). Each case brings its own parameters
+// (sp[2 * c + (sel ^ phase[c])]: the two ping-pong directions), so uneven
+// grids and different geometries share the launch. Force partials go to each
+// case's own segment slots (td.w != 0: the tile contains wall links), reduced
+// per case by k_force_reduce exactly as when the case runs alone.
 __global__ void __launch_bounds__(256) k_step_batch_exact(const StepParams *__restrict__ sp,
                                                           const int *__restrict__ phase,
                                                           const int4 *__restrict__ tiles, int ntiles,
-                                                          int sel, double *partials) {
+                                                          int sel, int tws) {
+    const int tx = threadIdx.x & ((1 << tws) - 1), ty = threadIdx.x >> tws;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int4 td = tiles[t];
         const StepParams &p = sp[2 * td.x + (sel ^ phase[td.x])];
-        const int i = td.y + threadIdx.x, j = td.z + threadIdx.y;
+        const int i = td.y + tx, j = td.z + ty;
         double mfx = 0.0, mfy = 0.0;
         bool link = false;
         const bool in = i < p.Nx && j < p.Ny;
@@ -159,8 +159,7 @@ __global__ void __launch_bounds__(256) k_step_batch_exact(const StepParams *__re
         } else {
             if (in) step_node_exact<false, true>(p, i, j, mfx, mfy, link);
         }
-        // td.w = 1 + partial slot of a tile that contains wall links, else 0.
-        if (td.w) block_reduce2_store(mfx, mfy, link, partials + 2 * (size_t)(td.w - 1));
+        if (td.w) segment_reduce2_store(mfx, mfy, link, i, j, p.Nx, p.seg_slot, p.mem_partials);
     }
 }
 
@@ -219,15 +218,14 @@ __global__ void k_stage_batch(const StageParams *__restrict__ list, const int *_
 }
 
 // Per-case deterministic sum of the per-tile force partials of a batched step.
-__global__ void k_force_reduce(const double *__restrict__ partials, const ForceSlot *__restrict__ slots,
-                               int nslots) {
+__global__ void k_force_reduce(const ForceSlot *__restrict__ slots, int nslots) {
     const int c = blockIdx.x;
     if (c >= nslots) return;
     const ForceSlot fs = slots[c];
     double a = 0.0, b = 0.0;
     for (int t = fs.t0 + (int)threadIdx.x; t < fs.t1; t += blockDim.x) {
-        a += partials[2 * (size_t)t];
-        b += partials[2 * (size_t)t + 1];
+        a += fs.partials[2 * (size_t)t];
+        b += fs.partials[2 * (size_t)t + 1];
     }
     __shared__ double sa[32], sb[32];
 #pragma unroll
@@ -610,9 +608,10 @@ cudaError_t stage(const StageParams &p, int store, cudaStream_t s) {
 }
 
 cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 *tiles, int ntiles,
-                             int sel, double *partials, int grid, cudaStream_t s) {
+                             int sel, int tws, int grid, cudaStream_t s) {
     if (ntiles == 0) return cudaSuccess;
-    k_step_batch_exact<<<grid, dim3(64, 4), 0, s>>>(sp, phase, tiles, ntiles, sel, partials);
+    if (tws < 5 || tws > 8) return cudaErrorInvalidValue;
+    k_step_batch_exact<<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
     return cudaGetLastError();
 }
 
@@ -641,9 +640,9 @@ cudaError_t finish_batch_exact(const FinishParams *fp, const int *phase, const i
     return cudaGetLastError();
 }
 
-cudaError_t force_reduce(const double *partials, const ForceSlot *slots, int n, cudaStream_t s) {
+cudaError_t force_reduce(const ForceSlot *slots, int n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_force_reduce<<<n, 256, 0, s>>>(partials, slots, n);
+    k_force_reduce<<<n, 256, 0, s>>>(slots, n);
     return cudaGetLastError();
 }
 

@@ -236,10 +236,7 @@ __global__ void __launch_bounds__(256, 5) k_step_shifted_geo(const FastStepParam
     float mfx = 0.f, mfy = 0.f;
     bool link = false;
     if (i < p.Nx && j < p.Ny) step_node_shifted<T, I, true, COLLIDE>(fp, i, j, mfx, mfy, link);
-    if (p.mem_partials) {
-        const int slot = p.blk_slot[blockIdx.y * gridDim.x + blockIdx.x];
-        if (slot >= 0) block_reduce2_store(mfx, mfy, link, p.mem_partials + 2 * (size_t)slot);
-    }
+    if (p.mem_partials) segment_reduce2_store(mfx, mfy, link, i, j, p.Nx, p.seg_slot, p.mem_partials);
 }
 
 // Batched form (see k_step_batch_exact in kernels_exact.cu).
@@ -247,11 +244,12 @@ template <typename T>
 __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepParams *__restrict__ sp,
                                                             const int *__restrict__ phase,
                                                             const int4 *__restrict__ tiles,
-                                                            int ntiles, int sel, double *partials) {
+                                                            int ntiles, int sel, int tws) {
+    const int tx = threadIdx.x & ((1 << tws) - 1), ty = threadIdx.x >> tws;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int4 td = tiles[t];
         const FastStepParams &fp = sp[2 * td.x + (sel ^ phase[td.x])];
-        const int i = td.y + threadIdx.x, j = td.z + threadIdx.y;
+        const int i = td.y + tx, j = td.z + ty;
         float mfx = 0.f, mfy = 0.f;
         bool link = false;
         const bool in = i < fp.s.Nx && j < fp.s.Ny;
@@ -260,7 +258,7 @@ __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepPar
         } else {
             if (in) step_node_shifted<T, long long, false, true>(fp, i, j, mfx, mfy, link);
         }
-        if (td.w) block_reduce2_store(mfx, mfy, link, partials + 2 * (size_t)(td.w - 1));
+        if (td.w) segment_reduce2_store(mfx, mfy, link, i, j, fp.s.Nx, fp.s.seg_slot, fp.s.mem_partials);
     }
 }
 
@@ -377,11 +375,11 @@ cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool co
 }
 
 cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
-                               int ntiles, int sel, double *partials, int store, int grid,
-                               cudaStream_t s) {
+                               int ntiles, int sel, int tws, int store, int grid, cudaStream_t s) {
     if (ntiles == 0) return cudaSuccess;
-    if (store == STORE_F32) k_step_batch_shifted<float><<<grid, dim3(64, 4), 0, s>>>(sp, phase, tiles, ntiles, sel, partials);
-    else k_step_batch_shifted<__half><<<grid, dim3(64, 4), 0, s>>>(sp, phase, tiles, ntiles, sel, partials);
+    if (tws < 5 || tws > 8) return cudaErrorInvalidValue;
+    if (store == STORE_F32) k_step_batch_shifted<float><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+    else k_step_batch_shifted<__half><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
     return cudaGetLastError();
 }
 

@@ -399,10 +399,15 @@ struct StepParams {
     double *bandf;            // [9][nslots], pre-collision f_new of band nodes
     double *bandm_next;       // [3][nslots], their moments (for the next step's BCs)
     // momentum-exchange force (null when the geometry has no wall links):
-    // blocks that contain wall links (blk_slot >= 0, known from the geometry)
-    // store their sum at mem_partials[2 * slot]; k_force_reduce adds them up.
+    // every 32-node row segment (j, i / 32) that contains wall links has a
+    // slot (seg_slot >= 0, numbered in row-major order from the geometry);
+    // the warp that steps it stores its sum at mem_partials[2 * slot] and
+    // k_force_reduce adds the slots up in order. A warp is always one such
+    // segment (block and tile widths are multiples of 32), so the sum does not
+    // depend on the block or tile shape, nor on whether the case runs alone or
+    // in a batch.
     double *mem_partials;
-    const int *blk_slot;      // [gridDim.x * gridDim.y]
+    const int *seg_slot;      // [Ny][(Nx + 31) / 32]
 };
 
 struct StageParams {

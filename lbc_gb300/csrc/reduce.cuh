@@ -74,22 +74,26 @@ __device__ __forceinline__ void reduce2_grid(double a, double b, double *partial
     }
 }
 
-// Block reduction of two doubles, stored by thread 0 at out[0..1] (fixed
-// order). `link`: this thread's node has wall links (its terms are nonzero).
-__device__ __forceinline__ void block_reduce2_store(double a, double b, bool link, double *out) {
-    __shared__ double sa[32], sb[32];
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int nthr = blockDim.x * blockDim.y;
-    warp_reduce2(a, b, link);
-    if ((tid & 31) == 0) { sa[tid >> 5] = a; sb[tid >> 5] = b; }
-    __syncthreads();
-    if (tid == 0) {
-        double ra = 0.0, rb = 0.0;
-        for (int w = 0; w < (nthr + 31) / 32; w++) { ra += sa[w]; rb += sb[w]; }
-        out[0] = ra;
-        out[1] = rb;
+// Sum of two doubles over the warp that holds the 32-node row segment
+// (j, i0 .. i0 + 31), i0 = i & ~31, stored by lane 0 at partials[2 * slot],
+// slot = seg_slot[j][i0 / 32]. Every lane of the warp must call it; lanes past
+// the grid pass link = false. `link`: this lane's node has wall links (its
+// terms are nonzero). Warps without links (most of the grid) return at once.
+__device__ __forceinline__ void segment_reduce2_store(double a, double b, bool link, int i, int j, int Nx,
+                                                      const int *__restrict__ seg_slot, double *partials) {
+    if (!__any_sync(0xffffffffu, link)) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
     }
-    __syncthreads();
+    if ((i & 31) == 0) {
+        const int slot = seg_slot[(size_t)j * ((Nx + 31) >> 5) + (i >> 5)];
+        if (slot >= 0) {
+            partials[2 * (size_t)slot] = a;
+            partials[2 * (size_t)slot + 1] = b;
+        }
+    }
 }
 
 }  // namespace lbm

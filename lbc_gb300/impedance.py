@@ -174,6 +174,7 @@ def run_liner_batch(n: int = 64, steps: int = 20000, storage: int = 1, seed: int
     batch = GpuBatch(solvers)
     nodes, lps = batch.info()
     ms = batch.run_timed(steps)
+    tuned, tile, _ = batch.autotune_status()
     med, mx, finite = [], [], True
     for p, s in zip(params, solvers):
         spec, _ = s.impedance_readback(LINER_ENTRY)
@@ -185,6 +186,7 @@ def run_liner_batch(n: int = 64, steps: int = 20000, storage: int = 1, seed: int
     med, mx = np.array(med), np.array(mx)
     return {"ducts": len(params), "nodes": int(nodes), "steps": steps, "ms": ms,
             "mlups": nodes * steps / (ms / 1e3) / 1e6, "launches_per_step": lps,
+            "tile": list(tile), "tile_tuned": tuned,
             "omegas": EDUCTION_OMEGAS.tolist(),
             "eduction_err_median": np.median(med, axis=0).tolist(),
             "eduction_err_max": np.max(mx, axis=0).tolist(), "finite": finite}

@@ -39,7 +39,12 @@ def main(argv=None):
     p.add_argument("--rate", type=float, default=200.0, help="arrival rate of the served stream (1/s)")
     p.add_argument("--max-active", type=int, default=64)
     p.add_argument("--chunk", type=int, default=1000)
+    p.add_argument("--autotune", action="store_true",
+                   help="tune block / tile shapes on the warm-up steps (LBM_GPU_AUTOTUNE=1)")
     a = p.parse_args(argv)
+    if a.autotune:
+        os.environ["LBM_GPU_AUTOTUNE"] = "1"
+        a.warmup = max(a.warmup, 80)
     if a.serve:
         from lbc_gb300 import serving
         stream = serving.make_stream(a.serve, rate=a.rate, scale=a.scale)
@@ -60,9 +65,11 @@ def main(argv=None):
     s.set_state(st)
     s.run(a.warmup)
     ms = s.run_timed(a.steps)
+    tuned, blk, us = s.autotune_status()
     print(json.dumps({"case": a.case, "Nx": case.Nx, "Ny": case.Ny, "storage": a.storage,
                       "steps": a.steps, "ms": round(ms, 3),
-                      "mlups": round(case.nodes * a.steps / (ms / 1e3) / 1e6, 1)}))
+                      "mlups": round(case.nodes * a.steps / (ms / 1e3) / 1e6, 1),
+                      "block": list(blk), "tuned": tuned}))
 
 
 if __name__ == "__main__":

@@ -82,6 +82,15 @@ def _bind_ext(lib: C.CDLL) -> None:
         "lbm_gpu_force_history": (C.c_int, [vp, dp, C.c_int]),
         "lbm_gpu_get_info": (C.c_int, [vp, C.POINTER(Info)]),
         "lbm_gpu_set_block": (C.c_int, [vp, C.c_int, C.c_int]),
+        "lbm_gpu_get_block": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "lbm_gpu_set_autotune": (C.c_int, [vp, C.c_int]),
+        "lbm_gpu_autotune_status": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                              C.POINTER(C.c_double)]),
+        "lbm_gpu_tune_cache_clear": (None, []),
+        "lbm_gpu_batch_set_tile": (C.c_int, [vp, C.c_int, C.c_int]),
+        "lbm_gpu_batch_set_autotune": (C.c_int, [vp, C.c_int]),
+        "lbm_gpu_batch_autotune_status": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                                    C.POINTER(C.c_int), C.POINTER(C.c_double)]),
         "lbm_gpu_batch_create": (C.c_int, [C.POINTER(vp), C.c_int, C.POINTER(vp)]),
         "lbm_gpu_batch_run": (C.c_int, [vp, C.c_int]),
         "lbm_gpu_batch_run_timed": (C.c_int, [vp, C.c_int, dp]),
@@ -295,6 +304,22 @@ class GpuSolver:
     def set_block(self, bx: int, by: int):
         _check(self.lib.lbm_gpu_set_block(self.h, bx, by), "lbm_gpu_set_block")
 
+    def block(self):
+        bx, by = C.c_int(), C.c_int()
+        _check(self.lib.lbm_gpu_get_block(self.h, C.byref(bx), C.byref(by)), "lbm_gpu_get_block")
+        return bx.value, by.value
+
+    def set_autotune(self, mode: int = 1):
+        """Tune the fused step's block shape on the next long enough run."""
+        _check(self.lib.lbm_gpu_set_autotune(self.h, mode), "lbm_gpu_set_autotune")
+
+    def autotune_status(self):
+        """(tuned, (bx, by), microseconds per step in the trial windows)."""
+        t, bx, by, us = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        _check(self.lib.lbm_gpu_autotune_status(self.h, C.byref(t), C.byref(bx), C.byref(by), C.byref(us)),
+               "lbm_gpu_autotune_status")
+        return bool(t.value), (bx.value, by.value), us.value
+
 
 class GpuBatch:
     """Independent cases of one storage type advanced together (lbm_gpu_batch_*)."""
@@ -319,6 +344,20 @@ class GpuBatch:
         n, l = C.c_longlong(), C.c_int()
         _check(self.lib.lbm_gpu_batch_info(self.h, C.byref(n), C.byref(l)), "lbm_gpu_batch_info")
         return n.value, l.value
+
+    def set_tile(self, tw: int, th: int):
+        _check(self.lib.lbm_gpu_batch_set_tile(self.h, tw, th), "lbm_gpu_batch_set_tile")
+
+    def set_autotune(self, mode: int = 1):
+        """Tune the bulk kernel's tile shape on the next long enough run."""
+        _check(self.lib.lbm_gpu_batch_set_autotune(self.h, mode), "lbm_gpu_batch_set_autotune")
+
+    def autotune_status(self):
+        """(tuned, (tw, th), microseconds per step in the trial windows)."""
+        t, tw, th, us = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        _check(self.lib.lbm_gpu_batch_autotune_status(self.h, C.byref(t), C.byref(tw), C.byref(th),
+                                                      C.byref(us)), "lbm_gpu_batch_autotune_status")
+        return bool(t.value), (tw.value, th.value), us.value
 
     def close(self):
         if getattr(self, "h", None):

@@ -21,8 +21,11 @@ than L2, so no flush is needed between steps.
 cores (oracle/_ref when lbc's sources were compiled here, else the oracle port)
 on the same workload.
 
-Multi-GPU (torchrun): every rank runs an independent replica (the path has no
-data exchange between cases); value sums over ranks, time is the max over ranks.
+Multi-GPU (torchrun): cases are independent, so nothing is exchanged on the
+data path. Each rank runs its own Taylor-Green replica (value sums over ranks,
+time is the max over ranks); the liner ducts (64 per rank) and the served
+stream (the request count times the ranks) are partitioned by work across
+ranks (lbc_gb300.sharding), and only totals and latencies are gathered.
 """
 import argparse
 import ctypes as C
@@ -149,12 +152,17 @@ def peaks():
 
 
 def traffic_per_launch(key):
-    """Per-launch DRAM bytes of the step kernel from the committed ncu summary."""
+    """Per-launch DRAM bytes (read + write) of the step kernel from the
+    committed ncu summary (profiles/step_kernel_traffic.txt), or None."""
     try:
-        with open(os.path.join(ROOT, "profiles", "step_kernel_traffic.json")) as fh:
-            return json.load(fh).get(key)
+        with open(os.path.join(ROOT, "profiles", "step_kernel_traffic.txt")) as fh:
+            for line in fh:
+                c = line.split()
+                if len(c) >= 4 and c[0] == key:
+                    return int(float(c[2]) + float(c[3]))
     except (OSError, ValueError):
         return None
+    return None
 
 
 def cpu_lib():
@@ -170,11 +178,18 @@ def cpu_lib():
     return LbcAbi(C.CDLL(so), "orc_"), "port"
 
 
+def omp_env():
+    """All host cores, one thread per core, threads kept near their data."""
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    os.environ.setdefault("OMP_PLACES", "cores")
+
+
 def cpu_time(n, seconds, max_steps=None):
     """Bounded sample of the workload on the host cores: main_lbm calls on the
     full grid until `seconds` of CPU time (at least 2 calls)."""
     from lbc_gb300 import cases
-    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    omp_env()
     lib, kind = cpu_lib()
     case, st = cases.taylor_green(n, n, 0.04, 0.56)
     bnd = lib.boundaries(case.bcs)
@@ -239,48 +254,90 @@ def run_ours(a, ws, rank, pg):
     del s16
     bytes16 = 2 * 9 * 2 * N
     t16 = ms16 / a.steps / 1e3
-    # Batched acoustic liner ducts (64 seeded ducts, one persistent launch per step).
+    # Batched acoustic liner ducts (64 seeded ducts per GPU, one persistent
+    # launch per step). With several ranks the 64 x N ducts are partitioned by
+    # work (nodes) and each rank runs its share as one batch.
+    from lbc_gb300 import sharding
     liners = None
     if not a.skip_liners:
         from lbc_gb300 import impedance as imp
-        r32 = imp.run_liner_batch(64, a.liner_steps, lbc_gb300.F32_SHIFTED)
-        r64 = imp.run_liner_batch(64, max(2, a.liner_steps // 20), lbc_gb300.F64)
-        liners = {"ducts": 64, "nodes": r32["nodes"], "f32_mlups": round(ws * r32["mlups"], 1),
-                  "f32_steps": r32["steps"], "fp64_mlups": round(ws * r64["mlups"], 1), "fp64_steps": r64["steps"],
-                  "ratio_f32_vs_fp64": round(r32["mlups"] / r64["mlups"], 2),
+        allp = imp.sample_liners(64 * ws, 2026)
+        mine = [allp[i] for i in sharding.share([p.nx * p.ny for p in allp], ws, rank)]
+        barrier(pg)
+        r32 = imp.run_liner_batch(steps=a.liner_steps, storage=lbc_gb300.F32_SHIFTED, params=mine)
+        barrier(pg)
+        r64 = imp.run_liner_batch(steps=max(2, a.liner_steps // 20), storage=lbc_gb300.F64, params=mine)
+        nodes_all = sharding.all_sum(pg, r32["nodes"])
+        fluid_all = sharding.all_sum(pg, r32["fluid_nodes"])
+        m32 = nodes_all * r32["steps"] / (sharding.all_max(pg, r32["ms"]) / 1e3) / 1e6
+        m64 = nodes_all * r64["steps"] / (sharding.all_max(pg, r64["ms"]) / 1e3) / 1e6
+        liners = {"ducts": 64 * ws, "nodes": int(nodes_all), "fluid_nodes": int(fluid_all),
+                  "f32_mlups": round(m32, 1), "f32_fluid_mlups": round(m32 * fluid_all / nodes_all, 1),
+                  "f32_steps": r32["steps"], "fp64_mlups": round(m64, 1), "fp64_steps": r64["steps"],
+                  "ratio_f32_vs_fp64": round(m32 / m64, 2),
                   "launches_per_step": r32["launches_per_step"],
                   "eduction_omegas": r32["omegas"],
                   "eduction_err_median_f32": [round(x, 5) for x in r32["eduction_err_median"]],
                   "eduction_err_max_f32": [round(x, 5) for x in r32["eduction_err_max"]],
                   "finite": r32["finite"] and r64["finite"]}
+        if ws > 1:
+            liners["eduction_note"] = "eduction errors of rank 0's ducts"
     # Serving: a seeded Poisson stream of channel / cylinder / liner requests
-    # (steps scaled down so the bench stays short), continuous batching.
+    # (steps scaled down so the bench stays short), continuous batching. With
+    # several ranks the stream has N times the requests, partitioned by work;
+    # each rank serves its share at the original arrival times.
     serve_res = None
     if not a.skip_serve:
+        import numpy as np
         from lbc_gb300 import serving
-        stream = serving.make_stream(a.serve_requests, rate=a.serve_rate, scale=a.serve_scale)
-        r = serving.serve(stream, max_active=64, chunk=500)
-        ser = serving.serial_fp64_estimate(stream)
-        serve_res = {"requests": r["requests"], "failed": r["failed"], "mlups": round(r["mlups"], 1),
-                     "p50_s": round(r["p50_s"], 3), "p99_s": round(r["p99_s"], 3),
-                     "makespan_s": round(r["makespan_s"], 2),
-                     "serial_fp64_mlups": round(ser["mlups"], 1),
-                     "vs_serial_fp64": round(r["mlups"] / ser["mlups"], 2),
-                     "stream": f"{a.serve_requests} requests, rate {a.serve_rate}/s, steps x{a.serve_scale} "
+        stream = serving.make_stream(a.serve_requests * ws, rate=a.serve_rate * ws, scale=a.serve_scale)
+        mine = [stream[i] for i in sharding.share([r.nx * r.ny * r.steps for r in stream], ws, rank)]
+        barrier(pg)
+        r = serving.serve(mine, max_active=64, chunk=500)
+        ser = serving.serial_fp64_estimate(mine)
+        lups_all = sharding.all_sum(pg, r["lups"])
+        span = sharding.all_max(pg, r["makespan_s"])
+        ser_s = sharding.all_max(pg, ser["seconds"])
+        failed = int(sharding.all_sum(pg, r["failed"]))
+        lats = r["latencies_s"]
+        if pg is not None:
+            parts = [None] * ws
+            pg.all_gather_object(parts, lats)
+            lats = [x for p_ in parts for x in p_]
+        mlups = lups_all / span / 1e6
+        ser_mlups = lups_all / ser_s / 1e6
+        serve_res = {"requests": len(stream), "failed": failed, "mlups": round(mlups, 1),
+                     "p50_s": round(float(np.percentile(lats, 50)), 3),
+                     "p99_s": round(float(np.percentile(lats, 99)), 3),
+                     "makespan_s": round(span, 2),
+                     "serial_fp64_mlups": round(ser_mlups, 1),
+                     "vs_serial_fp64": round(mlups / ser_mlups, 2),
+                     "stream": f"{len(stream)} requests, rate {a.serve_rate * ws}/s, steps x{a.serve_scale} "
                                "of U_log[5000, 50000], 80/20 FP32-shifted/FP64"}
     clocks = clk.stop()
     res["f16"] = {"mlups": ws * N * a.steps / (ms16 / 1e3) / 1e6, "ms_per_step": ms16 / a.steps,
                   "gbs": bytes16 / t16 / 1e9}
 
-    # Accuracy against the FP64 kernel (itself bit-identical to lbc) after E steps.
+    # Accuracy against the FP64 kernel (itself bit-identical to lbc) after E
+    # steps, and the kinetic-energy decay rate between E/2 and E steps (the
+    # Taylor-Green vortex decays as exp(-2 nu k^2 t), k^2 = 2 (2 pi / L)^2).
     E = 200
-    fields = {}
+    fields, rates = {}, {}
+
+    def energy(fl):
+        return float(np.sum(fl[1] ** 2 + fl[2] ** 2))
+
     for name, stg in (("f64", lbc_gb300.F64), ("f32", lbc_gb300.F32_SHIFTED), ("f16", lbc_gb300.F16_SHIFTED)):
         s = lbc_gb300.GpuSolver(case, stg)
         s.set_state(st)
-        s.run(E)
+        s.run(E // 2)
+        e_half = energy(s.get_fields())
+        s.run(E - E // 2)
         fields[name] = s.get_fields()
+        rates[name] = math.log(e_half / energy(fields[name])) / (E - E // 2)
         del s
+    nu = (0.56 - 0.5) / 3.0
+    rate_exact = 2.0 * nu * 2.0 * (2.0 * math.pi / n) ** 2
     r64, u64, v64 = fields["f64"]
     m0 = float(np.sum(st.rho))
     acc = {}
@@ -289,8 +346,10 @@ def run_ours(a, ws, rank, pg):
         acc[name] = {
             "u_l2_rel_vs_fp64": float(np.sqrt(np.sum((u - u64) ** 2 + (v - v64) ** 2) / np.sum(u64 ** 2 + v64 ** 2))),
             "mass_drift": float(np.sum(r) / m0 - 1.0),
+            "decay_rate_rel_err_vs_fp64": float(rates[name] / rates["f64"] - 1.0),
         }
     acc["f64_mass_drift"] = float(np.sum(r64) / m0 - 1.0)
+    acc["f64_decay_rate_rel_err_vs_analytic"] = float(rates["f64"] / rate_exact - 1.0)
 
     # End to end through lbc's main_lbm with page-locked host arrays (FP64).
     api = lbc_gb300.dropin()
@@ -347,9 +406,11 @@ def run_ours(a, ws, rank, pg):
                      "algorithmic_bytes_per_launch": bytes32},
         "fp64": {"value": round(res["f64"]["mlups"], 1), "ms_per_step": round(res["f64"]["ms_per_step"], 4),
                  "achieved_gbs": round(res["f64"]["gbs"], 1), "frac_hbm": round(res["f64"]["gbs"] / hbm, 4),
-                 "steps": res["f64"]["steps"], "parity": "bit-identical to lbc's FP64 CPU solver"},
+                 "traffic": traffic_per_launch(f"f64_{n}"), "steps": res["f64"]["steps"],
+                 "bound": "FP64 issue (about 115 FP64 lane-ops per node on a part with about 1.25 TFLOP/s FP64)",
+                 "parity": "bit-identical to lbc's FP64 CPU solver"},
         "fp16": {"value": round(res["f16"]["mlups"], 1), "achieved_gbs": round(res["f16"]["gbs"], 1),
-                 "frac_hbm": round(res["f16"]["gbs"] / hbm, 4)},
+                 "frac_hbm": round(res["f16"]["gbs"] / hbm, 4), "traffic": traffic_per_launch(f"f16_{n}")},
         "speedup_f32_vs_fp64": round(f32["mlups"] / res["f64"]["mlups"], 2),
         "accuracy_after_200_steps": acc,
         "e2e": e2e,
@@ -372,7 +433,7 @@ def run_reference(a, ws, rank, pg):
     # Each timed step is one main_lbm call on the full grid; the run is capped
     # at about two minutes.
     from lbc_gb300 import cases
-    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    omp_env()
     lib, kind = cpu_lib()
     case, st = cases.taylor_green(n, n, 0.04, 0.56)
     bnd = lib.boundaries(case.bcs)

@@ -164,8 +164,10 @@ def run_liner_batch(n: int = 64, steps: int = 20000, storage: int = 1, seed: int
     from .runtime import GpuBatch, GpuSolver
     params = params if params is not None else sample_liners(n, seed)
     solvers = []
+    fluid = 0
     for p in params:
         case, st = liner_duct(p)
+        fluid += int(np.count_nonzero(case.solid_mask == 0))
         s = GpuSolver(case, storage)
         R, m, K = liner_arrays(p)
         s.set_impedance_wall(LINER_ENTRY, R, m, K, TRACKED_OMEGAS, 1.0, MEAN_RATE, steps)
@@ -184,7 +186,7 @@ def run_liner_batch(n: int = 64, steps: int = 20000, storage: int = 1, seed: int
         rho, _, _ = s.get_fields()
         finite = finite and bool(np.all(np.isfinite(rho[1:-1, 1:-1])))
     med, mx = np.array(med), np.array(mx)
-    return {"ducts": len(params), "nodes": int(nodes), "steps": steps, "ms": ms,
+    return {"ducts": len(params), "nodes": int(nodes), "fluid_nodes": fluid, "steps": steps, "ms": ms,
             "mlups": nodes * steps / (ms / 1e3) / 1e6, "launches_per_step": lps,
             "tile": list(tile), "tile_tuned": tuned,
             "omegas": EDUCTION_OMEGAS.tolist(),

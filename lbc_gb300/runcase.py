@@ -49,6 +49,7 @@ def main(argv=None):
         from lbc_gb300 import serving
         stream = serving.make_stream(a.serve, rate=a.rate, scale=a.scale)
         r = serving.serve(stream, a.max_active, a.chunk)
+        r.pop("latencies_s")
         r["serial_fp64"] = serving.serial_fp64_estimate(stream)
         print(json.dumps(r))
         return

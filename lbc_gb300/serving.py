@@ -129,7 +129,8 @@ def serve(stream: List[Req], max_active: int = 64, chunk: int = 1000, budget_byt
     lats = np.array([lat[i] for i in ids])
     return {"requests": len(stream), "failed": len(failed), "lups": lups, "makespan_s": makespan,
             "mlups": lups / makespan / 1e6, "p50_s": float(np.percentile(lats, 50)),
-            "p99_s": float(np.percentile(lats, 99)), "busy_s": stats["busy_s"]}
+            "p99_s": float(np.percentile(lats, 99)), "busy_s": stats["busy_s"],
+            "latencies_s": lats.tolist()}
 
 
 def serial_fp64_estimate(stream: List[Req], sample: int = 8, seed: int = 1):

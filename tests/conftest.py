@@ -33,10 +33,15 @@ def _ensure_oracle():
                        capture_output=True)
 
 
-@pytest.fixture(scope="session")
-def oracle():
+def oracle_abi():
+    """The oracle's lbc-style API (built on first use)."""
     _ensure_oracle()
     return LbcAbi(C.CDLL(ORACLE_SO), "orc_")
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    return oracle_abi()
 
 
 @pytest.fixture(scope="session")

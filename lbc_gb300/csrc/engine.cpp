@@ -586,6 +586,8 @@ FastStepParams Solver::fast_params(const StepParams &p) const {
     fp.omega0f = (float)omega0_;
     fp.Fxf = (float)d_.Fx; fp.Fyf = (float)d_.Fy;
     fp.hFxf = (float)(0.5 * d_.Fx); fp.hFyf = (float)(0.5 * d_.Fy);
+    fp.h1f = 3.0f * fp.wf[1];
+    fp.h5f = (1.0f - 2.0f * fp.h1f) * 0.25f;
     return fp;
 }
 
@@ -947,11 +949,12 @@ template <class T> static bool balloc(std::vector<void *> &allocs, T **p, size_t
 
 // Static tables (tile list, stage entry lists, finish nodes, force slots) and
 // room for the per-direction parameter arrays, which run() refreshes.
-// Tiles of 2^tws x 2^(8 - tws) nodes over every case; w = 1 for tiles that
-// contain wall links (their warps store force partials).
+// Tiles of 2^tws x 2^(8 - tws) threads over every case (one node per thread in
+// FP64, two adjacent nodes in shifted storage); w = 1 for tiles that contain
+// wall links (their threads store force partials).
 std::vector<int4> Batch::make_tiles(int tws) const {
     std::vector<int4> tiles;
-    const int tw = 1 << tws, th = 256 >> tws;
+    const int tw = (store_ == STORE_F64 ? 1 : 2) << tws, th = 256 >> tws;
     for (int c = 0; c < (int)cases_.size(); c++) {
         Solver *s = cases_[c];
         const std::vector<uint8_t> &ln = s->link_nodes();
@@ -1094,6 +1097,7 @@ bool Batch::build() {
     for (int c = 0; c < nc; c++) {
         Solver *s = cases_[c];
         nodes_ += (long long)s->Nx() * s->Ny();
+        if (9LL * s->plane() >= (1LL << 31)) wide_ = true;
         if (s->has_mem()) force.push_back(s->force_slot());
         for (const int2 &w : s->wnodes()) fin_nodes.push_back(make_int4(c, w.x, w.y, 0));
         max_stages_ = std::max(max_stages_, (int)s->stages().size());
@@ -1132,7 +1136,7 @@ bool Batch::launch_batched(int sel) {
                                     grid_, stream_));
     else
         CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
-                                      store_, grid_, stream_));
+                                      store_, wide_, grid_, stream_));
     for (int s = 0; s < max_stages_; s++)
         CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], max_along_, store_, sel, stream_));
     if (nfin_) {

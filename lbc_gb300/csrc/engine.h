@@ -250,6 +250,7 @@ class Batch {
     long long nodes_ = 0;
     int ntiles_ = 0, grid_ = 0, max_stages_ = 0, max_along_ = 0, nfin_ = 0, nforce_ = 0;
     int tws_ = 6;
+    bool wide_ = false;  // some case needs 64-bit element offsets
     int launches_per_step_ = 0;
     void *d_sp_ = nullptr;         // StepParams or FastStepParams [2 * ncases]
     int *d_phase_ = nullptr;       // [ncases] (and stage entries)

@@ -79,6 +79,9 @@ struct FastStepParams {
     float wf[9];
     float omega0f;
     float Fxf, Fyf, hFxf, hFyf;   // FP32 copies (no per-thread FP64 conversions)
+    // odd-part coefficients of the equilibrium: h1 = fl(3 w1), h5 = (1 - 2 h1) / 4
+    // (2 h1 + 4 h5 = 1 holds exactly); the same bits as shifted_h() on the device
+    float h1f, h5f;
 };
 
 namespace launch {
@@ -118,8 +121,9 @@ cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool co
                          cudaStream_t s);
 cudaError_t finish_shifted(const FinishParams &p, int store, bool collide, cudaStream_t s);
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s);
+// wide: some case has 9 * plane >= 2^31 elements (64-bit element offsets).
 cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
-                               int ntiles, int sel, int tws, int store, int grid,
+                               int ntiles, int sel, int tws, int store, bool wide, int grid,
                                cudaStream_t s);
 int step_batch_shifted_grid(int store);
 cudaError_t finish_batch_shifted(const FinishParams *fp, const int *phase, const int4 *nodes, int n,

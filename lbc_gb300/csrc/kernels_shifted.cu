@@ -19,34 +19,78 @@ template <typename T> struct SV;
 // are computed rather than loaded (bounce-back interpolation, edge BCs) are
 // rounded to the storage type before the collision, so a run split into
 // chunks (whose boundaries store and reload them) gives the same bits.
+// ld2 / st2: two adjacent nodes of one row (an even column: the pair is 8- or
+// 4-byte aligned because the pitch and the planes are multiples of 64 nodes).
 template <> struct SV<float> {
     static __device__ __forceinline__ float ld(const float *p) { return __ldg(p); }
     static __device__ __forceinline__ float ld_plain(const float *p) { return *p; }
     static __device__ __forceinline__ void st(float *p, float v) { *p = v; }
     static __device__ __forceinline__ float rnd(float v) { return v; }
+    static __device__ __forceinline__ float2 ld2(const float *p) { return __ldg((const float2 *)p); }
+    static __device__ __forceinline__ void st2(float *p, float2 v) { *(float2 *)p = v; }
 };
 template <> struct SV<__half> {
     static __device__ __forceinline__ float ld(const __half *p) { return __half2float(__ldg(p)); }
     static __device__ __forceinline__ float ld_plain(const __half *p) { return __half2float(*p); }
     static __device__ __forceinline__ void st(__half *p, float v) { *p = __float2half_rn(v); }
     static __device__ __forceinline__ float rnd(float v) { return __half2float(__float2half_rn(v)); }
+    static __device__ __forceinline__ float2 ld2(const __half *p) { return __half22float2(__ldg((const __half2 *)p)); }
+    static __device__ __forceinline__ void st2(__half *p, float2 v) { *(__half2 *)p = __float22half2_rn(v); }
 };
+
+// ---------------------------------------------------------------- lane math
+// The arithmetic of one node (float) or of two adjacent nodes at once (float2,
+// Blackwell's packed FP32 instructions). Every operation is one correctly
+// rounded IEEE operation with no contraction left to the compiler, so a node
+// gets the same bits whichever form, kernel or launch shape computed it.
+__device__ __forceinline__ float v_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float v_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float v_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float v_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float v_rcp(float a) { return __frcp_rn(a); }
+__device__ __forceinline__ float v_floor_rho(float a) { return a < 1e-16f ? 1e-16f : a; }
+__device__ __forceinline__ float2 v_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// a - b rounded once: b * (-1) is exact.
+__device__ __forceinline__ float2 v_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 v_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 v_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 v_rcp(float2 a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
+__device__ __forceinline__ float2 v_floor_rho(float2 a) { return make_float2(v_floor_rho(a.x), v_floor_rho(a.y)); }
+template <class V> __device__ __forceinline__ V v_splat(float x);
+template <> __device__ __forceinline__ float v_splat<float>(float x) { return x; }
+template <> __device__ __forceinline__ float2 v_splat<float2>(float x) { return make_float2(x, x); }
+
+// h1 = fl(3 w1), h5 = (1 - 2 h1) / 4, as the host computes them.
+__device__ __forceinline__ void shifted_h(float w1, float &h1, float &h5) {
+    h1 = __fmul_rn(3.0f, w1);
+    h5 = __fmul_rn(__fsub_rn(1.0f, __fmul_rn(2.0f, h1)), 0.25f);
+}
 
 // Shifted moments: delta rho = sum g, j = sum c g (sum c w = 0). Jx, Jy are the
 // momentum including half the body force (rho u of lbc).
-__device__ __forceinline__ void moments_shifted(const float g[9], float hFx, float hFy, float &dr,
-                                                float &rho, float &ux, float &uy, float &Jx,
-                                                float &Jy) {
-    dr = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
-    const float jx = (g[1] - g[3]) + (g[5] - g[6]) + (g[8] - g[7]);
-    const float jy = (g[2] - g[4]) + (g[5] + g[6]) - (g[7] + g[8]);
-    rho = 1.0f + dr;
-    if (rho < 1e-16f) rho = 1e-16f;
-    const float inv = 1.0f / rho;
-    Jx = jx + hFx;
-    Jy = jy + hFy;
-    ux = Jx * inv;
-    uy = Jy * inv;
+template <class V>
+__device__ __forceinline__ void moments_v(const V g[9], V hFx, V hFy, V &dr, V &rho, V &ux, V &uy, V &Jx,
+                                          V &Jy) {
+    dr = v_add(v_add(v_add(v_add(g[0], g[1]), v_add(g[2], g[3])), v_add(v_add(g[4], g[5]), v_add(g[6], g[7]))),
+               g[8]);
+    const V jx = v_add(v_add(v_sub(g[1], g[3]), v_sub(g[5], g[6])), v_sub(g[8], g[7]));
+    const V jy = v_sub(v_add(v_sub(g[2], g[4]), v_add(g[5], g[6])), v_add(g[7], g[8]));
+    rho = v_floor_rho(v_add(v_splat<V>(1.0f), dr));
+    const V inv = v_rcp(rho);
+    Jx = v_add(jx, hFx);
+    Jy = v_add(jy, hFy);
+    ux = v_mul(Jx, inv);
+    uy = v_mul(Jy, inv);
+}
+
+// One pair of directions (k, opposite) of the equilibrium: X = w (dr + 4.5 J c
+// - rt) is the even part, Y = h J the odd part.
+template <class V>
+__device__ __forceinline__ void geq_pair(float w, float h, V dr, V c, V J, V nrt, V &a, V &b) {
+    const V X = v_mul(v_splat<V>(w), v_add(dr, v_fma(v_mul(v_splat<V>(4.5f), J), c, nrt)));
+    const V Y = v_mul(v_splat<V>(h), J);
+    a = v_add(X, Y);
+    b = v_sub(X, Y);
 }
 
 // BGK + Guo on shifted populations, g' = g + om (geq - g) + (1 - om/2) F_k,
@@ -57,42 +101,46 @@ __device__ __forceinline__ void moments_shifted(const float g[9], float hFx, flo
 // term uses J = rho u directly (no division), and the rest population closes
 // the mass. Rounded weights would otherwise bias every collision's momentum by
 // ~1e-8 in the same direction, an error that grows linearly with the steps.
-__device__ __forceinline__ void collide_shifted(float g[9], const float w[9], float dr, float rho,
-                                                float ux, float uy, float Jx, float Jy, float om,
-                                                bool force, float Fx, float Fy) {
-    const float h1 = 3.0f * w[1];
-    const float h5 = (1.0f - 2.0f * h1) * 0.25f;
-    const float rt = 1.5f * (Jx * ux + Jy * uy);  // rho * 1.5 u.u
-    float geq[9];
-    {
-        const float c = ux, J = Jx, X = w[1] * (dr + fmaf(4.5f * J, c, -rt)), Y = h1 * J;
-        geq[1] = X + Y; geq[3] = X - Y;
-    }
-    {
-        const float c = uy, J = Jy, X = w[2] * (dr + fmaf(4.5f * J, c, -rt)), Y = h1 * J;
-        geq[2] = X + Y; geq[4] = X - Y;
-    }
-    {
-        const float c = ux + uy, J = Jx + Jy, X = w[5] * (dr + fmaf(4.5f * J, c, -rt)), Y = h5 * J;
-        geq[5] = X + Y; geq[7] = X - Y;
-    }
-    {
-        const float c = uy - ux, J = Jy - Jx, X = w[6] * (dr + fmaf(4.5f * J, c, -rt)), Y = h5 * J;
-        geq[6] = X + Y; geq[8] = X - Y;
-    }
-    geq[0] = dr - (((geq[1] + geq[3]) + (geq[2] + geq[4])) + ((geq[5] + geq[7]) + (geq[6] + geq[8])));
+// The Guo term is evaluated per direction pair: with S = 9 (c.u)(c.F) - 3 u.F
+// and A = 3 c.F, F_k = w (S + A) and F_opp = w (S - A).
+template <class V>
+__device__ __forceinline__ void collide_v(V g[9], const float w[9], float h1, float h5, V dr, V ux, V uy,
+                                          V Jx, V Jy, V om, bool force, float Fx, float Fy) {
+    const V nrt = v_mul(v_splat<V>(-1.5f), v_fma(Jx, ux, v_mul(Jy, uy)));  // -rho * 1.5 u.u
+    V geq[9];
+    geq_pair(w[1], h1, dr, ux, Jx, nrt, geq[1], geq[3]);
+    geq_pair(w[2], h1, dr, uy, Jy, nrt, geq[2], geq[4]);
+    geq_pair(w[5], h5, dr, v_add(ux, uy), v_add(Jx, Jy), nrt, geq[5], geq[7]);
+    geq_pair(w[6], h5, dr, v_sub(uy, ux), v_sub(Jy, Jx), nrt, geq[6], geq[8]);
+    geq[0] = v_sub(dr, v_add(v_add(v_add(geq[1], geq[3]), v_add(geq[2], geq[4])),
+                             v_add(v_add(geq[5], geq[7]), v_add(geq[6], geq[8]))));
 #pragma unroll
-    for (int k = 0; k < 9; k++) g[k] = fmaf(om, geq[k] - g[k], g[k]);
+    for (int k = 0; k < 9; k++) g[k] = v_fma(om, v_sub(geq[k], g[k]), g[k]);
     if (force) {
-        const float uF = ux * Fx + uy * Fy;
-        const float gf = 1.0f - 0.5f * om;
+        const V Fxv = v_splat<V>(Fx), Fyv = v_splat<V>(Fy);
+        const V gf = v_fma(v_splat<V>(-0.5f), om, v_splat<V>(1.0f));
+        const V n3uF = v_mul(v_splat<V>(-3.0f), v_fma(ux, Fxv, v_mul(uy, Fyv)));  // -3 u.F
+        g[0] = v_fma(gf, v_mul(v_splat<V>(w[0]), n3uF), g[0]);
+        // (k, opp, c.u, c.F) for the four pairs
+        const V cu[4] = {ux, uy, v_add(ux, uy), v_sub(uy, ux)};
+        const V cF[4] = {Fxv, Fyv, v_splat<V>(Fx + Fy), v_splat<V>(Fy - Fx)};
+        const int ka[4] = {1, 2, 5, 6}, kb[4] = {3, 4, 7, 8};
 #pragma unroll
-        for (int k = 0; k < 9; k++) {
-            const float cu = cxk(k) * ux + cyk(k) * uy;
-            const float cF = cxk(k) * Fx + cyk(k) * Fy;
-            g[k] = fmaf(gf, w[k] * (3.0f * cF + 9.0f * cu * cF - 3.0f * uF), g[k]);
+        for (int q = 0; q < 4; q++) {
+            const V S = v_fma(v_mul(v_splat<V>(9.0f), cu[q]), cF[q], n3uF);
+            const V A = v_mul(v_splat<V>(3.0f), cF[q]);
+            const V wv = v_splat<V>(w[ka[q]]);
+            g[ka[q]] = v_fma(gf, v_mul(wv, v_add(S, A)), g[ka[q]]);
+            g[kb[q]] = v_fma(gf, v_mul(wv, v_sub(S, A)), g[kb[q]]);
         }
     }
+}
+
+// Scalar entry points used by the per-node paths.
+__device__ __forceinline__ void moments_shifted(const float g[9], float hFx, float hFy, float &dr,
+                                                float &rho, float &ux, float &uy, float &Jx,
+                                                float &Jy) {
+    moments_v<float>(g, hFx, hFy, dr, rho, ux, uy, Jx, Jy);
 }
 
 // Rare per-node outputs, kept out of line so the compiler cannot hoist their
@@ -132,9 +180,23 @@ __device__ __noinline__ void macro_store(const StepParams &p, size_t dn, int slo
     }
 }
 
-// One node of the fused step in shifted storage. I is the element-offset type:
-// int whenever all nine planes fit in 2^31 elements (fewer address
-// instructions), long long otherwise.
+__device__ __noinline__ void macro_store_pair(const StepParams &p, size_t dn, float2 dr, float2 ux, float2 uy) {
+    p.rho[dn] = 1.0 + (double)dr.x;
+    p.rho[dn + 1] = 1.0 + (double)dr.y;
+    p.ux[dn] = ux.x;
+    p.ux[dn + 1] = ux.y;
+    p.uy[dn] = uy.x;
+    p.uy[dn + 1] = uy.y;
+}
+
+__device__ __noinline__ float2 omega_pair(const double *omega, size_t dn) {
+    return make_float2((float)omega[dn], (float)omega[dn + 1]);
+}
+
+// One node of the fused step in shifted storage (solids, bounce-back links,
+// stale slots, edge-BC band: everything). I is the element-offset type: int
+// whenever all nine planes fit in 2^31 elements (fewer address instructions),
+// long long otherwise.
 template <typename T, typename I, bool FLAGS, bool COLLIDE>
 __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int i, int j,
                                                   float &mfx, float &mfy, bool &link) {
@@ -186,7 +248,7 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
                     val = own - (float)L.c2;
             }
             g[k] = SV<T>::rnd(val);
-            // Per-node link sum in FP32 (a few terms); block and case sums are FP64.
+            // Per-node link sum in FP32 (a few terms); segment and case sums are FP64.
             const float df = (own + val) + 2.0f * fp.wf[k];
             mfx -= df * cxk(k);
             mfy -= df * cyk(k);
@@ -200,47 +262,125 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
     }
     if (FLAGS && (fl & NF_BCW)) return;
     float dr, rho, ux, uy, Jx, Jy;
-    moments_shifted(g, fp.hFxf, fp.hFyf, dr, rho, ux, uy, Jx, Jy);
-    if (FLAGS) {
-        if (p.write_macro || slot >= 0) macro_store(p, dn, slot, dr, ux, uy);
-    } else if (p.write_macro) {
-        p.rho[dn] = 1.0 + (double)dr;
-        p.ux[dn] = ux;
-        p.uy[dn] = uy;
-    }
+    moments_v<float>(g, fp.hFxf, fp.hFyf, dr, rho, ux, uy, Jx, Jy);
+    if (p.write_macro || slot >= 0) macro_store(p, dn, slot, dr, ux, uy);
     if (COLLIDE) {
         const float om = p.omega ? (float)p.omega[dn] : fp.omega0f;
-        collide_shifted(g, fp.wf, dr, rho, ux, uy, Jx, Jy, om, p.has_force != 0, fp.Fxf, fp.Fyf);
+        collide_v<float>(g, fp.wf, fp.h1f, fp.h5f, dr, ux, uy, Jx, Jy, om, p.has_force != 0, fp.Fxf, fp.Fyf);
     }
 #pragma unroll
     for (int k = 0; k < 9; k++) SV<T>::st(Dst + (I)k * pl + node, g[k]);
 }
 
-// Fully periodic grid without solids or edge BCs: no flag word, 32 registers.
+// Two adjacent nodes (i0, i0 + 1) of one row, neither of them special (no
+// solid, link, stale slot, band or BC node): pair loads where the pull sources
+// are adjacent (c_x = 0), a pair and a single load otherwise (c_x = +-1), packed
+// FP32 arithmetic, pair stores. im = source column of i0 - 1, ip2 of i0 + 2
+// (wrapped or clamped like the per-node path).
+template <typename T, typename I, bool COLLIDE>
+__device__ __forceinline__ void step_pair_shifted(const FastStepParams &fp, int i0, int j, int im, int ip2,
+                                                  int jm, int jp) {
+    const StepParams &p = fp.s;
+    const T *S = (const T *)p.src;
+    T *Dst = (T *)p.dst;
+    const I pl = (I)p.plane;
+    const I r0 = (I)j * (I)p.pitch + (I)i0, rm = (I)jm * (I)p.pitch, rp = (I)jp * (I)p.pitch;
+    const I m0 = rm + (I)i0, p0 = rp + (I)i0;
+    float2 g[9], a;
+    g[0] = SV<T>::ld2(S + r0);
+    a = SV<T>::ld2(S + pl + r0);
+    g[1] = make_float2(SV<T>::ld(S + pl + (r0 - (I)i0 + (I)im)), a.x);
+    g[2] = SV<T>::ld2(S + 2 * pl + m0);
+    a = SV<T>::ld2(S + 3 * pl + r0);
+    g[3] = make_float2(a.y, SV<T>::ld(S + 3 * pl + (r0 - (I)i0 + (I)ip2)));
+    g[4] = SV<T>::ld2(S + 4 * pl + p0);
+    a = SV<T>::ld2(S + 5 * pl + m0);
+    g[5] = make_float2(SV<T>::ld(S + 5 * pl + rm + (I)im), a.x);
+    a = SV<T>::ld2(S + 6 * pl + m0);
+    g[6] = make_float2(a.y, SV<T>::ld(S + 6 * pl + rm + (I)ip2));
+    a = SV<T>::ld2(S + 7 * pl + p0);
+    g[7] = make_float2(a.y, SV<T>::ld(S + 7 * pl + rp + (I)ip2));
+    a = SV<T>::ld2(S + 8 * pl + p0);
+    g[8] = make_float2(SV<T>::ld(S + 8 * pl + rp + (I)im), a.x);
+    float2 dr, rho, ux, uy, Jx, Jy;
+    moments_v<float2>(g, v_splat<float2>(fp.hFxf), v_splat<float2>(fp.hFyf), dr, rho, ux, uy, Jx, Jy);
+    const size_t dn = (size_t)j * (size_t)p.Nx + (size_t)i0;
+    if (p.write_macro) macro_store_pair(p, dn, dr, ux, uy);
+    if (COLLIDE) {
+        const float2 om = p.omega ? omega_pair(p.omega, dn) : v_splat<float2>(fp.omega0f);
+        collide_v<float2>(g, fp.wf, fp.h1f, fp.h5f, dr, ux, uy, Jx, Jy, om, p.has_force != 0, fp.Fxf, fp.Fyf);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) SV<T>::st2(Dst + (I)k * pl + r0, g[k]);
+}
+
+// The nodes (i0, i0 + 1) of row j: the pair path when both exist and neither
+// is special, else each node on its own. ax, ay: the two nodes' wall-link force
+// terms (node i0 first), link: either has wall links.
+template <typename T, typename I, bool FLAGS, bool COLLIDE>
+__device__ __forceinline__ void step_two_shifted(const FastStepParams &fp, int i0, int j, double &ax,
+                                                 double &ay, bool &link) {
+    const StepParams &p = fp.s;
+    const bool two = i0 + 1 < p.Nx;
+    bool fast = two;
+    if (FLAGS && two) {
+        const uint32_t f2 = *(const uint32_t *)(p.flags + ((I)j * (I)p.pitch + (I)i0));
+        constexpr uint32_t kSlow = NF_SPECIAL_MASK | NF_SOLID | NF_BAND | NF_BCW | NF_LINKS;
+        fast = ((f2 | (f2 >> 16)) & kSlow) == 0;
+    }
+    if (fast) {
+        int im = i0 - 1, ip2 = i0 + 2, jm = j - 1, jp = j + 1;
+        if (p.px) { if (im < 0) im += p.Nx; if (ip2 >= p.Nx) ip2 -= p.Nx; }
+        else { im = max(im, 0); ip2 = min(ip2, p.Nx - 1); }
+        if (p.py) { if (jm < 0) jm += p.Ny; if (jp >= p.Ny) jp -= p.Ny; }
+        else { jm = max(jm, 0); jp = min(jp, p.Ny - 1); }
+        step_pair_shifted<T, I, COLLIDE>(fp, i0, j, im, ip2, jm, jp);
+        return;
+    }
+    float mx = 0.f, my = 0.f;
+    bool l = false;
+    step_node_shifted<T, I, FLAGS, COLLIDE>(fp, i0, j, mx, my, l);
+    ax = (double)mx;
+    ay = (double)my;
+    link = l;
+    if (two) {
+        mx = 0.f; my = 0.f; l = false;
+        step_node_shifted<T, I, FLAGS, COLLIDE>(fp, i0 + 1, j, mx, my, l);
+        ax += (double)mx;
+        ay += (double)my;
+        link = link || l;
+    }
+}
+
+// Fully periodic grid without solids or edge BCs: no flag word. Each thread
+// steps two adjacent nodes.
 template <typename T, typename I, bool COLLIDE>
 __global__ void __launch_bounds__(256) k_step_shifted_plain(const FastStepParams fp) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    float mfx = 0.f, mfy = 0.f;
+    double ax = 0.0, ay = 0.0;
     bool link = false;
-    if (i < fp.s.Nx && j < fp.s.Ny) step_node_shifted<T, I, false, COLLIDE>(fp, i, j, mfx, mfy, link);
+    if (i0 < fp.s.Nx && j < fp.s.Ny) step_two_shifted<T, I, false, COLLIDE>(fp, i0, j, ax, ay, link);
 }
 
-// General geometry (flag word per node). The occupancy hint keeps it at five
-// resident blocks per SM (48 registers) without spills.
+// General geometry (flag word per node), two adjacent nodes per thread. The
+// force partials of a 32-node segment come from half a warp.
 template <typename T, typename I, bool COLLIDE>
-__global__ void __launch_bounds__(256, 5) k_step_shifted_geo(const FastStepParams fp) {
+__global__ void __launch_bounds__(256, 4) k_step_shifted_geo(const FastStepParams fp) {
     const StepParams &p = fp.s;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    float mfx = 0.f, mfy = 0.f;
+    double ax = 0.0, ay = 0.0;
     bool link = false;
-    if (i < p.Nx && j < p.Ny) step_node_shifted<T, I, true, COLLIDE>(fp, i, j, mfx, mfy, link);
-    if (p.mem_partials) segment_reduce2_store(mfx, mfy, link, i, j, p.Nx, p.seg_slot, p.mem_partials);
+    if (i0 < p.Nx && j < p.Ny) step_two_shifted<T, I, true, COLLIDE>(fp, i0, j, ax, ay, link);
+    if (p.mem_partials) segment_pair_reduce2_store(ax, ay, link, i0, j, p.Nx, p.seg_slot, p.mem_partials);
 }
 
-// Batched form (see k_step_batch_exact in kernels_exact.cu).
-template <typename T>
+// Batched form (see k_step_batch_exact in kernels_exact.cu): tiles of
+// 2^(tws + 1) x 2^(8 - tws) nodes, two adjacent nodes per thread. Blocks stride
+// through the tile list, so the tiles in flight at any moment are neighbours
+// in memory (sequential DRAM streams, halo rows shared through L2).
+template <typename T, typename I>
 __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepParams *__restrict__ sp,
                                                             const int *__restrict__ phase,
                                                             const int4 *__restrict__ tiles,
@@ -249,16 +389,16 @@ __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepPar
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int4 td = tiles[t];
         const FastStepParams &fp = sp[2 * td.x + (sel ^ phase[td.x])];
-        const int i = td.y + tx, j = td.z + ty;
-        float mfx = 0.f, mfy = 0.f;
+        const int i0 = td.y + 2 * tx, j = td.z + ty;
+        double ax = 0.0, ay = 0.0;
         bool link = false;
-        const bool in = i < fp.s.Nx && j < fp.s.Ny;
+        const bool in = i0 < fp.s.Nx && j < fp.s.Ny;
         if (fp.s.flags) {
-            if (in) step_node_shifted<T, long long, true, true>(fp, i, j, mfx, mfy, link);
+            if (in) step_two_shifted<T, I, true, true>(fp, i0, j, ax, ay, link);
         } else {
-            if (in) step_node_shifted<T, long long, false, true>(fp, i, j, mfx, mfy, link);
+            if (in) step_two_shifted<T, I, false, true>(fp, i0, j, ax, ay, link);
         }
-        if (td.w) segment_reduce2_store(mfx, mfy, link, i, j, fp.s.Nx, fp.s.seg_slot, fp.s.mem_partials);
+        if (td.w) segment_pair_reduce2_store(ax, ay, link, i0, j, fp.s.Nx, fp.s.seg_slot, fp.s.mem_partials);
     }
 }
 
@@ -280,7 +420,9 @@ __device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 
     p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
     if (COLLIDE) {
         const float om = p.omega ? (float)p.omega[dn] : (float)p.omega0;
-        collide_shifted(g, wf, dr, rho, ux, uy, Jx, Jy, om, p.has_force != 0, (float)p.Fx, (float)p.Fy);
+        float h1, h5;
+        shifted_h(wf[1], h1, h5);
+        collide_v<float>(g, wf, h1, h5, dr, ux, uy, Jx, Jy, om, p.has_force != 0, (float)p.Fx, (float)p.Fy);
     }
     T *D = (T *)p.dst;
     const long long node = (long long)ij.y * p.pitch + ij.x;
@@ -330,7 +472,9 @@ __global__ void k_collide_shifted(const CollideParams p) {
         Jx = (float)(p.rho[dn] * p.ux[dn]);
         Jy = (float)(p.rho[dn] * p.uy[dn]);
     }
-    collide_shifted(g, wf, dr, rho, ux, uy, Jx, Jy, om, p.has_force != 0, (float)p.Fx, (float)p.Fy);
+    float h1, h5;
+    shifted_h(wf[1], h1, h5);
+    collide_v<float>(g, wf, h1, h5, dr, ux, uy, Jx, Jy, om, p.has_force != 0, (float)p.Fx, (float)p.Fy);
 #pragma unroll
     for (int k = 0; k < 9; k++) SV<T>::st(F + k * p.plane + node, g[k]);
 }
@@ -368,18 +512,24 @@ static void step_shifted_t(const FastStepParams &p, bool flags, bool collide, di
 
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
                          cudaStream_t s) {
-    const dim3 g((p.s.Nx + block.x - 1) / block.x, (p.s.Ny + block.y - 1) / block.y);
+    // Two nodes per thread along x.
+    const dim3 g((p.s.Nx + 2 * block.x - 1) / (2 * block.x), (p.s.Ny + block.y - 1) / block.y);
     if (store == STORE_F32) step_shifted_t<float>(p, flags, collide, g, block, s);
     else step_shifted_t<__half>(p, flags, collide, g, block, s);
     return cudaGetLastError();
 }
 
 cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
-                               int ntiles, int sel, int tws, int store, int grid, cudaStream_t s) {
+                               int ntiles, int sel, int tws, int store, bool wide, int grid, cudaStream_t s) {
     if (ntiles == 0) return cudaSuccess;
     if (tws < 5 || tws > 8) return cudaErrorInvalidValue;
-    if (store == STORE_F32) k_step_batch_shifted<float><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
-    else k_step_batch_shifted<__half><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+    if (store == STORE_F32) {
+        if (wide) k_step_batch_shifted<float, long long><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+        else k_step_batch_shifted<float, int><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+    } else {
+        if (wide) k_step_batch_shifted<__half, long long><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+        else k_step_batch_shifted<__half, int><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+    }
     return cudaGetLastError();
 }
 
@@ -387,8 +537,8 @@ int step_batch_shifted_grid(int store) {
     int nb = 0, dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (store == STORE_F32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_batch_shifted<float>, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_batch_shifted<__half>, 256, 0);
+    if (store == STORE_F32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_batch_shifted<float, int>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_batch_shifted<__half, int>, 256, 0);
     return nsm * (nb > 0 ? nb : 1);
 }
 

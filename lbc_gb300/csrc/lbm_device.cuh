@@ -401,9 +401,10 @@ struct StepParams {
     // momentum-exchange force (null when the geometry has no wall links):
     // every 32-node row segment (j, i / 32) that contains wall links has a
     // slot (seg_slot >= 0, numbered in row-major order from the geometry);
-    // the warp that steps it stores its sum at mem_partials[2 * slot] and
-    // k_force_reduce adds the slots up in order. A warp is always one such
-    // segment (block and tile widths are multiples of 32), so the sum does not
+    // the threads that step it (a warp of one node per thread in FP64, half a
+    // warp of two nodes per thread in shifted storage) store its sum at
+    // mem_partials[2 * slot] and k_force_reduce adds the slots up in order.
+    // Block and tile widths are multiples of 32 threads, so the sum does not
     // depend on the block or tile shape, nor on whether the case runs alone or
     // in a batch.
     double *mem_partials;

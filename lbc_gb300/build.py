@@ -2,7 +2,8 @@
 
 Translation units are compiled in parallel with nvcc:
   kernels_exact.cu    --fmad=false (lbc's FP64 rounding sequence, bit for bit)
-  kernels_shifted.cu  FP32/FP16 shifted-storage kernels (FMA allowed)
+  kernels_shifted.cu  FP32/FP16 shifted-storage kernels (--fmad=false as well: FMAs
+                      are written out, so every kernel rounds a node the same way)
   engine.cpp, dropin.cpp  host code (-ffp-contract=off: same host arithmetic on
                           x86-64 and aarch64)
 """
@@ -22,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 UNITS = [
     ("kernels_exact.cu", ["-O3", "-lineinfo", "--fmad=false"] + ARCH),
-    ("kernels_shifted.cu", ["-O3", "-lineinfo"] + ARCH),
+    ("kernels_shifted.cu", ["-O3", "-lineinfo", "--fmad=false"] + ARCH),
     ("engine.cpp", ["-O2"]),
     ("dropin.cpp", ["-O2"]),
     ("server.cpp", ["-O2"]),

@@ -301,7 +301,10 @@ bool Solver::build_geometry() {
         if (!dalloc(&d_colbase_, (size_t)Nx) || !dalloc(&d_rowbase_, (size_t)Ny)) return false;
         CK(cudaMemcpyAsync(d_colbase_, colbase.data(), Nx * sizeof(int), cudaMemcpyHostToDevice, stream_));
         CK(cudaMemcpyAsync(d_rowbase_, rowbase.data(), Ny * sizeof(int), cudaMemcpyHostToDevice, stream_));
-        if (!dalloc(&d_bandf_, (size_t)nslots_ * 9) || !dalloc(&d_bandm_[0], (size_t)nslots_ * 3) ||
+        // Band populations: FP64 f for FP64 storage, FP32 g = f - w otherwise.
+        const bool band_ok = d_.store == STORE_F64 ? dalloc(&d_bandf_, (size_t)nslots_ * 9)
+                                                   : dalloc(&d_bandg_, (size_t)nslots_ * 9);
+        if (!band_ok || !dalloc(&d_bandm_[0], (size_t)nslots_ * 3) ||
             !dalloc(&d_bandm_[1], (size_t)nslots_ * 3))
             return false;
         if (!dalloc(&d_wnodes_, wnodes.size()) || !dalloc(&d_seed_nodes_, seed_nodes.size()) ||
@@ -570,6 +573,7 @@ StepParams Solver::step_params(int src, int dst, bool write_macro, int bparity) 
     p.uy = macro_out_[2] ? macro_out_[2] : d_uy_;
     p.colbase = d_colbase_; p.rowbase = d_rowbase_; p.nslots = nslots_;
     p.bandf = d_bandf_;
+    p.bandg = d_bandg_;
     p.bandm_next = nslots_ ? d_bandm_[bparity ^ 1] : nullptr;
     if (has_mem_) {
         p.mem_partials = d_partials_;
@@ -598,7 +602,7 @@ StageParams Solver::stage_params(const Stage &st, int src, int bparity) const {
     s.kind = st.kind; s.index = st.index; s.along = st.along;
     s.val1 = st.d_val1; s.val2 = st.d_val2;
     s.flags = d_flags_; s.colbase = d_colbase_; s.rowbase = d_rowbase_; s.nslots = nslots_;
-    s.bandf = d_bandf_; s.bandm_prev = d_bandm_[bparity];
+    s.bandf = d_bandf_; s.bandg = d_bandg_; s.bandm_prev = d_bandm_[bparity];
     s.src = buf_[src];
     for (int k = 0; k < 9; k++) s.w[k] = d_.w[k];
     s.imp = st.d_imp;
@@ -734,7 +738,7 @@ FinishParams Solver::finish_params(int dst, bool write_macro, int bparity) const
     f.Nx = d_.Nx; f.Ny = d_.Ny; f.pitch = pitch_; f.plane = plane_;
     f.nw = nw_; f.wnodes = d_wnodes_;
     f.colbase = d_colbase_; f.rowbase = d_rowbase_; f.nslots = nslots_;
-    f.bandf = d_bandf_; f.bandm_next = nslots_ ? d_bandm_[bparity ^ 1] : nullptr;
+    f.bandf = d_bandf_; f.bandg = d_bandg_; f.bandm_next = nslots_ ? d_bandm_[bparity ^ 1] : nullptr;
     f.dst = buf_[dst];
     f.omega = d_omega_; f.omega0 = omega0_;
     f.has_force = (d_.Fx != 0.0 || d_.Fy != 0.0);

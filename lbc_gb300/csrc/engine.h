@@ -169,7 +169,8 @@ class Solver {
     double omega0_ = 1.0;
     int *d_colbase_ = nullptr, *d_rowbase_ = nullptr;
     int nslots_ = 0;
-    double *d_bandf_ = nullptr;
+    double *d_bandf_ = nullptr;  // FP64 storage
+    float *d_bandg_ = nullptr;   // shifted storage
     double *d_bandm_[2] = {nullptr, nullptr};
     int2 *d_wnodes_ = nullptr;
     int nw_ = 0;

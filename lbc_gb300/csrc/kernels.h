@@ -120,6 +120,10 @@ cudaError_t force_reduce(const ForceSlot *slots, int n, cudaStream_t s);
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
                          cudaStream_t s);
 cudaError_t finish_shifted(const FinishParams &p, int store, bool collide, cudaStream_t s);
+// Edge BCs of shifted storage in FP32 (launch::stage / stage_batch dispatch here).
+cudaError_t stage_shifted(const StageParams &p, int store, cudaStream_t s);
+cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, int max_along, int store,
+                                int sel, cudaStream_t s);
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s);
 // wide: some case has 9 * plane >= 2^31 elements (64-bit element offsets).
 cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,

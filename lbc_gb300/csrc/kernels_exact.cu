@@ -600,10 +600,9 @@ cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block
 
 // Edge kernels are FP64 and short: 32-thread blocks spread a line over many SMs.
 cudaError_t stage(const StageParams &p, int store, cudaStream_t s) {
+    if (store != STORE_F64) return stage_shifted(p, store, s);
     const int b = 32, g = (p.along + b - 1) / b;
-    if (store == STORE_F64) k_stage<double><<<g, b, 0, s>>>(p);
-    else if (store == STORE_F32) k_stage<float><<<g, b, 0, s>>>(p);
-    else k_stage<__half><<<g, b, 0, s>>>(p);
+    k_stage<double><<<g, b, 0, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -626,10 +625,9 @@ int step_batch_exact_grid() {
 cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int max_along, int store,
                         int sel, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
+    if (store != STORE_F64) return stage_batch_shifted(list, ephase, n, max_along, store, sel, s);
     const dim3 g((max_along + 31) / 32, n);
-    if (store == STORE_F64) k_stage_batch<double><<<g, 32, 0, s>>>(list, ephase, sel);
-    else if (store == STORE_F32) k_stage_batch<float><<<g, 32, 0, s>>>(list, ephase, sel);
-    else k_stage_batch<__half><<<g, 32, 0, s>>>(list, ephase, sel);
+    k_stage_batch<double><<<g, 32, 0, s>>>(list, ephase, sel);
     return cudaGetLastError();
 }
 

@@ -8,6 +8,7 @@
 // force reduction and the band values handed to the edge BCs.
 #include <cmath>
 
+#include "bc_shifted.cuh"
 #include "kernels.h"
 #include "lbm_device.cuh"
 #include "reduce.cuh"
@@ -155,20 +156,13 @@ __device__ __noinline__ void solid_node_outputs(const StepParams &p, int i, int 
         const int slot = band_slot(p.colbase, p.rowbase, i, j);
         const T *Dst = (const T *)p.dst;
 #pragma unroll
-        for (int k = 0; k < 9; k++)
-            p.bandf[(size_t)k * p.nslots + slot] = (double)SV<T>::ld_plain(Dst + k * p.plane + node) + p.w[k];
+        for (int k = 0; k < 9; k++) p.bandg[(size_t)k * p.nslots + slot] = SV<T>::ld_plain(Dst + k * p.plane + node);
         p.bandm_next[slot] = NAN;
         p.bandm_next[(size_t)p.nslots + slot] = NAN;
         p.bandm_next[2 * (size_t)p.nslots + slot] = NAN;
     }
 }
 
-__device__ __noinline__ void band_store_f(const StepParams &p, int slot, float g0, float g1, float g2,
-                                          float g3, float g4, float g5, float g6, float g7, float g8) {
-    const float g[9] = {g0, g1, g2, g3, g4, g5, g6, g7, g8};
-#pragma unroll
-    for (int k = 0; k < 9; k++) p.bandf[(size_t)k * p.nslots + slot] = (double)g[k] + p.w[k];
-}
 
 __device__ __noinline__ void macro_store(const StepParams &p, size_t dn, int slot, float dr, float ux,
                                          float uy) {
@@ -258,7 +252,8 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
     int slot = -1;
     if (FLAGS && (fl & NF_BAND)) {
         slot = band_slot(p.colbase, p.rowbase, i, j);
-        band_store_f(p, slot, g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7], g[8]);
+#pragma unroll
+        for (int k = 0; k < 9; k++) p.bandg[(size_t)k * p.nslots + slot] = g[k];
     }
     if (FLAGS && (fl & NF_BCW)) return;
     float dr, rho, ux, uy, Jx, Jy;
@@ -408,7 +403,7 @@ __device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 
     float g[9], wf[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) {
-        g[k] = SV<T>::rnd((float)(p.bandf[(size_t)k * p.nslots + slot] - p.w[k]));
+        g[k] = SV<T>::rnd(p.bandg[(size_t)k * p.nslots + slot]);
         wf[k] = (float)p.w[k];
     }
     float dr, rho, ux, uy, Jx, Jy;
@@ -479,7 +474,78 @@ __global__ void k_collide_shifted(const CollideParams p) {
     for (int k = 0; k < 9; k++) SV<T>::st(F + k * p.plane + node, g[k]);
 }
 
+// ---------------------------------------------------------------- edge BCs
+// The Boundary list on the band in FP32 (bc_shifted.cuh): band populations are
+// g, previous-step moments come from the FP64 band moments (rho - 1 formed in
+// FP64). The impedance wall's mass-spring-damper state and DFT stay FP64.
+template <typename T> struct BandAccessorS {
+    const StageParams &p;
+    __device__ int slot(int i, int j) const { return band_slot(p.colbase, p.rowbase, i, j); }
+    __device__ float get(int i, int j, int k) const { return p.bandg[(size_t)k * p.nslots + slot(i, j)]; }
+    __device__ void set(int i, int j, int k, float v) const { p.bandg[(size_t)k * p.nslots + slot(i, j)] = v; }
+    __device__ float drho(int i, int j) const { return (float)(p.bandm_prev[slot(i, j)] - 1.0); }
+    __device__ double rho64(int i, int j) const { return p.bandm_prev[slot(i, j)]; }
+    __device__ float ux(int i, int j) const { return (float)p.bandm_prev[(size_t)p.nslots + slot(i, j)]; }
+    __device__ float uy(int i, int j) const { return (float)p.bandm_prev[2 * (size_t)p.nslots + slot(i, j)]; }
+    __device__ float post(int i, int j, int k) const {
+        return SV<T>::ld_plain((const T *)p.src + k * p.plane + (long long)j * p.pitch + i);
+    }
+    __device__ bool solid(int i, int j) const { return (p.flags[(long long)j * p.pitch + i] & NF_SOLID) != 0; }
+};
+
+// One point of one Boundary entry (src/core/main_lbm.c:49-58), as stage_point
+// in kernels_exact.cu.
+template <typename T>
+__device__ __forceinline__ void stage_point_s(const StageParams &p, int t) {
+    BandAccessorS<T> a{p};
+    float w[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) w[k] = (float)p.w[k];
+    if (p.imp && p.kind == BC_VEL_BOT_REG && p.imp[(size_t)IMP_ACTIVE * p.along + t] != 0.0 &&
+        !a.solid(t, p.index)) {
+        const double vn = impedance_step(p.imp, p.along, p.imp_nf, t, a.rho64(t, p.index + 1), p.imp_alpha,
+                                         p.imp_cos, p.imp_sin, p.imp_wcos, p.imp_wsin, p.imp_windowed);
+        bc_regularized_s(a, w, t, p.index, t, p.index + 1, false, (float)p.val1[t], (float)(-vn));
+        return;
+    }
+    bc_apply_s(a, w, p.kind, p.Nx, p.Ny, p.index, t, p.val1, p.val2);
+}
+
+template <typename T>
+__global__ void k_stage_shifted(const StageParams p) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.along) return;
+    stage_point_s<T>(p, t);
+}
+
+template <typename T>
+__global__ void k_stage_batch_shifted(const StageParams *__restrict__ list, const int *__restrict__ ephase,
+                                      int sel) {
+    const int e = blockIdx.y;
+    const StageParams &p = list[2 * e + (sel ^ ephase[e])];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.along) return;
+    stage_point_s<T>(p, t);
+}
+
 namespace launch {
+
+cudaError_t stage_shifted(const StageParams &p, int store, cudaStream_t s) {
+    const int b = 64, g = (p.along + b - 1) / b;
+    if (store == STORE_F32) k_stage_shifted<float><<<g, b, 0, s>>>(p);
+    else k_stage_shifted<__half><<<g, b, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, int max_along, int store,
+                                int sel, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const dim3 g((max_along + 63) / 64, n);
+    if (store == STORE_F32) k_stage_batch_shifted<float><<<g, 64, 0, s>>>(list, ephase, sel);
+    else k_stage_batch_shifted<__half><<<g, 64, 0, s>>>(list, ephase, sel);
+    return cudaGetLastError();
+}
+
 
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s) {
     const dim3 b(64, 4);

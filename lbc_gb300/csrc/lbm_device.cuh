@@ -396,7 +396,8 @@ struct StepParams {
     // edge-BC band
     const int *colbase, *rowbase;
     int nslots;
-    double *bandf;            // [9][nslots], pre-collision f_new of band nodes
+    double *bandf;            // [9][nslots], pre-collision f_new of band nodes (FP64 storage)
+    float *bandg;             // [9][nslots], the same as g = f - w (shifted storage)
     double *bandm_next;       // [3][nslots], their moments (for the next step's BCs)
     // momentum-exchange force (null when the geometry has no wall links):
     // every 32-node row segment (j, i / 32) that contains wall links has a
@@ -425,7 +426,8 @@ struct StageParams {
     const uint16_t *flags;
     const int *colbase, *rowbase;
     int nslots;
-    double *bandf;
+    double *bandf;             // FP64 storage
+    float *bandg;              // shifted storage
     const double *bandm_prev;  // [3][nslots]
     const void *src;           // post-collision populations (periodic stages)
     double w[9];
@@ -438,7 +440,8 @@ struct FinishParams {
     const int2 *wnodes;        // (i, j) of every BC-written node
     const int *colbase, *rowbase;
     int nslots;
-    const double *bandf;
+    const double *bandf;       // FP64 storage
+    const float *bandg;        // shifted storage
     double *bandm_next;
     void *dst;
     const double *omega;

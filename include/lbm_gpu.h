@@ -59,6 +59,8 @@ typedef struct {
     int launches_per_step;         /* kernel launches per time step in the loop */
     size_t device_bytes;
     long long steps_done;
+    int edge_launches;             /* launches the edge stages take per step: consecutive
+                                      entries on disjoint nodes share one */
 } lbm_gpu_info;
 
 const char *lbm_gpu_last_error(void);

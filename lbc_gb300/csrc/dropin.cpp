@@ -722,6 +722,7 @@ int lbm_gpu_get_info(lbm_gpu_solver *s, lbm_gpu_info *info) {
     info->has_geometry = s->s->has_flags() ? 1 : 0;
     info->edge_stages = s->s->nstages();
     info->launches_per_step = s->s->launches_per_step();
+    info->edge_launches = (int)s->s->stage_groups().size();
     info->device_bytes = s->s->device_bytes();
     info->steps_done = s->s->steps_done();
     return LBM_GPU_OK;

@@ -22,6 +22,7 @@
 #include <map>
 #include <mutex>
 #include <set>
+#include <unordered_set>
 
 namespace lbm {
 
@@ -164,6 +165,7 @@ bool Solver::build_geometry() {
     for (int c : cols) { colbase[c] = ns; ns += Ny; }
     for (int r : rows) { rowbase[r] = ns; ns += Nx; }
     nslots_ = ns;
+    group_stages(solid);
     auto slot_of = [&](int i, int j) { return colbase[i] >= 0 ? colbase[i] + j : rowbase[j] + i; };
 
     // Flags and links.
@@ -330,6 +332,62 @@ bool Solver::build_geometry() {
     if (!upload_all_bc_values()) return false;
     CK(cudaStreamSynchronize(stream_));
     return true;
+}
+
+// Consecutive Boundary entries that touch disjoint band nodes run in one
+// launch. Entry s joins the current group unless it writes a node the group
+// reads or writes, or reads a node the group writes (lbc applies the list in
+// order, so such an entry must see, or must not yet see, the earlier writes).
+// Writes: the entry's non-solid line nodes. Reads within the step: those nodes
+// and, for entries that read their interior neighbour's populations
+// (regularized, convective), the neighbour of each; moments of the previous
+// step and post-collision sources (periodic entries) are not written by any
+// entry.
+template <class Solid> void Solver::group_stages(const Solid &solid) {
+    const int Nx = d_.Nx, Ny = d_.Ny;
+    groups_.clear();
+    std::unordered_set<long long> gw, gr;
+    auto id = [&](int i, int j) { return (long long)j * Nx + i; };
+    for (size_t s = 0; s < stages_.size(); s++) {
+        const Stage &st = stages_[s];
+        std::vector<long long> w, r;
+        auto line = [&](bool col, int idx, int di, int dj, bool reads_neighbour) {
+            const int n = col ? Ny : Nx;
+            for (int t = 0; t < n; t++) {
+                const int i = col ? idx : t, j = col ? t : idx;
+                if (solid(i, j)) continue;
+                w.push_back(id(i, j));
+                r.push_back(id(i, j));
+                if (reads_neighbour) r.push_back(id(i + di, j + dj));
+            }
+        };
+        const int x = st.index;
+        switch (st.kind) {
+        case BC_PERIODIC_X: line(true, 0, 0, 0, false); line(true, Nx - 1, 0, 0, false); r.clear(); break;
+        case BC_PERIODIC_Y: line(false, 0, 0, 0, false); line(false, Ny - 1, 0, 0, false); r.clear(); break;
+        case BC_VEL_IN_ZH: case BC_VEL_OUT_ZH: case BC_PRES_IN_ZH: case BC_PRES_OUT_ZH: line(true, x, 0, 0, false); break;
+        case BC_VEL_TOP_ZH: case BC_VEL_BOT_ZH: line(false, x, 0, 0, false); break;
+        case BC_CONV_IN: case BC_VEL_IN_REG: case BC_PRES_IN_REG: line(true, x, 1, 0, true); break;
+        case BC_CONV_OUT: case BC_VEL_OUT_REG: case BC_PRES_OUT_REG: line(true, x, -1, 0, true); break;
+        case BC_VEL_BOT_REG: case BC_PRES_BOT_REG: line(false, x, 0, 1, true); break;
+        case BC_VEL_TOP_REG: case BC_PRES_TOP_REG: line(false, x, 0, -1, true); break;
+        default: break;
+        }
+        bool conflict = groups_.empty();
+        for (long long v : w)
+            if (conflict || gw.count(v) || gr.count(v)) { conflict = true; break; }
+        if (!conflict)
+            for (long long v : r)
+                if (gw.count(v)) { conflict = true; break; }
+        if (conflict || groups_.back().size() >= (size_t)kStageGroupMax) {
+            groups_.emplace_back();
+            gw.clear();
+            gr.clear();
+        }
+        groups_.back().push_back((int)s);
+        gw.insert(w.begin(), w.end());
+        gr.insert(r.begin(), r.end());
+    }
 }
 
 // Which 32-node row segments (j, i / 32) contain wall links: the warp that
@@ -764,7 +822,20 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
     }
     if (has_mem_) CK(launch::force_reduce(d_force_slot_, 1, s));
     if (stages_.empty()) return true;
-    for (const Stage &st : stages_) CK(launch::stage(stage_params(st, src, bparity), d_.store, s));
+    for (const std::vector<int> &g : groups_) {
+        if (g.size() == 1) {
+            CK(launch::stage(stage_params(stages_[g[0]], src, bparity), d_.store, s));
+            continue;
+        }
+        StageGroup sg;
+        std::memset(&sg, 0, sizeof sg);
+        sg.n = (int)g.size();
+        for (int q = 0; q < sg.n; q++) {
+            sg.p[q] = stage_params(stages_[g[q]], src, bparity);
+            sg.max_along = std::max(sg.max_along, sg.p[q].along);
+        }
+        CK(launch::stage_group(sg, d_.store, s));
+    }
     const FinishParams f = finish_params(dst, write_macro, bparity);
     if (d_.store == STORE_F64) CK(launch::finish_exact(f, collide, s));
     else CK(launch::finish_shifted(f, d_.store, collide, s));
@@ -1104,7 +1175,7 @@ bool Batch::build() {
         if (9LL * s->plane() >= (1LL << 31)) wide_ = true;
         if (s->has_mem()) force.push_back(s->force_slot());
         for (const int2 &w : s->wnodes()) fin_nodes.push_back(make_int4(c, w.x, w.y, 0));
-        max_stages_ = std::max(max_stages_, (int)s->stages().size());
+        max_stages_ = std::max(max_stages_, (int)s->stage_groups().size());
         for (const Stage &st : s->stages()) max_along_ = std::max(max_along_, st.along);
     }
     if (!build_tiles(tws_)) return false;
@@ -1115,15 +1186,22 @@ bool Batch::build() {
     if (!check_cuda(cudaMalloc(&sp, psize * 2 * nc), "cudaMalloc batch")) return false;
     allocs_.push_back(sp);
     d_sp_ = sp;
-    if (!balloc(allocs_, &d_phase_, nc) || !balloc(allocs_, &d_fin_, 2 * nc) ||
+    // Entries per stage level (a case may put several stages in one level).
+    std::vector<int> level_cnt(max_stages_, 0);
+    for (Solver *c : cases_)
+        for (size_t l = 0; l < c->stage_groups().size(); l++) level_cnt[l] += (int)c->stage_groups()[l].size();
+    // d_phase_ is indexed by case (bulk, finish) and by level entry (stages).
+    int nphase = nc;
+    for (int cnt : level_cnt) nphase = std::max(nphase, cnt);
+    if (!balloc(allocs_, &d_phase_, nphase) || !balloc(allocs_, &d_fin_, 2 * nc) ||
         !balloc(allocs_, &d_fin_nodes_, fin_nodes.size()) || !balloc(allocs_, &d_force_, force.size()))
         return false;
-    CK(cudaMemsetAsync(d_phase_, 0, nc * sizeof(int), stream_));
+    CK(cudaMemsetAsync(d_phase_, 0, nphase * sizeof(int), stream_));
     if (nfin_) CK(cudaMemcpyAsync(d_fin_nodes_, fin_nodes.data(), fin_nodes.size() * sizeof(int4), cudaMemcpyHostToDevice, stream_));
     if (nforce_) CK(cudaMemcpyAsync(d_force_, force.data(), force.size() * sizeof(ForceSlot), cudaMemcpyHostToDevice, stream_));
+    // One launch per level: level l holds the l-th stage group of every case.
     for (int s = 0; s < max_stages_; s++) {
-        int cnt = 0;
-        for (Solver *c : cases_) cnt += (int)c->stages().size() > s ? 1 : 0;
+        const int cnt = level_cnt[s];
         StageParams *d = nullptr;
         if (!balloc(allocs_, &d, 2 * cnt)) return false;
         d_stage_lists_.push_back(d);
@@ -1198,10 +1276,11 @@ bool Batch::run(int nsteps) {
             }
             fin[2 * c] = s->finish_params(1 - cur, false, par);
             fin[2 * c + 1] = s->finish_params(cur, false, par ^ 1);
-            for (size_t k = 0; k < s->stages().size(); k++) {
-                lists[k].push_back(s->stage_params(s->stages()[k], cur, par));
-                lists[k].push_back(s->stage_params(s->stages()[k], 1 - cur, par ^ 1));
-            }
+            for (size_t l = 0; l < s->stage_groups().size(); l++)
+                for (int k : s->stage_groups()[l]) {
+                    lists[l].push_back(s->stage_params(s->stages()[k], cur, par));
+                    lists[l].push_back(s->stage_params(s->stages()[k], 1 - cur, par ^ 1));
+                }
         }
         if (store_ == STORE_F64)
             okk = okk && check_cuda(cudaMemcpyAsync(d_sp_, sp.data(), sp.size() * sizeof(StepParams), cudaMemcpyHostToDevice, stream_), "H2D");

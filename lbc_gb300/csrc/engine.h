@@ -95,7 +95,9 @@ class Solver {
     int current() const { return cur_; }
     long long steps_done() const { return steps_done_; }
     // Kernel launches per time step inside the loop (for launch counting).
-    int launches_per_step() const { return 1 + (int)stages_.size() + (nw_ > 0 ? 1 : 0); }
+    int launches_per_step() const {
+        return 1 + (has_mem_ ? 1 : 0) + (int)groups_.size() + (nw_ > 0 ? 1 : 0);
+    }
     bool set_block(dim3 b);
     dim3 block() const { return block_; }
     // Launch-shape tuning (tune.h). mode 1: take the cached block for this
@@ -114,6 +116,8 @@ class Solver {
     StageParams stage_params(const Stage &st, int src, int bparity) const;
     FinishParams finish_params(int dst, bool write_macro, int bparity) const;
     const std::vector<Stage> &stages() const { return stages_; }
+    // Consecutive stages that share one launch (indices into stages()).
+    const std::vector<std::vector<int>> &stage_groups() const { return groups_; }
     const std::vector<int2> &wnodes() const { return wnodes_host_; }
     bool has_mem() const { return has_mem_; }
     // 1 for fluid nodes with at least one solid pull source (wall link), [Ny][Nx].
@@ -185,6 +189,8 @@ class Solver {
     unsigned long long *hist_count_ptr_ = nullptr;
     double *d_stage_ = nullptr;  // AoS staging (FP64, 72 N bytes)
     std::vector<Stage> stages_;
+    std::vector<std::vector<int>> groups_;
+    template <class Solid> void group_stages(const Solid &solid);
     dim3 block_{64, 4, 1};
     cudaGraphExec_t pair_exec_ = nullptr;
     int pair_cur_ = -1, pair_parity_ = -1;

@@ -84,10 +84,20 @@ struct FastStepParams {
     float h1f, h5f;
 };
 
+// Up to kStageGroupMax Boundary entries that touch disjoint band nodes, in one
+// launch (blockIdx.y = member), passed by value.
+constexpr int kStageGroupMax = 6;
+struct StageGroup {
+    StageParams p[kStageGroupMax];
+    int n;
+    int max_along;
+};
+
 namespace launch {
 // exact FP64 (kernels_exact.cu)
 cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block, cudaStream_t s);
 cudaError_t stage(const StageParams &p, int store, cudaStream_t s);
+cudaError_t stage_group(const StageGroup &g, int store, cudaStream_t s);
 cudaError_t finish_exact(const FinishParams &p, bool collide, cudaStream_t s);
 cudaError_t collide_exact(const CollideParams &p, cudaStream_t s);
 cudaError_t collide_aos_exact(const CollideAosParams &p, cudaStream_t s);
@@ -122,6 +132,7 @@ cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool co
 cudaError_t finish_shifted(const FinishParams &p, int store, bool collide, cudaStream_t s);
 // Edge BCs of shifted storage in FP32 (launch::stage / stage_batch dispatch here).
 cudaError_t stage_shifted(const StageParams &p, int store, cudaStream_t s);
+cudaError_t stage_group_shifted(const StageGroup &g, int store, cudaStream_t s);
 cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, int max_along, int store,
                                 int sel, cudaStream_t s);
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s);

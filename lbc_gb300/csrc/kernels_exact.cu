@@ -205,6 +205,14 @@ __global__ void k_stage(const StageParams p) {
     stage_point<T>(p, t);
 }
 
+template <typename T>
+__global__ void k_stage_group(const StageGroup g) {
+    const StageParams &p = g.p[blockIdx.y];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.along) return;
+    stage_point<T>(p, t);
+}
+
 // Stage `s` of every case of a batch: blockIdx.y selects the case entry,
 // list[2 * e + (sel ^ phase)] its parameters for this ping-pong direction.
 template <typename T>
@@ -599,6 +607,13 @@ cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block
 }
 
 // Edge kernels are FP64 and short: 32-thread blocks spread a line over many SMs.
+cudaError_t stage_group(const StageGroup &g, int store, cudaStream_t s) {
+    if (store != STORE_F64) return stage_group_shifted(g, store, s);
+    const dim3 grid((g.max_along + 31) / 32, g.n);
+    k_stage_group<double><<<grid, 32, 0, s>>>(g);
+    return cudaGetLastError();
+}
+
 cudaError_t stage(const StageParams &p, int store, cudaStream_t s) {
     if (store != STORE_F64) return stage_shifted(p, store, s);
     const int b = 32, g = (p.along + b - 1) / b;

@@ -519,6 +519,14 @@ __global__ void k_stage_shifted(const StageParams p) {
 }
 
 template <typename T>
+__global__ void k_stage_group_shifted(const StageGroup g) {
+    const StageParams &p = g.p[blockIdx.y];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.along) return;
+    stage_point_s<T>(p, t);
+}
+
+template <typename T>
 __global__ void k_stage_batch_shifted(const StageParams *__restrict__ list, const int *__restrict__ ephase,
                                       int sel) {
     const int e = blockIdx.y;
@@ -534,6 +542,13 @@ cudaError_t stage_shifted(const StageParams &p, int store, cudaStream_t s) {
     const int b = 64, g = (p.along + b - 1) / b;
     if (store == STORE_F32) k_stage_shifted<float><<<g, b, 0, s>>>(p);
     else k_stage_shifted<__half><<<g, b, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t stage_group_shifted(const StageGroup &g, int store, cudaStream_t s) {
+    const dim3 grid((g.max_along + 63) / 64, g.n);
+    if (store == STORE_F32) k_stage_group_shifted<float><<<grid, 64, 0, s>>>(g);
+    else k_stage_group_shifted<__half><<<grid, 64, 0, s>>>(g);
     return cudaGetLastError();
 }
 

@@ -222,31 +222,54 @@ __device__ __forceinline__ double impedance_step(double *imp, int along, int nf,
                                                  const double *cw, const double *sw,
                                                  double wcos, double wsin, int windowed) {
 #define IMP(f) imp[(size_t)(f) * along + t]
-    const double rb = IMP(IMP_RHOBAR);
+    // The fields share one array, so the compiler cannot move a load above an
+    // earlier store to it: all loads of a group are issued before its stores
+    // (the node's state, then the DFT in groups of four frequencies), which
+    // keeps the chain to a few memory latencies. The arithmetic is the same
+    // sequence as a field-by-field update.
+    const double rb = IMP(IMP_RHOBAR), wc0 = IMP(IMP_WC), ws0 = IMP(IMP_WS);
+    const double x = IMP(IMP_X), v = IMP(IMP_V);
+    const double a11 = IMP(IMP_A11), a12 = IMP(IMP_A12), b1 = IMP(IMP_B1);
+    const double a21 = IMP(IMP_A21), a22 = IMP(IMP_A22), b2 = IMP(IMP_B2);
+    double cr[4], ci[4], ac[4][4];
+    auto load_group = [&](int f0) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (f0 + q >= nf) break;
+            cr[q] = IMP(imp_field(f0 + q, 0));
+            ci[q] = IMP(imp_field(f0 + q, 1));
+#pragma unroll
+            for (int m = 0; m < 4; m++) ac[q][m] = IMP(imp_field(f0 + q, 2 + m));
+        }
+    };
+    load_group(0);
     const double p = (rho_n - rb) / 3.0;
-    IMP(IMP_RHOBAR) = rb + alpha * (rho_n - rb);
     double win = 1.0;
     if (windowed) {
-        const double c = IMP(IMP_WC), s = IMP(IMP_WS);
-        win = 0.5 * (1.0 - c);
-        IMP(IMP_WC) = c * wcos - s * wsin;
-        IMP(IMP_WS) = s * wcos + c * wsin;
+        win = 0.5 * (1.0 - wc0);
+        IMP(IMP_WC) = wc0 * wcos - ws0 * wsin;
+        IMP(IMP_WS) = ws0 * wcos + wc0 * wsin;
     }
-    const double x = IMP(IMP_X), v = IMP(IMP_V);
-    const double xn = IMP(IMP_A11) * x + IMP(IMP_A12) * v + IMP(IMP_B1) * p;
-    const double vn = IMP(IMP_A21) * x + IMP(IMP_A22) * v + IMP(IMP_B2) * p;
+    IMP(IMP_RHOBAR) = rb + alpha * (rho_n - rb);
+    const double xn = a11 * x + a12 * v + b1 * p;
+    const double vn = a21 * x + a22 * v + b2 * p;
     IMP(IMP_X) = xn;
     IMP(IMP_V) = vn;
-    for (int f = 0; f < nf; f++) {
-        const double cr = IMP(imp_field(f, 0)), ci = IMP(imp_field(f, 1));
-        const double wp = win * p, wv = win * vn;
-        IMP(imp_field(f, 2)) += wp * cr;
-        IMP(imp_field(f, 3)) += wp * ci;
-        IMP(imp_field(f, 4)) += wv * cr;
-        IMP(imp_field(f, 5)) += wv * ci;
-        // advance the phasor e^{-i w n} by one step
-        IMP(imp_field(f, 0)) = cr * cw[f] + ci * sw[f];
-        IMP(imp_field(f, 1)) = ci * cw[f] - cr * sw[f];
+    const double wp = win * p, wv = win * vn;
+    for (int f0 = 0; f0 < nf; f0 += 4) {
+        if (f0 > 0) load_group(f0);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int f = f0 + q;
+            if (f >= nf) break;
+            IMP(imp_field(f, 2)) = ac[q][0] + wp * cr[q];
+            IMP(imp_field(f, 3)) = ac[q][1] + wp * ci[q];
+            IMP(imp_field(f, 4)) = ac[q][2] + wv * cr[q];
+            IMP(imp_field(f, 5)) = ac[q][3] + wv * ci[q];
+            // advance the phasor e^{-i w n} by one step
+            IMP(imp_field(f, 0)) = cr[q] * cw[f] + ci[q] * sw[f];
+            IMP(imp_field(f, 1)) = ci[q] * cw[f] - cr[q] * sw[f];
+        }
     }
     return vn;
 #undef IMP

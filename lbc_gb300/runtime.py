@@ -59,7 +59,7 @@ class Info(C.Structure):
     _fields_ = [("Nx", C.c_int), ("Ny", C.c_int), ("pitch", C.c_int), ("storage", C.c_int),
                 ("has_geometry", C.c_int), ("edge_stages", C.c_int),
                 ("launches_per_step", C.c_int), ("device_bytes", C.c_size_t),
-                ("steps_done", C.c_longlong)]
+                ("steps_done", C.c_longlong), ("edge_launches", C.c_int)]
 
 
 def _bind_ext(lib: C.CDLL) -> None:

@@ -73,5 +73,6 @@ def test_batch_info_counts_launches():
     b = GpuBatch([s for _, _, _, s in mixed])
     nodes, lps = b.info()
     assert nodes == sum(c.nodes for _, c, _, _ in mixed)
-    max_stages = max(s.info().edge_stages for _, _, _, s in mixed)
-    assert lps == 1 + max_stages + 2
+    levels = max(s.info().edge_launches for _, _, _, s in mixed)
+    assert 1 <= levels <= max(s.info().edge_stages for _, _, _, s in mixed)
+    assert lps == 1 + levels + 2

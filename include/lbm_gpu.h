@@ -175,14 +175,17 @@ int lbm_gpu_batch_destroy(lbm_gpu_batch *b);
 /* ---- Serving: a continuous-batching request loop.
  * Any thread prepares a request (case, initial state, step count; all inputs
  * are copied), optionally attaches an impedance wall, and enqueues it. Each
- * scheduling round (lbm_gpu_server_poll, or the server's own thread after
- * lbm_gpu_server_start) admits queued requests in arrival order while the
- * device-memory budget and the slot limit allow, advances all active requests
- * by one chunk (one graph-captured persistent batch per storage type, the
- * batches running concurrently), and retires finished ones: their fields (and
- * populations when asked for) are copied to host memory and their device
- * memory is freed. Results are identical to running each request alone
- * (lbm_gpu_run). budget_bytes = 0: 85 % of the free device memory. */
+ * storage type has a lane; a lane's round (lbm_gpu_server_poll runs one round
+ * of every lane in the caller's thread; lbm_gpu_server_start gives each lane
+ * its own thread) takes queued requests of its type in arrival order while the
+ * device-memory budget and the slot limit (over all lanes) allow, launches one
+ * chunk for its active requests (one graph-captured persistent batch, reused
+ * while the set of requests is unchanged), admits the taken requests while the
+ * chunk runs, then retires finished ones: their fields (and populations when
+ * asked for) are copied to host memory and their device memory is returned to
+ * the pool. Lanes run concurrently. Results are identical to running each
+ * request alone (lbm_gpu_run). budget_bytes = 0: 85 % of the free device
+ * memory. */
 typedef struct lbm_gpu_server lbm_gpu_server;
 int lbm_gpu_server_create(size_t budget_bytes, int max_active, int chunk_steps, lbm_gpu_server **out);
 /* Returns the request id (> 0) or a negative code. */
@@ -207,6 +210,11 @@ int lbm_gpu_server_fetch(lbm_gpu_server *srv, int id, double *f, double *f_new, 
 int lbm_gpu_server_release(lbm_gpu_server *srv, int id);
 int lbm_gpu_server_stats(lbm_gpu_server *srv, long long *lups_done, double *busy_s, int *queued,
                          int *active, size_t *bytes_in_use);
+/* Host time per phase of the scheduling rounds so far: out[0] rounds, [1]
+ * admission (solver setup and state upload), [2] batch construction, [3]
+ * launching and waiting for the chunks, [4] retiring (results to host, device
+ * memory freed), seconds. Writes min(n, 5) values. */
+int lbm_gpu_server_profile(lbm_gpu_server *srv, double *out, int n);
 int lbm_gpu_server_destroy(lbm_gpu_server *srv);
 
 /* ---- Force on caller-owned device memory, allocating nothing (no counterpart

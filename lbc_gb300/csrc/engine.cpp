@@ -42,10 +42,32 @@ bool check_cuda(cudaError_t e, const char *what) {
         if (!check_cuda((call), #call)) return false; \
     } while (0)
 
+// Device memory is stream-ordered (cudaMallocAsync / cudaFreeAsync on the
+// owner's stream, from the device's default pool): freeing a finished case
+// does not synchronize the device, so a server can retire cases while other
+// batches run.
+void use_retaining_pool() {
+    static std::mutex mu;
+    static std::set<int> done;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count(dev)) return;
+    done.insert(dev);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) return;
+    unsigned long long keep = ~0ull;  // keep freed blocks for reuse instead of returning them
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+}
+
+bool device_alloc(void **q, size_t bytes, cudaStream_t s) {
+    return check_cuda(cudaMallocAsync(q, bytes, s), "cudaMallocAsync");
+}
+
 template <class T> bool Solver::dalloc(T **p, size_t count) {
     if (count == 0) count = 1;
     void *q = nullptr;
-    if (!check_cuda(cudaMalloc(&q, count * sizeof(T)), "cudaMalloc")) return false;
+    if (!device_alloc(&q, count * sizeof(T), stream_)) return false;
     allocs_.push_back(q);
     dev_bytes_ += count * sizeof(T);
     *p = (T *)q;
@@ -61,6 +83,7 @@ Solver::Solver(const CaseDesc &d) : d_(d) {
     pitch_ = (d_.Nx + 63) / 64 * 64;
     plane_ = (long long)pitch_ * d_.Ny;
     if (!check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate")) return;
+    use_retaining_pool();
     if (!build_geometry()) return;
     ok_ = true;
     set_autotune(tune_default_mode());
@@ -68,7 +91,7 @@ Solver::Solver(const CaseDesc &d) : d_(d) {
 
 Solver::~Solver() {
     if (pair_exec_) cudaGraphExecDestroy(pair_exec_);
-    for (void *p : allocs_) cudaFree(p);
+    for (void *p : allocs_) cudaFreeAsync(p, stream_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -278,7 +301,7 @@ bool Solver::build_geometry() {
     // Device allocation.
     for (int b = 0; b < 2; b++) {
         void *p = nullptr;
-        if (!check_cuda(cudaMalloc(&p, (size_t)plane_ * 9 * esize_), "cudaMalloc populations")) return false;
+        if (!device_alloc(&p, (size_t)plane_ * 9 * esize_, stream_)) return false;
         allocs_.push_back(p);
         dev_bytes_ += (size_t)plane_ * 9 * esize_;
         buf_[b] = p;
@@ -884,6 +907,29 @@ bool Solver::capture_pair() {
     return true;
 }
 
+// This case's tiles for the batched kernel (x = 0, y = x0, z = y0, w = 1 when
+// the tile contains wall links), built once per tile shape: the batch
+// concatenates them instead of rescanning every node whenever it is rebuilt.
+const std::vector<int4> &Solver::tiles(int tws) const {
+    const int key = tws;
+    auto it = tile_cache_.find(key);
+    if (it != tile_cache_.end()) return it->second;
+    std::vector<int4> out;
+    const int Nx = d_.Nx, Ny = d_.Ny;
+    const int tw = (d_.store == STORE_F64 ? 1 : 2) << tws, th = 256 >> tws;
+    for (int y = 0; y < Ny; y += th)
+        for (int x = 0; x < Nx; x += tw) {
+            int w = 0;
+            if (has_mem_) {
+                for (int j = y; j < std::min(Ny, y + th) && !w; j++)
+                    for (int i = x; i < std::min(Nx, x + tw); i++)
+                        if (link_node_[(size_t)j * Nx + i]) { w = 1; break; }
+            }
+            out.push_back(make_int4(0, x, y, w));
+        }
+    return tile_cache_.emplace(key, std::move(out)).first->second;
+}
+
 std::string Solver::tune_key() const {
     return device_tag() + "/step/s" + std::to_string(d_.store) + "/" + std::to_string(d_.Nx) + "x" +
            std::to_string(d_.Ny) + (has_flags_ ? "/geo" : "/plain") + (has_mem_ ? "/mem" : "");
@@ -1009,14 +1055,18 @@ Batch::Batch(const std::vector<Solver *> &cases) : cases_(cases) {
 
 Batch::~Batch() {
     if (pair_exec_) cudaGraphExecDestroy(pair_exec_);
-    if (d_tiles_) cudaFree(d_tiles_);
-    for (void *p : allocs_) cudaFree(p);
+    if (params_ev_) {
+        cudaEventSynchronize(params_ev_);
+        cudaEventDestroy(params_ev_);
+    }
+    if (d_tiles_) cudaFreeAsync(d_tiles_, stream_);
+    for (void *p : allocs_) cudaFreeAsync(p, stream_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
-template <class T> static bool balloc(std::vector<void *> &allocs, T **p, size_t n) {
+template <class T> static bool balloc(std::vector<void *> &allocs, T **p, size_t n, cudaStream_t s) {
     void *q = nullptr;
-    if (!check_cuda(cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)), "cudaMalloc batch")) return false;
+    if (!device_alloc(&q, std::max<size_t>(n, 1) * sizeof(T), s)) return false;
     allocs.push_back(q);
     *p = (T *)q;
     return true;
@@ -1029,27 +1079,15 @@ template <class T> static bool balloc(std::vector<void *> &allocs, T **p, size_t
 // wall links (their threads store force partials).
 std::vector<int4> Batch::make_tiles(int tws) const {
     std::vector<int4> tiles;
-    const int tw = (store_ == STORE_F64 ? 1 : 2) << tws, th = 256 >> tws;
-    for (int c = 0; c < (int)cases_.size(); c++) {
-        Solver *s = cases_[c];
-        const std::vector<uint8_t> &ln = s->link_nodes();
-        for (int y = 0; y < s->Ny(); y += th)
-            for (int x = 0; x < s->Nx(); x += tw) {
-                int w = 0;
-                if (s->has_mem()) {
-                    for (int j = y; j < std::min(s->Ny(), y + th) && !w; j++)
-                        for (int i = x; i < std::min(s->Nx(), x + tw); i++)
-                            if (ln[(size_t)j * s->Nx() + i]) { w = 1; break; }
-                }
-                tiles.push_back(make_int4(c, x, y, w));
-            }
-    }
+    for (int c = 0; c < (int)cases_.size(); c++)
+        for (const int4 &t : cases_[c]->tiles(tws))
+            tiles.push_back(make_int4(c, t.y, t.z, t.w));
     return tiles;
 }
 
 bool Batch::upload_tiles(const std::vector<int4> &tiles, int4 **d) {
     *d = nullptr;
-    CK(cudaMalloc(d, std::max<size_t>(tiles.size(), 1) * sizeof(int4)));
+    if (!device_alloc((void **)d, std::max<size_t>(tiles.size(), 1) * sizeof(int4), stream_)) return false;
     CK(cudaMemcpyAsync(*d, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, stream_));
     return true;
 }
@@ -1057,7 +1095,7 @@ bool Batch::upload_tiles(const std::vector<int4> &tiles, int4 **d) {
 // Makes (d, n, tws) the tile list of the bulk kernel, freeing the previous
 // list when free_old is set (the caller has synchronized the stream).
 void Batch::install_tiles(int4 *d, int n, int tws, bool free_old) {
-    if (free_old && d_tiles_ && d_tiles_ != d) cudaFree(d_tiles_);
+    if (free_old && d_tiles_ && d_tiles_ != d) cudaFreeAsync(d_tiles_, stream_);
     d_tiles_ = d;
     ntiles_ = n;
     tws_ = tws;
@@ -1154,14 +1192,14 @@ int Batch::tune_online(int avail_pairs) {
     cudaStreamSynchronize(stream_);
     if (best >= 0) {
         install_tiles(d[best], n[best], kTileCand[best], false);
-        if (orig) cudaFree(orig);
+        if (orig) cudaFreeAsync(orig, stream_);
         tuned_ = true;
         tune_store(tune_key(), 1 << kTileCand[best], 256 >> kTileCand[best], tuned_us_);
     } else {
         install_tiles(orig, orig_n, orig_tws, false);
     }
     for (int c = 0; c < nc; c++)
-        if (d[c] && d[c] != d_tiles_) cudaFree(d[c]);
+        if (d[c] && d[c] != d_tiles_) cudaFreeAsync(d[c], stream_);
     return okk ? used : -1;
 }
 
@@ -1183,7 +1221,7 @@ bool Batch::build() {
     nforce_ = (int)force.size();
     const size_t psize = store_ == STORE_F64 ? sizeof(StepParams) : sizeof(FastStepParams);
     void *sp = nullptr;
-    if (!check_cuda(cudaMalloc(&sp, psize * 2 * nc), "cudaMalloc batch")) return false;
+    if (!device_alloc(&sp, psize * 2 * nc, stream_)) return false;
     allocs_.push_back(sp);
     d_sp_ = sp;
     // Entries per stage level (a case may put several stages in one level).
@@ -1193,8 +1231,8 @@ bool Batch::build() {
     // d_phase_ is indexed by case (bulk, finish) and by level entry (stages).
     int nphase = nc;
     for (int cnt : level_cnt) nphase = std::max(nphase, cnt);
-    if (!balloc(allocs_, &d_phase_, nphase) || !balloc(allocs_, &d_fin_, 2 * nc) ||
-        !balloc(allocs_, &d_fin_nodes_, fin_nodes.size()) || !balloc(allocs_, &d_force_, force.size()))
+    if (!balloc(allocs_, &d_phase_, nphase, stream_) || !balloc(allocs_, &d_fin_, 2 * nc, stream_) ||
+        !balloc(allocs_, &d_fin_nodes_, fin_nodes.size(), stream_) || !balloc(allocs_, &d_force_, force.size(), stream_))
         return false;
     CK(cudaMemsetAsync(d_phase_, 0, nphase * sizeof(int), stream_));
     if (nfin_) CK(cudaMemcpyAsync(d_fin_nodes_, fin_nodes.data(), fin_nodes.size() * sizeof(int4), cudaMemcpyHostToDevice, stream_));
@@ -1203,7 +1241,7 @@ bool Batch::build() {
     for (int s = 0; s < max_stages_; s++) {
         const int cnt = level_cnt[s];
         StageParams *d = nullptr;
-        if (!balloc(allocs_, &d, 2 * cnt)) return false;
+        if (!balloc(allocs_, &d, 2 * cnt, stream_)) return false;
         d_stage_lists_.push_back(d);
         stage_counts_.push_back(cnt);
     }
@@ -1259,12 +1297,19 @@ bool Batch::run(int nsteps) {
     for (Solver *c : cases_) okk = okk && c->begin_steps(stream_);
     const int mid = nsteps - 1;
     if (okk && mid > 0) {
-        // Parameters of both ping-pong directions from each case's current state.
+        // Parameters of both ping-pong directions from each case's current state,
+        // in host vectors that outlive the copies (the previous run's copies are
+        // waited for before the vectors are refilled).
         const int nc = (int)cases_.size();
-        std::vector<StepParams> sp(2 * nc);
-        std::vector<FastStepParams> fsp(store_ == STORE_F64 ? 0 : 2 * nc);
-        std::vector<FinishParams> fin(2 * nc);
-        std::vector<std::vector<StageParams>> lists(max_stages_);
+        if (params_ev_) okk = okk && check_cuda(cudaEventSynchronize(params_ev_), "event");
+        std::vector<StepParams> &sp = h_sp_;
+        std::vector<FastStepParams> &fsp = h_fsp_;
+        std::vector<FinishParams> &fin = h_fin_;
+        std::vector<std::vector<StageParams>> &lists = h_lists_;
+        sp.assign(2 * nc, StepParams());
+        fsp.assign(store_ == STORE_F64 ? 0 : 2 * nc, FastStepParams());
+        fin.assign(2 * nc, FinishParams());
+        lists.assign(max_stages_, std::vector<StageParams>());
         for (int c = 0; c < nc; c++) {
             Solver *s = cases_[c];
             const int cur = s->current(), par = s->parity();
@@ -1289,8 +1334,8 @@ bool Batch::run(int nsteps) {
         okk = okk && check_cuda(cudaMemcpyAsync(d_fin_, fin.data(), fin.size() * sizeof(FinishParams), cudaMemcpyHostToDevice, stream_), "H2D");
         for (int k = 0; k < max_stages_ && okk; k++)
             okk = check_cuda(cudaMemcpyAsync(d_stage_lists_[k], lists[k].data(), lists[k].size() * sizeof(StageParams), cudaMemcpyHostToDevice, stream_), "H2D");
-        // Host vectors must outlive the copies.
-        okk = okk && check_cuda(cudaStreamSynchronize(stream_), "sync");
+        if (!params_ev_) okk = okk && check_cuda(cudaEventCreateWithFlags(&params_ev_, cudaEventDisableTiming), "event");
+        okk = okk && check_cuda(cudaEventRecord(params_ev_, stream_), "event");
         int pairs = mid / 2;
         // Tuning takes its trial windows from the step pairs of this run.
         if (okk && tune_mode_ && !tuned_ && pairs >= 1 + 2 * kNTileCand) {

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -14,6 +15,10 @@ namespace lbm {
 void set_error(const std::string &msg);
 const char *last_error();
 bool check_cuda(cudaError_t e, const char *what);
+// Stream-ordered device allocation from the device's default pool (set up to
+// retain freed memory), freed with cudaFreeAsync on the owner's stream.
+bool device_alloc(void **q, size_t bytes, cudaStream_t s);
+void use_retaining_pool();
 
 // One entry of the Boundary list, resolved to a device BC kind.
 struct BCEntry {
@@ -129,6 +134,9 @@ class Solver {
     int hist_cap() const { return hist_cap_; }
     // Where this case's force is reduced from and written to.
     ForceSlot force_slot() const;
+    // Tiles of 2^tws x 2^(8 - tws) threads covering this case for the batched
+    // kernel (cached per shape).
+    const std::vector<int4> &tiles(int tws) const;
     // Impedance wall on Boundary entry `entry` (velocity_bottom_regularized):
     // per node R, m, K (m <= 0: keep the entry's own val2), nf <= 8 DFT
     // frequencies (rad / step), reference density for p' and the rate of its
@@ -202,6 +210,7 @@ class Solver {
     bool needs_old_dst_ = true;
     bool fields_are_moments_ = false;  // stored rho/u/v are the moments of the current populations
     std::vector<uint8_t> link_node_;
+    mutable std::map<int, std::vector<int4>> tile_cache_;
     int *d_seg_slot_ = nullptr;     // per 32-node row segment: force partial slot or -1
     int nlink_segs_ = 0;
     ForceSlot *d_force_slot_ = nullptr;
@@ -269,6 +278,12 @@ class Batch {
     ForceSlot *d_force_ = nullptr;
     cudaGraphExec_t pair_exec_ = nullptr;
     std::vector<void *> allocs_;
+    // host copies of the per-run parameters (kept until their uploads ran)
+    std::vector<StepParams> h_sp_;
+    std::vector<FastStepParams> h_fsp_;
+    std::vector<FinishParams> h_fin_;
+    std::vector<std::vector<StageParams>> h_lists_;
+    cudaEvent_t params_ev_ = nullptr;
 };
 
 // Maps lbc BC function pointers to device kinds (dropin.cpp).

@@ -1,20 +1,23 @@
 // server.cpp -- continuous-batching request loop over the GPU engine.
 //
 // Requests (a case, its initial state and a number of steps) are submitted by
-// any thread into a lock-protected queue. Each scheduling round:
-//   1. admits queued requests in arrival order while the device-memory budget
-//      and the slot limit allow (the state then lives on the device until the
-//      request finishes);
-//   2. advances every active request by one chunk: requests of one storage type
-//      form one Batch (one persistent kernel per step over all their tiles,
-//      graph-captured), the FP32/FP16 and FP64 batches run concurrently on
-//      their own streams; a chunk is the smallest remaining step count of the
-//      batch, capped at the chunk size, so requests join and leave between
-//      chunks;
-//   3. retires finished requests: their fields (and, on request, populations
-//      and impedance spectra) are copied to host memory and their device
-//      memory is freed for the next admissions.
-// Because Solver::run(a) followed by run(b) equals run(a + b) and every case's
+// any thread into a lock-protected queue. Each storage type (FP64, FP32-, FP16-
+// shifted) has its own lane: a thread that repeats rounds of
+//   1. taking queued requests of its storage type in arrival order while the
+//      device-memory budget and the slot limit (over all lanes) allow;
+//   2. launching one chunk for its active requests: they form one Batch (one
+//      persistent kernel per step over all their tiles, graph-captured),
+//      reused from the previous round while the set of requests is the same;
+//      a chunk is the smallest remaining step count of the set, capped at the
+//      chunk size, so requests join and leave between chunks;
+//   3. while that chunk runs on the device, admitting the requests taken in 1
+//      (device setup and state upload on their own streams);
+//   4. waiting for the chunk and retiring finished requests: their fields (and,
+//      on request, populations and impedance spectra) are copied to host memory
+//      and their device memory is returned to the pool (stream-ordered, so no
+//      device-wide synchronization).
+// The lanes' batches run concurrently on their own streams. Because
+// Solver::run(a) followed by run(b) equals run(a + b) and every case's
 // arithmetic is independent of the others in a batch, a request's result is
 // the same alone and in any mix.
 #include <chrono>
@@ -79,17 +82,31 @@ size_t estimate_bytes(const Request &r) {
 
 }  // namespace
 
+// One storage type's share of the server: its active requests and the batch
+// that advances them (rebuilt only when the set of request ids changes).
+struct Lane {
+    int storage = 0;
+    std::vector<Request *> active;
+    std::unique_ptr<Batch> batch;
+    std::vector<int> batch_ids;
+    std::thread worker;
+};
+
 struct lbm_gpu_server {
     std::mutex mu;
     std::map<int, std::unique_ptr<Request>> reqs;
     std::deque<Request *> queue;
-    std::vector<Request *> active;
+    Lane lanes[3];
+    int n_active = 0;  // over all lanes
     size_t budget = 0, in_use = 0;
     int max_active = 64;
     int chunk = 1000;
     int next_id = 1;
     long long lups_done = 0;
     double busy_s = 0;
+    // time spent per phase of the rounds (host wall clock)
+    long long rounds = 0;
+    double t_admit = 0, t_build = 0, t_run = 0, t_retire = 0;
     std::thread worker;
     std::atomic<bool> running{false};
     std::string err;
@@ -163,61 +180,86 @@ static bool retire(Request *r) {
     return okk;
 }
 
-// One scheduling round; returns the number of requests still queued or active.
-static int server_round(lbm_gpu_server *S) {
-    std::vector<Request *> admitted;
-    {
-        std::lock_guard<std::mutex> lk(S->mu);
-        while (!S->queue.empty() && (int)S->active.size() + (int)admitted.size() < S->max_active) {
-            Request *r = S->queue.front();
-            if (S->in_use + r->est_bytes > S->budget && !(S->active.empty() && admitted.empty())) break;
-            S->queue.pop_front();
-            admitted.push_back(r);
-            S->in_use += r->est_bytes;
+// Queued requests of this lane's storage type, in arrival order, while the
+// slot limit and the device-memory budget allow (one request is always let in
+// when nothing at all is active, so a request larger than the budget still
+// runs alone).
+static std::vector<Request *> take_admissions(lbm_gpu_server *S, Lane &L) {
+    std::vector<Request *> out;
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (auto it = S->queue.begin(); it != S->queue.end();) {
+        Request *r = *it;
+        if (r->storage != L.storage) {
+            ++it;
+            continue;
         }
+        if (S->n_active >= S->max_active) break;
+        if (S->in_use + r->est_bytes > S->budget && S->n_active > 0) break;
+        it = S->queue.erase(it);
+        out.push_back(r);
+        S->in_use += r->est_bytes;
+        S->n_active++;
     }
-    for (Request *r : admitted) {
-        const double ta = now_s();
-        const bool okk = admit(S, r);
-        std::lock_guard<std::mutex> lk(S->mu);
-        r->t_admit = ta;
-        if (okk) {
-            r->state = 2;
-            S->active.push_back(r);
-        } else {
-            r->state = 4;
-            r->t_done = now_s();
-            S->in_use -= r->est_bytes;
+    return out;
+}
+
+static void finish_request(lbm_gpu_server *S, Request *r, int st) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    r->t_done = now_s();
+    r->state = st;
+    S->in_use -= r->est_bytes;
+    S->n_active--;
+}
+
+// One round of one lane; returns the number of this lane's requests still
+// active plus the requests queued for any lane.
+static int lane_round(lbm_gpu_server *S, Lane &L) {
+    const std::vector<Request *> taken = take_admissions(S, L);
+    double t_b = 0, t_run0 = now_s();
+    bool launched = false, okk = true;
+    int n = 0;
+    if (!L.active.empty()) {
+        n = S->chunk;
+        std::vector<int> ids;
+        for (Request *r : L.active) {
+            n = std::min(n, r->remaining);
+            ids.push_back(r->id);
         }
-    }
-    if (!S->active.empty()) {
-        const double t0 = now_s();
-        // One batch per storage type, each advanced by its own chunk length.
-        std::vector<std::unique_ptr<Batch>> batches;
-        std::vector<std::vector<Request *>> groups(3);
-        for (Request *r : S->active) groups[r->storage].push_back(r);
-        std::vector<int> steps(3, 0);
-        bool okk = true;
-        for (int g = 0; g < 3; g++) {
-            if (groups[g].empty()) continue;
-            int n = S->chunk;
-            for (Request *r : groups[g]) n = std::min(n, r->remaining);
-            steps[g] = n;
+        if (!L.batch || ids != L.batch_ids) {
+            const double tb = now_s();
             std::vector<Solver *> sv;
-            for (Request *r : groups[g]) sv.push_back(r->solver.get());
-            std::unique_ptr<Batch> b(new Batch(sv));
-            okk = okk && b->ok() && b->run(n);
-            batches.push_back(std::move(b));
+            for (Request *r : L.active) sv.push_back(r->solver.get());
+            L.batch.reset(new Batch(sv));
+            L.batch_ids = ids;
+            t_b = now_s() - tb;
         }
-        for (auto &b : batches) okk = okk && check_cuda(cudaStreamSynchronize(b->stream()), "server");
-        for (int g = 0; g < 3; g++)
-            for (Request *r : groups[g]) {
-                r->remaining -= steps[g];
-                S->lups_done += (long long)r->Nx * r->Ny * steps[g];
-            }
-        batches.clear();
+        okk = L.batch->ok() && L.batch->run(n);
+        launched = true;
+    }
+    // Admissions overlap the chunk on the device.
+    const double t_adm0 = now_s();
+    std::vector<Request *> joined;
+    for (Request *r : taken) {
+        const double ta = now_s();
+        const bool good = admit(S, r);
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            r->t_admit = ta;
+            if (good) r->state = 2;
+        }
+        if (good) joined.push_back(r);
+        else finish_request(S, r, 4);
+    }
+    const double t_adm = now_s() - t_adm0;
+    double t_wait = 0, t_ret = 0;
+    if (launched) {
+        const double tw = now_s();
+        okk = okk && check_cuda(cudaStreamSynchronize(L.batch->stream()), "server");
+        t_wait = now_s() - tw;
+        const double tr = now_s();
         std::vector<Request *> keep;
-        for (Request *r : S->active) {
+        for (Request *r : L.active) {
+            r->remaining -= n;
             int st;
             if (!okk) {
                 r->error = last_error();
@@ -229,16 +271,38 @@ static int server_round(lbm_gpu_server *S) {
                 keep.push_back(r);
                 continue;
             }
-            std::lock_guard<std::mutex> lk(S->mu);
-            r->t_done = now_s();
-            r->state = st;
-            S->in_use -= r->est_bytes;
+            finish_request(S, r, st);
         }
-        S->active.swap(keep);
-        S->busy_s += now_s() - t0;
+        if (okk) {
+            std::lock_guard<std::mutex> lk(S->mu);
+            for (Request *r : L.active) S->lups_done += (long long)r->Nx * r->Ny * n;
+        }
+        if (keep.size() != L.active.size() || !okk) {
+            L.batch.reset();
+            L.batch_ids.clear();
+        }
+        L.active.swap(keep);
+        t_ret = now_s() - tr;
     }
+    L.active.insert(L.active.end(), joined.begin(), joined.end());
     std::lock_guard<std::mutex> lk(S->mu);
-    return (int)(S->queue.size() + S->active.size());
+    if (launched || !taken.empty()) {
+        S->rounds++;
+        S->t_admit += t_adm;
+        S->t_build += t_b;
+        S->t_run += (launched ? (t_adm0 - t_run0 - t_b) : 0.0) + t_wait;
+        S->t_retire += t_ret;
+        S->busy_s += now_s() - t_run0;
+    }
+    return (int)(S->queue.size() + L.active.size());
+}
+
+// One round of every lane (the caller's thread).
+static int server_round(lbm_gpu_server *S) {
+    int left = 0;
+    for (Lane &L : S->lanes) left = std::max(left, lane_round(S, L));
+    std::lock_guard<std::mutex> lk(S->mu);
+    return (int)S->queue.size() + S->n_active;
 }
 
 extern "C" {
@@ -260,6 +324,9 @@ int lbm_gpu_server_create(size_t budget_bytes, int max_active, int chunk_steps, 
     S->budget = budget_bytes;
     S->max_active = max_active;
     S->chunk = chunk_steps;
+    S->lanes[0].storage = LBM_GPU_F64;
+    S->lanes[1].storage = LBM_GPU_F32_SHIFTED;
+    S->lanes[2].storage = LBM_GPU_F16_SHIFTED;
     *out = S;
     return LBM_GPU_OK;
 }
@@ -357,19 +424,27 @@ int lbm_gpu_server_poll(lbm_gpu_server *S) {
 int lbm_gpu_server_start(lbm_gpu_server *S) {
     if (!S || S->running) return LBM_GPU_ERR_ARG;
     S->running = true;
-    S->worker = std::thread([S] {
-        while (S->running) {
-            const int left = server_round(S);
-            if (left == 0) std::this_thread::sleep_for(std::chrono::microseconds(200));
-        }
-    });
+    int dev = 0;
+    cudaGetDevice(&dev);
+    for (Lane &L : S->lanes) {
+        Lane *pl = &L;
+        L.worker = std::thread([S, pl, dev] {
+            cudaSetDevice(dev);
+            while (S->running) {
+                const bool busy = !pl->active.empty();
+                lane_round(S, *pl);
+                if (!busy && pl->active.empty()) std::this_thread::sleep_for(std::chrono::microseconds(200));
+            }
+        });
+    }
     return LBM_GPU_OK;
 }
 
 int lbm_gpu_server_stop(lbm_gpu_server *S) {
     if (!S) return LBM_GPU_ERR_ARG;
     S->running = false;
-    if (S->worker.joinable()) S->worker.join();
+    for (Lane &L : S->lanes)
+        if (L.worker.joinable()) L.worker.join();
     return LBM_GPU_OK;
 }
 
@@ -429,15 +504,29 @@ int lbm_gpu_server_stats(lbm_gpu_server *S, long long *lups_done, double *busy_s
     if (lups_done) *lups_done = S->lups_done;
     if (busy_s) *busy_s = S->busy_s;
     if (queued) *queued = (int)S->queue.size();
-    if (active) *active = (int)S->active.size();
+    if (active) *active = S->n_active;
     if (bytes_in_use) *bytes_in_use = S->in_use;
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_server_profile(lbm_gpu_server *S, double *out, int n) {
+    if (!S || !out || n < 1) {
+        set_error("bad arguments");
+        return LBM_GPU_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    const double v[5] = {(double)S->rounds, S->t_admit, S->t_build, S->t_run, S->t_retire};
+    for (int q = 0; q < n && q < 5; q++) out[q] = v[q];
     return LBM_GPU_OK;
 }
 
 int lbm_gpu_server_destroy(lbm_gpu_server *S) {
     if (!S) return LBM_GPU_OK;
     lbm_gpu_server_stop(S);
-    for (Request *r : S->active) r->solver.reset();
+    for (Lane &L : S->lanes) {
+        L.batch.reset();
+        for (Request *r : L.active) r->solver.reset();
+    }
     delete S;
     return LBM_GPU_OK;
 }

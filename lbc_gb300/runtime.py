@@ -113,6 +113,7 @@ def _bind_ext(lib: C.CDLL) -> None:
         "lbm_gpu_server_release": (C.c_int, [vp, C.c_int]),
         "lbm_gpu_server_stats": (C.c_int, [vp, C.POINTER(C.c_longlong), dp, C.POINTER(C.c_int),
                                            C.POINTER(C.c_int), C.POINTER(C.c_size_t)]),
+        "lbm_gpu_server_profile": (C.c_int, [vp, dp, C.c_int]),
         "lbm_gpu_server_destroy": (C.c_int, [vp]),
         "lbm_gpu_compute_force_mem_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_int, C.c_int,
                                                         C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -431,6 +432,12 @@ class GpuServer:
         _check(self.lib.lbm_gpu_server_stats(self.h, C.byref(l), C.byref(b), C.byref(q), C.byref(a), C.byref(m)),
                "lbm_gpu_server_stats")
         return {"lups": l.value, "busy_s": b.value, "queued": q.value, "active": a.value, "bytes": m.value}
+
+    def profile(self):
+        """Host seconds per phase of the scheduling rounds (lbm_gpu_server_profile)."""
+        out = np.zeros(5)
+        _check(self.lib.lbm_gpu_server_profile(self.h, dptr(out), 5), "lbm_gpu_server_profile")
+        return {"rounds": int(out[0]), "admit_s": out[1], "build_s": out[2], "run_s": out[3], "retire_s": out[4]}
 
     def close(self):
         if getattr(self, "h", None):

@@ -124,12 +124,14 @@ def serve(stream: List[Req], max_active: int = 64, chunk: int = 1000, budget_byt
     makespan = time.perf_counter() - t0
     srv.stop()
     stats = srv.stats()
+    prof = srv.profile()
     srv.close()
     lups = sum(r.nx * r.ny * r.steps for r in stream)
     lats = np.array([lat[i] for i in ids])
     return {"requests": len(stream), "failed": len(failed), "lups": lups, "makespan_s": makespan,
             "mlups": lups / makespan / 1e6, "p50_s": float(np.percentile(lats, 50)),
             "p99_s": float(np.percentile(lats, 99)), "busy_s": stats["busy_s"],
+            "phases": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in prof.items()},
             "latencies_s": lats.tolist()}
 
 

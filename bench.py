@@ -307,6 +307,7 @@ def run_ours(a, ws, rank, pg):
         mlups = lups_all / span / 1e6
         ser_mlups = lups_all / ser_s / 1e6
         serve_res = {"requests": len(stream), "failed": failed, "mlups": round(mlups, 1),
+                     "host_phases_s": r["phases"],
                      "p50_s": round(float(np.percentile(lats, 50)), 3),
                      "p99_s": round(float(np.percentile(lats, 99)), 3),
                      "makespan_s": round(span, 2),

@@ -213,7 +213,9 @@ int lbm_gpu_server_stats(lbm_gpu_server *srv, long long *lups_done, double *busy
 /* Host time per phase of the scheduling rounds so far: out[0] rounds, [1]
  * admission (solver setup and state upload), [2] batch construction, [3]
  * launching and waiting for the chunks, [4] retiring (results to host, device
- * memory freed), seconds. Writes min(n, 5) values. */
+ * memory freed), [5..7] wall time of the FP64, FP32 and FP16 lanes' rounds
+ * that ran a chunk; seconds (phases summed over lanes). Writes min(n, 8)
+ * values. */
 int lbm_gpu_server_profile(lbm_gpu_server *srv, double *out, int n);
 int lbm_gpu_server_destroy(lbm_gpu_server *srv);
 

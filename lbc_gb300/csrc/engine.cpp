@@ -1048,7 +1048,14 @@ Batch::Batch(const std::vector<Solver *> &cases) : cases_(cases) {
             return;
         }
     }
-    if (!check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate")) return;
+    // FP64 batches (FP64-issue bound, long) run at the lowest stream priority,
+    // shifted-storage batches at the highest, so that when both run at once
+    // (the server's lanes) free SMs go to the short, memory-bound FP32 steps.
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (!check_cuda(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking, store_ == STORE_F64 ? lo : hi),
+                    "cudaStreamCreateWithPriority"))
+        return;
     ok_ = build();
     if (ok_) set_autotune(tune_default_mode());
 }

@@ -86,6 +86,7 @@ size_t estimate_bytes(const Request &r) {
 // that advances them (rebuilt only when the set of request ids changes).
 struct Lane {
     int storage = 0;
+    double busy_s = 0;  // wall time of this lane's rounds that ran a chunk
     std::vector<Request *> active;
     std::unique_ptr<Batch> batch;
     std::vector<int> batch_ids;
@@ -293,6 +294,7 @@ static int lane_round(lbm_gpu_server *S, Lane &L) {
         S->t_run += (launched ? (t_adm0 - t_run0 - t_b) : 0.0) + t_wait;
         S->t_retire += t_ret;
         S->busy_s += now_s() - t_run0;
+        if (launched) L.busy_s += now_s() - t_run0;
     }
     return (int)(S->queue.size() + L.active.size());
 }
@@ -515,8 +517,9 @@ int lbm_gpu_server_profile(lbm_gpu_server *S, double *out, int n) {
         return LBM_GPU_ERR_ARG;
     }
     std::lock_guard<std::mutex> lk(S->mu);
-    const double v[5] = {(double)S->rounds, S->t_admit, S->t_build, S->t_run, S->t_retire};
-    for (int q = 0; q < n && q < 5; q++) out[q] = v[q];
+    const double v[8] = {(double)S->rounds, S->t_admit, S->t_build, S->t_run, S->t_retire,
+                         S->lanes[0].busy_s, S->lanes[1].busy_s, S->lanes[2].busy_s};
+    for (int q = 0; q < n && q < 8; q++) out[q] = v[q];
     return LBM_GPU_OK;
 }
 

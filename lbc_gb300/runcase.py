@@ -39,12 +39,21 @@ def main(argv=None):
     p.add_argument("--rate", type=float, default=200.0, help="arrival rate of the served stream (1/s)")
     p.add_argument("--max-active", type=int, default=64)
     p.add_argument("--chunk", type=int, default=1000)
+    p.add_argument("--wake", type=int, default=0,
+                   help="cylinder wake (2048 x 512, Re 100): Cd, Cl, St after this many steps")
     p.add_argument("--autotune", action="store_true",
                    help="tune block / tile shapes on the warm-up steps (LBM_GPU_AUTOTUNE=1)")
     a = p.parse_args(argv)
     if a.autotune:
         os.environ["LBM_GPU_AUTOTUNE"] = "1"
         a.warmup = max(a.warmup, 80)
+    if a.wake:
+        from lbc_gb300 import wake
+        h = wake.cylinder_forces(STORAGE[a.storage], a.wake)
+        r = wake.summary(h)
+        r.update({"storage": a.storage, "steps": a.wake})
+        print(json.dumps(r))
+        return
     if a.serve:
         from lbc_gb300 import serving
         stream = serving.make_stream(a.serve, rate=a.rate, scale=a.scale)

@@ -435,9 +435,10 @@ class GpuServer:
 
     def profile(self):
         """Host seconds per phase of the scheduling rounds (lbm_gpu_server_profile)."""
-        out = np.zeros(5)
-        _check(self.lib.lbm_gpu_server_profile(self.h, dptr(out), 5), "lbm_gpu_server_profile")
-        return {"rounds": int(out[0]), "admit_s": out[1], "build_s": out[2], "run_s": out[3], "retire_s": out[4]}
+        out = np.zeros(8)
+        _check(self.lib.lbm_gpu_server_profile(self.h, dptr(out), 8), "lbm_gpu_server_profile")
+        return {"rounds": int(out[0]), "admit_s": out[1], "build_s": out[2], "run_s": out[3], "retire_s": out[4],
+                "lane_f64_s": out[5], "lane_f32_s": out[6], "lane_f16_s": out[7]}
 
     def close(self):
         if getattr(self, "h", None):

@@ -25,6 +25,7 @@ extern "C" {
 #define LBM_GPU_ERR_ARG (-1)
 #define LBM_GPU_ERR_CUDA (-2)
 #define LBM_GPU_ERR_NOMEM (-3)
+#define LBM_GPU_ERR_IO (-4)
 
 /* Population storage. F64: lbc's arithmetic, bit for bit. F32/F16_SHIFTED:
  * populations stored as f_k - w_k in FP32 / FP16, collision in FP32. */
@@ -88,7 +89,27 @@ int lbm_gpu_set_bc_values(lbm_gpu_solver *s, int entry, const double *val1, cons
 int lbm_gpu_run(lbm_gpu_solver *s, int nsteps);
 /* Same as lbm_gpu_run, timed with CUDA events on the solver's stream. */
 int lbm_gpu_run_timed(lbm_gpu_solver *s, int nsteps, double *ms);
+/* Waits for the solver's device work and for a pending lbm_gpu_write_vtk. */
 int lbm_gpu_sync(lbm_gpu_solver *s);
+
+/* ---- Checkpoint / restart (no counterpart in lbc). Save writes everything a
+ * continued run reads: both population buffers as stored, rho/u/v, the edge
+ * band's moments, each Boundary entry's values and impedance-wall state, the
+ * last force and the force history. Load needs a solver created from the same
+ * case, with the same impedance walls set up and the same force-history
+ * capacity; save after lbm_gpu_run(a), load, lbm_gpu_run(b) then equals
+ * lbm_gpu_run(a + b) bit for bit. The file is raw host-order binary for this
+ * library (a header, then length-prefixed blocks). LBM_GPU_ERR_IO on a file or
+ * mismatch error (lbm_gpu_last_error says which). */
+int lbm_gpu_checkpoint_save(lbm_gpu_solver *s, const char *path);
+int lbm_gpu_checkpoint_load(lbm_gpu_solver *s, const char *path);
+
+/* ---- VTK output packed on the device: the bytes lbc's write_vtk_binary_2D
+ * writes for the stored fields (rho, u, v after the last run), the FP32
+ * big-endian payload packed by a kernel, copied to pinned memory and written
+ * by a host thread while the solver keeps stepping. The file is complete after
+ * lbm_gpu_sync, the next lbm_gpu_write_vtk or lbm_gpu_destroy. */
+int lbm_gpu_write_vtk(lbm_gpu_solver *s, const char *filename, double dx, double cu, double crho);
 
 /* Momentum-exchange force of the last step: *D = x, *L = y (as main_lbm). */
 int lbm_gpu_forces(lbm_gpu_solver *s, double *L, double *D);

@@ -28,6 +28,7 @@ UNITS = [
     ("dropin.cpp", ["-O2"]),
     ("server.cpp", ["-O2"]),
     ("tune.cpp", ["-O2"]),
+    ("io.cu", ["-O3", "-lineinfo"] + ARCH),
     ("noalloc.cu", ["-O3", "-lineinfo", "--fmad=false"] + ARCH),
 ]
 
@@ -68,7 +69,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(lambda u: _compile(*u), UNITS))
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared", "-cudart", "static"] + ARCH + objs + ["-o", tmp, "-ldl", "-lpthread"]
+    cmd = [nvcc(), "-shared", "-cudart", "static"] + ARCH + objs + ["-o", tmp, "-ldl", "-lpthread",
+                                                                    "-Xlinker", "--no-undefined"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stderr)

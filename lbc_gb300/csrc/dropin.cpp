@@ -675,7 +675,23 @@ int lbm_gpu_run_timed(lbm_gpu_solver *s, int nsteps, double *ms) {
 
 int lbm_gpu_sync(lbm_gpu_solver *s) {
     SOLVER_OR_FAIL(s);
-    return check_cuda(cudaStreamSynchronize(s->s->stream()), "sync") ? LBM_GPU_OK : LBM_GPU_ERR_CUDA;
+    if (!check_cuda(cudaStreamSynchronize(s->s->stream()), "sync")) return LBM_GPU_ERR_CUDA;
+    return s->s->vtk_wait() ? LBM_GPU_OK : LBM_GPU_ERR_IO;
+}
+
+int lbm_gpu_checkpoint_save(lbm_gpu_solver *s, const char *path) {
+    SOLVER_OR_FAIL(s);
+    return s->s->checkpoint_save(path) ? LBM_GPU_OK : LBM_GPU_ERR_IO;
+}
+
+int lbm_gpu_checkpoint_load(lbm_gpu_solver *s, const char *path) {
+    SOLVER_OR_FAIL(s);
+    return s->s->checkpoint_load(path) ? LBM_GPU_OK : LBM_GPU_ERR_IO;
+}
+
+int lbm_gpu_write_vtk(lbm_gpu_solver *s, const char *filename, double dx, double cu, double crho) {
+    SOLVER_OR_FAIL(s);
+    return s->s->write_vtk(filename, dx, cu, crho) ? LBM_GPU_OK : LBM_GPU_ERR_IO;
 }
 
 int lbm_gpu_forces(lbm_gpu_solver *s, double *L, double *D) {

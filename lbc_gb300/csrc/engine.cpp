@@ -90,6 +90,9 @@ Solver::Solver(const CaseDesc &d) : d_(d) {
 }
 
 Solver::~Solver() {
+    vtk_wait();
+    if (vtk_ev_) cudaEventDestroy(vtk_ev_);
+    if (h_vtk_) cudaFreeHost(h_vtk_);
     if (pair_exec_) cudaGraphExecDestroy(pair_exec_);
     for (void *p : allocs_) cudaFreeAsync(p, stream_);
     if (stream_) cudaStreamDestroy(stream_);

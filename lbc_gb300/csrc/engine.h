@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "kernels.h"
@@ -145,6 +146,17 @@ class Solver {
                        const double *omegas, double rho_ref, double alpha, int window);
     // out[((t * nf) + f) * 4 + {0,1,2,3}] = (P re, P im, V re, V im); state[t*2+{0,1}] = (x, v)
     bool impedance_readback(int entry, double *out, double *state);
+    // Population checkpoint (io.cpp): everything a continued run reads, so
+    // that save after run(a), load into a solver of the same case (with the
+    // same impedance-wall setup and force-history capacity) and run(b) equal
+    // run(a + b) bit for bit.
+    bool checkpoint_save(const char *path);
+    bool checkpoint_load(const char *path);
+    // Device-packed VTK of the stored fields (io.cpp): lbc's
+    // write_vtk_binary_2D bytes, packed on the device and written by a host
+    // thread while the solver keeps stepping; finished by vtk_wait().
+    bool write_vtk(const char *path, double dx, double cu, double crho);
+    bool vtk_wait();
     bool begin_steps(cudaStream_t s);
     bool end_steps(cudaStream_t s);
     void advance(int nsteps);
@@ -211,6 +223,13 @@ class Solver {
     bool fields_are_moments_ = false;  // stored rho/u/v are the moments of the current populations
     std::vector<uint8_t> link_node_;
     mutable std::map<int, std::vector<int4>> tile_cache_;
+    // VTK packing: device staging, pinned host copy, the writer thread
+    unsigned char *d_vtk_ = nullptr, *h_vtk_ = nullptr;
+    size_t vtk_bytes_ = 0;
+    cudaEvent_t vtk_ev_ = nullptr;
+    std::thread *vtk_thread_ = nullptr;
+    bool vtk_ok_ = true;
+    std::string vtk_err_;
     int *d_seg_slot_ = nullptr;     // per 32-node row segment: force partial slot or -1
     int nlink_segs_ = 0;
     ForceSlot *d_force_slot_ = nullptr;

@@ -83,6 +83,9 @@ def _bind_ext(lib: C.CDLL) -> None:
         "lbm_gpu_get_info": (C.c_int, [vp, C.POINTER(Info)]),
         "lbm_gpu_set_block": (C.c_int, [vp, C.c_int, C.c_int]),
         "lbm_gpu_get_block": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "lbm_gpu_checkpoint_save": (C.c_int, [vp, C.c_char_p]),
+        "lbm_gpu_checkpoint_load": (C.c_int, [vp, C.c_char_p]),
+        "lbm_gpu_write_vtk": (C.c_int, [vp, C.c_char_p, C.c_double, C.c_double, C.c_double]),
         "lbm_gpu_set_autotune": (C.c_int, [vp, C.c_int]),
         "lbm_gpu_autotune_status": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                               C.POINTER(C.c_double)]),
@@ -309,6 +312,17 @@ class GpuSolver:
         bx, by = C.c_int(), C.c_int()
         _check(self.lib.lbm_gpu_get_block(self.h, C.byref(bx), C.byref(by)), "lbm_gpu_get_block")
         return bx.value, by.value
+
+    def checkpoint_save(self, path: str):
+        _check(self.lib.lbm_gpu_checkpoint_save(self.h, os.fsencode(path)), "lbm_gpu_checkpoint_save")
+
+    def checkpoint_load(self, path: str):
+        _check(self.lib.lbm_gpu_checkpoint_load(self.h, os.fsencode(path)), "lbm_gpu_checkpoint_load")
+
+    def write_vtk(self, path: str, dx: float = 1.0, cu: float = 1.0, crho: float = 1.0):
+        """lbc's VTK file of the stored fields, packed on the device; complete
+        after sync()."""
+        _check(self.lib.lbm_gpu_write_vtk(self.h, os.fsencode(path), dx, cu, crho), "lbm_gpu_write_vtk")
 
     def set_autotune(self, mode: int = 1):
         """Tune the fused step's block shape on the next long enough run."""

@@ -6,7 +6,9 @@ final state and the per-step force of each run, and copies the first records
 of lbc's shipped cylinder force history
 (cases/cylinder/sol/forces_IBB_res_20_Re_20.00_tau_0.90.bin).
 
-    python tests/golden/make_golden.py [LBC_SOURCE_DIR]
+    python tests/golden/make_golden.py [LBC_SOURCE_DIR] [--vtk-only]
+
+It also writes lbc_small.vtk: lbc's write_vtk_binary_2D on a small seeded field.
 """
 import ctypes as C
 import os
@@ -24,10 +26,41 @@ from lbc_gb300.abi import LbcAbi  # noqa: E402
 import casezoo  # noqa: E402
 
 
+VTK_ARGS = (7, 5, 0.5, 2.0, 3.0)  # Nx, Ny, dx, cu, crho
+
+
+def vtk_inputs():
+    rng = np.random.default_rng(7)
+    Nx, Ny = VTK_ARGS[:2]
+    u = rng.uniform(-0.1, 0.1, (Ny, Nx))
+    v = rng.uniform(-0.1, 0.1, (Ny, Nx))
+    rho = 1.0 + rng.uniform(-0.01, 0.01, (Ny, Nx))
+    u[2, 3] = np.nan  # lbc's moments are NaN at solid nodes
+    return u, v, rho
+
+
+def write_vtk_fixture(lib):
+    """lbc's write_vtk_binary_2D on a small seeded field -> lbc_small.vtk."""
+    Nx, Ny, dx, cu, crho = VTK_ARGS
+    u, v, rho = vtk_inputs()
+    fn = lib.ref_write_vtk_binary_2D
+    dp = C.POINTER(C.c_double)
+    fn.restype = None
+    fn.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_double, dp, dp, dp, C.c_double, C.c_double]
+    out = os.path.join(HERE, "lbc_small.vtk")
+    fn(out.encode(), Nx, Ny, dx, u.ctypes.data_as(dp), v.ctypes.data_as(dp), rho.ctypes.data_as(dp), cu, crho)
+    print("wrote", out)
+
+
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LBC_REF", "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    src = args[0] if args else os.environ.get("LBC_REF", "/root/reference")
     subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), src], check=True)
-    ref = LbcAbi(C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libref_lbc.so")), "ref_")
+    lib = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libref_lbc.so"))
+    write_vtk_fixture(lib)
+    if "--vtk-only" in sys.argv:
+        return
+    ref = LbcAbi(lib, "ref_")
     for name, builder, steps in casezoo.standard_cases():
         case, st = builder()
         forces = ref.run(case, st, steps, record_forces=True)

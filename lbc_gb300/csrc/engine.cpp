@@ -1221,6 +1221,7 @@ bool Batch::build() {
         Solver *s = cases_[c];
         nodes_ += (long long)s->Nx() * s->Ny();
         if (9LL * s->plane() >= (1LL << 31)) wide_ = true;
+        if (s->has_force()) any_force_ = true;
         if (s->has_mem()) force.push_back(s->force_slot());
         for (const int2 &w : s->wnodes()) fin_nodes.push_back(make_int4(c, w.x, w.y, 0));
         max_stages_ = std::max(max_stages_, (int)s->stage_groups().size());
@@ -1266,7 +1267,7 @@ bool Batch::launch_batched(int sel) {
                                     grid_, stream_));
     else
         CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
-                                      store_, wide_, grid_, stream_));
+                                      store_, wide_, any_force_, grid_, stream_));
     for (int s = 0; s < max_stages_; s++)
         CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], max_along_, store_, sel, stream_));
     if (nfin_) {

@@ -126,6 +126,7 @@ class Solver {
     const std::vector<std::vector<int>> &stage_groups() const { return groups_; }
     const std::vector<int2> &wnodes() const { return wnodes_host_; }
     bool has_mem() const { return has_mem_; }
+    bool has_force() const { return d_.Fx != 0.0 || d_.Fy != 0.0; }
     // 1 for fluid nodes with at least one solid pull source (wall link), [Ny][Nx].
     const std::vector<uint8_t> &link_nodes() const { return link_node_; }
     int parity() const { return parity_; }
@@ -286,6 +287,7 @@ class Batch {
     int ntiles_ = 0, grid_ = 0, max_stages_ = 0, max_along_ = 0, nfin_ = 0, nforce_ = 0;
     int tws_ = 6;
     bool wide_ = false;  // some case needs 64-bit element offsets
+    bool any_force_ = false;  // some case has a body force
     int launches_per_step_ = 0;
     void *d_sp_ = nullptr;         // StepParams or FastStepParams [2 * ncases]
     int *d_phase_ = nullptr;       // [ncases] (and stage entries)

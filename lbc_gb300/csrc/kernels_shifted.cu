@@ -68,14 +68,14 @@ __device__ __forceinline__ void shifted_h(float w1, float &h1, float &h5) {
 }
 
 // Shifted moments: delta rho = sum g, j = sum c g (sum c w = 0). Jx, Jy are the
-// momentum including half the body force (rho u of lbc).
+// momentum including half the body force (rho u of lbc); jx, jy without it.
 template <class V>
 __device__ __forceinline__ void moments_v(const V g[9], V hFx, V hFy, V &dr, V &rho, V &ux, V &uy, V &Jx,
-                                          V &Jy) {
+                                          V &Jy, V &jx, V &jy) {
     dr = v_add(v_add(v_add(v_add(g[0], g[1]), v_add(g[2], g[3])), v_add(v_add(g[4], g[5]), v_add(g[6], g[7]))),
                g[8]);
-    const V jx = v_add(v_add(v_sub(g[1], g[3]), v_sub(g[5], g[6])), v_sub(g[8], g[7]));
-    const V jy = v_sub(v_add(v_sub(g[2], g[4]), v_add(g[5], g[6])), v_add(g[7], g[8]));
+    jx = v_add(v_add(v_sub(g[1], g[3]), v_sub(g[5], g[6])), v_sub(g[8], g[7]));
+    jy = v_sub(v_add(v_sub(g[2], g[4]), v_add(g[5], g[6])), v_add(g[7], g[8]));
     rho = v_floor_rho(v_add(v_splat<V>(1.0f), dr));
     const V inv = v_rcp(rho);
     Jx = v_add(jx, hFx);
@@ -85,14 +85,16 @@ __device__ __forceinline__ void moments_v(const V g[9], V hFx, V hFy, V &dr, V &
 }
 
 // One pair of directions (k, opposite) of the equilibrium: X = w (dr + 4.5 J c
-// - rt) is the even part, h J the odd part, added to X with one rounding
-// (X +- h J as FMAs: rounding h J first doubles the FP32 velocity error of a
-// Taylor-Green run against FP64).
+// - rt) is the even part, h o the odd part, added to X with one rounding
+// (X +- h o as FMAs: rounding h o first doubles the FP32 velocity error of a
+// Taylor-Green run against FP64). The odd part takes the momentum without
+// the half force, o = c.j; the force enters the odd part separately (see
+// collide_v).
 template <class V>
-__device__ __forceinline__ void geq_pair(float w, float h, V dr, V c, V J, V nrt, V &a, V &b) {
+__device__ __forceinline__ void geq_pair(float w, float h, V dr, V c, V J, V o, V nrt, V &a, V &b) {
     const V X = v_mul(v_splat<V>(w), v_add(dr, v_fma(v_mul(v_splat<V>(4.5f), J), c, nrt)));
-    a = v_fma(v_splat<V>(h), J, X);
-    b = v_fma(v_splat<V>(-h), J, X);
+    a = v_fma(v_splat<V>(h), o, X);
+    b = v_fma(v_splat<V>(-h), o, X);
 }
 
 // BGK + Guo on shifted populations, g' = g + om (geq - g) + (1 - om/2) F_k,
@@ -103,46 +105,65 @@ __device__ __forceinline__ void geq_pair(float w, float h, V dr, V c, V J, V nrt
 // term uses J = rho u directly (no division), and the rest population closes
 // the mass. Rounded weights would otherwise bias every collision's momentum by
 // ~1e-8 in the same direction, an error that grows linearly with the steps.
-// The Guo term is evaluated per direction pair: with S = 9 (c.u)(c.F) - 3 u.F
-// and A = 3 c.F, F_k = w (S + A) and F_opp = w (S - A).
-template <class V>
+//
+// With a body force, J = j + F/2 would round F/2 (~1e-7) against j: an error of
+// the same sign every step, which drove a forced channel 6.6e-5 away from FP64
+// in 20,000 steps. Instead the odd part relaxes towards h (c.j) and the whole
+// odd forcing, om h c.F/2 + (1 - om/2) 3 w c.F = h c.F (h = 3 w), is added as
+// one small term; the even forcing is (1 - om/2) w S, S = 9 (c.u)(c.F) - 3 u.F.
+// The relaxation and the forcing are summed first (one FMA) and added to g with
+// a single rounding. Channel 256 x 64 against FP64 after 20,000 steps: u L2
+// error 5.0e-7 (6.6e-5 before).
+template <class V, bool FORCE>
 __device__ __forceinline__ void collide_v(V g[9], const float w[9], float h1, float h5, V dr, V ux, V uy,
-                                          V Jx, V Jy, V om, bool force, float Fx, float Fy) {
+                                          V Jx, V Jy, V jx, V jy, V om, bool force, float Fx, float Fy) {
     const V nrt = v_mul(v_splat<V>(-1.5f), v_fma(Jx, ux, v_mul(Jy, uy)));  // -rho * 1.5 u.u
+    // Without a body force j = J exactly: one set of momenta stays live.
+    const bool forced = FORCE && force;
+    if (!FORCE) {
+        jx = Jx;
+        jy = Jy;
+    }
     V geq[9];
-    geq_pair(w[1], h1, dr, ux, Jx, nrt, geq[1], geq[3]);
-    geq_pair(w[2], h1, dr, uy, Jy, nrt, geq[2], geq[4]);
-    geq_pair(w[5], h5, dr, v_add(ux, uy), v_add(Jx, Jy), nrt, geq[5], geq[7]);
-    geq_pair(w[6], h5, dr, v_sub(uy, ux), v_sub(Jy, Jx), nrt, geq[6], geq[8]);
+    geq_pair(w[1], h1, dr, ux, Jx, jx, nrt, geq[1], geq[3]);
+    geq_pair(w[2], h1, dr, uy, Jy, jy, nrt, geq[2], geq[4]);
+    geq_pair(w[5], h5, dr, v_add(ux, uy), v_add(Jx, Jy), v_add(jx, jy), nrt, geq[5], geq[7]);
+    geq_pair(w[6], h5, dr, v_sub(uy, ux), v_sub(Jy, Jx), v_sub(jy, jx), nrt, geq[6], geq[8]);
     geq[0] = v_sub(dr, v_add(v_add(v_add(geq[1], geq[3]), v_add(geq[2], geq[4])),
                              v_add(v_add(geq[5], geq[7]), v_add(geq[6], geq[8]))));
+    if (!forced) {
+        // A force-free case: one FMA per population. Kernels that may see
+        // forced cases (FORCE) take this branch per case at run time, so a
+        // case gets the same bits alone and in any batch.
 #pragma unroll
-    for (int k = 0; k < 9; k++) g[k] = v_fma(om, v_sub(geq[k], g[k]), g[k]);
-    if (force) {
-        const V Fxv = v_splat<V>(Fx), Fyv = v_splat<V>(Fy);
-        const V gf = v_fma(v_splat<V>(-0.5f), om, v_splat<V>(1.0f));
-        const V n3uF = v_mul(v_splat<V>(-3.0f), v_fma(ux, Fxv, v_mul(uy, Fyv)));  // -3 u.F
-        g[0] = v_fma(gf, v_mul(v_splat<V>(w[0]), n3uF), g[0]);
-        // (k, opp, c.u, c.F) for the four pairs
-        const V cu[4] = {ux, uy, v_add(ux, uy), v_sub(uy, ux)};
-        const V cF[4] = {Fxv, Fyv, v_splat<V>(Fx + Fy), v_splat<V>(Fy - Fx)};
-        const int ka[4] = {1, 2, 5, 6}, kb[4] = {3, 4, 7, 8};
+        for (int k = 0; k < 9; k++) g[k] = v_fma(om, v_sub(geq[k], g[k]), g[k]);
+        return;
+    }
+    const V Fxv = v_splat<V>(Fx), Fyv = v_splat<V>(Fy);
+    const V gf = v_fma(v_splat<V>(-0.5f), om, v_splat<V>(1.0f));
+    const V n3uF = v_mul(v_splat<V>(-3.0f), v_fma(ux, Fxv, v_mul(uy, Fyv)));  // -3 u.F
+    g[0] = v_add(g[0], v_fma(om, v_sub(geq[0], g[0]), v_mul(gf, v_mul(v_splat<V>(w[0]), n3uF))));
+    const V cu[4] = {ux, uy, v_add(ux, uy), v_sub(uy, ux)};
+    const float cFs[4] = {Fx, Fy, Fx + Fy, Fy - Fx};
+    const float hs[4] = {h1, h1, h5, h5};
+    const int ka[4] = {1, 2, 5, 6}, kb[4] = {3, 4, 7, 8};
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const V S = v_fma(v_mul(v_splat<V>(9.0f), cu[q]), cF[q], n3uF);
-            const V A = v_mul(v_splat<V>(3.0f), cF[q]);
-            const V wv = v_splat<V>(w[ka[q]]);
-            g[ka[q]] = v_fma(gf, v_mul(wv, v_add(S, A)), g[ka[q]]);
-            g[kb[q]] = v_fma(gf, v_mul(wv, v_sub(S, A)), g[kb[q]]);
-        }
+    for (int q = 0; q < 4; q++) {
+        const V cF = v_splat<V>(cFs[q]);
+        const V S = v_fma(v_mul(v_splat<V>(9.0f), cu[q]), cF, n3uF);
+        const V E = v_mul(gf, v_mul(v_splat<V>(w[ka[q]]), S));
+        const V O = v_splat<V>(hs[q] * cFs[q]);
+        const int a = ka[q], b = kb[q];
+        g[a] = v_add(g[a], v_fma(om, v_sub(geq[a], g[a]), v_add(E, O)));
+        g[b] = v_add(g[b], v_fma(om, v_sub(geq[b], g[b]), v_sub(E, O)));
     }
 }
 
 // Scalar entry points used by the per-node paths.
 __device__ __forceinline__ void moments_shifted(const float g[9], float hFx, float hFy, float &dr,
                                                 float &rho, float &ux, float &uy, float &Jx,
-                                                float &Jy) {
-    moments_v<float>(g, hFx, hFy, dr, rho, ux, uy, Jx, Jy);
+                                                float &Jy, float &jx, float &jy) {
+    moments_v<float>(g, hFx, hFy, dr, rho, ux, uy, Jx, Jy, jx, jy);
 }
 
 // Rare per-node outputs, kept out of line so the compiler cannot hoist their
@@ -192,7 +213,7 @@ __device__ __noinline__ float2 omega_pair(const double *omega, size_t dn) {
 // stale slots, edge-BC band: everything). I is the element-offset type: int
 // whenever all nine planes fit in 2^31 elements (fewer address instructions),
 // long long otherwise.
-template <typename T, typename I, bool FLAGS, bool COLLIDE>
+template <typename T, typename I, bool FLAGS, bool COLLIDE, bool FORCE>
 __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int i, int j,
                                                   float &mfx, float &mfy, bool &link) {
     const StepParams &p = fp.s;
@@ -257,12 +278,13 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
         for (int k = 0; k < 9; k++) p.bandg[(size_t)k * p.nslots + slot] = g[k];
     }
     if (FLAGS && (fl & NF_BCW)) return;
-    float dr, rho, ux, uy, Jx, Jy;
-    moments_v<float>(g, fp.hFxf, fp.hFyf, dr, rho, ux, uy, Jx, Jy);
+    float dr, rho, ux, uy, Jx, Jy, jx, jy;
+    moments_v<float>(g, fp.hFxf, fp.hFyf, dr, rho, ux, uy, Jx, Jy, jx, jy);
     if (p.write_macro || slot >= 0) macro_store(p, dn, slot, dr, ux, uy);
     if (COLLIDE) {
         const float om = p.omega ? (float)p.omega[dn] : fp.omega0f;
-        collide_v<float>(g, fp.wf, fp.h1f, fp.h5f, dr, ux, uy, Jx, Jy, om, p.has_force != 0, fp.Fxf, fp.Fyf);
+        collide_v<float, FORCE>(g, fp.wf, fp.h1f, fp.h5f, dr, ux, uy, Jx, Jy, jx, jy, om, p.has_force != 0,
+                                fp.Fxf, fp.Fyf);
     }
 #pragma unroll
     for (int k = 0; k < 9; k++) SV<T>::st(Dst + (I)k * pl + node, g[k]);
@@ -273,7 +295,7 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
 // are adjacent (c_x = 0), a pair and a single load otherwise (c_x = +-1), packed
 // FP32 arithmetic, pair stores. im = source column of i0 - 1, ip2 of i0 + 2
 // (wrapped or clamped like the per-node path).
-template <typename T, typename I, bool COLLIDE>
+template <typename T, typename I, bool COLLIDE, bool FORCE>
 __device__ __forceinline__ void step_pair_shifted(const FastStepParams &fp, int i0, int j, int im, int ip2,
                                                   int jm, int jp) {
     const StepParams &p = fp.s;
@@ -298,13 +320,14 @@ __device__ __forceinline__ void step_pair_shifted(const FastStepParams &fp, int 
     g[7] = make_float2(a.y, SV<T>::ld(S + 7 * pl + rp + (I)ip2));
     a = SV<T>::ld2(S + 8 * pl + p0);
     g[8] = make_float2(SV<T>::ld(S + 8 * pl + rp + (I)im), a.x);
-    float2 dr, rho, ux, uy, Jx, Jy;
-    moments_v<float2>(g, v_splat<float2>(fp.hFxf), v_splat<float2>(fp.hFyf), dr, rho, ux, uy, Jx, Jy);
+    float2 dr, rho, ux, uy, Jx, Jy, jx, jy;
+    moments_v<float2>(g, v_splat<float2>(fp.hFxf), v_splat<float2>(fp.hFyf), dr, rho, ux, uy, Jx, Jy, jx, jy);
     const size_t dn = (size_t)j * (size_t)p.Nx + (size_t)i0;
     if (p.write_macro) macro_store_pair(p, dn, dr, ux, uy);
     if (COLLIDE) {
         const float2 om = p.omega ? omega_pair(p.omega, dn) : v_splat<float2>(fp.omega0f);
-        collide_v<float2>(g, fp.wf, fp.h1f, fp.h5f, dr, ux, uy, Jx, Jy, om, p.has_force != 0, fp.Fxf, fp.Fyf);
+        collide_v<float2, FORCE>(g, fp.wf, fp.h1f, fp.h5f, dr, ux, uy, Jx, Jy, jx, jy, om, p.has_force != 0,
+                                 fp.Fxf, fp.Fyf);
     }
 #pragma unroll
     for (int k = 0; k < 9; k++) SV<T>::st2(Dst + (I)k * pl + r0, g[k]);
@@ -313,7 +336,7 @@ __device__ __forceinline__ void step_pair_shifted(const FastStepParams &fp, int 
 // The nodes (i0, i0 + 1) of row j: the pair path when both exist and neither
 // is special, else each node on its own. ax, ay: the two nodes' wall-link force
 // terms (node i0 first), link: either has wall links.
-template <typename T, typename I, bool FLAGS, bool COLLIDE>
+template <typename T, typename I, bool FLAGS, bool COLLIDE, bool FORCE>
 __device__ __forceinline__ void step_two_shifted(const FastStepParams &fp, int i0, int j, double &ax,
                                                  double &ay, bool &link) {
     const StepParams &p = fp.s;
@@ -330,18 +353,18 @@ __device__ __forceinline__ void step_two_shifted(const FastStepParams &fp, int i
         else { im = max(im, 0); ip2 = min(ip2, p.Nx - 1); }
         if (p.py) { if (jm < 0) jm += p.Ny; if (jp >= p.Ny) jp -= p.Ny; }
         else { jm = max(jm, 0); jp = min(jp, p.Ny - 1); }
-        step_pair_shifted<T, I, COLLIDE>(fp, i0, j, im, ip2, jm, jp);
+        step_pair_shifted<T, I, COLLIDE, FORCE>(fp, i0, j, im, ip2, jm, jp);
         return;
     }
     float mx = 0.f, my = 0.f;
     bool l = false;
-    step_node_shifted<T, I, FLAGS, COLLIDE>(fp, i0, j, mx, my, l);
+    step_node_shifted<T, I, FLAGS, COLLIDE, FORCE>(fp, i0, j, mx, my, l);
     ax = (double)mx;
     ay = (double)my;
     link = l;
     if (two) {
         mx = 0.f; my = 0.f; l = false;
-        step_node_shifted<T, I, FLAGS, COLLIDE>(fp, i0 + 1, j, mx, my, l);
+        step_node_shifted<T, I, FLAGS, COLLIDE, FORCE>(fp, i0 + 1, j, mx, my, l);
         ax += (double)mx;
         ay += (double)my;
         link = link || l;
@@ -352,26 +375,26 @@ __device__ __forceinline__ void step_two_shifted(const FastStepParams &fp, int i
 // steps two adjacent nodes. Five resident blocks per SM (48 registers, no
 // spills) keep more loads in flight than the unconstrained 64 registers
 // (measured: FP16 135 -> 147 GLUPS on 4096^2).
-template <typename T, typename I, bool COLLIDE>
+template <typename T, typename I, bool COLLIDE, bool FORCE>
 __global__ void __launch_bounds__(256, 5) k_step_shifted_plain(const FastStepParams fp) {
     const int i0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     double ax = 0.0, ay = 0.0;
     bool link = false;
-    if (i0 < fp.s.Nx && j < fp.s.Ny) step_two_shifted<T, I, false, COLLIDE>(fp, i0, j, ax, ay, link);
+    if (i0 < fp.s.Nx && j < fp.s.Ny) step_two_shifted<T, I, false, COLLIDE, FORCE>(fp, i0, j, ax, ay, link);
 }
 
 // General geometry (flag word per node), two adjacent nodes per thread. The
 // force partials of a 32-node segment come from half a warp. Five resident
 // blocks per SM (48 registers; the few spills are in the per-node path).
-template <typename T, typename I, bool COLLIDE>
+template <typename T, typename I, bool COLLIDE, bool FORCE>
 __global__ void __launch_bounds__(256, 5) k_step_shifted_geo(const FastStepParams fp) {
     const StepParams &p = fp.s;
     const int i0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     double ax = 0.0, ay = 0.0;
     bool link = false;
-    if (i0 < p.Nx && j < p.Ny) step_two_shifted<T, I, true, COLLIDE>(fp, i0, j, ax, ay, link);
+    if (i0 < p.Nx && j < p.Ny) step_two_shifted<T, I, true, COLLIDE, FORCE>(fp, i0, j, ax, ay, link);
     if (p.mem_partials) segment_pair_reduce2_store(ax, ay, link, i0, j, p.Nx, p.seg_slot, p.mem_partials);
 }
 
@@ -379,7 +402,7 @@ __global__ void __launch_bounds__(256, 5) k_step_shifted_geo(const FastStepParam
 // 2^(tws + 1) x 2^(8 - tws) nodes, two adjacent nodes per thread. Blocks stride
 // through the tile list, so the tiles in flight at any moment are neighbours
 // in memory (sequential DRAM streams, halo rows shared through L2).
-template <typename T, typename I>
+template <typename T, typename I, bool FORCE>
 __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepParams *__restrict__ sp,
                                                             const int *__restrict__ phase,
                                                             const int4 *__restrict__ tiles,
@@ -392,10 +415,11 @@ __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepPar
         double ax = 0.0, ay = 0.0;
         bool link = false;
         const bool in = i0 < fp.s.Nx && j < fp.s.Ny;
-        if (fp.s.flags) {
-            if (in) step_two_shifted<T, I, true, true>(fp, i0, j, ax, ay, link);
-        } else {
-            if (in) step_two_shifted<T, I, false, true>(fp, i0, j, ax, ay, link);
+        // FORCE: some case of the batch has a body force; force-free cases
+        // still take their own (force-free) arithmetic per case (collide_v).
+        if (in) {
+            if (fp.s.flags) step_two_shifted<T, I, true, true, FORCE>(fp, i0, j, ax, ay, link);
+            else step_two_shifted<T, I, false, true, FORCE>(fp, i0, j, ax, ay, link);
         }
         if (td.w) segment_pair_reduce2_store(ax, ay, link, i0, j, fp.s.Nx, fp.s.seg_slot, fp.s.mem_partials);
     }
@@ -410,8 +434,8 @@ __device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 
         g[k] = SV<T>::rnd(p.bandg[(size_t)k * p.nslots + slot]);
         wf[k] = (float)p.w[k];
     }
-    float dr, rho, ux, uy, Jx, Jy;
-    moments_shifted(g, (float)p.hFx, (float)p.hFy, dr, rho, ux, uy, Jx, Jy);
+    float dr, rho, ux, uy, Jx, Jy, jx, jy;
+    moments_shifted(g, (float)p.hFx, (float)p.hFy, dr, rho, ux, uy, Jx, Jy, jx, jy);
     const size_t dn = (size_t)ij.y * p.Nx + ij.x;
     if (p.write_macro) { p.rho[dn] = 1.0 + (double)dr; p.ux[dn] = ux; p.uy[dn] = uy; }
     p.bandm_next[slot] = 1.0 + (double)dr;
@@ -421,7 +445,9 @@ __device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 
         const float om = p.omega ? (float)p.omega[dn] : (float)p.omega0;
         float h1, h5;
         shifted_h(wf[1], h1, h5);
-        collide_v<float>(g, wf, h1, h5, dr, ux, uy, Jx, Jy, om, p.has_force != 0, (float)p.Fx, (float)p.Fy);
+        if (p.has_force) collide_v<float, true>(g, wf, h1, h5, dr, ux, uy, Jx, Jy, jx, jy, om, true, (float)p.Fx,
+                                                (float)p.Fy);
+        else collide_v<float, false>(g, wf, h1, h5, dr, ux, uy, Jx, Jy, jx, jy, om, false, 0.f, 0.f);
     }
     T *D = (T *)p.dst;
     const long long node = (long long)ij.y * p.pitch + ij.x;
@@ -460,20 +486,25 @@ __global__ void k_collide_shifted(const CollideParams p) {
 #pragma unroll
     for (int k = 0; k < 9; k++) { g[k] = SV<T>::ld_plain(F + k * p.plane + node); wf[k] = (float)p.w[k]; }
     const float om = p.omega ? (float)p.omega[dn] : (float)p.omega0;
-    float dr, rho, ux, uy, Jx, Jy;
+    float dr, rho, ux, uy, Jx, Jy, jx, jy;
     if (p.from_pops) {
-        moments_shifted(g, (float)(0.5 * p.Fx), (float)(0.5 * p.Fy), dr, rho, ux, uy, Jx, Jy);
+        moments_shifted(g, (float)(0.5 * p.Fx), (float)(0.5 * p.Fy), dr, rho, ux, uy, Jx, Jy, jx, jy);
     } else {
+        // the stored fields: rho, u = (j + F/2) / rho
         rho = (float)p.rho[dn];
         dr = (float)(p.rho[dn] - 1.0);
         ux = (float)p.ux[dn];
         uy = (float)p.uy[dn];
         Jx = (float)(p.rho[dn] * p.ux[dn]);
         Jy = (float)(p.rho[dn] * p.uy[dn]);
+        jx = (float)(p.rho[dn] * p.ux[dn] - 0.5 * p.Fx);
+        jy = (float)(p.rho[dn] * p.uy[dn] - 0.5 * p.Fy);
     }
     float h1, h5;
     shifted_h(wf[1], h1, h5);
-    collide_v<float>(g, wf, h1, h5, dr, ux, uy, Jx, Jy, om, p.has_force != 0, (float)p.Fx, (float)p.Fy);
+    if (p.has_force) collide_v<float, true>(g, wf, h1, h5, dr, ux, uy, Jx, Jy, jx, jy, om, true, (float)p.Fx,
+                                            (float)p.Fy);
+    else collide_v<float, false>(g, wf, h1, h5, dr, ux, uy, Jx, Jy, jx, jy, om, false, 0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < 9; k++) SV<T>::st(F + k * p.plane + node, g[k]);
 }
@@ -575,16 +606,25 @@ cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s) {
 }
 
 
+template <typename T, typename I, bool FORCE>
+static void step_shifted_tif(const FastStepParams &p, bool flags, bool collide, dim3 g, dim3 b,
+                             cudaStream_t s) {
+    if (flags) {
+        if (collide) k_step_shifted_geo<T, I, true, FORCE><<<g, b, 0, s>>>(p);
+        else k_step_shifted_geo<T, I, false, FORCE><<<g, b, 0, s>>>(p);
+    } else {
+        if (collide) k_step_shifted_plain<T, I, true, FORCE><<<g, b, 0, s>>>(p);
+        else k_step_shifted_plain<T, I, false, FORCE><<<g, b, 0, s>>>(p);
+    }
+}
+
+// The body force is a template parameter: force-free kernels carry no forcing
+// code (fewer registers).
 template <typename T, typename I>
 static void step_shifted_ti(const FastStepParams &p, bool flags, bool collide, dim3 g, dim3 b,
                             cudaStream_t s) {
-    if (flags) {
-        if (collide) k_step_shifted_geo<T, I, true><<<g, b, 0, s>>>(p);
-        else k_step_shifted_geo<T, I, false><<<g, b, 0, s>>>(p);
-    } else {
-        if (collide) k_step_shifted_plain<T, I, true><<<g, b, 0, s>>>(p);
-        else k_step_shifted_plain<T, I, false><<<g, b, 0, s>>>(p);
-    }
+    if (p.s.has_force) step_shifted_tif<T, I, true>(p, flags, collide, g, b, s);
+    else step_shifted_tif<T, I, false>(p, flags, collide, g, b, s);
 }
 
 template <typename T>
@@ -604,16 +644,24 @@ cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool co
     return cudaGetLastError();
 }
 
+template <typename T, bool FORCE>
+static void step_batch_shifted_tf(const FastStepParams *sp, const int *phase, const int4 *tiles, int ntiles,
+                                  int sel, int tws, bool wide, int grid, cudaStream_t s) {
+    if (wide) k_step_batch_shifted<T, long long, FORCE><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+    else k_step_batch_shifted<T, int, FORCE><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+}
+
 cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
-                               int ntiles, int sel, int tws, int store, bool wide, int grid, cudaStream_t s) {
+                               int ntiles, int sel, int tws, int store, bool wide, bool force, int grid,
+                               cudaStream_t s) {
     if (ntiles == 0) return cudaSuccess;
     if (tws < 5 || tws > 8) return cudaErrorInvalidValue;
     if (store == STORE_F32) {
-        if (wide) k_step_batch_shifted<float, long long><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
-        else k_step_batch_shifted<float, int><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+        if (force) step_batch_shifted_tf<float, true>(sp, phase, tiles, ntiles, sel, tws, wide, grid, s);
+        else step_batch_shifted_tf<float, false>(sp, phase, tiles, ntiles, sel, tws, wide, grid, s);
     } else {
-        if (wide) k_step_batch_shifted<__half, long long><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
-        else k_step_batch_shifted<__half, int><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+        if (force) step_batch_shifted_tf<__half, true>(sp, phase, tiles, ntiles, sel, tws, wide, grid, s);
+        else step_batch_shifted_tf<__half, false>(sp, phase, tiles, ntiles, sel, tws, wide, grid, s);
     }
     return cudaGetLastError();
 }
@@ -622,8 +670,8 @@ int step_batch_shifted_grid(int store) {
     int nb = 0, dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (store == STORE_F32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_batch_shifted<float, int>, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_batch_shifted<__half, int>, 256, 0);
+    if (store == STORE_F32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_batch_shifted<float, int, true>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_batch_shifted<__half, int, true>, 256, 0);
     return nsm * (nb > 0 ? nb : 1);
 }
 

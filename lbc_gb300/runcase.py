@@ -41,6 +41,8 @@ def main(argv=None):
     p.add_argument("--chunk", type=int, default=1000)
     p.add_argument("--wake", type=int, default=0,
                    help="cylinder wake (2048 x 512, Re 100): Cd, Cl, St after this many steps")
+    p.add_argument("--vs-f64", action="store_true",
+                   help="also run the case in FP64 for the same steps; report the u L2 error against it")
     p.add_argument("--autotune", action="store_true",
                    help="tune block / tile shapes on the warm-up steps (LBM_GPU_AUTOTUNE=1)")
     a = p.parse_args(argv)
@@ -76,10 +78,24 @@ def main(argv=None):
     s.run(a.warmup)
     ms = s.run_timed(a.steps)
     tuned, blk, us = s.autotune_status()
-    print(json.dumps({"case": a.case, "Nx": case.Nx, "Ny": case.Ny, "storage": a.storage,
-                      "steps": a.steps, "ms": round(ms, 3),
-                      "mlups": round(case.nodes * a.steps / (ms / 1e3) / 1e6, 1),
-                      "block": list(blk), "tuned": tuned}))
+    out = {"case": a.case, "Nx": case.Nx, "Ny": case.Ny, "storage": a.storage,
+           "steps": a.steps, "ms": round(ms, 3),
+           "mlups": round(case.nodes * a.steps / (ms / 1e3) / 1e6, 1),
+           "block": list(blk), "tuned": tuned}
+    if a.vs_f64:
+        import numpy as np
+        r, u, v = s.get_fields()
+        ref = GpuSolver(case, STORAGE["f64"])
+        ref.set_state(st)
+        ref.run(a.warmup)
+        ms64 = ref.run_timed(a.steps)
+        r64, u64, v64 = ref.get_fields()
+        m = case.solid_mask == 0
+        out["f64_mlups"] = round(case.nodes * a.steps / (ms64 / 1e3) / 1e6, 1)
+        out["u_l2_rel_vs_f64"] = float(np.sqrt(np.sum((u[m] - u64[m]) ** 2 + (v[m] - v64[m]) ** 2) /
+                                               np.sum(u64[m] ** 2 + v64[m] ** 2)))
+        out["mass_rel_vs_f64"] = float(np.sum(r[m]) / np.sum(r64[m]) - 1.0)
+    print(json.dumps(out))
 
 
 if __name__ == "__main__":

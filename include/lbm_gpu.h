@@ -209,7 +209,9 @@ int lbm_gpu_batch_destroy(lbm_gpu_batch *b);
  * memory. */
 typedef struct lbm_gpu_server lbm_gpu_server;
 int lbm_gpu_server_create(size_t budget_bytes, int max_active, int chunk_steps, lbm_gpu_server **out);
-/* Returns the request id (> 0) or a negative code. */
+/* Returns the request id (> 0) or a negative code. f = f_new = NULL: the
+ * request starts from f = f_new = f_eq(rho, u, v) (lbc's equilibrium, formed
+ * when the request is admitted), so a queued request holds only rho, u, v. */
 int lbm_gpu_server_prepare(lbm_gpu_server *srv, const lbm_gpu_case *c, const double *f,
                            const double *f_new, const double *rho, const double *u, const double *v,
                            int nsteps, int keep_populations);

@@ -62,6 +62,7 @@ struct Request {
     std::vector<BCEntry> bcs;
     std::vector<std::vector<double>> bc_vals;  // 2 per entry
     std::vector<double> f, f_new, rho, u, v;    // inputs, then results
+    bool from_equilibrium = false;              // f = f_new = f_eq(rho, u, v) at admission
     int nsteps = 0, remaining = 0;
     bool keep_populations = false;
     ImpSpec imp;
@@ -146,7 +147,24 @@ static bool admit(lbm_gpu_server *S, Request *r) {
         r->error = last_error();
         return false;
     }
-    if (!s->set_state(r->f.data(), r->f_new.data(), r->rho.data(), r->u.data(), r->v.data()) ||
+    if (r->from_equilibrium) {
+        // f_eq in lbc's operation order (as its case mains initialise f);
+        // host memory for it only while the request is admitted.
+        static const int kCX[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+        static const int kCY[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+        const size_t N = (size_t)r->Nx * r->Ny;
+        r->f.resize(N * 9);
+        for (size_t n = 0; n < N; n++) {
+            const double ux = r->u[n], uy = r->v[n], rho = r->rho[n];
+            const double v_sq = ux * ux + uy * uy;
+            for (int k = 0; k < 9; k++) {
+                const double cu = (double)kCX[k] * ux + (double)kCY[k] * uy;
+                r->f[n * 9 + k] = r->w[k] * rho * (1.0 + 3.0 * cu + 4.5 * cu * cu - 1.5 * v_sq);
+            }
+        }
+    }
+    const double *fn = r->from_equilibrium ? r->f.data() : r->f_new.data();
+    if (!s->set_state(r->f.data(), fn, r->rho.data(), r->u.data(), r->v.data()) ||
         !check_cuda(cudaStreamSynchronize(s->stream()), "admit")) {
         r->error = last_error();
         return false;
@@ -336,7 +354,7 @@ int lbm_gpu_server_create(size_t budget_bytes, int max_active, int chunk_steps, 
 int lbm_gpu_server_prepare(lbm_gpu_server *S, const lbm_gpu_case *c, const double *f,
                            const double *f_new, const double *rho, const double *u, const double *v,
                            int nsteps, int keep_populations) {
-    if (!S || !c || !f || !f_new || !rho || !u || !v || nsteps < 1) {
+    if (!S || !c || !rho || !u || !v || nsteps < 1 || (!f) != (!f_new)) {
         set_error("bad arguments");
         return LBM_GPU_ERR_ARG;
     }
@@ -369,8 +387,12 @@ int lbm_gpu_server_prepare(lbm_gpu_server *S, const lbm_gpu_case *c, const doubl
         r->bc_vals.push_back(v1 ? std::vector<double>(v1, v1 + along) : std::vector<double>());
         r->bc_vals.push_back(v2 ? std::vector<double>(v2, v2 + along) : std::vector<double>());
     }
-    r->f.assign(f, f + 9 * N);
-    r->f_new.assign(f_new, f_new + 9 * N);
+    if (f) {
+        r->f.assign(f, f + 9 * N);
+        r->f_new.assign(f_new, f_new + 9 * N);
+    } else {
+        r->from_equilibrium = true;
+    }
     r->rho.assign(rho, rho + N);
     r->u.assign(u, u + N);
     r->v.assign(v, v + N);

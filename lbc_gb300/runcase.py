@@ -59,7 +59,7 @@ def main(argv=None):
     if a.serve:
         from lbc_gb300 import serving
         stream = serving.make_stream(a.serve, rate=a.rate, scale=a.scale)
-        r = serving.serve(stream, a.max_active, a.chunk)
+        r = serving.serve(stream, a.max_active, a.chunk, prebuild=a.serve <= 400)
         r.pop("latencies_s")
         r["serial_fp64"] = serving.serial_fp64_estimate(stream)
         print(json.dumps(r))

@@ -395,10 +395,14 @@ class GpuServer:
         self.meta = {}
 
     def submit(self, case: Case, st: State, nsteps: int, storage: int, keep_populations=False,
-               impedance=None) -> int:
-        """impedance: (entry, R, m, K, omegas, rho_ref, alpha, window) or None."""
+               impedance=None, from_equilibrium=False) -> int:
+        """impedance: (entry, R, m, K, omegas, rho_ref, alpha, window) or None.
+        from_equilibrium: start from f = f_eq(rho, u, v) formed at admission
+        (st.f and st.f_new are not sent)."""
         d, keep = case_desc(self.lib, case, storage)
-        rid = self.lib.lbm_gpu_server_prepare(self.h, C.byref(d), dptr(st.f), dptr(st.f_new), dptr(st.rho),
+        f = None if from_equilibrium else dptr(st.f)
+        fn = None if from_equilibrium else dptr(st.f_new)
+        rid = self.lib.lbm_gpu_server_prepare(self.h, C.byref(d), f, fn, dptr(st.rho),
                                               dptr(st.u), dptr(st.v), nsteps, 1 if keep_populations else 0)
         if rid <= 0:
             raise RuntimeError("lbm_gpu_server_prepare failed: " + last_error())

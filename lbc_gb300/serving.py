@@ -94,19 +94,28 @@ def make_stream(n: int = 2000, seed: int = 2026, rate: float = 50.0, scale: floa
     return out
 
 
-def serve(stream: List[Req], max_active: int = 64, chunk: int = 1000, budget_bytes: int = 0):
+def serve(stream: List[Req], max_active: int = 64, chunk: int = 1000, budget_bytes: int = 0,
+          prebuild: bool = True):
     """Submit each request at its arrival time to a running server; wait for
-    all; return per-request latencies and totals."""
-    built = [build_request(r) for r in stream]
+    all; return per-request latencies and totals. Every request starts from
+    the equilibrium of its initial rho, u, v (formed by the server at
+    admission). prebuild=False builds each request's case at its arrival
+    instead of all of them up front (long streams: bounded host memory)."""
+    built = [build_request(r) for r in stream] if prebuild else None
     srv = GpuServer(budget_bytes, max_active, chunk)
     srv.start()
     t0 = time.perf_counter()
     ids = []
-    for r, (case, st, spec) in zip(stream, built):
+    for q, r in enumerate(stream):
+        if built is not None:
+            case, st, spec = built[q]
         now = time.perf_counter() - t0
         if r.arrival > now:
             time.sleep(r.arrival - now)
-        ids.append(srv.submit(case, st, r.steps, r.storage, impedance=spec))
+        if built is None:
+            case, st, spec = build_request(r)
+        ids.append(srv.submit(case, st, r.steps, r.storage, impedance=spec, from_equilibrium=True))
+        del case, st
     lat, done = {}, set()
     failed = []
     while len(done) < len(ids):

@@ -88,3 +88,27 @@ def test_threaded_server_and_failed_request():
         rho, u, v, _ = _alone(r)
         assert same(res["rho"], rho)
     srv.close()
+
+
+def test_requests_started_from_equilibrium():
+    """A request sent without populations starts from lbc's f_eq(rho, u, v),
+    formed by the server: the result equals the request run alone from the
+    same equilibrium computed on the host."""
+    from lbc_gb300 import GpuServer
+    stream = _stream()[:5]
+    srv = GpuServer(0, 64, 60)
+    ids = []
+    for r in stream:
+        case, st, spec = serving.build_request(r)
+        ids.append(srv.submit(case, st, r.steps, r.storage, impedance=spec, from_equilibrium=True))
+    while srv.poll() > 0:
+        pass
+    for r, rid in zip(stream, ids):
+        assert srv.status(rid)[0] == 3
+        res = srv.fetch(rid)
+        rho, u, v, spec = _alone(r)
+        assert same(res["rho"], rho) and same(res["u"], u) and same(res["v"], v), r
+        if spec is not None:
+            assert same(res["spectra"], spec)
+        srv.release(rid)
+    srv.close()

@@ -57,7 +57,9 @@ typedef struct {
     int Nx, Ny, pitch, storage;
     int has_geometry;              /* 0: fully periodic, no solids, no edge BCs */
     int edge_stages;               /* Boundary entries run as edge kernels */
-    int launches_per_step;         /* kernel launches per time step in the loop */
+    int launches_per_step;         /* kernel launches per time step in the loop: the bulk
+                                      step plus edge_launches (these also finish the
+                                      BC-written nodes and reduce the wall force) */
     size_t device_bytes;
     long long steps_done;
     int edge_launches;             /* launches the edge stages take per step: consecutive

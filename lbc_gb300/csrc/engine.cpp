@@ -191,7 +191,7 @@ bool Solver::build_geometry() {
     for (int c : cols) { colbase[c] = ns; ns += Ny; }
     for (int r : rows) { rowbase[r] = ns; ns += Nx; }
     nslots_ = ns;
-    group_stages(solid);
+    group_stages(solid, colbase, rowbase);
     auto slot_of = [&](int i, int j) { return colbase[i] >= 0 ? colbase[i] + j : rowbase[j] + i; };
 
     // Flags and links.
@@ -339,6 +339,10 @@ bool Solver::build_geometry() {
             !dalloc(&d_seed_slots_, seed_slots.size()))
             return false;
         if (nw_) CK(cudaMemcpyAsync(d_wnodes_, wnodes.data(), wnodes.size() * sizeof(int2), cudaMemcpyHostToDevice, stream_));
+        if (fuse_) {
+            if (!dalloc(&d_last_, last_host_.size())) return false;
+            CK(cudaMemcpyAsync(d_last_, last_host_.data(), last_host_.size() * sizeof(short), cudaMemcpyHostToDevice, stream_));
+        }
         if (nseed_) {
             CK(cudaMemcpyAsync(d_seed_nodes_, seed_nodes.data(), seed_nodes.size() * sizeof(int2), cudaMemcpyHostToDevice, stream_));
             CK(cudaMemcpyAsync(d_seed_slots_, seed_slots.data(), seed_slots.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
@@ -369,9 +373,18 @@ bool Solver::build_geometry() {
 // (regularized, convective), the neighbour of each; moments of the previous
 // step and post-collision sources (periodic entries) are not written by any
 // entry.
-template <class Solid> void Solver::group_stages(const Solid &solid) {
+// The last entry that writes a node also finishes it (moments, collision,
+// store into the destination buffer and the band moments of the next step) in
+// its own launch: no entry reads what the finish writes, and no later entry
+// writes the node again. That needs one thread per node within the entry; a
+// periodic entry on a grid one node wide visits each node twice, and such a
+// case keeps the separate finish launch.
+template <class Solid>
+void Solver::group_stages(const Solid &solid, const std::vector<int> &colbase, const std::vector<int> &rowbase) {
     const int Nx = d_.Nx, Ny = d_.Ny;
     groups_.clear();
+    last_host_.assign((size_t)nslots_, (short)-1);
+    fuse_ = stages_.size() < 32767;
     std::unordered_set<long long> gw, gr;
     auto id = [&](int i, int j) { return (long long)j * Nx + i; };
     for (size_t s = 0; s < stages_.size(); s++) {
@@ -398,6 +411,12 @@ template <class Solid> void Solver::group_stages(const Solid &solid) {
         case BC_VEL_BOT_REG: case BC_PRES_BOT_REG: line(false, x, 0, 1, true); break;
         case BC_VEL_TOP_REG: case BC_PRES_TOP_REG: line(false, x, 0, -1, true); break;
         default: break;
+        }
+        for (long long v : w) {
+            const int i = (int)(v % Nx), j = (int)(v / Nx);
+            const int slot = colbase[i] >= 0 ? colbase[i] + j : rowbase[j] + i;
+            if (last_host_[slot] == (short)s) fuse_ = false;  // two threads of this entry
+            last_host_[slot] = (short)s;
         }
         bool conflict = groups_.empty();
         for (long long v : w)
@@ -689,6 +708,8 @@ StageParams Solver::stage_params(const Stage &st, int src, int bparity) const {
     s.bandf = d_bandf_; s.bandg = d_bandg_; s.bandm_prev = d_bandm_[bparity];
     s.src = buf_[src];
     for (int k = 0; k < 9; k++) s.w[k] = d_.w[k];
+    s.last = fuse_ ? d_last_ : nullptr;
+    s.entry = (int)(&st - stages_.data());
     s.imp = st.d_imp;
     s.imp_nf = st.imp_nf;
     s.imp_alpha = st.imp_alpha;
@@ -835,8 +856,9 @@ FinishParams Solver::finish_params(int dst, bool write_macro, int bparity) const
     return f;
 }
 
-// One time step src -> dst: fused bulk kernel, then the Boundary list in order
-// and the finish kernel for BC-written nodes.
+// One time step src -> dst: fused bulk kernel, then the Boundary list in order,
+// one launch per stage group, whose threads finish the BC-written nodes (a
+// separate finish launch only for cases that cannot fuse it).
 bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int bparity,
                          cudaStream_t s) {
     if (!s) s = stream_;
@@ -846,13 +868,15 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
     } else {
         CK(launch::step_shifted(fast_params(p), d_.store, has_flags_, collide, block_, s));
     }
-    if (has_mem_) CK(launch::force_reduce(d_force_slot_, 1, s));
-    if (stages_.empty()) return true;
-    for (const std::vector<int> &g : groups_) {
-        if (g.size() == 1) {
-            CK(launch::stage(stage_params(stages_[g[0]], src, bparity), d_.store, s));
-            continue;
-        }
+    if (groups_.empty()) {
+        if (has_mem_) CK(launch::force_reduce(d_force_slot_, 1, s));
+        return true;
+    }
+    // The force (from the bulk kernel's partials) rides in the first stage
+    // launch; fused stages finish their nodes (group_stages).
+    const FinishParams f = finish_params(dst, write_macro, bparity);
+    for (size_t gi = 0; gi < groups_.size(); gi++) {
+        const std::vector<int> &g = groups_[gi];
         StageGroup sg;
         std::memset(&sg, 0, sizeof sg);
         sg.n = (int)g.size();
@@ -860,11 +884,15 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
             sg.p[q] = stage_params(stages_[g[q]], src, bparity);
             sg.max_along = std::max(sg.max_along, sg.p[q].along);
         }
-        CK(launch::stage_group(sg, d_.store, s));
+        sg.fin = f;
+        sg.fs = d_force_slot_;
+        sg.nfs = (gi == 0 && has_mem_) ? 1 : 0;
+        CK(launch::stage_group(sg, d_.store, collide, s));
     }
-    const FinishParams f = finish_params(dst, write_macro, bparity);
-    if (d_.store == STORE_F64) CK(launch::finish_exact(f, collide, s));
-    else CK(launch::finish_shifted(f, d_.store, collide, s));
+    if (!fuse_) {
+        if (d_.store == STORE_F64) CK(launch::finish_exact(f, collide, s));
+        else CK(launch::finish_shifted(f, d_.store, collide, s));
+    }
     return true;
 }
 
@@ -1223,7 +1251,8 @@ bool Batch::build() {
         if (9LL * s->plane() >= (1LL << 31)) wide_ = true;
         if (s->has_force()) any_force_ = true;
         if (s->has_mem()) force.push_back(s->force_slot());
-        for (const int2 &w : s->wnodes()) fin_nodes.push_back(make_int4(c, w.x, w.y, 0));
+        if (!s->fused_finish())
+            for (const int2 &w : s->wnodes()) fin_nodes.push_back(make_int4(c, w.x, w.y, 0));
         max_stages_ = std::max(max_stages_, (int)s->stage_groups().size());
         for (const Stage &st : s->stages()) max_along_ = std::max(max_along_, st.along);
     }
@@ -1256,7 +1285,8 @@ bool Batch::build() {
         d_stage_lists_.push_back(d);
         stage_counts_.push_back(cnt);
     }
-    launches_per_step_ = 1 + max_stages_ + (nfin_ ? 1 : 0) + (nforce_ ? 1 : 0);
+    // The force reductions ride in the first stage level's launch.
+    launches_per_step_ = 1 + max_stages_ + (nfin_ ? 1 : 0) + (nforce_ && max_stages_ == 0 ? 1 : 0);
     CK(cudaStreamSynchronize(stream_));
     return true;
 }
@@ -1269,12 +1299,13 @@ bool Batch::launch_batched(int sel) {
         CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
                                       store_, wide_, any_force_, grid_, stream_));
     for (int s = 0; s < max_stages_; s++)
-        CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], max_along_, store_, sel, stream_));
+        CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], max_along_, store_, sel, d_force_,
+                               s == 0 ? nforce_ : 0, stream_));
     if (nfin_) {
         if (store_ == STORE_F64) CK(launch::finish_batch_exact(d_fin_, d_phase_, d_fin_nodes_, nfin_, sel, stream_));
         else CK(launch::finish_batch_shifted(d_fin_, d_phase_, d_fin_nodes_, nfin_, sel, store_, stream_));
     }
-    if (nforce_) CK(launch::force_reduce(d_force_, nforce_, stream_));
+    if (nforce_ && max_stages_ == 0) CK(launch::force_reduce(d_force_, nforce_, stream_));
     return true;
 }
 
@@ -1335,7 +1366,9 @@ bool Batch::run(int nsteps) {
             for (size_t l = 0; l < s->stage_groups().size(); l++)
                 for (int k : s->stage_groups()[l]) {
                     lists[l].push_back(s->stage_params(s->stages()[k], cur, par));
+                    lists[l].back().fin = d_fin_ + 2 * c;
                     lists[l].push_back(s->stage_params(s->stages()[k], 1 - cur, par ^ 1));
+                    lists[l].back().fin = d_fin_ + 2 * c + 1;
                 }
         }
         if (store_ == STORE_F64)

@@ -102,7 +102,8 @@ class Solver {
     long long steps_done() const { return steps_done_; }
     // Kernel launches per time step inside the loop (for launch counting).
     int launches_per_step() const {
-        return 1 + (has_mem_ ? 1 : 0) + (int)groups_.size() + (nw_ > 0 ? 1 : 0);
+        if (groups_.empty()) return 1 + (has_mem_ ? 1 : 0);
+        return 1 + (int)groups_.size() + (!fuse_ && nw_ > 0 ? 1 : 0);
     }
     bool set_block(dim3 b);
     dim3 block() const { return block_; }
@@ -125,6 +126,8 @@ class Solver {
     // Consecutive stages that share one launch (indices into stages()).
     const std::vector<std::vector<int>> &stage_groups() const { return groups_; }
     const std::vector<int2> &wnodes() const { return wnodes_host_; }
+    // The stage launches finish the BC-written nodes (no separate finish).
+    bool fused_finish() const { return fuse_; }
     bool has_mem() const { return has_mem_; }
     bool has_force() const { return d_.Fx != 0.0 || d_.Fy != 0.0; }
     // 1 for fluid nodes with at least one solid pull source (wall link), [Ny][Nx].
@@ -211,7 +214,13 @@ class Solver {
     double *d_stage_ = nullptr;  // AoS staging (FP64, 72 N bytes)
     std::vector<Stage> stages_;
     std::vector<std::vector<int>> groups_;
-    template <class Solid> void group_stages(const Solid &solid);
+    template <class Solid>
+    void group_stages(const Solid &solid, const std::vector<int> &colbase, const std::vector<int> &rowbase);
+    // Per band slot: the last stage (index into stages_) that writes the node,
+    // -1 for none; fuse_ when every written node has one thread in that stage.
+    std::vector<short> last_host_;
+    short *d_last_ = nullptr;
+    bool fuse_ = false;
     dim3 block_{64, 4, 1};
     cudaGraphExec_t pair_exec_ = nullptr;
     int pair_cur_ = -1, pair_parity_ = -1;
@@ -240,11 +249,12 @@ class Solver {
 };
 
 // Many independent cases of one storage type advanced together: per step one
-// persistent bulk kernel over the flattened tile list of all cases, the i-th
-// Boundary entry of every case in one launch, one finish launch for all
-// BC-written nodes and one per-case force reduction. The steps between the
-// per-case first collision and final step run from a captured two-step graph.
-// Each case ends exactly as Solver::run(n) would leave it.
+// persistent bulk kernel over the flattened tile list of all cases, then one
+// launch per stage level (the l-th stage group of every case) whose threads
+// also finish the nodes their entry wrote last; the first level's launch also
+// reduces every case's force. The steps between the per-case first collision
+// and final step run from a captured two-step graph. Each case ends exactly
+// as Solver::run(n) would leave it.
 class Batch {
   public:
     explicit Batch(const std::vector<Solver *> &cases);

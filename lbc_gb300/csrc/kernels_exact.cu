@@ -13,6 +13,7 @@
 //   * k_collide_exact   in-place collision with stored rho/u/v (first step)
 //   * AoS kernels       lbc's standalone functions on lbc's own layout
 //   * transposes        lbc AoS <-> device SoA, with FP32/FP16 shifted storage
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 
@@ -198,66 +199,6 @@ __device__ __forceinline__ void stage_point(const StageParams &p, int t) {
     bc_apply(a, p.w, p.kind, p.Nx, p.Ny, p.index, t, p.val1, p.val2);
 }
 
-template <typename T>
-__global__ void k_stage(const StageParams p) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.along) return;
-    stage_point<T>(p, t);
-}
-
-template <typename T>
-__global__ void k_stage_group(const StageGroup g) {
-    const StageParams &p = g.p[blockIdx.y];
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.along) return;
-    stage_point<T>(p, t);
-}
-
-// Stage `s` of every case of a batch: blockIdx.y selects the case entry,
-// list[2 * e + (sel ^ phase)] its parameters for this ping-pong direction.
-template <typename T>
-__global__ void k_stage_batch(const StageParams *__restrict__ list, const int *__restrict__ ephase,
-                              int sel) {
-    const int e = blockIdx.y;
-    const StageParams &p = list[2 * e + (sel ^ ephase[e])];
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.along) return;
-    stage_point<T>(p, t);
-}
-
-// Per-case deterministic sum of the per-tile force partials of a batched step.
-__global__ void k_force_reduce(const ForceSlot *__restrict__ slots, int nslots) {
-    const int c = blockIdx.x;
-    if (c >= nslots) return;
-    const ForceSlot fs = slots[c];
-    double a = 0.0, b = 0.0;
-    for (int t = fs.t0 + (int)threadIdx.x; t < fs.t1; t += blockDim.x) {
-        a += fs.partials[2 * (size_t)t];
-        b += fs.partials[2 * (size_t)t + 1];
-    }
-    __shared__ double sa[32], sb[32];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, o);
-        b += __shfl_down_sync(0xffffffffu, b, o);
-    }
-    if ((threadIdx.x & 31) == 0) { sa[threadIdx.x >> 5] = a; sb[threadIdx.x >> 5] = b; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double ra = 0.0, rb = 0.0;
-        for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) { ra += sa[w]; rb += sb[w]; }
-        fs.out[0] = ra;
-        fs.out[1] = rb;
-        if (fs.hist) {
-            const unsigned long long k = *fs.hist_count;
-            const int slot = (int)(k % (unsigned long long)fs.hist_cap);
-            fs.hist[2 * slot] = ra;
-            fs.hist[2 * slot + 1] = rb;
-            *fs.hist_count = k + 1ull;
-        }
-    }
-}
-
 // Moments and collision of every node an edge BC wrote.
 template <bool COLLIDE>
 __device__ __forceinline__ void finish_node_exact(const FinishParams &p, int2 ij) {
@@ -280,6 +221,55 @@ __device__ __forceinline__ void finish_node_exact(const FinishParams &p, int2 ij
     const long long node = (long long)ij.y * p.pitch + ij.x;
 #pragma unroll
     for (int k = 0; k < 9; k++) D[k * p.plane + node] = f[k];
+}
+
+// Finish of a node by the Boundary entry that wrote it last (StageParams.last).
+template <bool COLLIDE>
+__device__ __forceinline__ void stage_finish(const StageParams &p, const FinishParams &f, int t) {
+    const int2 ij = stage_node(p.kind, p.Nx, p.Ny, p.index, t);
+    if (p.flags[(long long)ij.y * p.pitch + ij.x] & NF_SOLID) return;
+    if (p.last[band_slot(p.colbase, p.rowbase, ij.x, ij.y)] != p.entry) return;
+    finish_node_exact<COLLIDE>(f, ij);
+}
+
+// One group of Boundary entries of a case (blockIdx.y = member), each fused
+// member finishing its nodes; row n reduces the case's force.
+template <typename T, bool COLLIDE>
+__global__ void k_stage_group(const StageGroup g) {
+    if ((int)blockIdx.y >= g.n) {
+        if (blockIdx.x == 0 && threadIdx.x < 32) force_reduce_warp(*g.fs, (int)threadIdx.x);
+        return;
+    }
+    const StageParams &p = g.p[blockIdx.y];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.along) return;
+    stage_point<T>(p, t);
+    if (p.last) stage_finish<COLLIDE>(p, g.fin, t);
+}
+
+// Stage level of every case of a batch: blockIdx.y selects the case entry,
+// list[2 * e + (sel ^ phase)] its parameters for this ping-pong direction;
+// rows n.. reduce the force slots fs[].
+template <typename T>
+__global__ void k_stage_batch(const StageParams *__restrict__ list, const int *__restrict__ ephase,
+                              int sel, int n, const ForceSlot *__restrict__ fs) {
+    const int e = blockIdx.y;
+    if (e >= n) {
+        if (blockIdx.x == 0 && threadIdx.x < 32) force_reduce_warp(fs[e - n], (int)threadIdx.x);
+        return;
+    }
+    const StageParams &p = list[2 * e + (sel ^ ephase[e])];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.along) return;
+    stage_point<T>(p, t);
+    if (p.last) stage_finish<true>(p, *p.fin, t);
+}
+
+// Per-case force of a step from its segment partials (one warp per case).
+__global__ void k_force_reduce(const ForceSlot *__restrict__ slots, int nslots) {
+    const int c = blockIdx.x;
+    if (c >= nslots) return;
+    force_reduce_warp(slots[c], (int)threadIdx.x);
 }
 
 template <bool COLLIDE>
@@ -607,17 +597,12 @@ cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block
 }
 
 // Edge kernels are FP64 and short: 32-thread blocks spread a line over many SMs.
-cudaError_t stage_group(const StageGroup &g, int store, cudaStream_t s) {
-    if (store != STORE_F64) return stage_group_shifted(g, store, s);
-    const dim3 grid((g.max_along + 31) / 32, g.n);
-    k_stage_group<double><<<grid, 32, 0, s>>>(g);
-    return cudaGetLastError();
-}
-
-cudaError_t stage(const StageParams &p, int store, cudaStream_t s) {
-    if (store != STORE_F64) return stage_shifted(p, store, s);
-    const int b = 32, g = (p.along + b - 1) / b;
-    k_stage<double><<<g, b, 0, s>>>(p);
+cudaError_t stage_group(const StageGroup &g, int store, bool collide, cudaStream_t s) {
+    if (g.n < 1 || g.n > kStageGroupMax || (g.nfs && !g.fs)) return cudaErrorInvalidValue;
+    if (store != STORE_F64) return stage_group_shifted(g, store, collide, s);
+    const dim3 grid((g.max_along + 31) / 32, g.n + (g.nfs ? 1 : 0));
+    if (collide) k_stage_group<double, true><<<grid, 32, 0, s>>>(g);
+    else k_stage_group<double, false><<<grid, 32, 0, s>>>(g);
     return cudaGetLastError();
 }
 
@@ -637,11 +622,11 @@ cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 
 int step_batch_exact_grid() { return 1 << 30; }
 
 cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int max_along, int store,
-                        int sel, cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
-    if (store != STORE_F64) return stage_batch_shifted(list, ephase, n, max_along, store, sel, s);
-    const dim3 g((max_along + 31) / 32, n);
-    k_stage_batch<double><<<g, 32, 0, s>>>(list, ephase, sel);
+                        int sel, const ForceSlot *fs, int nfs, cudaStream_t s) {
+    if (n + nfs == 0) return cudaSuccess;
+    if (store != STORE_F64) return stage_batch_shifted(list, ephase, n, max_along, store, sel, fs, nfs, s);
+    const dim3 g(std::max(1, (max_along + 31) / 32), n + nfs);
+    k_stage_batch<double><<<g, 32, 0, s>>>(list, ephase, sel, n, fs);
     return cudaGetLastError();
 }
 
@@ -654,7 +639,7 @@ cudaError_t finish_batch_exact(const FinishParams *fp, const int *phase, const i
 
 cudaError_t force_reduce(const ForceSlot *slots, int n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_force_reduce<<<n, 256, 0, s>>>(slots, n);
+    k_force_reduce<<<n, 32, 0, s>>>(slots, n);
     return cudaGetLastError();
 }
 

@@ -6,6 +6,7 @@
 // force, moments, BGK + Guo collision. Storing g instead of f keeps the relative
 // precision of the small deviations from the rest state; FP64 is used only for the
 // force reduction and the band values handed to the edge BCs.
+#include <algorithm>
 #include <cmath>
 
 #include "bc_shifted.cuh"
@@ -546,56 +547,65 @@ __device__ __forceinline__ void stage_point_s(const StageParams &p, int t) {
     bc_apply_s(a, w, p.kind, p.Nx, p.Ny, p.index, t, p.val1, p.val2);
 }
 
-template <typename T>
-__global__ void k_stage_shifted(const StageParams p) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.along) return;
-    stage_point_s<T>(p, t);
+// Finish of a node by the Boundary entry that wrote it last (StageParams.last).
+template <typename T, bool COLLIDE>
+__device__ __forceinline__ void stage_finish_s(const StageParams &p, const FinishParams &f, int t) {
+    const int2 ij = stage_node(p.kind, p.Nx, p.Ny, p.index, t);
+    if (p.flags[(long long)ij.y * p.pitch + ij.x] & NF_SOLID) return;
+    if (p.last[band_slot(p.colbase, p.rowbase, ij.x, ij.y)] != p.entry) return;
+    finish_node_shifted<T, COLLIDE>(f, ij);
 }
 
-template <typename T>
+template <typename T, bool COLLIDE>
 __global__ void k_stage_group_shifted(const StageGroup g) {
+    if ((int)blockIdx.y >= g.n) {
+        if (blockIdx.x == 0 && threadIdx.x < 32) force_reduce_warp(*g.fs, (int)threadIdx.x);
+        return;
+    }
     const StageParams &p = g.p[blockIdx.y];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
     stage_point_s<T>(p, t);
+    if (p.last) stage_finish_s<T, COLLIDE>(p, g.fin, t);
 }
 
 template <typename T>
 __global__ void k_stage_batch_shifted(const StageParams *__restrict__ list, const int *__restrict__ ephase,
-                                      int sel) {
+                                      int sel, int n, const ForceSlot *__restrict__ fs) {
     const int e = blockIdx.y;
+    if (e >= n) {
+        if (blockIdx.x == 0 && threadIdx.x < 32) force_reduce_warp(fs[e - n], (int)threadIdx.x);
+        return;
+    }
     const StageParams &p = list[2 * e + (sel ^ ephase[e])];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
     stage_point_s<T>(p, t);
+    if (p.last) stage_finish_s<T, true>(p, *p.fin, t);
 }
 
 namespace launch {
 
-cudaError_t stage_shifted(const StageParams &p, int store, cudaStream_t s) {
-    const int b = 64, g = (p.along + b - 1) / b;
-    if (store == STORE_F32) k_stage_shifted<float><<<g, b, 0, s>>>(p);
-    else k_stage_shifted<__half><<<g, b, 0, s>>>(p);
-    return cudaGetLastError();
-}
-
-cudaError_t stage_group_shifted(const StageGroup &g, int store, cudaStream_t s) {
-    const dim3 grid((g.max_along + 63) / 64, g.n);
-    if (store == STORE_F32) k_stage_group_shifted<float><<<grid, 64, 0, s>>>(g);
-    else k_stage_group_shifted<__half><<<grid, 64, 0, s>>>(g);
+cudaError_t stage_group_shifted(const StageGroup &g, int store, bool collide, cudaStream_t s) {
+    const dim3 grid((g.max_along + 63) / 64, g.n + (g.nfs ? 1 : 0));
+    if (store == STORE_F32) {
+        if (collide) k_stage_group_shifted<float, true><<<grid, 64, 0, s>>>(g);
+        else k_stage_group_shifted<float, false><<<grid, 64, 0, s>>>(g);
+    } else {
+        if (collide) k_stage_group_shifted<__half, true><<<grid, 64, 0, s>>>(g);
+        else k_stage_group_shifted<__half, false><<<grid, 64, 0, s>>>(g);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, int max_along, int store,
-                                int sel, cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
-    const dim3 g((max_along + 63) / 64, n);
-    if (store == STORE_F32) k_stage_batch_shifted<float><<<g, 64, 0, s>>>(list, ephase, sel);
-    else k_stage_batch_shifted<__half><<<g, 64, 0, s>>>(list, ephase, sel);
+                                int sel, const ForceSlot *fs, int nfs, cudaStream_t s) {
+    if (n + nfs == 0) return cudaSuccess;
+    const dim3 g(std::max(1, (max_along + 63) / 64), n + nfs);
+    if (store == STORE_F32) k_stage_batch_shifted<float><<<g, 64, 0, s>>>(list, ephase, sel, n, fs);
+    else k_stage_batch_shifted<__half><<<g, 64, 0, s>>>(list, ephase, sel, n, fs);
     return cudaGetLastError();
 }
-
 
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s) {
     const dim3 b(64, 4);

@@ -435,6 +435,8 @@ struct StepParams {
     const int *seg_slot;      // [Ny][(Nx + 31) / 32]
 };
 
+struct FinishParams;
+
 struct StageParams {
     int Nx, Ny, pitch;
     long long plane;
@@ -454,6 +456,13 @@ struct StageParams {
     const double *bandm_prev;  // [3][nslots]
     const void *src;           // post-collision populations (periodic stages)
     double w[9];
+    // Finish in the same launch: the thread of a node whose last writer in
+    // the Boundary list is this entry (last[slot] == entry) computes the
+    // node's moments and collision right after the entry's BC. last is null
+    // when the case finishes its BC-written nodes in a separate launch.
+    const short *last;
+    int entry;
+    const FinishParams *fin;   // batches: the case's finish parameters (solo: by value)
 };
 
 struct FinishParams {
@@ -479,6 +488,14 @@ struct FinishParams {
 __device__ __forceinline__ int band_slot(const int *colbase, const int *rowbase, int i, int j) {
     const int c = colbase[i];
     return c >= 0 ? c + j : rowbase[j] + i;
+}
+
+// The node that thread t of a Boundary entry works on (bc_apply's mapping:
+// periodic entries enumerate both edge lines, t < along / 2 the first).
+__device__ __forceinline__ int2 stage_node(int kind, int Nx, int Ny, int index, int t) {
+    if (kind == BC_PERIODIC_X) return make_int2(t < Ny ? 0 : Nx - 1, t % Ny);
+    if (kind == BC_PERIODIC_Y) return make_int2(t % Nx, t < Nx ? 0 : Ny - 1);
+    return bc_is_column(kind) ? make_int2(index, t) : make_int2(t, index);
 }
 
 }  // namespace lbm

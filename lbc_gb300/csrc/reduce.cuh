@@ -15,6 +15,51 @@ __device__ __forceinline__ void warp_reduce2(double &a, double &b, bool link) {
     }
 }
 
+// One case's force from its segment partials, by one full warp (every lane
+// calls it): the sum of partials[2 t], partials[2 t + 1] over t in [t0, t1)
+// into out[0..1] and the next history slot. The order is fixed and does not
+// depend on the launch: 256 strided running sums (sum v holds t = t0 + v +
+// 256 k in increasing k; lane l keeps v = l + 32 q, q = 0..7, eight loads in
+// flight), each group of 32 folded by a shuffle tree, the 8 folds added in q
+// order.
+template <class Slot>
+__device__ __forceinline__ void force_reduce_warp(const Slot &fs, int lane) {
+    double a[8], b[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) { a[q] = 0.0; b[q] = 0.0; }
+    for (int base = fs.t0; base < fs.t1; base += 256) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int t = base + 32 * q + lane;
+            if (t < fs.t1) {
+                a[q] += fs.partials[2 * (size_t)t];
+                b[q] += fs.partials[2 * (size_t)t + 1];
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a[q] += __shfl_down_sync(0xffffffffu, a[q], o);
+            b[q] += __shfl_down_sync(0xffffffffu, b[q], o);
+        }
+    }
+    if (lane != 0) return;
+    double ra = 0.0, rb = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) { ra += a[q]; rb += b[q]; }
+    fs.out[0] = ra;
+    fs.out[1] = rb;
+    if (fs.hist) {
+        const unsigned long long k = *fs.hist_count;
+        const int slot = (int)(k % (unsigned long long)fs.hist_cap);
+        fs.hist[2 * slot] = ra;
+        fs.hist[2 * slot + 1] = rb;
+        *fs.hist_count = k + 1ull;
+    }
+}
+
 // Deterministic block + grid reduction of two doubles. Every thread of every
 // block must call it. Blocks write partials; the last block to arrive sums them
 // in block order and writes out[0..1] (and, when a history ring is given, the

@@ -60,11 +60,11 @@ __device__ __forceinline__ void bc_regularized_s(A &a, const float w[9], int ib,
 }
 
 // One point t of one Boundary entry (the FP32 counterpart of bc_apply).
-// val1 / val2 are lbc's FP64 value arrays; pressure values enter as
+// v1 / v2 are the entry's FP64 values at t; pressure values enter as
 // rho - 1, formed in FP64.
 template <class A>
 __device__ __forceinline__ void bc_apply_s(A &a, const float w[9], int kind, int Nx, int Ny, int index, int t,
-                                           const double *val1, const double *val2) {
+                                           double v1, double v2) {
     if (kind == BC_PERIODIC_X || kind == BC_PERIODIC_Y) {
         // src/bc/periodic_x.c:19-50 / periodic_y.c:19-50
         if (kind == BC_PERIODIC_X) {
@@ -106,7 +106,7 @@ __device__ __forceinline__ void bc_apply_s(A &a, const float w[9], int kind, int
     const float c23 = 2.0f / 3.0f, c16 = 1.0f / 6.0f;
     switch (kind) {
     case BC_VEL_IN_ZH: {  // src/bc/velocity_inlet.c:25-39
-        const float U = (float)val1[t], V = (float)val2[t];
+        const float U = (float)v1, V = (float)v2;
         const float g0 = a.get(ib, jb, 0), g2 = a.get(ib, jb, 2), g3 = a.get(ib, jb, 3),
                     g4 = a.get(ib, jb, 4), g6 = a.get(ib, jb, 6), g7 = a.get(ib, jb, 7);
         const float r = (1.0f + (g0 + g2 + g4 + 2.0f * (g3 + g6 + g7))) / (1.0f - U);
@@ -115,7 +115,7 @@ __device__ __forceinline__ void bc_apply_s(A &a, const float w[9], int kind, int
         a.set(ib, jb, 8, g6 + c16 * r * U + 0.5f * (g2 - g4) - 0.5f * r * V);
     } break;
     case BC_VEL_OUT_ZH: {  // src/bc/velocity_outlet.c:25-39
-        const float U = (float)val1[t], V = (float)val2[t];
+        const float U = (float)v1, V = (float)v2;
         const float g0 = a.get(ib, jb, 0), g2 = a.get(ib, jb, 2), g4 = a.get(ib, jb, 4),
                     g1 = a.get(ib, jb, 1), g5 = a.get(ib, jb, 5), g8 = a.get(ib, jb, 8);
         const float r = (1.0f + (g0 + g2 + g4 + 2.0f * (g1 + g5 + g8))) / (1.0f + U);
@@ -124,7 +124,7 @@ __device__ __forceinline__ void bc_apply_s(A &a, const float w[9], int kind, int
         a.set(ib, jb, 7, g5 + 0.5f * (g2 - g4) - c16 * r * U - 0.5f * r * V);
     } break;
     case BC_VEL_TOP_ZH: {  // src/bc/velocity_top.c:25-39
-        const float U = (float)val1[t], V = (float)val2[t];
+        const float U = (float)v1, V = (float)v2;
         const float g0 = a.get(ib, jb, 0), g1 = a.get(ib, jb, 1), g2 = a.get(ib, jb, 2),
                     g3 = a.get(ib, jb, 3), g5 = a.get(ib, jb, 5), g6 = a.get(ib, jb, 6);
         const float r = (1.0f + (g0 + g1 + g3 + 2.0f * (g2 + g5 + g6))) / (1.0f + V);
@@ -133,7 +133,7 @@ __device__ __forceinline__ void bc_apply_s(A &a, const float w[9], int kind, int
         a.set(ib, jb, 8, g6 - 0.5f * (g1 - g3) + 0.5f * r * U - c16 * r * V);
     } break;
     case BC_VEL_BOT_ZH: {  // src/bc/velocity_bottom.c:25-39 (second write to 7 kept, :39)
-        const float U = (float)val1[t], V = (float)val2[t];
+        const float U = (float)v1, V = (float)v2;
         const float g0 = a.get(ib, jb, 0), g1 = a.get(ib, jb, 1), g3 = a.get(ib, jb, 3),
                     g4 = a.get(ib, jb, 4), g7 = a.get(ib, jb, 7), g8 = a.get(ib, jb, 8);
         const float r = (1.0f + (g0 + g1 + g3 + 2.0f * (g4 + g7 + g8))) / (1.0f - V);
@@ -142,7 +142,7 @@ __device__ __forceinline__ void bc_apply_s(A &a, const float w[9], int kind, int
         a.set(ib, jb, 7, g8 + 0.5f * (g1 - g3) - 0.5f * r * U + c16 * r * V);
     } break;
     case BC_PRES_IN_ZH: {  // src/bc/pressure_inlet.c:25-39
-        const float R = (float)val1[t], dR = (float)(val1[t] - 1.0);
+        const float R = (float)v1, dR = (float)(v1 - 1.0);
         const float g0 = a.get(ib, jb, 0), g2 = a.get(ib, jb, 2), g4 = a.get(ib, jb, 4),
                     g3 = a.get(ib, jb, 3), g6 = a.get(ib, jb, 6), g7 = a.get(ib, jb, 7);
         // U = 1 - (1 + G) / R = (dR - G) / R
@@ -153,7 +153,7 @@ __device__ __forceinline__ void bc_apply_s(A &a, const float w[9], int kind, int
         a.set(ib, jb, 8, g6 + c16 * R * U + 0.5f * (g2 - g4) - 0.5f * R * V);
     } break;
     case BC_PRES_OUT_ZH: {  // src/bc/pressure_outlet.c:25-39
-        const float R = (float)val1[t], dR = (float)(val1[t] - 1.0);
+        const float R = (float)v1, dR = (float)(v1 - 1.0);
         const float g0 = a.get(ib, jb, 0), g2 = a.get(ib, jb, 2), g4 = a.get(ib, jb, 4),
                     g1 = a.get(ib, jb, 1), g5 = a.get(ib, jb, 5), g8 = a.get(ib, jb, 8);
         // U = (1 + G) / R - 1 = (G - dR) / R
@@ -171,14 +171,14 @@ __device__ __forceinline__ void bc_apply_s(A &a, const float w[9], int kind, int
 #pragma unroll
         for (int k = 0; k < 9; k++) a.set(ib, jb, k, a.get(ib - 1, jb, k));
         break;
-    case BC_VEL_IN_REG: bc_regularized_s(a, w, ib, jb, ib + 1, jb, false, (float)val1[t], (float)val2[t]); break;
-    case BC_VEL_OUT_REG: bc_regularized_s(a, w, ib, jb, ib - 1, jb, false, (float)val1[t], (float)val2[t]); break;
-    case BC_VEL_BOT_REG: bc_regularized_s(a, w, ib, jb, ib, jb + 1, false, (float)val1[t], (float)val2[t]); break;
-    case BC_VEL_TOP_REG: bc_regularized_s(a, w, ib, jb, ib, jb - 1, false, (float)val1[t], (float)val2[t]); break;
-    case BC_PRES_IN_REG: bc_regularized_s(a, w, ib, jb, ib + 1, jb, true, (float)(val1[t] - 1.0), 0.f); break;
-    case BC_PRES_OUT_REG: bc_regularized_s(a, w, ib, jb, ib - 1, jb, true, (float)(val1[t] - 1.0), 0.f); break;
-    case BC_PRES_BOT_REG: bc_regularized_s(a, w, ib, jb, ib, jb + 1, true, (float)(val1[t] - 1.0), 0.f); break;
-    case BC_PRES_TOP_REG: bc_regularized_s(a, w, ib, jb, ib, jb - 1, true, (float)(val1[t] - 1.0), 0.f); break;
+    case BC_VEL_IN_REG: bc_regularized_s(a, w, ib, jb, ib + 1, jb, false, (float)v1, (float)v2); break;
+    case BC_VEL_OUT_REG: bc_regularized_s(a, w, ib, jb, ib - 1, jb, false, (float)v1, (float)v2); break;
+    case BC_VEL_BOT_REG: bc_regularized_s(a, w, ib, jb, ib, jb + 1, false, (float)v1, (float)v2); break;
+    case BC_VEL_TOP_REG: bc_regularized_s(a, w, ib, jb, ib, jb - 1, false, (float)v1, (float)v2); break;
+    case BC_PRES_IN_REG: bc_regularized_s(a, w, ib, jb, ib + 1, jb, true, (float)(v1 - 1.0), 0.f); break;
+    case BC_PRES_OUT_REG: bc_regularized_s(a, w, ib, jb, ib - 1, jb, true, (float)(v1 - 1.0), 0.f); break;
+    case BC_PRES_BOT_REG: bc_regularized_s(a, w, ib, jb, ib, jb + 1, true, (float)(v1 - 1.0), 0.f); break;
+    case BC_PRES_TOP_REG: bc_regularized_s(a, w, ib, jb, ib, jb - 1, true, (float)(v1 - 1.0), 0.f); break;
     default: break;
     }
 }

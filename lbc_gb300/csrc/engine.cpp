@@ -82,7 +82,13 @@ Solver::Solver(const CaseDesc &d) : d_(d) {
     esize_ = d_.store == STORE_F64 ? 8 : (d_.store == STORE_F32 ? 4 : 2);
     pitch_ = (d_.Nx + 63) / 64 * 64;
     plane_ = (long long)pitch_ * d_.Ny;
-    if (!check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate")) return;
+    // Highest stream priority: a case's own work is short (setup, a run
+    // alone, results), and when a server admits it while batches run, its
+    // setup kernels take the next free SMs instead of waiting for a gap
+    // between the batches' steps.
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (!check_cuda(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking, hi), "cudaStreamCreate")) return;
     use_retaining_pool();
     if (!build_geometry()) return;
     ok_ = true;
@@ -869,7 +875,7 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
         CK(launch::step_shifted(fast_params(p), d_.store, has_flags_, collide, block_, s));
     }
     if (groups_.empty()) {
-        if (has_mem_) CK(launch::force_reduce(d_force_slot_, 1, s));
+        if (has_mem_) CK(launch::force_reduce(d_force_slot_, 1, true, s));
         return true;
     }
     // The force (from the bulk kernel's partials) rides in the first stage
@@ -887,7 +893,7 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
         sg.fin = f;
         sg.fs = d_force_slot_;
         sg.nfs = (gi == 0 && has_mem_) ? 1 : 0;
-        CK(launch::stage_group(sg, d_.store, collide, s));
+        CK(launch::stage_group(sg, d_.store, collide, gi == 0, s));
     }
     if (!fuse_) {
         if (d_.store == STORE_F64) CK(launch::finish_exact(f, collide, s));
@@ -1300,12 +1306,12 @@ bool Batch::launch_batched(int sel) {
                                       store_, wide_, any_force_, grid_, stream_));
     for (int s = 0; s < max_stages_; s++)
         CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], max_along_, store_, sel, d_force_,
-                               s == 0 ? nforce_ : 0, stream_));
+                               s == 0 ? nforce_ : 0, s == 0, stream_));
     if (nfin_) {
         if (store_ == STORE_F64) CK(launch::finish_batch_exact(d_fin_, d_phase_, d_fin_nodes_, nfin_, sel, stream_));
         else CK(launch::finish_batch_shifted(d_fin_, d_phase_, d_fin_nodes_, nfin_, sel, store_, stream_));
     }
-    if (nforce_ && max_stages_ == 0) CK(launch::force_reduce(d_force_, nforce_, stream_));
+    if (nforce_ && max_stages_ == 0) CK(launch::force_reduce(d_force_, nforce_, true, stream_));
     return true;
 }
 

@@ -103,7 +103,9 @@ namespace launch {
 cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block, cudaStream_t s);
 // collide: the finish of fused members applies the collision (false only in
 // the final step of a run, which leaves pre-collision populations).
-cudaError_t stage_group(const StageGroup &g, int store, bool collide, cudaStream_t s);
+// after_bulk (here, stage_batch and force_reduce): the previous launch in s is
+// a bulk step kernel; the launch overlaps its tail (pdl.cuh).
+cudaError_t stage_group(const StageGroup &g, int store, bool collide, bool after_bulk, cudaStream_t s);
 cudaError_t finish_exact(const FinishParams &p, bool collide, cudaStream_t s);
 cudaError_t collide_exact(const CollideParams &p, cudaStream_t s);
 cudaError_t collide_aos_exact(const CollideAosParams &p, cudaStream_t s);
@@ -129,19 +131,19 @@ int step_batch_exact_grid();
 // One level of a batch's Boundary lists (n entries); nfs > 0 adds one block
 // row per force slot fs[0 .. nfs).
 cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int max_along, int store,
-                        int sel, const ForceSlot *fs, int nfs, cudaStream_t s);
+                        int sel, const ForceSlot *fs, int nfs, bool after_bulk, cudaStream_t s);
 cudaError_t finish_batch_exact(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
                                int sel, cudaStream_t s);
-cudaError_t force_reduce(const ForceSlot *slots, int n, cudaStream_t s);
+cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStream_t s);
 
 // shifted storage (kernels_shifted.cu)
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
                          cudaStream_t s);
 cudaError_t finish_shifted(const FinishParams &p, int store, bool collide, cudaStream_t s);
 // Edge BCs of shifted storage in FP32 (launch::stage_group / stage_batch dispatch here).
-cudaError_t stage_group_shifted(const StageGroup &g, int store, bool collide, cudaStream_t s);
+cudaError_t stage_group_shifted(const StageGroup &g, int store, bool collide, bool after_bulk, cudaStream_t s);
 cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, int max_along, int store,
-                                int sel, const ForceSlot *fs, int nfs, cudaStream_t s);
+                                int sel, const ForceSlot *fs, int nfs, bool after_bulk, cudaStream_t s);
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s);
 // wide: some case has 9 * plane >= 2^31 elements (64-bit element offsets).
 // force: some case has a body force (the forced kernel form serves all cases).

@@ -19,6 +19,7 @@
 
 #include "kernels.h"
 #include "lbm_device.cuh"
+#include "pdl.cuh"
 #include "reduce.cuh"
 
 namespace lbm {
@@ -128,6 +129,7 @@ __device__ __forceinline__ void step_node_exact(const StepParams &p, int i, int 
 
 template <bool FLAGS, bool COLLIDE>
 __global__ void __launch_bounds__(256) k_step_exact(const StepParams p) {
+    pdl_launch_dependents();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     double mfx = 0.0, mfy = 0.0;
@@ -147,6 +149,7 @@ __global__ void __launch_bounds__(256) k_step_batch_exact(const StepParams *__re
                                                           const int *__restrict__ phase,
                                                           const int4 *__restrict__ tiles, int ntiles,
                                                           int sel, int tws) {
+    pdl_launch_dependents();
     const int tx = threadIdx.x & ((1 << tws) - 1), ty = threadIdx.x >> tws;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int4 td = tiles[t];
@@ -166,43 +169,51 @@ __global__ void __launch_bounds__(256) k_step_batch_exact(const StepParams *__re
 
 // ---------------------------------------------------------------- edge BCs
 
+// The band as lbc's BC functions see it. Lookups of the thread's own node and
+// of its interior neighbour come from the thread's preload (StagePre).
 template <typename T> struct BandAccessor {
     const StageParams &p;
-    __device__ int slot(int i, int j) const { return band_slot(p.colbase, p.rowbase, i, j); }
+    const StagePre &c;
+    __device__ int slot(int i, int j) const {
+        if (i == c.ij.x && j == c.ij.y) return c.slot;
+        if (i == c.nij.x && j == c.nij.y) return c.nslot;
+        return band_slot(p.colbase, p.rowbase, i, j);
+    }
+    __device__ bool nb(int i, int j) const { return i == c.nij.x && j == c.nij.y; }
     __device__ double get(int i, int j, int k) const { return p.bandf[(size_t)k * p.nslots + slot(i, j)]; }
     __device__ void set(int i, int j, int k, double v) const { p.bandf[(size_t)k * p.nslots + slot(i, j)] = v; }
-    __device__ double rho(int i, int j) const { return p.bandm_prev[slot(i, j)]; }
-    __device__ double ux(int i, int j) const { return p.bandm_prev[(size_t)p.nslots + slot(i, j)]; }
-    __device__ double uy(int i, int j) const { return p.bandm_prev[2 * (size_t)p.nslots + slot(i, j)]; }
+    __device__ double rho(int i, int j) const { return nb(i, j) ? c.nrho : p.bandm_prev[slot(i, j)]; }
+    __device__ double ux(int i, int j) const {
+        return nb(i, j) ? c.nux : p.bandm_prev[(size_t)p.nslots + slot(i, j)];
+    }
+    __device__ double uy(int i, int j) const {
+        return nb(i, j) ? c.nuy : p.bandm_prev[2 * (size_t)p.nslots + slot(i, j)];
+    }
     __device__ double post(int i, int j, int k) const {
         return Store<T>::to_f64(((const T *)p.src)[k * p.plane + (long long)j * p.pitch + i], p.w[k]);
     }
-    __device__ bool solid(int i, int j) const { return (p.flags[(long long)j * p.pitch + i] & NF_SOLID) != 0; }
+    __device__ bool solid(int i, int j) const {
+        if (i == c.ij.x && j == c.ij.y) return c.solid;
+        return (p.flags[(long long)j * p.pitch + i] & NF_SOLID) != 0;
+    }
 };
 
-// One entry of lbc's Boundary list (src/core/main_lbm.c:49-58), applied to the
-// pre-collision f_new of the band nodes. Entries run as separate launches in list
-// order, so each sees the writes of the previous ones, as in lbc.
+// One entry of lbc's Boundary list (src/core/main_lbm.c:49-58) at point t,
+// applied to the pre-collision f_new of the band nodes, after the preload c.
+// Entries in different launches see the writes of the earlier ones, as in lbc.
 template <typename T>
-__device__ __forceinline__ void stage_point(const StageParams &p, int t) {
-    BandAccessor<T> a{p};
-    if (p.imp && p.kind == BC_VEL_BOT_REG && p.imp[(size_t)IMP_ACTIVE * p.along + t] != 0.0 &&
-        !a.solid(t, p.index)) {
-        // Impedance wall on this node: the regularized bottom BC with the
-        // normal velocity from the node's mass-spring-damper.
-        const double vn = impedance_step(p.imp, p.along, p.imp_nf, t, a.rho(t, p.index + 1),
-                                         p.imp_alpha, p.imp_cos, p.imp_sin, p.imp_wcos,
-                                         p.imp_wsin, p.imp_windowed);
-        bc_regularized(a, p.w, t, p.index, t, p.index + 1, false, p.val1[t], -vn);
+__device__ __forceinline__ void stage_point(const StageParams &p, const StagePre &c, int t) {
+    BandAccessor<T> a{p, c};
+    if (c.imp) {
+        bc_regularized(a, p.w, t, p.index, t, p.index + 1, false, c.v1, c.v2);
         return;
     }
-    bc_apply(a, p.w, p.kind, p.Nx, p.Ny, p.index, t, p.val1, p.val2);
+    bc_apply(a, p.w, p.kind, p.Nx, p.Ny, p.index, t, c.v1, c.v2);
 }
 
-// Moments and collision of every node an edge BC wrote.
+// Moments and collision of a node an edge BC wrote (band slot `slot`).
 template <bool COLLIDE>
-__device__ __forceinline__ void finish_node_exact(const FinishParams &p, int2 ij) {
-    const int slot = band_slot(p.colbase, p.rowbase, ij.x, ij.y);
+__device__ __forceinline__ void finish_node_exact(const FinishParams &p, int2 ij, int slot) {
     double f[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) f[k] = p.bandf[(size_t)k * p.nslots + slot];
@@ -223,28 +234,25 @@ __device__ __forceinline__ void finish_node_exact(const FinishParams &p, int2 ij
     for (int k = 0; k < 9; k++) D[k * p.plane + node] = f[k];
 }
 
-// Finish of a node by the Boundary entry that wrote it last (StageParams.last).
-template <bool COLLIDE>
-__device__ __forceinline__ void stage_finish(const StageParams &p, const FinishParams &f, int t) {
-    const int2 ij = stage_node(p.kind, p.Nx, p.Ny, p.index, t);
-    if (p.flags[(long long)ij.y * p.pitch + ij.x] & NF_SOLID) return;
-    if (p.last[band_slot(p.colbase, p.rowbase, ij.x, ij.y)] != p.entry) return;
-    finish_node_exact<COLLIDE>(f, ij);
-}
-
-// One group of Boundary entries of a case (blockIdx.y = member), each fused
-// member finishing its nodes; row n reduces the case's force.
+// One group of Boundary entries of a case (blockIdx.y = member); a member
+// thread finishes its node when its entry is the node's last writer
+// (StageParams.last); row n reduces the case's force. Launched right behind
+// the bulk kernel (pdl.cuh): everything up to pdl_wait() reads only what the
+// bulk kernel does not write.
 template <typename T, bool COLLIDE>
 __global__ void k_stage_group(const StageGroup g) {
     if ((int)blockIdx.y >= g.n) {
+        pdl_wait();
         if (blockIdx.x == 0 && threadIdx.x < 32) force_reduce_warp(*g.fs, (int)threadIdx.x);
         return;
     }
     const StageParams &p = g.p[blockIdx.y];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
-    stage_point<T>(p, t);
-    if (p.last) stage_finish<COLLIDE>(p, g.fin, t);
+    const StagePre c = stage_preload(p, t);
+    pdl_wait();
+    stage_point<T>(p, c, t);
+    if (c.fin) finish_node_exact<COLLIDE>(g.fin, c.ij, c.slot);
 }
 
 // Stage level of every case of a batch: blockIdx.y selects the case entry,
@@ -255,18 +263,22 @@ __global__ void k_stage_batch(const StageParams *__restrict__ list, const int *_
                               int sel, int n, const ForceSlot *__restrict__ fs) {
     const int e = blockIdx.y;
     if (e >= n) {
+        pdl_wait();
         if (blockIdx.x == 0 && threadIdx.x < 32) force_reduce_warp(fs[e - n], (int)threadIdx.x);
         return;
     }
     const StageParams &p = list[2 * e + (sel ^ ephase[e])];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
-    stage_point<T>(p, t);
-    if (p.last) stage_finish<true>(p, *p.fin, t);
+    const StagePre c = stage_preload(p, t);
+    pdl_wait();
+    stage_point<T>(p, c, t);
+    if (c.fin) finish_node_exact<true>(*p.fin, c.ij, c.slot);
 }
 
 // Per-case force of a step from its segment partials (one warp per case).
 __global__ void k_force_reduce(const ForceSlot *__restrict__ slots, int nslots) {
+    pdl_wait();
     const int c = blockIdx.x;
     if (c >= nslots) return;
     force_reduce_warp(slots[c], (int)threadIdx.x);
@@ -276,7 +288,8 @@ template <bool COLLIDE>
 __global__ void k_finish_exact(const FinishParams p) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.nw) return;
-    finish_node_exact<COLLIDE>(p, p.wnodes[t]);
+    const int2 ij = p.wnodes[t];
+    finish_node_exact<COLLIDE>(p, ij, band_slot(p.colbase, p.rowbase, ij.x, ij.y));
 }
 
 // BC-written nodes of every case of a batch: nodes[t] = (case, i, j).
@@ -285,7 +298,8 @@ __global__ void k_finish_batch_exact(const FinishParams *__restrict__ fp, const 
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int4 c = nodes[t];
-    finish_node_exact<true>(fp[2 * c.x + (sel ^ phase[c.x])], make_int2(c.y, c.z));
+    const FinishParams &f = fp[2 * c.x + (sel ^ phase[c.x])];
+    finish_node_exact<true>(f, make_int2(c.y, c.z), band_slot(f.colbase, f.rowbase, c.y, c.z));
 }
 
 // In-place collision with the stored rho/u/v (src/core/collision.c:18-40); used
@@ -525,7 +539,7 @@ __global__ void k_aos_bc(AosArgs a, int kind, int index, int along, const double
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= along) return;
     AosAccessor acc{a};
-    bc_apply(acc, a.w, kind, a.Nx, a.Ny, index, t, val1, val2);
+    bc_apply(acc, a.w, kind, a.Nx, a.Ny, index, t, val1 ? val1[t] : 0.0, val2 ? val2[t] : 0.0);
 }
 
 // ---- Mei initialisation (src/core/mei_initialization.c:50-127) on AoS arrays.
@@ -597,13 +611,12 @@ cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block
 }
 
 // Edge kernels are FP64 and short: 32-thread blocks spread a line over many SMs.
-cudaError_t stage_group(const StageGroup &g, int store, bool collide, cudaStream_t s) {
+cudaError_t stage_group(const StageGroup &g, int store, bool collide, bool after_bulk, cudaStream_t s) {
     if (g.n < 1 || g.n > kStageGroupMax || (g.nfs && !g.fs)) return cudaErrorInvalidValue;
-    if (store != STORE_F64) return stage_group_shifted(g, store, collide, s);
+    if (store != STORE_F64) return stage_group_shifted(g, store, collide, after_bulk, s);
     const dim3 grid((g.max_along + 31) / 32, g.n + (g.nfs ? 1 : 0));
-    if (collide) k_stage_group<double, true><<<grid, 32, 0, s>>>(g);
-    else k_stage_group<double, false><<<grid, 32, 0, s>>>(g);
-    return cudaGetLastError();
+    if (collide) return launch_follower(after_bulk, k_stage_group<double, true>, grid, dim3(32), s, g);
+    return launch_follower(after_bulk, k_stage_group<double, false>, grid, dim3(32), s, g);
 }
 
 cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 *tiles, int ntiles,
@@ -622,12 +635,12 @@ cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 
 int step_batch_exact_grid() { return 1 << 30; }
 
 cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int max_along, int store,
-                        int sel, const ForceSlot *fs, int nfs, cudaStream_t s) {
+                        int sel, const ForceSlot *fs, int nfs, bool after_bulk, cudaStream_t s) {
     if (n + nfs == 0) return cudaSuccess;
-    if (store != STORE_F64) return stage_batch_shifted(list, ephase, n, max_along, store, sel, fs, nfs, s);
+    if (store != STORE_F64)
+        return stage_batch_shifted(list, ephase, n, max_along, store, sel, fs, nfs, after_bulk, s);
     const dim3 g(std::max(1, (max_along + 31) / 32), n + nfs);
-    k_stage_batch<double><<<g, 32, 0, s>>>(list, ephase, sel, n, fs);
-    return cudaGetLastError();
+    return launch_follower(after_bulk, k_stage_batch<double>, g, dim3(32), s, list, ephase, sel, n, fs);
 }
 
 cudaError_t finish_batch_exact(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
@@ -637,10 +650,9 @@ cudaError_t finish_batch_exact(const FinishParams *fp, const int *phase, const i
     return cudaGetLastError();
 }
 
-cudaError_t force_reduce(const ForceSlot *slots, int n, cudaStream_t s) {
+cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_force_reduce<<<n, 32, 0, s>>>(slots, n);
-    return cudaGetLastError();
+    return launch_follower(after_bulk, k_force_reduce, dim3(n), dim3(32), s, slots, n);
 }
 
 cudaError_t finish_exact(const FinishParams &p, bool collide, cudaStream_t s) {

@@ -12,6 +12,7 @@
 #include "bc_shifted.cuh"
 #include "kernels.h"
 #include "lbm_device.cuh"
+#include "pdl.cuh"
 #include "reduce.cuh"
 
 namespace lbm {
@@ -295,17 +296,16 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
 // solid, link, stale slot, band or BC node): pair loads where the pull sources
 // are adjacent (c_x = 0), a pair and a single load otherwise (c_x = +-1), packed
 // FP32 arithmetic, pair stores. im = source column of i0 - 1, ip2 of i0 + 2
-// (wrapped or clamped like the per-node path).
-template <typename T, typename I, bool COLLIDE, bool FORCE>
-__device__ __forceinline__ void step_pair_shifted(const FastStepParams &fp, int i0, int j, int im, int ip2,
-                                                  int jm, int jp) {
-    const StepParams &p = fp.s;
+// (wrapped or clamped like the per-node path), so every load is in bounds
+// whatever the nodes' flags say.
+template <typename T, typename I>
+__device__ __forceinline__ void load_pair_shifted(const StepParams &p, int i0, int j, int im, int ip2, int jm,
+                                                  int jp, float2 g[9]) {
     const T *S = (const T *)p.src;
-    T *Dst = (T *)p.dst;
     const I pl = (I)p.plane;
     const I r0 = (I)j * (I)p.pitch + (I)i0, rm = (I)jm * (I)p.pitch, rp = (I)jp * (I)p.pitch;
     const I m0 = rm + (I)i0, p0 = rp + (I)i0;
-    float2 g[9], a;
+    float2 a;
     g[0] = SV<T>::ld2(S + r0);
     a = SV<T>::ld2(S + pl + r0);
     g[1] = make_float2(SV<T>::ld(S + pl + (r0 - (I)i0 + (I)im)), a.x);
@@ -321,6 +321,14 @@ __device__ __forceinline__ void step_pair_shifted(const FastStepParams &fp, int 
     g[7] = make_float2(a.y, SV<T>::ld(S + 7 * pl + rp + (I)ip2));
     a = SV<T>::ld2(S + 8 * pl + p0);
     g[8] = make_float2(SV<T>::ld(S + 8 * pl + rp + (I)im), a.x);
+}
+
+template <typename T, typename I, bool COLLIDE, bool FORCE>
+__device__ __forceinline__ void collide_store_pair_shifted(const FastStepParams &fp, int i0, int j, float2 g[9]) {
+    const StepParams &p = fp.s;
+    T *Dst = (T *)p.dst;
+    const I pl = (I)p.plane;
+    const I r0 = (I)j * (I)p.pitch + (I)i0;
     float2 dr, rho, ux, uy, Jx, Jy, jx, jy;
     moments_v<float2>(g, v_splat<float2>(fp.hFxf), v_splat<float2>(fp.hFyf), dr, rho, ux, uy, Jx, Jy, jx, jy);
     const size_t dn = (size_t)j * (size_t)p.Nx + (size_t)i0;
@@ -335,27 +343,31 @@ __device__ __forceinline__ void step_pair_shifted(const FastStepParams &fp, int 
 }
 
 // The nodes (i0, i0 + 1) of row j: the pair path when both exist and neither
-// is special, else each node on its own. ax, ay: the two nodes' wall-link force
-// terms (node i0 first), link: either has wall links.
+// is special, else each node on its own. The pair's loads are issued together
+// with the load of its flag words (not after them), so the common case waits
+// for memory once; the per-node path, taken by the few special nodes, loads
+// again. ax, ay: the two nodes' wall-link force terms (node i0 first), link:
+// either has wall links.
 template <typename T, typename I, bool FLAGS, bool COLLIDE, bool FORCE>
 __device__ __forceinline__ void step_two_shifted(const FastStepParams &fp, int i0, int j, double &ax,
                                                  double &ay, bool &link) {
     const StepParams &p = fp.s;
     const bool two = i0 + 1 < p.Nx;
-    bool fast = two;
-    if (FLAGS && two) {
-        const uint32_t f2 = *(const uint32_t *)(p.flags + ((I)j * (I)p.pitch + (I)i0));
-        constexpr uint32_t kSlow = NF_SPECIAL_MASK | NF_SOLID | NF_BAND | NF_BCW | NF_LINKS;
-        fast = ((f2 | (f2 >> 16)) & kSlow) == 0;
-    }
-    if (fast) {
+    if (two) {
+        uint32_t f2 = 0;
+        if (FLAGS) f2 = *(const uint32_t *)(p.flags + ((I)j * (I)p.pitch + (I)i0));
         int im = i0 - 1, ip2 = i0 + 2, jm = j - 1, jp = j + 1;
         if (p.px) { if (im < 0) im += p.Nx; if (ip2 >= p.Nx) ip2 -= p.Nx; }
         else { im = max(im, 0); ip2 = min(ip2, p.Nx - 1); }
         if (p.py) { if (jm < 0) jm += p.Ny; if (jp >= p.Ny) jp -= p.Ny; }
         else { jm = max(jm, 0); jp = min(jp, p.Ny - 1); }
-        step_pair_shifted<T, I, COLLIDE, FORCE>(fp, i0, j, im, ip2, jm, jp);
-        return;
+        float2 g[9];
+        load_pair_shifted<T, I>(p, i0, j, im, ip2, jm, jp, g);
+        constexpr uint32_t kSlow = NF_SPECIAL_MASK | NF_SOLID | NF_BAND | NF_BCW | NF_LINKS;
+        if (!FLAGS || ((f2 | (f2 >> 16)) & kSlow) == 0) {
+            collide_store_pair_shifted<T, I, COLLIDE, FORCE>(fp, i0, j, g);
+            return;
+        }
     }
     float mx = 0.f, my = 0.f;
     bool l = false;
@@ -378,6 +390,7 @@ __device__ __forceinline__ void step_two_shifted(const FastStepParams &fp, int i
 // (measured: FP16 135 -> 147 GLUPS on 4096^2).
 template <typename T, typename I, bool COLLIDE, bool FORCE>
 __global__ void __launch_bounds__(256, 5) k_step_shifted_plain(const FastStepParams fp) {
+    pdl_launch_dependents();
     const int i0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     double ax = 0.0, ay = 0.0;
@@ -390,6 +403,7 @@ __global__ void __launch_bounds__(256, 5) k_step_shifted_plain(const FastStepPar
 // blocks per SM (48 registers; the few spills are in the per-node path).
 template <typename T, typename I, bool COLLIDE, bool FORCE>
 __global__ void __launch_bounds__(256, 5) k_step_shifted_geo(const FastStepParams fp) {
+    pdl_launch_dependents();
     const StepParams &p = fp.s;
     const int i0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -408,6 +422,7 @@ __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepPar
                                                             const int *__restrict__ phase,
                                                             const int4 *__restrict__ tiles,
                                                             int ntiles, int sel, int tws) {
+    pdl_launch_dependents();
     const int tx = threadIdx.x & ((1 << tws) - 1), ty = threadIdx.x >> tws;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int4 td = tiles[t];
@@ -427,8 +442,7 @@ __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepPar
 }
 
 template <typename T, bool COLLIDE>
-__device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 ij) {
-    const int slot = band_slot(p.colbase, p.rowbase, ij.x, ij.y);
+__device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 ij, int slot) {
     float g[9], wf[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) {
@@ -460,7 +474,8 @@ template <typename T, bool COLLIDE>
 __global__ void k_finish_shifted(const FinishParams p) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.nw) return;
-    finish_node_shifted<T, COLLIDE>(p, p.wnodes[t]);
+    const int2 ij = p.wnodes[t];
+    finish_node_shifted<T, COLLIDE>(p, ij, band_slot(p.colbase, p.rowbase, ij.x, ij.y));
 }
 
 template <typename T>
@@ -469,7 +484,8 @@ __global__ void k_finish_batch_shifted(const FinishParams *__restrict__ fp, cons
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int4 c = nodes[t];
-    finish_node_shifted<T, true>(fp[2 * c.x + (sel ^ phase[c.x])], make_int2(c.y, c.z));
+    const FinishParams &f = fp[2 * c.x + (sel ^ phase[c.x])];
+    finish_node_shifted<T, true>(f, make_int2(c.y, c.z), band_slot(f.colbase, f.rowbase, c.y, c.z));
 }
 
 // In-place collision of shifted populations with the stored (FP64) rho/u/v:
@@ -516,57 +532,59 @@ __global__ void k_collide_shifted(const CollideParams p) {
 // FP64). The impedance wall's mass-spring-damper state and DFT stay FP64.
 template <typename T> struct BandAccessorS {
     const StageParams &p;
-    __device__ int slot(int i, int j) const { return band_slot(p.colbase, p.rowbase, i, j); }
+    const StagePre &c;
+    __device__ int slot(int i, int j) const {
+        if (i == c.ij.x && j == c.ij.y) return c.slot;
+        if (i == c.nij.x && j == c.nij.y) return c.nslot;
+        return band_slot(p.colbase, p.rowbase, i, j);
+    }
+    __device__ bool nb(int i, int j) const { return i == c.nij.x && j == c.nij.y; }
+    __device__ double m(int q, int i, int j) const { return p.bandm_prev[(size_t)q * p.nslots + slot(i, j)]; }
     __device__ float get(int i, int j, int k) const { return p.bandg[(size_t)k * p.nslots + slot(i, j)]; }
     __device__ void set(int i, int j, int k, float v) const { p.bandg[(size_t)k * p.nslots + slot(i, j)] = v; }
-    __device__ float drho(int i, int j) const { return (float)(p.bandm_prev[slot(i, j)] - 1.0); }
-    __device__ double rho64(int i, int j) const { return p.bandm_prev[slot(i, j)]; }
-    __device__ float ux(int i, int j) const { return (float)p.bandm_prev[(size_t)p.nslots + slot(i, j)]; }
-    __device__ float uy(int i, int j) const { return (float)p.bandm_prev[2 * (size_t)p.nslots + slot(i, j)]; }
+    __device__ float drho(int i, int j) const { return (float)((nb(i, j) ? c.nrho : m(0, i, j)) - 1.0); }
+    __device__ double rho64(int i, int j) const { return nb(i, j) ? c.nrho : m(0, i, j); }
+    __device__ float ux(int i, int j) const { return (float)(nb(i, j) ? c.nux : m(1, i, j)); }
+    __device__ float uy(int i, int j) const { return (float)(nb(i, j) ? c.nuy : m(2, i, j)); }
     __device__ float post(int i, int j, int k) const {
         return SV<T>::ld_plain((const T *)p.src + k * p.plane + (long long)j * p.pitch + i);
     }
-    __device__ bool solid(int i, int j) const { return (p.flags[(long long)j * p.pitch + i] & NF_SOLID) != 0; }
+    __device__ bool solid(int i, int j) const {
+        if (i == c.ij.x && j == c.ij.y) return c.solid;
+        return (p.flags[(long long)j * p.pitch + i] & NF_SOLID) != 0;
+    }
 };
 
-// One point of one Boundary entry (src/core/main_lbm.c:49-58), as stage_point
-// in kernels_exact.cu.
+// One point of one Boundary entry (src/core/main_lbm.c:49-58) after its
+// preload, as stage_point in kernels_exact.cu.
 template <typename T>
-__device__ __forceinline__ void stage_point_s(const StageParams &p, int t) {
-    BandAccessorS<T> a{p};
+__device__ __forceinline__ void stage_point_s(const StageParams &p, const StagePre &c, int t) {
+    BandAccessorS<T> a{p, c};
     float w[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) w[k] = (float)p.w[k];
-    if (p.imp && p.kind == BC_VEL_BOT_REG && p.imp[(size_t)IMP_ACTIVE * p.along + t] != 0.0 &&
-        !a.solid(t, p.index)) {
-        const double vn = impedance_step(p.imp, p.along, p.imp_nf, t, a.rho64(t, p.index + 1), p.imp_alpha,
-                                         p.imp_cos, p.imp_sin, p.imp_wcos, p.imp_wsin, p.imp_windowed);
-        bc_regularized_s(a, w, t, p.index, t, p.index + 1, false, (float)p.val1[t], (float)(-vn));
+    if (c.imp) {
+        bc_regularized_s(a, w, t, p.index, t, p.index + 1, false, (float)c.v1, (float)c.v2);
         return;
     }
-    bc_apply_s(a, w, p.kind, p.Nx, p.Ny, p.index, t, p.val1, p.val2);
+    bc_apply_s(a, w, p.kind, p.Nx, p.Ny, p.index, t, c.v1, c.v2);
 }
 
-// Finish of a node by the Boundary entry that wrote it last (StageParams.last).
-template <typename T, bool COLLIDE>
-__device__ __forceinline__ void stage_finish_s(const StageParams &p, const FinishParams &f, int t) {
-    const int2 ij = stage_node(p.kind, p.Nx, p.Ny, p.index, t);
-    if (p.flags[(long long)ij.y * p.pitch + ij.x] & NF_SOLID) return;
-    if (p.last[band_slot(p.colbase, p.rowbase, ij.x, ij.y)] != p.entry) return;
-    finish_node_shifted<T, COLLIDE>(f, ij);
-}
-
+// As k_stage_group / k_stage_batch in kernels_exact.cu.
 template <typename T, bool COLLIDE>
 __global__ void k_stage_group_shifted(const StageGroup g) {
     if ((int)blockIdx.y >= g.n) {
+        pdl_wait();
         if (blockIdx.x == 0 && threadIdx.x < 32) force_reduce_warp(*g.fs, (int)threadIdx.x);
         return;
     }
     const StageParams &p = g.p[blockIdx.y];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
-    stage_point_s<T>(p, t);
-    if (p.last) stage_finish_s<T, COLLIDE>(p, g.fin, t);
+    const StagePre c = stage_preload(p, t);
+    pdl_wait();
+    stage_point_s<T>(p, c, t);
+    if (c.fin) finish_node_shifted<T, COLLIDE>(g.fin, c.ij, c.slot);
 }
 
 template <typename T>
@@ -574,37 +592,38 @@ __global__ void k_stage_batch_shifted(const StageParams *__restrict__ list, cons
                                       int sel, int n, const ForceSlot *__restrict__ fs) {
     const int e = blockIdx.y;
     if (e >= n) {
+        pdl_wait();
         if (blockIdx.x == 0 && threadIdx.x < 32) force_reduce_warp(fs[e - n], (int)threadIdx.x);
         return;
     }
     const StageParams &p = list[2 * e + (sel ^ ephase[e])];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
-    stage_point_s<T>(p, t);
-    if (p.last) stage_finish_s<T, true>(p, *p.fin, t);
+    const StagePre c = stage_preload(p, t);
+    pdl_wait();
+    stage_point_s<T>(p, c, t);
+    if (c.fin) finish_node_shifted<T, true>(*p.fin, c.ij, c.slot);
 }
 
 namespace launch {
 
-cudaError_t stage_group_shifted(const StageGroup &g, int store, bool collide, cudaStream_t s) {
-    const dim3 grid((g.max_along + 63) / 64, g.n + (g.nfs ? 1 : 0));
+cudaError_t stage_group_shifted(const StageGroup &g, int store, bool collide, bool after_bulk, cudaStream_t s) {
+    const dim3 grid((g.max_along + 63) / 64, g.n + (g.nfs ? 1 : 0)), b(64);
     if (store == STORE_F32) {
-        if (collide) k_stage_group_shifted<float, true><<<grid, 64, 0, s>>>(g);
-        else k_stage_group_shifted<float, false><<<grid, 64, 0, s>>>(g);
-    } else {
-        if (collide) k_stage_group_shifted<__half, true><<<grid, 64, 0, s>>>(g);
-        else k_stage_group_shifted<__half, false><<<grid, 64, 0, s>>>(g);
+        if (collide) return launch_follower(after_bulk, k_stage_group_shifted<float, true>, grid, b, s, g);
+        return launch_follower(after_bulk, k_stage_group_shifted<float, false>, grid, b, s, g);
     }
-    return cudaGetLastError();
+    if (collide) return launch_follower(after_bulk, k_stage_group_shifted<__half, true>, grid, b, s, g);
+    return launch_follower(after_bulk, k_stage_group_shifted<__half, false>, grid, b, s, g);
 }
 
 cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, int max_along, int store,
-                                int sel, const ForceSlot *fs, int nfs, cudaStream_t s) {
+                                int sel, const ForceSlot *fs, int nfs, bool after_bulk, cudaStream_t s) {
     if (n + nfs == 0) return cudaSuccess;
-    const dim3 g(std::max(1, (max_along + 63) / 64), n + nfs);
-    if (store == STORE_F32) k_stage_batch_shifted<float><<<g, 64, 0, s>>>(list, ephase, sel, n, fs);
-    else k_stage_batch_shifted<__half><<<g, 64, 0, s>>>(list, ephase, sel, n, fs);
-    return cudaGetLastError();
+    const dim3 g(std::max(1, (max_along + 63) / 64), n + nfs), b(64);
+    if (store == STORE_F32)
+        return launch_follower(after_bulk, k_stage_batch_shifted<float>, g, b, s, list, ephase, sel, n, fs);
+    return launch_follower(after_bulk, k_stage_batch_shifted<__half>, g, b, s, list, ephase, sel, n, fs);
 }
 
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s) {

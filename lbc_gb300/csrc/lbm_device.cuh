@@ -277,8 +277,7 @@ __device__ __forceinline__ double impedance_step(double *imp, int along, int nf,
 
 template <class A>
 __device__ __forceinline__ void bc_apply(A &a, const double w[9], int kind, int Nx, int Ny,
-                                         int index, int t, const double *val1,
-                                         const double *val2) {
+                                         int index, int t, double v1, double v2) {
     const bool col = bc_is_column(kind);
     int ib, jb;
     if (kind == BC_PERIODIC_X || kind == BC_PERIODIC_Y) {
@@ -321,7 +320,7 @@ __device__ __forceinline__ void bc_apply(A &a, const double w[9], int kind, int 
     if (a.solid(ib, jb)) return;
     switch (kind) {
     case BC_VEL_IN_ZH: {  // src/bc/velocity_inlet.c:25-39
-        const double U = val1[t], V = val2[t];
+        const double U = v1, V = v2;
         const double f0 = a.get(ib, jb, 0), f2 = a.get(ib, jb, 2), f3 = a.get(ib, jb, 3),
                      f4 = a.get(ib, jb, 4), f6 = a.get(ib, jb, 6), f7 = a.get(ib, jb, 7);
         const double r = (f0 + f2 + f4 + 2.0 * (f3 + f6 + f7)) / (1.0 - U);
@@ -330,7 +329,7 @@ __device__ __forceinline__ void bc_apply(A &a, const double w[9], int kind, int 
         a.set(ib, jb, 8, f6 + (1.0 / 6.0) * r * U + 0.5 * (f2 - f4) - (1.0 / 2.0) * r * V);
     } break;
     case BC_VEL_OUT_ZH: {  // src/bc/velocity_outlet.c:25-39
-        const double U = val1[t], V = val2[t];
+        const double U = v1, V = v2;
         const double f0 = a.get(ib, jb, 0), f2 = a.get(ib, jb, 2), f4 = a.get(ib, jb, 4),
                      f1 = a.get(ib, jb, 1), f5 = a.get(ib, jb, 5), f8 = a.get(ib, jb, 8);
         const double r = (f0 + f2 + f4 + 2.0 * (f1 + f5 + f8)) / (1.0 + U);
@@ -339,7 +338,7 @@ __device__ __forceinline__ void bc_apply(A &a, const double w[9], int kind, int 
         a.set(ib, jb, 7, f5 + 0.5 * (f2 - f4) - (1.0 / 6.0) * r * U - (1.0 / 2.0) * r * V);
     } break;
     case BC_VEL_TOP_ZH: {  // src/bc/velocity_top.c:25-39
-        const double U = val1[t], V = val2[t];
+        const double U = v1, V = v2;
         const double f0 = a.get(ib, jb, 0), f1 = a.get(ib, jb, 1), f2 = a.get(ib, jb, 2),
                      f3 = a.get(ib, jb, 3), f5 = a.get(ib, jb, 5), f6 = a.get(ib, jb, 6);
         const double r = (f0 + f1 + f3 + 2 * (f2 + f5 + f6)) / (1 + V);
@@ -348,7 +347,7 @@ __device__ __forceinline__ void bc_apply(A &a, const double w[9], int kind, int 
         a.set(ib, jb, 8, f6 - (f1 - f3) / 2.0 + 0.5 * r * U - 1.0 / 6.0 * r * V);
     } break;
     case BC_VEL_BOT_ZH: {  // src/bc/velocity_bottom.c:25-39 (second write to 7 kept, :39)
-        const double U = val1[t], V = val2[t];
+        const double U = v1, V = v2;
         const double f0 = a.get(ib, jb, 0), f1 = a.get(ib, jb, 1), f3 = a.get(ib, jb, 3),
                      f4 = a.get(ib, jb, 4), f7 = a.get(ib, jb, 7), f8 = a.get(ib, jb, 8);
         const double r = (f0 + f1 + f3 + 2 * (f4 + f7 + f8)) / (1 - V);
@@ -357,7 +356,7 @@ __device__ __forceinline__ void bc_apply(A &a, const double w[9], int kind, int 
         a.set(ib, jb, 7, f8 + (f1 - f3) / 2.0 - 0.5 * r * U + 1.0 / 6.0 * r * V);
     } break;
     case BC_PRES_IN_ZH: {  // src/bc/pressure_inlet.c:25-39
-        const double R = val1[t];
+        const double R = v1;
         const double f0 = a.get(ib, jb, 0), f2 = a.get(ib, jb, 2), f4 = a.get(ib, jb, 4),
                      f3 = a.get(ib, jb, 3), f6 = a.get(ib, jb, 6), f7 = a.get(ib, jb, 7);
         const double U = 1.0 - (f0 + f2 + f4 + 2.0 * (f3 + f6 + f7)) / R;
@@ -367,7 +366,7 @@ __device__ __forceinline__ void bc_apply(A &a, const double w[9], int kind, int 
         a.set(ib, jb, 8, f6 + (1.0 / 6.0) * R * U + 0.5 * (f2 - f4) - (1.0 / 2.0) * R * V);
     } break;
     case BC_PRES_OUT_ZH: {  // src/bc/pressure_outlet.c:25-39
-        const double R = val1[t];
+        const double R = v1;
         const double f0 = a.get(ib, jb, 0), f2 = a.get(ib, jb, 2), f4 = a.get(ib, jb, 4),
                      f1 = a.get(ib, jb, 1), f5 = a.get(ib, jb, 5), f8 = a.get(ib, jb, 8);
         const double U = (f0 + f2 + f4 + 2.0 * (f1 + f5 + f8)) / R - 1.0;
@@ -384,14 +383,14 @@ __device__ __forceinline__ void bc_apply(A &a, const double w[9], int kind, int 
 #pragma unroll
         for (int k = 0; k < 9; k++) a.set(ib, jb, k, a.get(ib - 1, jb, k));
         break;
-    case BC_VEL_IN_REG: bc_regularized(a, w, ib, jb, ib + 1, jb, false, val1[t], val2[t]); break;
-    case BC_VEL_OUT_REG: bc_regularized(a, w, ib, jb, ib - 1, jb, false, val1[t], val2[t]); break;
-    case BC_VEL_BOT_REG: bc_regularized(a, w, ib, jb, ib, jb + 1, false, val1[t], val2[t]); break;
-    case BC_VEL_TOP_REG: bc_regularized(a, w, ib, jb, ib, jb - 1, false, val1[t], val2[t]); break;
-    case BC_PRES_IN_REG: bc_regularized(a, w, ib, jb, ib + 1, jb, true, val1[t], 0.0); break;
-    case BC_PRES_OUT_REG: bc_regularized(a, w, ib, jb, ib - 1, jb, true, val1[t], 0.0); break;
-    case BC_PRES_BOT_REG: bc_regularized(a, w, ib, jb, ib, jb + 1, true, val1[t], 0.0); break;
-    case BC_PRES_TOP_REG: bc_regularized(a, w, ib, jb, ib, jb - 1, true, val1[t], 0.0); break;
+    case BC_VEL_IN_REG: bc_regularized(a, w, ib, jb, ib + 1, jb, false, v1, v2); break;
+    case BC_VEL_OUT_REG: bc_regularized(a, w, ib, jb, ib - 1, jb, false, v1, v2); break;
+    case BC_VEL_BOT_REG: bc_regularized(a, w, ib, jb, ib, jb + 1, false, v1, v2); break;
+    case BC_VEL_TOP_REG: bc_regularized(a, w, ib, jb, ib, jb - 1, false, v1, v2); break;
+    case BC_PRES_IN_REG: bc_regularized(a, w, ib, jb, ib + 1, jb, true, v1, 0.0); break;
+    case BC_PRES_OUT_REG: bc_regularized(a, w, ib, jb, ib - 1, jb, true, v1, 0.0); break;
+    case BC_PRES_BOT_REG: bc_regularized(a, w, ib, jb, ib, jb + 1, true, v1, 0.0); break;
+    case BC_PRES_TOP_REG: bc_regularized(a, w, ib, jb, ib, jb - 1, true, v1, 0.0); break;
     default: break;
     }
 }
@@ -496,6 +495,61 @@ __device__ __forceinline__ int2 stage_node(int kind, int Nx, int Ny, int index, 
     if (kind == BC_PERIODIC_X) return make_int2(t < Ny ? 0 : Nx - 1, t % Ny);
     if (kind == BC_PERIODIC_Y) return make_int2(t % Nx, t < Nx ? 0 : Ny - 1);
     return bc_is_column(kind) ? make_int2(index, t) : make_int2(t, index);
+}
+
+// The interior neighbour whose populations or moments a Boundary entry reads
+// at node ij (the band's read lines), x = -1 for entries that read none.
+__device__ __forceinline__ int2 stage_neighbour(int kind, int2 ij) {
+    switch (kind) {
+    case BC_PRES_IN_ZH: case BC_CONV_IN: case BC_VEL_IN_REG: case BC_PRES_IN_REG: return make_int2(ij.x + 1, ij.y);
+    case BC_PRES_OUT_ZH: case BC_CONV_OUT: case BC_VEL_OUT_REG: case BC_PRES_OUT_REG: return make_int2(ij.x - 1, ij.y);
+    case BC_VEL_BOT_REG: case BC_PRES_BOT_REG: return make_int2(ij.x, ij.y + 1);
+    case BC_VEL_TOP_REG: case BC_PRES_TOP_REG: return make_int2(ij.x, ij.y - 1);
+    default: return make_int2(-1, -1);
+    }
+}
+
+// What stage thread t reads that the bulk kernel of the same step does not
+// write: its node's solid flag and band slot, the neighbour's slot and
+// previous-step moments, the entry's values at t, whether it finishes the
+// node, and the impedance wall's update (which depends only on the
+// neighbour's previous density and the wall's own state). Loaded before
+// pdl_wait(), so that after the bulk kernel ends only the band populations,
+// the BC arithmetic and the finish remain. The band accessors answer from it.
+struct StagePre {
+    int2 ij, nij;
+    int slot, nslot;
+    bool solid, fin, imp;
+    double nrho, nux, nuy;
+    double v1, v2;   // v2 = -(wall velocity) on impedance nodes (imp)
+};
+
+__device__ __forceinline__ StagePre stage_preload(const StageParams &p, int t) {
+    StagePre c;
+    c.ij = stage_node(p.kind, p.Nx, p.Ny, p.index, t);
+    c.nij = stage_neighbour(p.kind, c.ij);
+    c.solid = (p.flags[(long long)c.ij.y * p.pitch + c.ij.x] & NF_SOLID) != 0;
+    c.slot = band_slot(p.colbase, p.rowbase, c.ij.x, c.ij.y);
+    c.nslot = 0;
+    c.nrho = c.nux = c.nuy = 0.0;
+    if (c.nij.x >= 0) {
+        c.nslot = band_slot(p.colbase, p.rowbase, c.nij.x, c.nij.y);
+        c.nrho = p.bandm_prev[c.nslot];
+        c.nux = p.bandm_prev[(size_t)p.nslots + c.nslot];
+        c.nuy = p.bandm_prev[2 * (size_t)p.nslots + c.nslot];
+    }
+    c.v1 = p.val1 ? p.val1[t] : 0.0;
+    c.v2 = p.val2 ? p.val2[t] : 0.0;
+    c.fin = p.last != nullptr && !c.solid && p.last[c.slot] == p.entry;
+    c.imp = false;
+    if (p.imp && p.kind == BC_VEL_BOT_REG && p.imp[(size_t)IMP_ACTIVE * p.along + t] != 0.0 && !c.solid) {
+        // Impedance wall on this node: the regularized bottom BC with the
+        // normal velocity from the node's mass-spring-damper.
+        c.v2 = -impedance_step(p.imp, p.along, p.imp_nf, t, c.nrho, p.imp_alpha, p.imp_cos, p.imp_sin, p.imp_wcos,
+                               p.imp_wsin, p.imp_windowed);
+        c.imp = true;
+    }
+    return c;
 }
 
 }  // namespace lbm

@@ -18,44 +18,33 @@ __device__ __forceinline__ void warp_reduce2(double &a, double &b, bool link) {
 // One case's force from its segment partials, by one full warp (every lane
 // calls it): the sum of partials[2 t], partials[2 t + 1] over t in [t0, t1)
 // into out[0..1] and the next history slot. The order is fixed and does not
-// depend on the launch: 256 strided running sums (sum v holds t = t0 + v +
-// 256 k in increasing k; lane l keeps v = l + 32 q, q = 0..7, eight loads in
-// flight), each group of 32 folded by a shuffle tree, the 8 folds added in q
-// order.
+// depend on the launch: lane l keeps the running sum of t = t0 + l + 32 k in
+// increasing k, and a shuffle tree folds the 32 sums. FP64 adds are the cost
+// on GB300 (about 64 cycles per warp instruction on one SM sub-partition), so
+// the order is the one with the fewest: n / 32 + 5 per component.
 template <class Slot>
 __device__ __forceinline__ void force_reduce_warp(const Slot &fs, int lane) {
-    double a[8], b[8];
-#pragma unroll
-    for (int q = 0; q < 8; q++) { a[q] = 0.0; b[q] = 0.0; }
-    for (int base = fs.t0; base < fs.t1; base += 256) {
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
-            const int t = base + 32 * q + lane;
-            if (t < fs.t1) {
-                a[q] += fs.partials[2 * (size_t)t];
-                b[q] += fs.partials[2 * (size_t)t + 1];
-            }
-        }
+    const int t0 = fs.t0, t1 = fs.t1;
+    const double2 *part = (const double2 *)fs.partials;
+    double a = 0.0, b = 0.0;
+    for (int t = t0 + lane; t < t1; t += 32) {
+        const double2 v = part[t];
+        a += v.x;
+        b += v.y;
     }
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            a[q] += __shfl_down_sync(0xffffffffu, a[q], o);
-            b[q] += __shfl_down_sync(0xffffffffu, b[q], o);
-        }
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
     }
     if (lane != 0) return;
-    double ra = 0.0, rb = 0.0;
-#pragma unroll
-    for (int q = 0; q < 8; q++) { ra += a[q]; rb += b[q]; }
-    fs.out[0] = ra;
-    fs.out[1] = rb;
+    fs.out[0] = a;
+    fs.out[1] = b;
     if (fs.hist) {
         const unsigned long long k = *fs.hist_count;
         const int slot = (int)(k % (unsigned long long)fs.hist_cap);
-        fs.hist[2 * slot] = ra;
-        fs.hist[2 * slot + 1] = rb;
+        fs.hist[2 * slot] = a;
+        fs.hist[2 * slot + 1] = b;
         *fs.hist_count = k + 1ull;
     }
 }

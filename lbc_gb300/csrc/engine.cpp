@@ -713,7 +713,10 @@ StageParams Solver::stage_params(const Stage &st, int src, int bparity) const {
     s.flags = d_flags_; s.colbase = d_colbase_; s.rowbase = d_rowbase_; s.nslots = nslots_;
     s.bandf = d_bandf_; s.bandg = d_bandg_; s.bandm_prev = d_bandm_[bparity];
     s.src = buf_[src];
-    for (int k = 0; k < 9; k++) s.w[k] = d_.w[k];
+    for (int k = 0; k < 9; k++) {
+        s.w[k] = d_.w[k];
+        s.wf[k] = (float)d_.w[k];
+    }
     s.last = fuse_ ? d_last_ : nullptr;
     s.entry = (int)(&st - stages_.data());
     s.imp = st.d_imp;
@@ -854,7 +857,13 @@ FinishParams Solver::finish_params(int dst, bool write_macro, int bparity) const
     f.omega = d_omega_; f.omega0 = omega0_;
     f.has_force = (d_.Fx != 0.0 || d_.Fy != 0.0);
     f.Fx = d_.Fx; f.Fy = d_.Fy; f.hFx = 0.5 * d_.Fx; f.hFy = 0.5 * d_.Fy;
-    for (int k = 0; k < 9; k++) f.w[k] = d_.w[k];
+    for (int k = 0; k < 9; k++) {
+        f.w[k] = d_.w[k];
+        f.wf[k] = (float)d_.w[k];
+    }
+    f.omega0f = (float)omega0_;
+    f.Fxf = (float)d_.Fx; f.Fyf = (float)d_.Fy;
+    f.hFxf = (float)f.hFx; f.hFyf = (float)f.hFy;
     f.write_macro = write_macro ? 1 : 0;
     f.rho = macro_out_[0] ? macro_out_[0] : d_rho_;
     f.ux = macro_out_[1] ? macro_out_[1] : d_ux_;

@@ -249,7 +249,7 @@ __global__ void k_stage_group(const StageGroup g) {
     const StageParams &p = g.p[blockIdx.y];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
-    const StagePre c = stage_preload(p, t);
+    const StagePre c = stage_preload(p, t, p.kind);
     pdl_wait();
     stage_point<T>(p, c, t);
     if (c.fin) finish_node_exact<COLLIDE>(g.fin, c.ij, c.slot);
@@ -270,7 +270,7 @@ __global__ void k_stage_batch(const StageParams *__restrict__ list, const int *_
     const StageParams &p = list[2 * e + (sel ^ ephase[e])];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
-    const StagePre c = stage_preload(p, t);
+    const StagePre c = stage_preload(p, t, p.kind);
     pdl_wait();
     stage_point<T>(p, c, t);
     if (c.fin) finish_node_exact<true>(*p.fin, c.ij, c.slot);

@@ -441,33 +441,39 @@ __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepPar
     }
 }
 
+// live = false: the same instructions without their stores (the stage
+// threads' instruction-cache warm-up, stage_thread_s). Band populations are
+// read at L2 (__ldcg), never from a possibly stale L1 line.
 template <typename T, bool COLLIDE>
-__device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 ij, int slot) {
+__device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 ij, int slot, bool live = true) {
     float g[9], wf[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) {
-        g[k] = SV<T>::rnd(p.bandg[(size_t)k * p.nslots + slot]);
-        wf[k] = (float)p.w[k];
+        g[k] = SV<T>::rnd(__ldcg(p.bandg + (size_t)k * p.nslots + slot));
+        wf[k] = p.wf[k];
     }
     float dr, rho, ux, uy, Jx, Jy, jx, jy;
-    moments_shifted(g, (float)p.hFx, (float)p.hFy, dr, rho, ux, uy, Jx, Jy, jx, jy);
+    moments_shifted(g, p.hFxf, p.hFyf, dr, rho, ux, uy, Jx, Jy, jx, jy);
     const size_t dn = (size_t)ij.y * p.Nx + ij.x;
-    if (p.write_macro) { p.rho[dn] = 1.0 + (double)dr; p.ux[dn] = ux; p.uy[dn] = uy; }
-    p.bandm_next[slot] = 1.0 + (double)dr;
-    p.bandm_next[(size_t)p.nslots + slot] = ux;
-    p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
+    if (live && p.write_macro) { p.rho[dn] = 1.0 + (double)dr; p.ux[dn] = ux; p.uy[dn] = uy; }
+    if (live) {
+        p.bandm_next[slot] = 1.0 + (double)dr;
+        p.bandm_next[(size_t)p.nslots + slot] = ux;
+        p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
+    }
     if (COLLIDE) {
-        const float om = p.omega ? (float)p.omega[dn] : (float)p.omega0;
+        const float om = p.omega ? (float)p.omega[dn] : p.omega0f;
         float h1, h5;
         shifted_h(wf[1], h1, h5);
-        if (p.has_force) collide_v<float, true>(g, wf, h1, h5, dr, ux, uy, Jx, Jy, jx, jy, om, true, (float)p.Fx,
-                                                (float)p.Fy);
+        if (p.has_force) collide_v<float, true>(g, wf, h1, h5, dr, ux, uy, Jx, Jy, jx, jy, om, true, p.Fxf, p.Fyf);
         else collide_v<float, false>(g, wf, h1, h5, dr, ux, uy, Jx, Jy, jx, jy, om, false, 0.f, 0.f);
     }
     T *D = (T *)p.dst;
     const long long node = (long long)ij.y * p.pitch + ij.x;
+    if (live) {
 #pragma unroll
-    for (int k = 0; k < 9; k++) SV<T>::st(D + k * p.plane + node, g[k]);
+        for (int k = 0; k < 9; k++) SV<T>::st(D + k * p.plane + node, g[k]);
+    }
 }
 
 template <typename T, bool COLLIDE>
@@ -533,6 +539,7 @@ __global__ void k_collide_shifted(const CollideParams p) {
 template <typename T> struct BandAccessorS {
     const StageParams &p;
     const StagePre &c;
+    bool live;  // false: no stores (instruction-cache warm-up pass)
     __device__ int slot(int i, int j) const {
         if (i == c.ij.x && j == c.ij.y) return c.slot;
         if (i == c.nij.x && j == c.nij.y) return c.nslot;
@@ -540,8 +547,10 @@ template <typename T> struct BandAccessorS {
     }
     __device__ bool nb(int i, int j) const { return i == c.nij.x && j == c.nij.y; }
     __device__ double m(int q, int i, int j) const { return p.bandm_prev[(size_t)q * p.nslots + slot(i, j)]; }
-    __device__ float get(int i, int j, int k) const { return p.bandg[(size_t)k * p.nslots + slot(i, j)]; }
-    __device__ void set(int i, int j, int k, float v) const { p.bandg[(size_t)k * p.nslots + slot(i, j)] = v; }
+    __device__ float get(int i, int j, int k) const { return __ldcg(p.bandg + (size_t)k * p.nslots + slot(i, j)); }
+    __device__ void set(int i, int j, int k, float v) const {
+        if (live) p.bandg[(size_t)k * p.nslots + slot(i, j)] = v;
+    }
     __device__ float drho(int i, int j) const { return (float)((nb(i, j) ? c.nrho : m(0, i, j)) - 1.0); }
     __device__ double rho64(int i, int j) const { return nb(i, j) ? c.nrho : m(0, i, j); }
     __device__ float ux(int i, int j) const { return (float)(nb(i, j) ? c.nux : m(1, i, j)); }
@@ -558,16 +567,52 @@ template <typename T> struct BandAccessorS {
 // One point of one Boundary entry (src/core/main_lbm.c:49-58) after its
 // preload, as stage_point in kernels_exact.cu.
 template <typename T>
-__device__ __forceinline__ void stage_point_s(const StageParams &p, const StagePre &c, int t) {
-    BandAccessorS<T> a{p, c};
+__device__ __forceinline__ void stage_point_s(const StageParams &p, const StagePre &c, int t, int kind,
+                                              bool live) {
+    BandAccessorS<T> a{p, c, live};
     float w[9];
 #pragma unroll
-    for (int k = 0; k < 9; k++) w[k] = (float)p.w[k];
-    if (c.imp) {
+    for (int k = 0; k < 9; k++) w[k] = p.wf[k];
+    if (kind == BC_VEL_BOT_REG && c.imp) {
         bc_regularized_s(a, w, t, p.index, t, p.index + 1, false, (float)c.v1, (float)c.v2);
         return;
     }
-    bc_apply_s(a, w, p.kind, p.Nx, p.Ny, p.index, t, c.v1, c.v2);
+    bc_apply_s(a, w, kind, p.Nx, p.Ny, p.index, t, c.v1, c.v2);
+}
+
+// One stage thread, specialised on the entry's kind: preload, wait for the
+// bulk kernel, the BC, the finish. The edge launch runs a few warps per SM
+// on a cold instruction cache, and instruction fetch, not arithmetic, sets
+// its duration; so each kind is one short region of code, and the thread
+// first runs it once without stores (pass 0, while the bulk kernel still
+// runs: the band values it reads are stale and discarded), so that the pass
+// that counts, after the wait, runs from a warm cache.
+template <typename T, bool COLLIDE, int KIND>
+__device__ __forceinline__ void stage_thread_s(const StageParams &p, const FinishParams &f, int t) {
+    const StagePre c = stage_preload(p, t, KIND);
+#pragma unroll 1
+    for (int pass = 0; pass < 2; pass++) {
+        const bool live = pass != 0;
+        if (live) pdl_wait();
+        stage_point_s<T>(p, c, t, KIND, live);
+        if (c.fin) finish_node_shifted<T, COLLIDE>(f, c.ij, c.slot, live);
+    }
+}
+
+template <typename T, bool COLLIDE>
+__device__ __forceinline__ void stage_dispatch_s(const StageParams &p, const FinishParams &f, int t) {
+    switch (p.kind) {
+#define LBM_STAGE_KIND(K) \
+    case K: stage_thread_s<T, COLLIDE, K>(p, f, t); break;
+    LBM_STAGE_KIND(BC_VEL_IN_ZH) LBM_STAGE_KIND(BC_VEL_OUT_ZH) LBM_STAGE_KIND(BC_VEL_TOP_ZH)
+    LBM_STAGE_KIND(BC_VEL_BOT_ZH) LBM_STAGE_KIND(BC_PRES_IN_ZH) LBM_STAGE_KIND(BC_PRES_OUT_ZH)
+    LBM_STAGE_KIND(BC_CONV_IN) LBM_STAGE_KIND(BC_CONV_OUT) LBM_STAGE_KIND(BC_PERIODIC_X)
+    LBM_STAGE_KIND(BC_PERIODIC_Y) LBM_STAGE_KIND(BC_VEL_IN_REG) LBM_STAGE_KIND(BC_VEL_OUT_REG)
+    LBM_STAGE_KIND(BC_VEL_TOP_REG) LBM_STAGE_KIND(BC_VEL_BOT_REG) LBM_STAGE_KIND(BC_PRES_IN_REG)
+    LBM_STAGE_KIND(BC_PRES_OUT_REG) LBM_STAGE_KIND(BC_PRES_TOP_REG) LBM_STAGE_KIND(BC_PRES_BOT_REG)
+#undef LBM_STAGE_KIND
+    default: pdl_wait(); break;
+    }
 }
 
 // As k_stage_group / k_stage_batch in kernels_exact.cu.
@@ -581,10 +626,7 @@ __global__ void k_stage_group_shifted(const StageGroup g) {
     const StageParams &p = g.p[blockIdx.y];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
-    const StagePre c = stage_preload(p, t);
-    pdl_wait();
-    stage_point_s<T>(p, c, t);
-    if (c.fin) finish_node_shifted<T, COLLIDE>(g.fin, c.ij, c.slot);
+    stage_dispatch_s<T, COLLIDE>(p, g.fin, t);
 }
 
 template <typename T>
@@ -599,10 +641,7 @@ __global__ void k_stage_batch_shifted(const StageParams *__restrict__ list, cons
     const StageParams &p = list[2 * e + (sel ^ ephase[e])];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
-    const StagePre c = stage_preload(p, t);
-    pdl_wait();
-    stage_point_s<T>(p, c, t);
-    if (c.fin) finish_node_shifted<T, true>(*p.fin, c.ij, c.slot);
+    stage_dispatch_s<T, true>(p, *p.fin, t);
 }
 
 namespace launch {

@@ -455,6 +455,7 @@ struct StageParams {
     const double *bandm_prev;  // [3][nslots]
     const void *src;           // post-collision populations (periodic stages)
     double w[9];
+    float wf[9];               // FP32 copies (shifted storage: no FP64 conversions per thread)
     // Finish in the same launch: the thread of a node whose last writer in
     // the Boundary list is this entry (last[slot] == entry) computes the
     // node's moments and collision right after the entry's BC. last is null
@@ -482,6 +483,9 @@ struct FinishParams {
     double w[9];
     int write_macro;
     double *rho, *ux, *uy;
+    // FP32 copies of the above (shifted storage)
+    float wf[9];
+    float omega0f, Fxf, Fyf, hFxf, hFyf;
 };
 
 __device__ __forceinline__ int band_slot(const int *colbase, const int *rowbase, int i, int j) {
@@ -524,10 +528,10 @@ struct StagePre {
     double v1, v2;   // v2 = -(wall velocity) on impedance nodes (imp)
 };
 
-__device__ __forceinline__ StagePre stage_preload(const StageParams &p, int t) {
+__device__ __forceinline__ StagePre stage_preload(const StageParams &p, int t, int kind) {
     StagePre c;
-    c.ij = stage_node(p.kind, p.Nx, p.Ny, p.index, t);
-    c.nij = stage_neighbour(p.kind, c.ij);
+    c.ij = stage_node(kind, p.Nx, p.Ny, p.index, t);
+    c.nij = stage_neighbour(kind, c.ij);
     c.solid = (p.flags[(long long)c.ij.y * p.pitch + c.ij.x] & NF_SOLID) != 0;
     c.slot = band_slot(p.colbase, p.rowbase, c.ij.x, c.ij.y);
     c.nslot = 0;
@@ -542,7 +546,7 @@ __device__ __forceinline__ StagePre stage_preload(const StageParams &p, int t) {
     c.v2 = p.val2 ? p.val2[t] : 0.0;
     c.fin = p.last != nullptr && !c.solid && p.last[c.slot] == p.entry;
     c.imp = false;
-    if (p.imp && p.kind == BC_VEL_BOT_REG && p.imp[(size_t)IMP_ACTIVE * p.along + t] != 0.0 && !c.solid) {
+    if (kind == BC_VEL_BOT_REG && p.imp && p.imp[(size_t)IMP_ACTIVE * p.along + t] != 0.0 && !c.solid) {
         // Impedance wall on this node: the regularized bottom BC with the
         // normal velocity from the node's mass-spring-damper.
         c.v2 = -impedance_step(p.imp, p.along, p.imp_nf, t, c.nrho, p.imp_alpha, p.imp_cos, p.imp_sin, p.imp_wcos,

@@ -300,6 +300,23 @@ bool Solver::build_geometry() {
         }
     }
     has_flags_ = any_special || !stages_.empty() || !d_.px || !d_.py;
+    // Shifted storage: the nodes the clean-pair kernels leave out (both nodes
+    // of every pair (2m, 2m + 1) of a row with a special node, and the last
+    // column of an odd-width grid), in row-major order.
+    special_host_.clear();
+    if (d_.store != STORE_F64) {
+        const uint16_t slow = NF_SPECIAL_MASK | NF_SOLID | NF_BAND | NF_BCW | NF_LINKS;
+        for (int j = 0; j < Ny; j++)
+            for (int i0 = 0; i0 < Nx; i0 += 2) {
+                const bool two = i0 + 1 < Nx;
+                const size_t n0 = (size_t)j * pitch_ + i0;
+                const bool sp = !two || (flags[n0] & slow) || (flags[n0 + 1] & slow);
+                if (!sp) continue;
+                special_host_.push_back(make_int2(i0, j));
+                if (two) special_host_.push_back(make_int2(i0 + 1, j));
+            }
+    }
+    nspecial_ = (int)special_host_.size();
     needs_old_dst_ = any_special;  // solid nodes or off-grid pull sources
     wnodes_host_ = wnodes;
     has_links_ = want_links && !links.empty();
@@ -321,6 +338,10 @@ bool Solver::build_geometry() {
     if (has_flags_) {
         if (!dalloc(&d_flags_, flags.size())) return false;
         CK(cudaMemcpyAsync(d_flags_, flags.data(), flags.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, stream_));
+    }
+    if (nspecial_) {
+        if (!dalloc(&d_special_, special_host_.size())) return false;
+        CK(cudaMemcpyAsync(d_special_, special_host_.data(), special_host_.size() * sizeof(int2), cudaMemcpyHostToDevice, stream_));
     }
     if (has_links_) {
         if (!dalloc(&d_link_off_, link_off.size()) || !dalloc(&d_links_, links.size())) return false;
@@ -446,16 +467,32 @@ void Solver::group_stages(const Solid &solid, const std::vector<int> &colbase, c
 // order. The table does not depend on the launch shape.
 bool Solver::compute_segment_slots() {
     const int Nx = d_.Nx, Ny = d_.Ny;
-    const int nseg = (Nx + 31) / 32;
-    std::vector<int> slot((size_t)nseg * Ny, -1);
+    std::vector<int> slot;
     int n = 0;
-    for (int j = 0; j < Ny; j++)
-        for (int g = 0; g < nseg; g++) {
+    if (d_.store == STORE_F64) {
+        // per 32-node row segment
+        const int nseg = (Nx + 31) / 32;
+        slot.assign((size_t)nseg * Ny, -1);
+        for (int j = 0; j < Ny; j++)
+            for (int g = 0; g < nseg; g++) {
+                bool any = false;
+                for (int i = 32 * g; i < std::min(Nx, 32 * g + 32); i++)
+                    if (link_node_[(size_t)j * Nx + i]) { any = true; break; }
+                if (any) slot[(size_t)j * nseg + g] = n++;
+            }
+    } else {
+        // per 32-entry chunk of the special-node list (wall-link nodes are special)
+        const int nch = (nspecial_ + 31) / 32;
+        slot.assign((size_t)std::max(nch, 1), -1);
+        for (int c = 0; c < nch; c++) {
             bool any = false;
-            for (int i = 32 * g; i < std::min(Nx, 32 * g + 32); i++)
-                if (link_node_[(size_t)j * Nx + i]) { any = true; break; }
-            if (any) slot[(size_t)j * nseg + g] = n++;
+            for (int q = 32 * c; q < std::min(nspecial_, 32 * c + 32); q++) {
+                const int2 ij = special_host_[q];
+                if (link_node_[(size_t)ij.y * Nx + ij.x]) { any = true; break; }
+            }
+            if (any) slot[c] = n++;
         }
+    }
     nlink_segs_ = n;
     if (!dalloc(&d_seg_slot_, slot.size()) || !dalloc(&d_partials_, 2 * (size_t)std::max(n, 1))) return false;
     CK(cudaMemcpyAsync(d_seg_slot_, slot.data(), slot.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
@@ -686,7 +723,8 @@ StepParams Solver::step_params(int src, int dst, bool write_macro, int bparity) 
     p.bandm_next = nslots_ ? d_bandm_[bparity ^ 1] : nullptr;
     if (has_mem_) {
         p.mem_partials = d_partials_;
-        p.seg_slot = d_seg_slot_;
+        if (d_.store == STORE_F64) p.seg_slot = d_seg_slot_;
+        else p.chunk_slot = d_seg_slot_;
     }
     return p;
 }
@@ -881,7 +919,11 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
     if (d_.store == STORE_F64) {
         CK(launch::step_exact(p, has_flags_, collide, block_, s));
     } else {
-        CK(launch::step_shifted(fast_params(p), d_.store, has_flags_, collide, block_, s));
+        const FastStepParams fp = fast_params(p);
+        // The clean pairs, then the special nodes overlapping their last wave
+        // (the plain kernel of a flag-free grid steps its own odd column).
+        CK(launch::step_shifted(fp, d_.store, has_flags_, collide, block_, false, s));
+        if (special_launch()) CK(launch::special_shifted(fp, d_special_, nspecial_, d_.store, true, collide, true, s));
     }
     if (groups_.empty()) {
         if (has_mem_) CK(launch::force_reduce(d_force_slot_, 1, true, s));
@@ -1272,6 +1314,17 @@ bool Batch::build() {
         for (const Stage &st : s->stages()) max_along_ = std::max(max_along_, st.along);
     }
     if (!build_tiles(tws_)) return false;
+    // Shifted storage: every case's special nodes, each case's list padded to
+    // a multiple of 32 so that a warp steps one force chunk of one case.
+    std::vector<int4> special;
+    if (store_ != STORE_F64)
+        for (int c = 0; c < nc; c++) {
+            const std::vector<int2> &sl = cases_[c]->special_nodes();
+            const int n = (int)sl.size(), padded = (n + 31) / 32 * 32;
+            for (int q = 0; q < padded; q++)
+                special.push_back(q < n ? make_int4(c, sl[q].x, sl[q].y, q >> 5) : make_int4(c, -1, -1, q >> 5));
+        }
+    nspecial_ = (int)special.size();
     nfin_ = (int)fin_nodes.size();
     nforce_ = (int)force.size();
     const size_t psize = store_ == STORE_F64 ? sizeof(StepParams) : sizeof(FastStepParams);
@@ -1292,6 +1345,10 @@ bool Batch::build() {
     CK(cudaMemsetAsync(d_phase_, 0, nphase * sizeof(int), stream_));
     if (nfin_) CK(cudaMemcpyAsync(d_fin_nodes_, fin_nodes.data(), fin_nodes.size() * sizeof(int4), cudaMemcpyHostToDevice, stream_));
     if (nforce_) CK(cudaMemcpyAsync(d_force_, force.data(), force.size() * sizeof(ForceSlot), cudaMemcpyHostToDevice, stream_));
+    if (nspecial_) {
+        if (!balloc(allocs_, &d_special_, special.size(), stream_)) return false;
+        CK(cudaMemcpyAsync(d_special_, special.data(), special.size() * sizeof(int4), cudaMemcpyHostToDevice, stream_));
+    }
     // One launch per level: level l holds the l-th stage group of every case.
     for (int s = 0; s < max_stages_; s++) {
         const int cnt = level_cnt[s];
@@ -1301,18 +1358,23 @@ bool Batch::build() {
         stage_counts_.push_back(cnt);
     }
     // The force reductions ride in the first stage level's launch.
-    launches_per_step_ = 1 + max_stages_ + (nfin_ ? 1 : 0) + (nforce_ && max_stages_ == 0 ? 1 : 0);
+    launches_per_step_ = 1 + (nspecial_ ? 1 : 0) + max_stages_ + (nfin_ ? 1 : 0) + (nforce_ && max_stages_ == 0 ? 1 : 0);
     CK(cudaStreamSynchronize(stream_));
     return true;
 }
 
 bool Batch::launch_batched(int sel) {
-    if (store_ == STORE_F64)
+    if (store_ == STORE_F64) {
         CK(launch::step_batch_exact((const StepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
                                     grid_, stream_));
-    else
+    } else {
+        // the clean pairs, then the special nodes overlapping their tail
         CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
-                                      store_, wide_, any_force_, grid_, stream_));
+                                      store_, wide_, any_force_, grid_, false, stream_));
+        if (nspecial_)
+            CK(launch::special_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_special_, nspecial_, sel,
+                                             store_, wide_, any_force_, true, stream_));
+    }
     for (int s = 0; s < max_stages_; s++)
         CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], max_along_, store_, sel, d_force_,
                                s == 0 ? nforce_ : 0, s == 0, stream_));

@@ -102,9 +102,16 @@ class Solver {
     long long steps_done() const { return steps_done_; }
     // Kernel launches per time step inside the loop (for launch counting).
     int launches_per_step() const {
-        if (groups_.empty()) return 1 + (has_mem_ ? 1 : 0);
-        return 1 + (int)groups_.size() + (!fuse_ && nw_ > 0 ? 1 : 0);
+        const int bulk = 1 + (special_launch() ? 1 : 0);
+        if (groups_.empty()) return bulk + (has_mem_ ? 1 : 0);
+        return bulk + (int)groups_.size() + (!fuse_ && nw_ > 0 ? 1 : 0);
     }
+    // Shifted storage: the nodes the clean-pair kernels leave to the
+    // special-node kernel (row-major; both nodes of a pair with a special
+    // node, and an odd last column). Launched on its own for grids with a
+    // flag word; in batches for every case.
+    const std::vector<int2> &special_nodes() const { return special_host_; }
+    bool special_launch() const { return d_.store != STORE_F64 && has_flags_ && nspecial_ > 0; }
     bool set_block(dim3 b);
     dim3 block() const { return block_; }
     // Launch-shape tuning (tune.h). mode 1: take the cached block for this
@@ -240,7 +247,10 @@ class Solver {
     std::thread *vtk_thread_ = nullptr;
     bool vtk_ok_ = true;
     std::string vtk_err_;
-    int *d_seg_slot_ = nullptr;     // per 32-node row segment: force partial slot or -1
+    int *d_seg_slot_ = nullptr;     // per 32-node row segment (FP64) or 32-entry special-list chunk: force slot or -1
+    std::vector<int2> special_host_;
+    int2 *d_special_ = nullptr;
+    int nspecial_ = 0;
     int nlink_segs_ = 0;
     ForceSlot *d_force_slot_ = nullptr;
     bool compute_segment_slots();
@@ -249,12 +259,13 @@ class Solver {
 };
 
 // Many independent cases of one storage type advanced together: per step one
-// persistent bulk kernel over the flattened tile list of all cases, then one
-// launch per stage level (the l-th stage group of every case) whose threads
-// also finish the nodes their entry wrote last; the first level's launch also
-// reduces every case's force. The steps between the per-case first collision
-// and final step run from a captured two-step graph. Each case ends exactly
-// as Solver::run(n) would leave it.
+// persistent bulk kernel over the flattened tile list of all cases (shifted
+// storage: clean node pairs, then one launch over every case's special nodes),
+// then one launch per stage level (the l-th stage group of every case) whose
+// threads also finish the nodes their entry wrote last; the first level's
+// launch also reduces every case's force. The steps between the per-case
+// first collision and final step run from a captured two-step graph. Each
+// case ends exactly as Solver::run(n) would leave it.
 class Batch {
   public:
     explicit Batch(const std::vector<Solver *> &cases);
@@ -307,6 +318,8 @@ class Batch {
     FinishParams *d_fin_ = nullptr;
     int4 *d_fin_nodes_ = nullptr;
     ForceSlot *d_force_ = nullptr;
+    int4 *d_special_ = nullptr;    // (case, i, j, chunk), shifted storage
+    int nspecial_ = 0;
     cudaGraphExec_t pair_exec_ = nullptr;
     std::vector<void *> allocs_;
     // host copies of the per-run parameters (kept until their uploads ran)

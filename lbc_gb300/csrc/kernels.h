@@ -137,9 +137,20 @@ cudaError_t finish_batch_exact(const FinishParams *fp, const int *phase, const i
 cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStream_t s);
 
 // shifted storage (kernels_shifted.cu)
+// after_special: launch as a programmatic follower of the previous kernel
+// (unused: the special-node kernel follows the step kernel).
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
-                         cudaStream_t s);
+                         bool after_special, cudaStream_t s);
 cudaError_t finish_shifted(const FinishParams &p, int store, bool collide, cudaStream_t s);
+// The special nodes of a case (nodes[0 .. n)) on the per-node path; flags: the
+// case has a flag word. Launched right after the case's clean-pair kernel
+// (after_bulk), it overlaps that kernel's last wave and completes after it.
+cudaError_t special_shifted(const FastStepParams &p, const int2 *nodes, int n, int store, bool flags, bool collide,
+                            bool after_bulk, cudaStream_t s);
+// The special nodes of a batch: nodes[q] = (case, i, j, chunk), n a multiple
+// of 32 (each case's list padded to 32 entries, i = -1).
+cudaError_t special_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *nodes, int n, int sel,
+                                  int store, bool wide, bool force, bool after_bulk, cudaStream_t s);
 // Edge BCs of shifted storage in FP32 (launch::stage_group / stage_batch dispatch here).
 cudaError_t stage_group_shifted(const StageGroup &g, int store, bool collide, bool after_bulk, cudaStream_t s);
 cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, int max_along, int store,
@@ -149,7 +160,7 @@ cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s);
 // force: some case has a body force (the forced kernel form serves all cases).
 cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
                                int ntiles, int sel, int tws, int store, bool wide, bool force, int grid,
-                               cudaStream_t s);
+                               bool after_special, cudaStream_t s);
 int step_batch_shifted_grid(int store);
 cudaError_t finish_batch_shifted(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
                                  int sel, int store, cudaStream_t s);

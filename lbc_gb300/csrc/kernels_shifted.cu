@@ -220,18 +220,19 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
                                                   float &mfx, float &mfy, bool &link) {
     const StepParams &p = fp.s;
     const I node = (I)j * (I)p.pitch + (I)i;
-    const uint16_t fl = FLAGS ? p.flags[node] : (uint16_t)0;
     const size_t dn = (size_t)j * (size_t)p.Nx + (size_t)i;
-    if (FLAGS && (fl & NF_SOLID)) {
-        solid_node_outputs<T>(p, i, j, (long long)node, dn, fl);
-        return;
-    }
     const T *S = (const T *)p.src;
     T *Dst = (T *)p.dst;
     const I pl = (I)p.plane;
-    // Source neighbours: wrapped on periodic axes, clamped otherwise so that
-    // all nine loads are in bounds and can be issued at once; the flag word
-    // then says which of them to replace.
+    // The loads come in three waves of independent loads, not one chain: (1)
+    // the flag word, the nine pulled populations, the node's eight own
+    // opposite populations and its cut-link offset; (2) the cut-link records
+    // of its flagged directions; (3) the populations behind interpolated
+    // links and the stale slots of off-grid sources. Source neighbours are
+    // wrapped on periodic axes and clamped otherwise, so that every load of
+    // wave 1 is in bounds whatever the flags say. (Measured: the own
+    // populations loaded in wave 2, for flagged directions only, cost the
+    // channel and the cylinder 2-4 %.)
     int im = i - 1, ip = i + 1, jm = j - 1, jp = j + 1;
     if (p.px) { if (im < 0) im += p.Nx; if (ip >= p.Nx) ip -= p.Nx; }
     else { im = max(im, 0); ip = min(ip, p.Nx - 1); }
@@ -239,35 +240,58 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
     else { jm = max(jm, 0); jp = min(jp, p.Ny - 1); }
     const I r0 = (I)j * (I)p.pitch, rm = (I)jm * (I)p.pitch, rp = (I)jp * (I)p.pitch;
     const I so[9] = {r0 + i, r0 + im, rm + i, r0 + ip, rp + i, rm + im, rm + ip, rp + ip, rp + im};
+    const uint16_t fl = FLAGS ? p.flags[node] : (uint16_t)0;
     float g[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) g[k] = SV<T>::ld(S + (I)k * pl + so[k]);
-    if (FLAGS && (fl & NF_SPECIAL_MASK)) {
-        const Link *lk = (fl & NF_LINKS) ? p.links + p.link_off[node] : nullptr;
+    int lo = 0;
+    float own[9];
+    if (FLAGS) {
 #pragma unroll
-        for (int k = 0; k < 9; k++) {
-            if (!(fl & (1u << k))) continue;
+        for (int k = 1; k < 9; k++) own[k] = SV<T>::ld(S + (I)oppk(k) * pl + node);
+        if (p.link_off) lo = p.link_off[node];
+    }
+    if (FLAGS && (fl & NF_SOLID)) {
+        solid_node_outputs<T>(p, i, j, (long long)node, dn, fl);
+        return;
+    }
+    if (FLAGS && (fl & NF_SPECIAL_MASK)) {
+        const bool has_links = (fl & NF_LINKS) != 0;
+        bool off[9];
+        Link L[9];
+        int m = 0;
+#pragma unroll
+        for (int k = 1; k < 9; k++) {
             const int si = i - cxk(k), sj = j - cyk(k);
-            const bool off = (!p.px && (si < 0 || si >= p.Nx)) || (!p.py && (sj < 0 || sj >= p.Ny));
-            if (off) {
+            off[k] = (!p.px && (si < 0 || si >= p.Nx)) || (!p.py && (sj < 0 || sj >= p.Ny));
+            // link records in direction order, one per flagged on-grid direction
+            if ((fl & (1u << k)) && !off[k] && has_links) L[k] = p.links[lo + m++];
+        }
+        float behind[9];
+#pragma unroll
+        for (int k = 1; k < 9; k++) {
+            behind[k] = 0.f;
+            if (!(fl & (1u << k))) continue;
+            if (off[k]) {
                 g[k] = SV<T>::ld_plain(Dst + (I)k * pl + node);
-                continue;
+            } else if (has_links) {
+                if (L[k].mode == LINK_IBB_LO) behind[k] = SV<T>::ld(S + (I)oppk(k) * pl + (I)L[k].behind);
+                else if (L[k].mode == LINK_IBB_HI) behind[k] = SV<T>::ld(S + (I)k * pl + (I)L[k].behind);
             }
-            const int ko = oppk(k);
-            const float own = SV<T>::ld(S + (I)ko * pl + node);
-            float val = own;
-            if (lk) {
-                const Link L = *lk++;
-                if (L.mode == LINK_IBB_LO)
-                    val = (float)L.c1 * own + (float)L.c2 * SV<T>::ld(S + (I)ko * pl + (I)L.behind);
-                else if (L.mode == LINK_IBB_HI)
-                    val = (float)L.c1 * own + (float)L.c2 * SV<T>::ld(S + (I)k * pl + (I)L.behind);
-                else if (L.mode == LINK_MOVING)
-                    val = own - (float)L.c2;
+        }
+#pragma unroll
+        for (int k = 1; k < 9; k++) {
+            if (!(fl & (1u << k)) || off[k]) continue;
+            float val = own[k];
+            if (has_links) {
+                if (L[k].mode == LINK_IBB_LO || L[k].mode == LINK_IBB_HI)
+                    val = (float)L[k].c1 * own[k] + (float)L[k].c2 * behind[k];
+                else if (L[k].mode == LINK_MOVING)
+                    val = own[k] - (float)L[k].c2;
             }
             g[k] = SV<T>::rnd(val);
-            // Per-node link sum in FP32 (a few terms); segment and case sums are FP64.
-            const float df = (own + val) + 2.0f * fp.wf[k];
+            // Per-node link sum in FP32 (a few terms); chunk and case sums are FP64.
+            const float df = (own[k] + val) + 2.0f * fp.wf[k];
             mfx -= df * cxk(k);
             mfy -= df * cyk(k);
             link = true;
@@ -342,81 +366,95 @@ __device__ __forceinline__ void collide_store_pair_shifted(const FastStepParams 
     for (int k = 0; k < 9; k++) SV<T>::st2(Dst + (I)k * pl + r0, g[k]);
 }
 
-// The nodes (i0, i0 + 1) of row j: the pair path when both exist and neither
-// is special, else each node on its own. The pair's loads are issued together
-// with the load of its flag words (not after them), so the common case waits
-// for memory once; the per-node path, taken by the few special nodes, loads
-// again. ax, ay: the two nodes' wall-link force terms (node i0 first), link:
-// either has wall links.
+// Flag bits that take a node off the pair path: a solid or off-grid pull
+// source, solid, edge-BC band or BC-written, cut links.
+constexpr uint32_t kSpecialFlags = NF_SPECIAL_MASK | NF_SOLID | NF_BAND | NF_BCW | NF_LINKS;
+
+// The pair (i0, i0 + 1) of row j when both nodes exist and neither is
+// special; nothing otherwise (those nodes are on the case's special-node
+// list). The pair's loads are issued together with the load of its flag
+// words, so the common case waits for memory once.
 template <typename T, typename I, bool FLAGS, bool COLLIDE, bool FORCE>
-__device__ __forceinline__ void step_two_shifted(const FastStepParams &fp, int i0, int j, double &ax,
-                                                 double &ay, bool &link) {
+__device__ __forceinline__ void step_pair_clean(const FastStepParams &fp, int i0, int j) {
     const StepParams &p = fp.s;
-    const bool two = i0 + 1 < p.Nx;
-    if (two) {
-        uint32_t f2 = 0;
-        if (FLAGS) f2 = *(const uint32_t *)(p.flags + ((I)j * (I)p.pitch + (I)i0));
-        int im = i0 - 1, ip2 = i0 + 2, jm = j - 1, jp = j + 1;
-        if (p.px) { if (im < 0) im += p.Nx; if (ip2 >= p.Nx) ip2 -= p.Nx; }
-        else { im = max(im, 0); ip2 = min(ip2, p.Nx - 1); }
-        if (p.py) { if (jm < 0) jm += p.Ny; if (jp >= p.Ny) jp -= p.Ny; }
-        else { jm = max(jm, 0); jp = min(jp, p.Ny - 1); }
-        float2 g[9];
-        load_pair_shifted<T, I>(p, i0, j, im, ip2, jm, jp, g);
-        constexpr uint32_t kSlow = NF_SPECIAL_MASK | NF_SOLID | NF_BAND | NF_BCW | NF_LINKS;
-        if (!FLAGS || ((f2 | (f2 >> 16)) & kSlow) == 0) {
-            collide_store_pair_shifted<T, I, COLLIDE, FORCE>(fp, i0, j, g);
-            return;
-        }
-    }
-    float mx = 0.f, my = 0.f;
-    bool l = false;
-    step_node_shifted<T, I, FLAGS, COLLIDE, FORCE>(fp, i0, j, mx, my, l);
-    ax = (double)mx;
-    ay = (double)my;
-    link = l;
-    if (two) {
-        mx = 0.f; my = 0.f; l = false;
-        step_node_shifted<T, I, FLAGS, COLLIDE, FORCE>(fp, i0 + 1, j, mx, my, l);
-        ax += (double)mx;
-        ay += (double)my;
-        link = link || l;
-    }
+    if (i0 + 1 >= p.Nx) return;
+    uint32_t f2 = 0;
+    if (FLAGS) f2 = *(const uint32_t *)(p.flags + ((I)j * (I)p.pitch + (I)i0));
+    int im = i0 - 1, ip2 = i0 + 2, jm = j - 1, jp = j + 1;
+    if (p.px) { if (im < 0) im += p.Nx; if (ip2 >= p.Nx) ip2 -= p.Nx; }
+    else { im = max(im, 0); ip2 = min(ip2, p.Nx - 1); }
+    if (p.py) { if (jm < 0) jm += p.Ny; if (jp >= p.Ny) jp -= p.Ny; }
+    else { jm = max(jm, 0); jp = min(jp, p.Ny - 1); }
+    float2 g[9];
+    load_pair_shifted<T, I>(p, i0, j, im, ip2, jm, jp, g);
+    if (FLAGS && ((f2 | (f2 >> 16)) & kSpecialFlags) != 0) return;
+    collide_store_pair_shifted<T, I, COLLIDE, FORCE>(fp, i0, j, g);
 }
 
 // Fully periodic grid without solids or edge BCs: no flag word. Each thread
-// steps two adjacent nodes. Five resident blocks per SM (48 registers, no
-// spills) keep more loads in flight than the unconstrained 64 registers
-// (measured: FP16 135 -> 147 GLUPS on 4096^2).
+// steps two adjacent nodes; the last column of an odd-width grid takes the
+// per-node path. Five resident blocks per SM (48 registers, no spills) keep
+// more loads in flight than the unconstrained 64 registers (measured: FP16
+// 135 -> 147 GLUPS on 4096^2).
 template <typename T, typename I, bool COLLIDE, bool FORCE>
 __global__ void __launch_bounds__(256, 5) k_step_shifted_plain(const FastStepParams fp) {
     pdl_launch_dependents();
     const int i0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    double ax = 0.0, ay = 0.0;
-    bool link = false;
-    if (i0 < fp.s.Nx && j < fp.s.Ny) step_two_shifted<T, I, false, COLLIDE, FORCE>(fp, i0, j, ax, ay, link);
+    if (i0 >= fp.s.Nx || j >= fp.s.Ny) return;
+    if (i0 + 1 < fp.s.Nx) {
+        step_pair_clean<T, I, false, COLLIDE, FORCE>(fp, i0, j);
+    } else {
+        float mx = 0.f, my = 0.f;
+        bool l = false;
+        step_node_shifted<T, I, false, COLLIDE, FORCE>(fp, i0, j, mx, my, l);
+    }
 }
 
-// General geometry (flag word per node), two adjacent nodes per thread. The
-// force partials of a 32-node segment come from half a warp. Five resident
-// blocks per SM (48 registers; the few spills are in the per-node path).
+// General geometry (flag word per node): the clean pairs only. The per-node
+// path is in k_step_special_shifted, over the case's list of special nodes
+// (every node of a pair with a special node, and an odd last column); kept
+// out of this kernel, it costs the common path no registers, spills or
+// instruction-cache space (measured: cylinder 2048x512 step 21.3 -> 14.2 us
+// with the special nodes left out).
 template <typename T, typename I, bool COLLIDE, bool FORCE>
 __global__ void __launch_bounds__(256, 5) k_step_shifted_geo(const FastStepParams fp) {
     pdl_launch_dependents();
-    const StepParams &p = fp.s;
     const int i0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    double ax = 0.0, ay = 0.0;
+    if (i0 < fp.s.Nx && j < fp.s.Ny) step_pair_clean<T, I, true, COLLIDE, FORCE>(fp, i0, j);
+}
+
+// The special nodes of a case, one per thread, on the per-node path (same
+// arithmetic as the pair path, so a node's bits do not depend on which path
+// steps it). Wall-link force terms are summed per 32-entry chunk of the list.
+// It reads and writes nothing the clean-pair kernel touches, so it is
+// launched right behind it and overlaps its last wave (pdl.cuh); it waits for
+// that kernel only at its end, so that what follows sees both. (Launched the
+// other way round, the clean-pair blocks must each wait at their end and hold
+// their SMs: measured slower.)
+template <typename T, typename I, bool FLAGS, bool COLLIDE, bool FORCE>
+__global__ void __launch_bounds__(128) k_step_special_shifted(const FastStepParams fp,
+                                                              const int2 *__restrict__ nodes, int n) {
+    pdl_launch_dependents();
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    float mx = 0.f, my = 0.f;
     bool link = false;
-    if (i0 < p.Nx && j < p.Ny) step_two_shifted<T, I, true, COLLIDE, FORCE>(fp, i0, j, ax, ay, link);
-    if (p.mem_partials) segment_pair_reduce2_store(ax, ay, link, i0, j, p.Nx, p.seg_slot, p.mem_partials);
+    if (q < n) {
+        const int2 ij = nodes[q];
+        step_node_shifted<T, I, FLAGS, COLLIDE, FORCE>(fp, ij.x, ij.y, mx, my, link);
+    }
+    if (fp.s.mem_partials)
+        chunk_reduce2_store((double)mx, (double)my, link, q >> 5, fp.s.chunk_slot, fp.s.mem_partials);
+    pdl_wait();
 }
 
 // Batched form (see k_step_batch_exact in kernels_exact.cu): tiles of
-// 2^(tws + 1) x 2^(8 - tws) nodes, two adjacent nodes per thread. Blocks stride
-// through the tile list, so the tiles in flight at any moment are neighbours
-// in memory (sequential DRAM streams, halo rows shared through L2).
+// 2^(tws + 1) x 2^(8 - tws) nodes, two adjacent nodes per thread, clean pairs
+// only (the special nodes of all cases are k_step_batch_special_shifted's).
+// Blocks stride through the tile list, so the tiles in flight at any moment
+// are neighbours in memory (sequential DRAM streams, halo rows shared through
+// L2).
 template <typename T, typename I, bool FORCE>
 __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepParams *__restrict__ sp,
                                                             const int *__restrict__ phase,
@@ -428,17 +466,39 @@ __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepPar
         const int4 td = tiles[t];
         const FastStepParams &fp = sp[2 * td.x + (sel ^ phase[td.x])];
         const int i0 = td.y + 2 * tx, j = td.z + ty;
-        double ax = 0.0, ay = 0.0;
-        bool link = false;
-        const bool in = i0 < fp.s.Nx && j < fp.s.Ny;
         // FORCE: some case of the batch has a body force; force-free cases
         // still take their own (force-free) arithmetic per case (collide_v).
-        if (in) {
-            if (fp.s.flags) step_two_shifted<T, I, true, true, FORCE>(fp, i0, j, ax, ay, link);
-            else step_two_shifted<T, I, false, true, FORCE>(fp, i0, j, ax, ay, link);
+        if (i0 < fp.s.Nx && j < fp.s.Ny) {
+            if (fp.s.flags) step_pair_clean<T, I, true, true, FORCE>(fp, i0, j);
+            else step_pair_clean<T, I, false, true, FORCE>(fp, i0, j);
         }
-        if (td.w) segment_pair_reduce2_store(ax, ay, link, i0, j, fp.s.Nx, fp.s.seg_slot, fp.s.mem_partials);
     }
+}
+
+// The special nodes of every case of a batch: nodes[q] = (case, i, j, chunk),
+// each case's list padded to a multiple of 32 entries (padding: i = -1), so
+// that a warp holds one chunk of one case and the force partials are those of
+// the case alone.
+template <typename T, typename I, bool FORCE>
+__global__ void __launch_bounds__(128) k_step_batch_special_shifted(const FastStepParams *__restrict__ sp,
+                                                                    const int *__restrict__ phase,
+                                                                    const int4 *__restrict__ nodes, int n,
+                                                                    int sel) {
+    pdl_launch_dependents();
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) {  // n is a multiple of 32: whole warps
+        const int4 e = nodes[q];
+        const FastStepParams &fp = sp[2 * e.x + (sel ^ phase[e.x])];
+        float mx = 0.f, my = 0.f;
+        bool link = false;
+        if (e.y >= 0) {
+            if (fp.s.flags) step_node_shifted<T, I, true, true, FORCE>(fp, e.y, e.z, mx, my, link);
+            else step_node_shifted<T, I, false, true, FORCE>(fp, e.y, e.z, mx, my, link);
+        }
+        if (fp.s.mem_partials)
+            chunk_reduce2_store((double)mx, (double)my, link, e.w, fp.s.chunk_slot, fp.s.mem_partials);
+    }
+    pdl_wait();
 }
 
 // live = false: the same instructions without their stores (the stage
@@ -675,63 +735,116 @@ cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s) {
 
 
 template <typename T, typename I, bool FORCE>
-static void step_shifted_tif(const FastStepParams &p, bool flags, bool collide, dim3 g, dim3 b,
-                             cudaStream_t s) {
+static cudaError_t step_shifted_tif(const FastStepParams &p, bool flags, bool collide, bool after, dim3 g, dim3 b,
+                                    cudaStream_t s) {
     if (flags) {
-        if (collide) k_step_shifted_geo<T, I, true, FORCE><<<g, b, 0, s>>>(p);
-        else k_step_shifted_geo<T, I, false, FORCE><<<g, b, 0, s>>>(p);
-    } else {
-        if (collide) k_step_shifted_plain<T, I, true, FORCE><<<g, b, 0, s>>>(p);
-        else k_step_shifted_plain<T, I, false, FORCE><<<g, b, 0, s>>>(p);
+        if (collide) return launch_follower(after, k_step_shifted_geo<T, I, true, FORCE>, g, b, s, p);
+        return launch_follower(after, k_step_shifted_geo<T, I, false, FORCE>, g, b, s, p);
     }
+    if (collide) return launch_follower(after, k_step_shifted_plain<T, I, true, FORCE>, g, b, s, p);
+    return launch_follower(after, k_step_shifted_plain<T, I, false, FORCE>, g, b, s, p);
 }
 
 // The body force is a template parameter: force-free kernels carry no forcing
 // code (fewer registers).
 template <typename T, typename I>
-static void step_shifted_ti(const FastStepParams &p, bool flags, bool collide, dim3 g, dim3 b,
-                            cudaStream_t s) {
-    if (p.s.has_force) step_shifted_tif<T, I, true>(p, flags, collide, g, b, s);
-    else step_shifted_tif<T, I, false>(p, flags, collide, g, b, s);
+static cudaError_t step_shifted_ti(const FastStepParams &p, bool flags, bool collide, bool after, dim3 g, dim3 b,
+                                   cudaStream_t s) {
+    if (p.s.has_force) return step_shifted_tif<T, I, true>(p, flags, collide, after, g, b, s);
+    return step_shifted_tif<T, I, false>(p, flags, collide, after, g, b, s);
 }
 
 template <typename T>
-static void step_shifted_t(const FastStepParams &p, bool flags, bool collide, dim3 g, dim3 b,
-                           cudaStream_t s) {
+static cudaError_t step_shifted_t(const FastStepParams &p, bool flags, bool collide, bool after, dim3 g, dim3 b,
+                                  cudaStream_t s) {
     // 32-bit element offsets whenever all nine planes fit.
-    if (9LL * p.s.plane < (1LL << 31)) step_shifted_ti<T, int>(p, flags, collide, g, b, s);
-    else step_shifted_ti<T, long long>(p, flags, collide, g, b, s);
+    if (9LL * p.s.plane < (1LL << 31)) return step_shifted_ti<T, int>(p, flags, collide, after, g, b, s);
+    return step_shifted_ti<T, long long>(p, flags, collide, after, g, b, s);
 }
 
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
-                         cudaStream_t s) {
+                         bool after_special, cudaStream_t s) {
     // Two nodes per thread along x.
     const dim3 g((p.s.Nx + 2 * block.x - 1) / (2 * block.x), (p.s.Ny + block.y - 1) / block.y);
-    if (store == STORE_F32) step_shifted_t<float>(p, flags, collide, g, block, s);
-    else step_shifted_t<__half>(p, flags, collide, g, block, s);
-    return cudaGetLastError();
+    if (store == STORE_F32) return step_shifted_t<float>(p, flags, collide, after_special, g, block, s);
+    return step_shifted_t<__half>(p, flags, collide, after_special, g, block, s);
+}
+
+template <typename T, typename I, bool FORCE>
+static cudaError_t special_shifted_tif(const FastStepParams &p, const int2 *nodes, int n, bool flags, bool collide,
+                                       bool after_bulk, cudaStream_t s) {
+    const dim3 g((n + 127) / 128), b(128);
+    if (flags) {
+        if (collide) return launch_follower(after_bulk, k_step_special_shifted<T, I, true, true, FORCE>, g, b, s, p, nodes, n);
+        return launch_follower(after_bulk, k_step_special_shifted<T, I, true, false, FORCE>, g, b, s, p, nodes, n);
+    }
+    if (collide) return launch_follower(after_bulk, k_step_special_shifted<T, I, false, true, FORCE>, g, b, s, p, nodes, n);
+    return launch_follower(after_bulk, k_step_special_shifted<T, I, false, false, FORCE>, g, b, s, p, nodes, n);
+}
+
+template <typename T>
+static cudaError_t special_shifted_t(const FastStepParams &p, const int2 *nodes, int n, bool flags, bool collide,
+                                     bool after_bulk, cudaStream_t s) {
+    const bool wide = 9LL * p.s.plane >= (1LL << 31);
+    if (p.s.has_force) {
+        if (wide) return special_shifted_tif<T, long long, true>(p, nodes, n, flags, collide, after_bulk, s);
+        return special_shifted_tif<T, int, true>(p, nodes, n, flags, collide, after_bulk, s);
+    }
+    if (wide) return special_shifted_tif<T, long long, false>(p, nodes, n, flags, collide, after_bulk, s);
+    return special_shifted_tif<T, int, false>(p, nodes, n, flags, collide, after_bulk, s);
+}
+
+cudaError_t special_shifted(const FastStepParams &p, const int2 *nodes, int n, int store, bool flags, bool collide,
+                            bool after_bulk, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    if (store == STORE_F32) return special_shifted_t<float>(p, nodes, n, flags, collide, after_bulk, s);
+    return special_shifted_t<__half>(p, nodes, n, flags, collide, after_bulk, s);
 }
 
 template <typename T, bool FORCE>
-static void step_batch_shifted_tf(const FastStepParams *sp, const int *phase, const int4 *tiles, int ntiles,
-                                  int sel, int tws, bool wide, int grid, cudaStream_t s) {
-    if (wide) k_step_batch_shifted<T, long long, FORCE><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
-    else k_step_batch_shifted<T, int, FORCE><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+static cudaError_t special_batch_shifted_tf(const FastStepParams *sp, const int *phase, const int4 *nodes, int n,
+                                            int sel, bool wide, bool after_bulk, cudaStream_t s) {
+    const dim3 g((n + 127) / 128), b(128);
+    if (wide)
+        return launch_follower(after_bulk, k_step_batch_special_shifted<T, long long, FORCE>, g, b, s, sp, phase,
+                               nodes, n, sel);
+    return launch_follower(after_bulk, k_step_batch_special_shifted<T, int, FORCE>, g, b, s, sp, phase, nodes, n,
+                           sel);
+}
+
+cudaError_t special_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *nodes, int n, int sel,
+                                  int store, bool wide, bool force, bool after_bulk, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    if (n % 32) return cudaErrorInvalidValue;
+    if (store == STORE_F32) {
+        if (force) return special_batch_shifted_tf<float, true>(sp, phase, nodes, n, sel, wide, after_bulk, s);
+        return special_batch_shifted_tf<float, false>(sp, phase, nodes, n, sel, wide, after_bulk, s);
+    }
+    if (force) return special_batch_shifted_tf<__half, true>(sp, phase, nodes, n, sel, wide, after_bulk, s);
+    return special_batch_shifted_tf<__half, false>(sp, phase, nodes, n, sel, wide, after_bulk, s);
+}
+
+template <typename T, bool FORCE>
+static cudaError_t step_batch_shifted_tf(const FastStepParams *sp, const int *phase, const int4 *tiles, int ntiles,
+                                         int sel, int tws, bool wide, int grid, bool after, cudaStream_t s) {
+    if (wide)
+        return launch_follower(after, k_step_batch_shifted<T, long long, FORCE>, dim3(grid), dim3(256), s, sp, phase,
+                               tiles, ntiles, sel, tws);
+    return launch_follower(after, k_step_batch_shifted<T, int, FORCE>, dim3(grid), dim3(256), s, sp, phase, tiles,
+                           ntiles, sel, tws);
 }
 
 cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
                                int ntiles, int sel, int tws, int store, bool wide, bool force, int grid,
-                               cudaStream_t s) {
+                               bool after_special, cudaStream_t s) {
     if (ntiles == 0) return cudaSuccess;
     if (tws < 5 || tws > 8) return cudaErrorInvalidValue;
     if (store == STORE_F32) {
-        if (force) step_batch_shifted_tf<float, true>(sp, phase, tiles, ntiles, sel, tws, wide, grid, s);
-        else step_batch_shifted_tf<float, false>(sp, phase, tiles, ntiles, sel, tws, wide, grid, s);
-    } else {
-        if (force) step_batch_shifted_tf<__half, true>(sp, phase, tiles, ntiles, sel, tws, wide, grid, s);
-        else step_batch_shifted_tf<__half, false>(sp, phase, tiles, ntiles, sel, tws, wide, grid, s);
+        if (force) return step_batch_shifted_tf<float, true>(sp, phase, tiles, ntiles, sel, tws, wide, grid, after_special, s);
+        return step_batch_shifted_tf<float, false>(sp, phase, tiles, ntiles, sel, tws, wide, grid, after_special, s);
     }
-    return cudaGetLastError();
+    if (force) return step_batch_shifted_tf<__half, true>(sp, phase, tiles, ntiles, sel, tws, wide, grid, after_special, s);
+    return step_batch_shifted_tf<__half, false>(sp, phase, tiles, ntiles, sel, tws, wide, grid, after_special, s);
 }
 
 int step_batch_shifted_grid(int store) {

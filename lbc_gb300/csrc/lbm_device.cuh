@@ -421,17 +421,18 @@ struct StepParams {
     double *bandf;            // [9][nslots], pre-collision f_new of band nodes (FP64 storage)
     float *bandg;             // [9][nslots], the same as g = f - w (shifted storage)
     double *bandm_next;       // [3][nslots], their moments (for the next step's BCs)
-    // momentum-exchange force (null when the geometry has no wall links):
-    // every 32-node row segment (j, i / 32) that contains wall links has a
-    // slot (seg_slot >= 0, numbered in row-major order from the geometry);
-    // the threads that step it (a warp of one node per thread in FP64, half a
-    // warp of two nodes per thread in shifted storage) store its sum at
-    // mem_partials[2 * slot] and k_force_reduce adds the slots up in order.
-    // Block and tile widths are multiples of 32 threads, so the sum does not
-    // depend on the block or tile shape, nor on whether the case runs alone or
-    // in a batch.
+    // momentum-exchange force (null when the geometry has no wall links).
+    // FP64 storage: every 32-node row segment (j, i / 32) that contains wall
+    // links has a slot (seg_slot >= 0, numbered in row-major order from the
+    // geometry); the warp that steps it stores its sum at mem_partials[2 *
+    // slot]. Shifted storage: wall-link nodes are special nodes, stepped from
+    // the case's special-node list, and every 32-entry chunk of that list
+    // that contains links has a slot (chunk_slot[chunk] >= 0). k_force_reduce
+    // adds the slots up in order. Neither depends on the block or tile shape,
+    // nor on whether the case runs alone or in a batch.
     double *mem_partials;
-    const int *seg_slot;      // [Ny][(Nx + 31) / 32]
+    const int *seg_slot;      // [Ny][(Nx + 31) / 32] (FP64 storage)
+    const int *chunk_slot;    // [special list length / 32] (shifted storage)
 };
 
 struct FinishParams;

@@ -130,20 +130,19 @@ __device__ __forceinline__ void segment_reduce2_store(double a, double b, bool l
     }
 }
 
-// As segment_reduce2_store for threads that each step two adjacent nodes
-// (i0, i0 + 1), i0 even: a 32-node segment is half a warp (lanes 0-15 or
-// 16-31), summed in a fixed order into the lane with i0 % 32 == 0. Every lane
-// of the warp must call it.
-__device__ __forceinline__ void segment_pair_reduce2_store(double a, double b, bool link, int i0, int j, int Nx,
-                                                           const int *__restrict__ seg_slot, double *partials) {
+// Force partial of one 32-entry chunk of a special-node list (one warp;
+// every lane must call it): the lanes' terms in a fixed shuffle tree, stored
+// at the chunk's slot when the chunk contains wall links.
+__device__ __forceinline__ void chunk_reduce2_store(double a, double b, bool link, int chunk,
+                                                    const int *__restrict__ chunk_slot, double *partials) {
     if (!__any_sync(0xffffffffu, link)) return;
 #pragma unroll
-    for (int o = 8; o > 0; o >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, o, 16);
-        b += __shfl_down_sync(0xffffffffu, b, o, 16);
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
     }
-    if ((i0 & 31) == 0) {
-        const int slot = seg_slot[(size_t)j * ((Nx + 31) >> 5) + (i0 >> 5)];
+    if ((threadIdx.x & 31) == 0) {
+        const int slot = chunk_slot[chunk];
         if (slot >= 0) {
             partials[2 * (size_t)slot] = a;
             partials[2 * (size_t)slot + 1] = b;

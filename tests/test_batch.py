@@ -75,12 +75,13 @@ def test_batch_info_counts_launches():
     assert nodes == sum(c.nodes for _, c, _, _ in mixed)
     levels = max(s.info().edge_launches for _, _, _, s in mixed)
     assert 1 <= levels <= max(s.info().edge_stages for _, _, _, s in mixed)
-    # bulk step + one launch per stage level; the levels also finish the
-    # BC-written nodes and reduce the wall forces
-    assert lps == 1 + levels
+    # special nodes + clean pairs + one launch per stage level; the levels
+    # also finish the BC-written nodes and reduce the wall forces
+    assert lps == 2 + levels
     for _, _, _, s in mixed:
         i = s.info()
+        bulk = 2 if i.has_geometry else 1  # flag-free grids: one plain kernel
         if i.edge_launches:
-            assert i.launches_per_step == 1 + i.edge_launches
+            assert i.launches_per_step == bulk + i.edge_launches
         else:  # the bulk step, and the force reduction when there are walls
-            assert i.launches_per_step in (1, 2)
+            assert i.launches_per_step in (bulk, bulk + 1)

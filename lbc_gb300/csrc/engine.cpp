@@ -1307,6 +1307,7 @@ bool Batch::build() {
         nodes_ += (long long)s->Nx() * s->Ny();
         if (9LL * s->plane() >= (1LL << 31)) wide_ = true;
         if (s->has_force()) any_force_ = true;
+        if (!s->has_flags()) all_flags_ = false;
         if (s->has_mem()) force.push_back(s->force_slot());
         if (!s->fused_finish())
             for (const int2 &w : s->wnodes()) fin_nodes.push_back(make_int4(c, w.x, w.y, 0));
@@ -1370,7 +1371,7 @@ bool Batch::launch_batched(int sel) {
     } else {
         // the clean pairs, then the special nodes overlapping their tail
         CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
-                                      store_, wide_, any_force_, grid_, false, stream_));
+                                      store_, wide_, any_force_, all_flags_, grid_, false, stream_));
         if (nspecial_)
             CK(launch::special_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_special_, nspecial_, sel,
                                              store_, wide_, any_force_, true, stream_));

@@ -309,6 +309,7 @@ class Batch {
     int tws_ = 6;
     bool wide_ = false;  // some case needs 64-bit element offsets
     bool any_force_ = false;  // some case has a body force
+    bool all_flags_ = true;   // every case has a flag word
     int launches_per_step_ = 0;
     void *d_sp_ = nullptr;         // StepParams or FastStepParams [2 * ncases]
     int *d_phase_ = nullptr;       // [ncases] (and stage entries)

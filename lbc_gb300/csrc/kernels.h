@@ -158,9 +158,10 @@ cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int 
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s);
 // wide: some case has 9 * plane >= 2^31 elements (64-bit element offsets).
 // force: some case has a body force (the forced kernel form serves all cases).
+// all_flags: every case has a flag word (the flag-free pair form is left out).
 cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
-                               int ntiles, int sel, int tws, int store, bool wide, bool force, int grid,
-                               bool after_special, cudaStream_t s);
+                               int ntiles, int sel, int tws, int store, bool wide, bool force, bool all_flags,
+                               int grid, bool after_special, cudaStream_t s);
 int step_batch_shifted_grid(int store);
 cudaError_t finish_batch_shifted(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
                                  int sel, int store, cudaStream_t s);

@@ -842,6 +842,7 @@ bool Solver::set_impedance(int entry, const double *R, const double *m, const do
         h[(size_t)IMP_WC * n + t] = 1.0;
         for (int f = 0; f < nf; f++) h[(size_t)imp_field(f, 0) * n + t] = 1.0;
     }
+    if (!st->d_vn && !dalloc(&st->d_vn, (size_t)n)) return false;
     if (!st->d_imp || st->imp_nf != nf) {
         if (!dalloc(&st->d_imp, h.size())) return false;
     }
@@ -1358,8 +1359,39 @@ bool Batch::build() {
         d_stage_lists_.push_back(d);
         stage_counts_.push_back(cnt);
     }
+    // Shifted storage: impedance walls are advanced ahead of their stage, in
+    // the special-node launch (entries numbered as run() fills the lists).
+    if (store_ != STORE_F64) {
+        std::vector<ImpWall> walls;
+        std::vector<int2> imp;
+        std::vector<int> next(max_stages_, 0);
+        for (Solver *c : cases_)
+            for (size_t l = 0; l < c->stage_groups().size(); l++)
+                for (int k : c->stage_groups()[l]) {
+                    const Stage &st = c->stages()[k];
+                    const int e = next[l]++;
+                    if (!st.d_imp || !st.d_vn || st.kind != BC_VEL_BOT_REG) continue;
+                    ImpWall w;
+                    std::memset(&w, 0, sizeof w);
+                    w.pair = d_stage_lists_[l] + 2 * e;
+                    w.entry = e;
+                    w.vn = st.d_vn;
+                    for (int t0 = 0; t0 < st.along; t0 += 128) imp.push_back(make_int2((int)walls.size(), t0));
+                    walls.push_back(w);
+                    wall_at_.push_back(make_int2((int)l, e));
+                }
+        nimp_ = (int)imp.size();
+        if (nimp_) {
+            if (!balloc(allocs_, &d_walls_, walls.size(), stream_) || !balloc(allocs_, &d_imp_, imp.size(), stream_))
+                return false;
+            CK(cudaMemcpyAsync(d_walls_, walls.data(), walls.size() * sizeof(ImpWall), cudaMemcpyHostToDevice, stream_));
+            CK(cudaMemcpyAsync(d_imp_, imp.data(), imp.size() * sizeof(int2), cudaMemcpyHostToDevice, stream_));
+            walls_host_ = walls;
+        }
+    }
     // The force reductions ride in the first stage level's launch.
-    launches_per_step_ = 1 + (nspecial_ ? 1 : 0) + max_stages_ + (nfin_ ? 1 : 0) + (nforce_ && max_stages_ == 0 ? 1 : 0);
+    launches_per_step_ = 1 + (nspecial_ || nimp_ ? 1 : 0) + max_stages_ + (nfin_ ? 1 : 0) +
+                         (nforce_ && max_stages_ == 0 ? 1 : 0);
     CK(cudaStreamSynchronize(stream_));
     return true;
 }
@@ -1372,9 +1404,9 @@ bool Batch::launch_batched(int sel) {
         // the clean pairs, then the special nodes overlapping their tail
         CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
                                       store_, wide_, any_force_, all_flags_, grid_, false, stream_));
-        if (nspecial_)
+        if (nspecial_ || nimp_)
             CK(launch::special_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_special_, nspecial_, sel,
-                                             store_, wide_, any_force_, true, stream_));
+                                             d_walls_, d_imp_, nimp_, store_, wide_, any_force_, true, stream_));
     }
     for (int s = 0; s < max_stages_; s++)
         CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], max_along_, store_, sel, d_force_,
@@ -1448,6 +1480,12 @@ bool Batch::run(int nsteps) {
                     lists[l].push_back(s->stage_params(s->stages()[k], 1 - cur, par ^ 1));
                     lists[l].back().fin = d_fin_ + 2 * c + 1;
                 }
+        }
+        // Walls advanced ahead: their stages read the velocities.
+        for (size_t w = 0; w < wall_at_.size(); w++) {
+            const int2 le = wall_at_[w];
+            lists[le.x][2 * le.y].vn = walls_host_[w].vn;
+            lists[le.x][2 * le.y + 1].vn = walls_host_[w].vn;
         }
         if (store_ == STORE_F64)
             okk = okk && check_cuda(cudaMemcpyAsync(d_sp_, sp.data(), sp.size() * sizeof(StepParams), cudaMemcpyHostToDevice, stream_), "H2D");

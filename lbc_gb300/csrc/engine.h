@@ -49,6 +49,8 @@ struct Stage {
     double *d_val1 = nullptr, *d_val2 = nullptr;
     // impedance wall (bottom regularized entries only)
     double *d_imp = nullptr;
+    double *d_vn = nullptr;     // wall velocity of the current step, when a batch computes it ahead
+
     int imp_nf = 0;
     double imp_alpha = 0.0;
     double imp_wcos = 1.0, imp_wsin = 0.0;
@@ -321,6 +323,12 @@ class Batch {
     ForceSlot *d_force_ = nullptr;
     int4 *d_special_ = nullptr;    // (case, i, j, chunk), shifted storage
     int nspecial_ = 0;
+    // impedance walls advanced in the special-node launch (shifted storage)
+    ImpWall *d_walls_ = nullptr;
+    int2 *d_imp_ = nullptr;         // (wall, first node) per 128-node block
+    int nimp_ = 0;
+    std::vector<ImpWall> walls_host_;
+    std::vector<int2> wall_at_;     // (level, entry) of each wall's stage
     cudaGraphExec_t pair_exec_ = nullptr;
     std::vector<void *> allocs_;
     // host copies of the per-run parameters (kept until their uploads ran)

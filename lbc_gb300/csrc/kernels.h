@@ -98,6 +98,16 @@ struct StageGroup {
     int nfs;
 };
 
+// An impedance wall of a batch advanced ahead of its stage: the entry's
+// stage parameters for both directions (pair[sel ^ phase[entry]]) and the
+// buffer the stage reads the wall velocities from.
+struct ImpWall {
+    const StageParams *pair;
+    int entry;
+    int pad;
+    double *vn;
+};
+
 namespace launch {
 // exact FP64 (kernels_exact.cu)
 cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block, cudaStream_t s);
@@ -148,9 +158,11 @@ cudaError_t finish_shifted(const FinishParams &p, int store, bool collide, cudaS
 cudaError_t special_shifted(const FastStepParams &p, const int2 *nodes, int n, int store, bool flags, bool collide,
                             bool after_bulk, cudaStream_t s);
 // The special nodes of a batch: nodes[q] = (case, i, j, chunk), n a multiple
-// of 32 (each case's list padded to 32 entries, i = -1).
+// of 32 (each case's list padded to 32 entries, i = -1); then nimp blocks of
+// impedance-wall updates, imp[b] = (wall, first of 128 nodes).
 cudaError_t special_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *nodes, int n, int sel,
-                                  int store, bool wide, bool force, bool after_bulk, cudaStream_t s);
+                                  const ImpWall *walls, const int2 *imp, int nimp, int store, bool wide, bool force,
+                                  bool after_bulk, cudaStream_t s);
 // Edge BCs of shifted storage in FP32 (launch::stage_group / stage_batch dispatch here).
 cudaError_t stage_group_shifted(const StageGroup &g, int store, bool collide, bool after_bulk, cudaStream_t s);
 cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, int max_along, int store,

@@ -482,12 +482,29 @@ __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepPar
 // each case's list padded to a multiple of 32 entries (padding: i = -1), so
 // that a warp holds one chunk of one case and the force partials are those of
 // the case alone.
+// Blocks from nsb on advance the batch's impedance walls for this step
+// (impedance_ahead): imp[b - nsb] = (wall, first node) of 128 nodes, walls[w]
+// = the wall's stage parameters for both directions and its velocity buffer.
+// That FP64 work depends only on the previous step's moments, so it runs here,
+// beside the latency-bound special nodes, instead of at the head of the edge
+// launch.
 template <typename T, typename I, bool FORCE>
 __global__ void __launch_bounds__(128) k_step_batch_special_shifted(const FastStepParams *__restrict__ sp,
                                                                     const int *__restrict__ phase,
                                                                     const int4 *__restrict__ nodes, int n,
-                                                                    int sel) {
+                                                                    int sel, int nsb,
+                                                                    const ImpWall *__restrict__ walls,
+                                                                    const int2 *__restrict__ imp) {
     pdl_launch_dependents();
+    if ((int)blockIdx.x >= nsb) {
+        const int2 b = imp[blockIdx.x - nsb];
+        const ImpWall &w = walls[b.x];
+        const StageParams &p = w.pair[sel ^ phase[w.entry]];
+        const int t = b.y + (int)threadIdx.x;
+        if (t < p.along) impedance_ahead(p, w.vn, t);
+        pdl_wait();
+        return;
+    }
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q < n) {  // n is a multiple of 32: whole warps
         const int4 e = nodes[q];
@@ -652,11 +669,15 @@ __device__ __forceinline__ void stage_point_s(const StageParams &p, const StageP
 // that counts, after the wait, runs from a warm cache.
 template <typename T, bool COLLIDE, int KIND>
 __device__ __forceinline__ void stage_thread_s(const StageParams &p, const FinishParams &f, int t) {
-    const StagePre c = stage_preload(p, t, KIND);
+    StagePre c = stage_preload(p, t, KIND);
 #pragma unroll 1
     for (int pass = 0; pass < 2; pass++) {
         const bool live = pass != 0;
-        if (live) pdl_wait();
+        if (live) {
+            pdl_wait();
+            // impedance wall advanced ahead (batches): its velocity is ready now
+            if (KIND == BC_VEL_BOT_REG && c.imp && p.vn) c.v2 = -__ldcg(p.vn + t);
+        }
         stage_point_s<T>(p, c, t, KIND, live);
         if (c.fin) finish_node_shifted<T, COLLIDE>(f, c.ij, c.slot, live);
     }
@@ -806,25 +827,30 @@ cudaError_t special_shifted(const FastStepParams &p, const int2 *nodes, int n, i
 
 template <typename T, bool FORCE>
 static cudaError_t special_batch_shifted_tf(const FastStepParams *sp, const int *phase, const int4 *nodes, int n,
-                                            int sel, bool wide, bool after_bulk, cudaStream_t s) {
-    const dim3 g((n + 127) / 128), b(128);
+                                            int sel, const ImpWall *walls, const int2 *imp, int nimp, bool wide,
+                                            bool after_bulk, cudaStream_t s) {
+    const int nsb = (n + 127) / 128;
+    const dim3 g(nsb + nimp), b(128);
     if (wide)
         return launch_follower(after_bulk, k_step_batch_special_shifted<T, long long, FORCE>, g, b, s, sp, phase,
-                               nodes, n, sel);
+                               nodes, n, sel, nsb, walls, imp);
     return launch_follower(after_bulk, k_step_batch_special_shifted<T, int, FORCE>, g, b, s, sp, phase, nodes, n,
-                           sel);
+                           sel, nsb, walls, imp);
 }
 
 cudaError_t special_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *nodes, int n, int sel,
-                                  int store, bool wide, bool force, bool after_bulk, cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
+                                  const ImpWall *walls, const int2 *imp, int nimp, int store, bool wide, bool force,
+                                  bool after_bulk, cudaStream_t s) {
+    if (n + nimp == 0) return cudaSuccess;
     if (n % 32) return cudaErrorInvalidValue;
     if (store == STORE_F32) {
-        if (force) return special_batch_shifted_tf<float, true>(sp, phase, nodes, n, sel, wide, after_bulk, s);
-        return special_batch_shifted_tf<float, false>(sp, phase, nodes, n, sel, wide, after_bulk, s);
+        if (force)
+            return special_batch_shifted_tf<float, true>(sp, phase, nodes, n, sel, walls, imp, nimp, wide, after_bulk, s);
+        return special_batch_shifted_tf<float, false>(sp, phase, nodes, n, sel, walls, imp, nimp, wide, after_bulk, s);
     }
-    if (force) return special_batch_shifted_tf<__half, true>(sp, phase, nodes, n, sel, wide, after_bulk, s);
-    return special_batch_shifted_tf<__half, false>(sp, phase, nodes, n, sel, wide, after_bulk, s);
+    if (force)
+        return special_batch_shifted_tf<__half, true>(sp, phase, nodes, n, sel, walls, imp, nimp, wide, after_bulk, s);
+    return special_batch_shifted_tf<__half, false>(sp, phase, nodes, n, sel, walls, imp, nimp, wide, after_bulk, s);
 }
 
 template <typename T, bool FORCE, bool ALLFLAGS>

@@ -20,6 +20,7 @@
 // Solver::run(a) followed by run(b) equals run(a + b) and every case's
 // arithmetic is independent of the others in a batch, a request's result is
 // the same alone and in any mix.
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <deque>
@@ -203,16 +204,29 @@ static bool retire(Request *r) {
 // slot limit and the device-memory budget allow (one request is always let in
 // when nothing at all is active, so a request larger than the budget still
 // runs alone).
+// Requests of this lane's storage type, in arrival order, while the slot
+// limit and the memory budget allow. The FP64 lane holds at most a quarter of
+// the slots while requests of another type are queued or running: FP64
+// requests step at GB300's FP64 rate, about 12x slower per node than FP32,
+// and without the cap they accumulate in the active set and leave the
+// shorter requests queued behind them.
 static std::vector<Request *> take_admissions(lbm_gpu_server *S, Lane &L) {
     std::vector<Request *> out;
     std::lock_guard<std::mutex> lk(S->mu);
+    int cap = S->max_active;
+    if (L.storage == STORE_F64) {
+        bool others = S->n_active > (int)L.active.size();
+        for (const Request *r : S->queue)
+            if (r->storage != L.storage) { others = true; break; }
+        if (others) cap = std::max(1, S->max_active / 4);
+    }
     for (auto it = S->queue.begin(); it != S->queue.end();) {
         Request *r = *it;
         if (r->storage != L.storage) {
             ++it;
             continue;
         }
-        if (S->n_active >= S->max_active) break;
+        if (S->n_active >= S->max_active || (int)(L.active.size() + out.size()) >= cap) break;
         if (S->in_use + r->est_bytes > S->budget && S->n_active > 0) break;
         it = S->queue.erase(it);
         out.push_back(r);

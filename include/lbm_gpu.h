@@ -149,8 +149,9 @@ int lbm_gpu_msd_zoh(double R, double m, double K, double *A, double *b);
 int lbm_gpu_get_info(lbm_gpu_solver *s, lbm_gpu_info *info);
 /* Thread-block shape of the fused step (bx * by <= 256, bx multiple of 32).
  * No result depends on it: populations, fields and the momentum-exchange force
- * (summed per 32-node row segment in a fixed order) are bit-identical for
- * every shape. */
+ * (summed in a fixed order per 32-node row segment in FP64 storage, per
+ * 32-entry chunk of the case's special-node list in shifted storage) are
+ * bit-identical for every shape. */
 int lbm_gpu_set_block(lbm_gpu_solver *s, int bx, int by);
 int lbm_gpu_get_block(lbm_gpu_solver *s, int *bx, int *by);
 

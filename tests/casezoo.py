@@ -150,6 +150,10 @@ def standard_cases():
         ("zoo_ibb", zoo_ibb, 60),
         ("zoo_open_edges", zoo_open_edges, 60),
         ("zoo_convective_chain", zoo_convective_chain, 60),
+        # odd widths: the last column has no pair partner (per-node path in
+        # the plain kernel, special-node list in geometry kernels and batches)
+        ("taylor_green_odd", lambda: cases.taylor_green(47, 33, 0.04, 0.56), 100),
+        ("cylinder_odd", lambda: cases.cylinder_wake(95, 33, D=8, xc=24, yc=16), 60),
     ]
 
 

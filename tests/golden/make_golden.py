@@ -6,7 +6,7 @@ final state and the per-step force of each run, and copies the first records
 of lbc's shipped cylinder force history
 (cases/cylinder/sol/forces_IBB_res_20_Re_20.00_tau_0.90.bin).
 
-    python tests/golden/make_golden.py [LBC_SOURCE_DIR] [--vtk-only]
+    python tests/golden/make_golden.py [LBC_SOURCE_DIR] [--vtk-only] [--only=NAME,NAME]
 
 It also writes lbc_small.vtk: lbc's write_vtk_binary_2D on a small seeded field.
 """
@@ -61,12 +61,17 @@ def main():
     if "--vtk-only" in sys.argv:
         return
     ref = LbcAbi(lib, "ref_")
+    only = [a.split("=", 1)[1].split(",") for a in sys.argv[1:] if a.startswith("--only=")]
     for name, builder, steps in casezoo.standard_cases():
+        if only and name not in only[0]:
+            continue
         case, st = builder()
         forces = ref.run(case, st, steps, record_forces=True)
         np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), f=st.f, f_new=st.f_new,
                             rho=st.rho, u=st.u, v=st.v, forces=forces, steps=steps)
         print("wrote", name, steps, "steps")
+    if only:
+        return
     g = np.fromfile(os.path.join(src, "cases", "cylinder", "sol",
                                  "forces_IBB_res_20_Re_20.00_tau_0.90.bin")).reshape(-1, 3)
     np.save(os.path.join(HERE, "lbc_cylinder_forces_res20_first300.npy"), g[:300])

@@ -11,7 +11,8 @@ from lbc_gb300 import cases
 pytestmark = pytest.mark.gpu
 FIELDS = ("f", "f_new", "rho", "u", "v")
 MIX = ["zoo_ibb", "zoo_convective_chain", "zoo_zh_mixed", "taylor_green", "poiseuille",
-       "zoo_periodic_late", "zoo_pressure_reg", "cylinder_wake_small", "zoo_open_edges", "liner"]
+       "zoo_periodic_late", "zoo_pressure_reg", "cylinder_wake_small", "zoo_open_edges", "liner",
+       "taylor_green_odd", "cylinder_odd"]
 
 
 def _build(n):

@@ -96,7 +96,8 @@ def test_resident_run_matches_lbc(oracle, name):
 
 
 @pytest.mark.parametrize("storage", ["f64", "f32", "f16"])
-@pytest.mark.parametrize("name", ["zoo_ibb", "zoo_convective_chain", "taylor_green", "zoo_open_edges"])
+@pytest.mark.parametrize("name", ["zoo_ibb", "zoo_convective_chain", "taylor_green", "zoo_open_edges",
+                                  "taylor_green_odd", "cylinder_odd"])
 def test_chunked_runs_and_block_shapes_agree(name, storage):
     """run(a); run(b) == run(a + b) bit for bit, and the result does not
     depend on the thread-block shape (no races between nodes)."""

@@ -923,7 +923,7 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
         const FastStepParams fp = fast_params(p);
         // The clean pairs, then the special nodes overlapping their last wave
         // (the plain kernel of a flag-free grid steps its own odd column).
-        CK(launch::step_shifted(fp, d_.store, has_flags_, collide, block_, false, s));
+        CK(launch::step_shifted(fp, d_.store, has_flags_, collide, block_, s));
         if (special_launch()) CK(launch::special_shifted(fp, d_special_, nspecial_, d_.store, true, collide, true, s));
     }
     if (groups_.empty()) {
@@ -1403,7 +1403,7 @@ bool Batch::launch_batched(int sel) {
     } else {
         // the clean pairs, then the special nodes overlapping their tail
         CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
-                                      store_, wide_, any_force_, all_flags_, grid_, false, stream_));
+                                      store_, wide_, any_force_, all_flags_, grid_, stream_));
         if (nspecial_ || nimp_)
             CK(launch::special_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_special_, nspecial_, sel,
                                              d_walls_, d_imp_, nimp_, store_, wide_, any_force_, true, stream_));

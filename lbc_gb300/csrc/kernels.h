@@ -147,10 +147,8 @@ cudaError_t finish_batch_exact(const FinishParams *fp, const int *phase, const i
 cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStream_t s);
 
 // shifted storage (kernels_shifted.cu)
-// after_special: launch as a programmatic follower of the previous kernel
-// (unused: the special-node kernel follows the step kernel).
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
-                         bool after_special, cudaStream_t s);
+                         cudaStream_t s);
 cudaError_t finish_shifted(const FinishParams &p, int store, bool collide, cudaStream_t s);
 // The special nodes of a case (nodes[0 .. n)) on the per-node path; flags: the
 // case has a flag word. Launched right after the case's clean-pair kernel
@@ -173,7 +171,7 @@ cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s);
 // all_flags: every case has a flag word (the flag-free pair form is left out).
 cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
                                int ntiles, int sel, int tws, int store, bool wide, bool force, bool all_flags,
-                               int grid, bool after_special, cudaStream_t s);
+                               int grid, cudaStream_t s);
 int step_batch_shifted_grid(int store);
 cudaError_t finish_batch_shifted(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
                                  int sel, int store, cudaStream_t s);

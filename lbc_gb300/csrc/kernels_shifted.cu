@@ -787,11 +787,12 @@ static cudaError_t step_shifted_t(const FastStepParams &p, bool flags, bool coll
 }
 
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
-                         bool after_special, cudaStream_t s) {
-    // Two nodes per thread along x.
+                         cudaStream_t s) {
+    // Two nodes per thread along x; an ordinary launch (what follows it is
+    // launched as its programmatic follower).
     const dim3 g((p.s.Nx + 2 * block.x - 1) / (2 * block.x), (p.s.Ny + block.y - 1) / block.y);
-    if (store == STORE_F32) return step_shifted_t<float>(p, flags, collide, after_special, g, block, s);
-    return step_shifted_t<__half>(p, flags, collide, after_special, g, block, s);
+    if (store == STORE_F32) return step_shifted_t<float>(p, flags, collide, false, g, block, s);
+    return step_shifted_t<__half>(p, flags, collide, false, g, block, s);
 }
 
 template <typename T, typename I, bool FORCE>
@@ -873,7 +874,8 @@ static cudaError_t step_batch_shifted_tf(const FastStepParams *sp, const int *ph
 
 cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
                                int ntiles, int sel, int tws, int store, bool wide, bool force, bool all_flags,
-                               int grid, bool after_special, cudaStream_t s) {
+                               int grid, cudaStream_t s) {
+    const bool after_special = false;  // an ordinary launch
     if (ntiles == 0) return cudaSuccess;
     if (tws < 5 || tws > 8) return cudaErrorInvalidValue;
     if (store == STORE_F32) {

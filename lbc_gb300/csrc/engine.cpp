@@ -197,7 +197,7 @@ bool Solver::build_geometry() {
     for (int c : cols) { colbase[c] = ns; ns += Ny; }
     for (int r : rows) { rowbase[r] = ns; ns += Nx; }
     nslots_ = ns;
-    group_stages(solid, colbase, rowbase);
+    if (!group_stages(solid, colbase, rowbase)) return false;
     auto slot_of = [&](int i, int j) { return colbase[i] >= 0 ? colbase[i] + j : rowbase[j] + i; };
 
     // Flags and links.
@@ -213,7 +213,7 @@ bool Solver::build_geometry() {
     if (want_links) link_off.assign((size_t)pitch_ * Ny, 0);
     link_node_.assign((size_t)Nx * Ny, 0);
     bool any_special = false, any_solid_link = false;
-    std::vector<int2> wnodes, seed_nodes;
+    std::vector<int2> seed_nodes;
     std::vector<int> seed_slots;
     for (int j = 0; j < Ny; j++) {
         for (int i = 0; i < Nx; i++) {
@@ -232,10 +232,7 @@ bool Solver::build_geometry() {
                 any_special = true;
                 continue;
             }
-            if (bcw) {
-                fl |= NF_BCW;
-                wnodes.push_back(make_int2(i, j));
-            }
+            if (bcw) fl |= NF_BCW;
             int first_link = (int)links.size();
             bool has_link = false;
             for (int k = 1; k < 9; k++) {
@@ -318,10 +315,8 @@ bool Solver::build_geometry() {
     }
     nspecial_ = (int)special_host_.size();
     needs_old_dst_ = any_special;  // solid nodes or off-grid pull sources
-    wnodes_host_ = wnodes;
     has_links_ = want_links && !links.empty();
     has_mem_ = any_solid_link;
-    nw_ = (int)wnodes.size();
     nseed_ = (int)seed_nodes.size();
 
     // Device allocation.
@@ -362,14 +357,11 @@ bool Solver::build_geometry() {
         if (!band_ok || !dalloc(&d_bandm_[0], (size_t)nslots_ * 3) ||
             !dalloc(&d_bandm_[1], (size_t)nslots_ * 3))
             return false;
-        if (!dalloc(&d_wnodes_, wnodes.size()) || !dalloc(&d_seed_nodes_, seed_nodes.size()) ||
+        if (!dalloc(&d_seed_nodes_, seed_nodes.size()) ||
             !dalloc(&d_seed_slots_, seed_slots.size()))
             return false;
-        if (nw_) CK(cudaMemcpyAsync(d_wnodes_, wnodes.data(), wnodes.size() * sizeof(int2), cudaMemcpyHostToDevice, stream_));
-        if (fuse_) {
-            if (!dalloc(&d_last_, last_host_.size())) return false;
-            CK(cudaMemcpyAsync(d_last_, last_host_.data(), last_host_.size() * sizeof(short), cudaMemcpyHostToDevice, stream_));
-        }
+        if (!dalloc(&d_last_, last_host_.size())) return false;
+        CK(cudaMemcpyAsync(d_last_, last_host_.data(), last_host_.size() * sizeof(short), cudaMemcpyHostToDevice, stream_));
         if (nseed_) {
             CK(cudaMemcpyAsync(d_seed_nodes_, seed_nodes.data(), seed_nodes.size() * sizeof(int2), cudaMemcpyHostToDevice, stream_));
             CK(cudaMemcpyAsync(d_seed_slots_, seed_slots.data(), seed_slots.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
@@ -403,15 +395,18 @@ bool Solver::build_geometry() {
 // The last entry that writes a node also finishes it (moments, collision,
 // store into the destination buffer and the band moments of the next step) in
 // its own launch: no entry reads what the finish writes, and no later entry
-// writes the node again. That needs one thread per node within the entry; a
-// periodic entry on a grid one node wide visits each node twice, and such a
-// case keeps the separate finish launch.
+// writes the node again. That needs one thread per node within an entry,
+// which holds on every grid of at least 2 x 2 (a periodic entry on a grid one
+// node wide would visit its nodes twice).
 template <class Solid>
-void Solver::group_stages(const Solid &solid, const std::vector<int> &colbase, const std::vector<int> &rowbase) {
+bool Solver::group_stages(const Solid &solid, const std::vector<int> &colbase, const std::vector<int> &rowbase) {
     const int Nx = d_.Nx, Ny = d_.Ny;
     groups_.clear();
     last_host_.assign((size_t)nslots_, (short)-1);
-    fuse_ = stages_.size() < 32767;
+    if (stages_.size() >= 32767) {
+        set_error("too many Boundary entries");
+        return false;
+    }
     std::unordered_set<long long> gw, gr;
     auto id = [&](int i, int j) { return (long long)j * Nx + i; };
     for (size_t s = 0; s < stages_.size(); s++) {
@@ -442,7 +437,10 @@ void Solver::group_stages(const Solid &solid, const std::vector<int> &colbase, c
         for (long long v : w) {
             const int i = (int)(v % Nx), j = (int)(v / Nx);
             const int slot = colbase[i] >= 0 ? colbase[i] + j : rowbase[j] + i;
-            if (last_host_[slot] == (short)s) fuse_ = false;  // two threads of this entry
+            if (last_host_[slot] == (short)s) {
+                set_error("boundary entry " + std::to_string(st.entry) + " writes a node twice");
+                return false;
+            }
             last_host_[slot] = (short)s;
         }
         bool conflict = groups_.empty();
@@ -460,6 +458,7 @@ void Solver::group_stages(const Solid &solid, const std::vector<int> &colbase, c
         gw.insert(w.begin(), w.end());
         gr.insert(r.begin(), r.end());
     }
+    return true;
 }
 
 // Which 32-node row segments (j, i / 32) contain wall links: the warp that
@@ -755,7 +754,7 @@ StageParams Solver::stage_params(const Stage &st, int src, int bparity) const {
         s.w[k] = d_.w[k];
         s.wf[k] = (float)d_.w[k];
     }
-    s.last = fuse_ ? d_last_ : nullptr;
+    s.last = d_last_;
     s.entry = (int)(&st - stages_.data());
     s.imp = st.d_imp;
     s.imp_nf = st.imp_nf;
@@ -889,7 +888,6 @@ FinishParams Solver::finish_params(int dst, bool write_macro, int bparity) const
     FinishParams f;
     std::memset(&f, 0, sizeof f);
     f.Nx = d_.Nx; f.Ny = d_.Ny; f.pitch = pitch_; f.plane = plane_;
-    f.nw = nw_; f.wnodes = d_wnodes_;
     f.colbase = d_colbase_; f.rowbase = d_rowbase_; f.nslots = nslots_;
     f.bandf = d_bandf_; f.bandg = d_bandg_; f.bandm_next = nslots_ ? d_bandm_[bparity ^ 1] : nullptr;
     f.dst = buf_[dst];
@@ -911,8 +909,7 @@ FinishParams Solver::finish_params(int dst, bool write_macro, int bparity) const
 }
 
 // One time step src -> dst: fused bulk kernel, then the Boundary list in order,
-// one launch per stage group, whose threads finish the BC-written nodes (a
-// separate finish launch only for cases that cannot fuse it).
+// one launch per stage group, whose threads finish the BC-written nodes.
 bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int bparity,
                          cudaStream_t s) {
     if (!s) s = stream_;
@@ -946,10 +943,6 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
         sg.fs = d_force_slot_;
         sg.nfs = (gi == 0 && has_mem_) ? 1 : 0;
         CK(launch::stage_group(sg, d_.store, collide, gi == 0, s));
-    }
-    if (!fuse_) {
-        if (d_.store == STORE_F64) CK(launch::finish_exact(f, collide, s));
-        else CK(launch::finish_shifted(f, d_.store, collide, s));
     }
     return true;
 }
@@ -1302,7 +1295,6 @@ int Batch::tune_online(int avail_pairs) {
 bool Batch::build() {
     const int nc = (int)cases_.size();
     std::vector<ForceSlot> force;
-    std::vector<int4> fin_nodes;
     for (int c = 0; c < nc; c++) {
         Solver *s = cases_[c];
         nodes_ += (long long)s->Nx() * s->Ny();
@@ -1310,8 +1302,6 @@ bool Batch::build() {
         if (s->has_force()) any_force_ = true;
         if (!s->has_flags()) all_flags_ = false;
         if (s->has_mem()) force.push_back(s->force_slot());
-        if (!s->fused_finish())
-            for (const int2 &w : s->wnodes()) fin_nodes.push_back(make_int4(c, w.x, w.y, 0));
         max_stages_ = std::max(max_stages_, (int)s->stage_groups().size());
         for (const Stage &st : s->stages()) max_along_ = std::max(max_along_, st.along);
     }
@@ -1327,7 +1317,6 @@ bool Batch::build() {
                 special.push_back(q < n ? make_int4(c, sl[q].x, sl[q].y, q >> 5) : make_int4(c, -1, -1, q >> 5));
         }
     nspecial_ = (int)special.size();
-    nfin_ = (int)fin_nodes.size();
     nforce_ = (int)force.size();
     const size_t psize = store_ == STORE_F64 ? sizeof(StepParams) : sizeof(FastStepParams);
     void *sp = nullptr;
@@ -1342,10 +1331,9 @@ bool Batch::build() {
     int nphase = nc;
     for (int cnt : level_cnt) nphase = std::max(nphase, cnt);
     if (!balloc(allocs_, &d_phase_, nphase, stream_) || !balloc(allocs_, &d_fin_, 2 * nc, stream_) ||
-        !balloc(allocs_, &d_fin_nodes_, fin_nodes.size(), stream_) || !balloc(allocs_, &d_force_, force.size(), stream_))
+        !balloc(allocs_, &d_force_, force.size(), stream_))
         return false;
     CK(cudaMemsetAsync(d_phase_, 0, nphase * sizeof(int), stream_));
-    if (nfin_) CK(cudaMemcpyAsync(d_fin_nodes_, fin_nodes.data(), fin_nodes.size() * sizeof(int4), cudaMemcpyHostToDevice, stream_));
     if (nforce_) CK(cudaMemcpyAsync(d_force_, force.data(), force.size() * sizeof(ForceSlot), cudaMemcpyHostToDevice, stream_));
     if (nspecial_) {
         if (!balloc(allocs_, &d_special_, special.size(), stream_)) return false;
@@ -1390,8 +1378,7 @@ bool Batch::build() {
         }
     }
     // The force reductions ride in the first stage level's launch.
-    launches_per_step_ = 1 + (nspecial_ || nimp_ ? 1 : 0) + max_stages_ + (nfin_ ? 1 : 0) +
-                         (nforce_ && max_stages_ == 0 ? 1 : 0);
+    launches_per_step_ = 1 + (nspecial_ || nimp_ ? 1 : 0) + max_stages_ + (nforce_ && max_stages_ == 0 ? 1 : 0);
     CK(cudaStreamSynchronize(stream_));
     return true;
 }
@@ -1411,10 +1398,6 @@ bool Batch::launch_batched(int sel) {
     for (int s = 0; s < max_stages_; s++)
         CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], max_along_, store_, sel, d_force_,
                                s == 0 ? nforce_ : 0, s == 0, stream_));
-    if (nfin_) {
-        if (store_ == STORE_F64) CK(launch::finish_batch_exact(d_fin_, d_phase_, d_fin_nodes_, nfin_, sel, stream_));
-        else CK(launch::finish_batch_shifted(d_fin_, d_phase_, d_fin_nodes_, nfin_, sel, store_, stream_));
-    }
     if (nforce_ && max_stages_ == 0) CK(launch::force_reduce(d_force_, nforce_, true, stream_));
     return true;
 }

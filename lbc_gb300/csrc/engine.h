@@ -106,7 +106,7 @@ class Solver {
     int launches_per_step() const {
         const int bulk = 1 + (special_launch() ? 1 : 0);
         if (groups_.empty()) return bulk + (has_mem_ ? 1 : 0);
-        return bulk + (int)groups_.size() + (!fuse_ && nw_ > 0 ? 1 : 0);
+        return bulk + (int)groups_.size();
     }
     // Shifted storage: the nodes the clean-pair kernels leave to the
     // special-node kernel (row-major; both nodes of a pair with a special
@@ -134,9 +134,6 @@ class Solver {
     const std::vector<Stage> &stages() const { return stages_; }
     // Consecutive stages that share one launch (indices into stages()).
     const std::vector<std::vector<int>> &stage_groups() const { return groups_; }
-    const std::vector<int2> &wnodes() const { return wnodes_host_; }
-    // The stage launches finish the BC-written nodes (no separate finish).
-    bool fused_finish() const { return fuse_; }
     bool has_mem() const { return has_mem_; }
     bool has_force() const { return d_.Fx != 0.0 || d_.Fy != 0.0; }
     // 1 for fluid nodes with at least one solid pull source (wall link), [Ny][Nx].
@@ -209,8 +206,6 @@ class Solver {
     double *d_bandf_ = nullptr;  // FP64 storage
     float *d_bandg_ = nullptr;   // shifted storage
     double *d_bandm_[2] = {nullptr, nullptr};
-    int2 *d_wnodes_ = nullptr;
-    int nw_ = 0;
     int2 *d_seed_nodes_ = nullptr;
     int *d_seed_slots_ = nullptr;
     int nseed_ = 0;
@@ -224,12 +219,10 @@ class Solver {
     std::vector<Stage> stages_;
     std::vector<std::vector<int>> groups_;
     template <class Solid>
-    void group_stages(const Solid &solid, const std::vector<int> &colbase, const std::vector<int> &rowbase);
-    // Per band slot: the last stage (index into stages_) that writes the node,
-    // -1 for none; fuse_ when every written node has one thread in that stage.
+    bool group_stages(const Solid &solid, const std::vector<int> &colbase, const std::vector<int> &rowbase);
+    // Per band slot: the last stage (index into stages_) that writes the node, -1 for none.
     std::vector<short> last_host_;
     short *d_last_ = nullptr;
-    bool fuse_ = false;
     dim3 block_{64, 4, 1};
     cudaGraphExec_t pair_exec_ = nullptr;
     int pair_cur_ = -1, pair_parity_ = -1;
@@ -237,7 +230,6 @@ class Solver {
     size_t dev_bytes_ = 0;
     long long steps_done_ = 0;
     std::vector<void *> allocs_;
-    std::vector<int2> wnodes_host_;
     bool needs_old_dst_ = true;
     bool fields_are_moments_ = false;  // stored rho/u/v are the moments of the current populations
     std::vector<uint8_t> link_node_;
@@ -307,7 +299,7 @@ class Batch {
     bool ok_ = false;
     cudaStream_t stream_ = nullptr;
     long long nodes_ = 0;
-    int ntiles_ = 0, grid_ = 0, max_stages_ = 0, max_along_ = 0, nfin_ = 0, nforce_ = 0;
+    int ntiles_ = 0, grid_ = 0, max_stages_ = 0, max_along_ = 0, nforce_ = 0;
     int tws_ = 6;
     bool wide_ = false;  // some case needs 64-bit element offsets
     bool any_force_ = false;  // some case has a body force
@@ -319,7 +311,6 @@ class Batch {
     std::vector<StageParams *> d_stage_lists_;
     std::vector<int> stage_counts_;
     FinishParams *d_fin_ = nullptr;
-    int4 *d_fin_nodes_ = nullptr;
     ForceSlot *d_force_ = nullptr;
     int4 *d_special_ = nullptr;    // (case, i, j, chunk), shifted storage
     int nspecial_ = 0;

@@ -85,9 +85,9 @@ struct FastStepParams {
 };
 
 // Up to kStageGroupMax Boundary entries that touch disjoint band nodes, in one
-// launch (blockIdx.y = member), passed by value. Members with p.last set
-// finish their nodes with `fin`; nfs > 0 adds one row of blocks (blockIdx.y
-// = n) whose first warp reduces the case's force slot *fs.
+// launch (blockIdx.y = member), passed by value. Members finish the nodes
+// their entry writes last with `fin`; nfs > 0 adds one row of blocks
+// (blockIdx.y = n) whose first warp reduces the case's force slot *fs.
 constexpr int kStageGroupMax = 6;
 struct StageGroup {
     StageParams p[kStageGroupMax];
@@ -116,7 +116,6 @@ cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block
 // after_bulk (here, stage_batch and force_reduce): the previous launch in s is
 // a bulk step kernel; the launch overlaps its tail (pdl.cuh).
 cudaError_t stage_group(const StageGroup &g, int store, bool collide, bool after_bulk, cudaStream_t s);
-cudaError_t finish_exact(const FinishParams &p, bool collide, cudaStream_t s);
 cudaError_t collide_exact(const CollideParams &p, cudaStream_t s);
 cudaError_t collide_aos_exact(const CollideAosParams &p, cudaStream_t s);
 cudaError_t aos_to_soa(const double *aos, void *soa, int store, int Nx, int Ny, int pitch,
@@ -142,14 +141,11 @@ int step_batch_exact_grid();
 // row per force slot fs[0 .. nfs).
 cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int max_along, int store,
                         int sel, const ForceSlot *fs, int nfs, bool after_bulk, cudaStream_t s);
-cudaError_t finish_batch_exact(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
-                               int sel, cudaStream_t s);
 cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStream_t s);
 
 // shifted storage (kernels_shifted.cu)
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
                          cudaStream_t s);
-cudaError_t finish_shifted(const FinishParams &p, int store, bool collide, cudaStream_t s);
 // The special nodes of a case (nodes[0 .. n)) on the per-node path; flags: the
 // case has a flag word. Launched right after the case's clean-pair kernel
 // (after_bulk), it overlaps that kernel's last wave and completes after it.
@@ -173,8 +169,6 @@ cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const
                                int ntiles, int sel, int tws, int store, bool wide, bool force, bool all_flags,
                                int grid, cudaStream_t s);
 int step_batch_shifted_grid(int store);
-cudaError_t finish_batch_shifted(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
-                                 int sel, int store, cudaStream_t s);
 }  // namespace launch
 
 }  // namespace lbm

@@ -8,8 +8,10 @@
 //   * k_step_exact      fused pull step (stream + halfway/interpolated/moving-wall
 //                       bounce-back + stale slots + MEM force + moments + BGK/Guo
 //                       collision), one thread per node, SoA planes
-//   * k_stage           one edge BC of the Boundary list on the band buffer
-//   * k_finish_exact    moments + collision of BC-written nodes
+//   * k_stage_group     a group of edge BCs of the Boundary list on the band
+//                       buffer; each thread then finishes (moments + collision)
+//                       the node its entry writes last; k_stage_batch for batches
+//   * k_force_reduce    per-case force from its partials
 //   * k_collide_exact   in-place collision with stored rho/u/v (first step)
 //   * AoS kernels       lbc's standalone functions on lbc's own layout
 //   * transposes        lbc AoS <-> device SoA, with FP32/FP16 shifted storage
@@ -282,24 +284,6 @@ __global__ void k_force_reduce(const ForceSlot *__restrict__ slots, int nslots) 
     const int c = blockIdx.x;
     if (c >= nslots) return;
     force_reduce_warp(slots[c], (int)threadIdx.x);
-}
-
-template <bool COLLIDE>
-__global__ void k_finish_exact(const FinishParams p) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.nw) return;
-    const int2 ij = p.wnodes[t];
-    finish_node_exact<COLLIDE>(p, ij, band_slot(p.colbase, p.rowbase, ij.x, ij.y));
-}
-
-// BC-written nodes of every case of a batch: nodes[t] = (case, i, j).
-__global__ void k_finish_batch_exact(const FinishParams *__restrict__ fp, const int *__restrict__ phase,
-                                     const int4 *__restrict__ nodes, int n, int sel) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const int4 c = nodes[t];
-    const FinishParams &f = fp[2 * c.x + (sel ^ phase[c.x])];
-    finish_node_exact<true>(f, make_int2(c.y, c.z), band_slot(f.colbase, f.rowbase, c.y, c.z));
 }
 
 // In-place collision with the stored rho/u/v (src/core/collision.c:18-40); used
@@ -643,24 +627,9 @@ cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int m
     return launch_follower(after_bulk, k_stage_batch<double>, g, dim3(32), s, list, ephase, sel, n, fs);
 }
 
-cudaError_t finish_batch_exact(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
-                               int sel, cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
-    k_finish_batch_exact<<<(n + 31) / 32, 32, 0, s>>>(fp, phase, nodes, n, sel);
-    return cudaGetLastError();
-}
-
 cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     return launch_follower(after_bulk, k_force_reduce, dim3(n), dim3(32), s, slots, n);
-}
-
-cudaError_t finish_exact(const FinishParams &p, bool collide, cudaStream_t s) {
-    if (p.nw == 0) return cudaSuccess;
-    const int b = 32, g = (p.nw + b - 1) / b;
-    if (collide) k_finish_exact<true><<<g, b, 0, s>>>(p);
-    else k_finish_exact<false><<<g, b, 0, s>>>(p);
-    return cudaGetLastError();
 }
 
 cudaError_t collide_exact(const CollideParams &p, cudaStream_t s) {

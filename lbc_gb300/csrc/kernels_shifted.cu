@@ -556,24 +556,6 @@ __device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 
     }
 }
 
-template <typename T, bool COLLIDE>
-__global__ void k_finish_shifted(const FinishParams p) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.nw) return;
-    const int2 ij = p.wnodes[t];
-    finish_node_shifted<T, COLLIDE>(p, ij, band_slot(p.colbase, p.rowbase, ij.x, ij.y));
-}
-
-template <typename T>
-__global__ void k_finish_batch_shifted(const FinishParams *__restrict__ fp, const int *__restrict__ phase,
-                                       const int4 *__restrict__ nodes, int n, int sel) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const int4 c = nodes[t];
-    const FinishParams &f = fp[2 * c.x + (sel ^ phase[c.x])];
-    finish_node_shifted<T, true>(f, make_int2(c.y, c.z), band_slot(f.colbase, f.rowbase, c.y, c.z));
-}
-
 // In-place collision of shifted populations with the stored (FP64) rho/u/v:
 // the first step of a run (src/core/collision.c:18-40).
 template <typename T>
@@ -899,27 +881,6 @@ int step_batch_shifted_grid(int store) {
     if (store == STORE_F32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_batch_shifted<float, int, true, false>, 256, 0);
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_batch_shifted<__half, int, true, false>, 256, 0);
     return nsm * (nb > 0 ? nb : 1);
-}
-
-cudaError_t finish_batch_shifted(const FinishParams *fp, const int *phase, const int4 *nodes, int n,
-                                 int sel, int store, cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
-    if (store == STORE_F32) k_finish_batch_shifted<float><<<(n + 127) / 128, 128, 0, s>>>(fp, phase, nodes, n, sel);
-    else k_finish_batch_shifted<__half><<<(n + 127) / 128, 128, 0, s>>>(fp, phase, nodes, n, sel);
-    return cudaGetLastError();
-}
-
-cudaError_t finish_shifted(const FinishParams &p, int store, bool collide, cudaStream_t s) {
-    if (p.nw == 0) return cudaSuccess;
-    const int b = 128, g = (p.nw + b - 1) / b;
-    if (store == STORE_F32) {
-        if (collide) k_finish_shifted<float, true><<<g, b, 0, s>>>(p);
-        else k_finish_shifted<float, false><<<g, b, 0, s>>>(p);
-    } else {
-        if (collide) k_finish_shifted<__half, true><<<g, b, 0, s>>>(p);
-        else k_finish_shifted<__half, false><<<g, b, 0, s>>>(p);
-    }
-    return cudaGetLastError();
 }
 
 }  // namespace launch

@@ -30,7 +30,7 @@ enum : uint16_t {
     NF_SPECIAL_MASK = 0x01FF,  // bit k: the pull source x - c_k is solid or off a non-periodic edge
     NF_SOLID = 1u << 9,        // node is solid (never written)
     NF_BAND = 1u << 10,        // node's pre-collision populations feed the edge-BC pipeline
-    NF_BCW = 1u << 11,         // node is written by an edge BC (collided by the finish kernel)
+    NF_BCW = 1u << 11,         // node is written by an edge BC (collided by the stage launch)
     NF_LINKS = 1u << 12,       // node owns entries in the cut-link table (IBB / moving wall)
 };
 
@@ -459,8 +459,7 @@ struct StageParams {
     float wf[9];               // FP32 copies (shifted storage: no FP64 conversions per thread)
     // Finish in the same launch: the thread of a node whose last writer in
     // the Boundary list is this entry (last[slot] == entry) computes the
-    // node's moments and collision right after the entry's BC. last is null
-    // when the case finishes its BC-written nodes in a separate launch.
+    // node's moments and collision right after the entry's BC.
     const short *last;
     int entry;
     const FinishParams *fin;   // batches: the case's finish parameters (solo: by value)
@@ -473,8 +472,6 @@ struct StageParams {
 struct FinishParams {
     int Nx, Ny, pitch;
     long long plane;
-    int nw;                    // number of BC-written nodes
-    const int2 *wnodes;        // (i, j) of every BC-written node
     const int *colbase, *rowbase;
     int nslots;
     const double *bandf;       // FP64 storage
@@ -549,7 +546,7 @@ __device__ __forceinline__ StagePre stage_preload(const StageParams &p, int t, i
     }
     c.v1 = p.val1 ? p.val1[t] : 0.0;
     c.v2 = p.val2 ? p.val2[t] : 0.0;
-    c.fin = p.last != nullptr && !c.solid && p.last[c.slot] == p.entry;
+    c.fin = !c.solid && p.last[c.slot] == p.entry;
     c.imp = false;
     if (kind == BC_VEL_BOT_REG && p.imp && p.imp[(size_t)IMP_ACTIVE * p.along + t] != 0.0 && !c.solid) {
         // Impedance wall on this node: the regularized bottom BC with the

@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--skip-liners", action="store_true")
     p.add_argument("--liner-steps", type=int, default=20000)
+    p.add_argument("--cavity-steps", type=int, default=5000,
+                   help="lid-driven cavity 2048^2 (moving-wall lid, Re 1000) steps in FP32 and FP64; 0: skip")
     p.add_argument("--skip-serve", action="store_true")
     p.add_argument("--serve-requests", type=int, default=200)
     p.add_argument("--serve-scale", type=float, default=0.05)
@@ -282,6 +284,33 @@ def run_ours(a, ws, rank, pg):
                   "finite": r32["finite"] and r64["finite"]}
         if ws > 1:
             liners["eduction_note"] = "eduction errors of rank 0's ducts"
+    # Lid-driven cavity, 2048^2, moving-wall bounce-back lid, Re 1000: FP32 and
+    # FP64 from the same state (one replica per rank), the FP32 u error against
+    # FP64 after the same steps.
+    cavity = None
+    if a.cavity_steps > 0:
+        ccase, cst = cases.cavity_moving_wall(2048, 0.1, 1000.0)
+        cres = {}
+        for name, storage in (("f32", lbc_gb300.F32_SHIFTED), ("f64", lbc_gb300.F64)):
+            cs = lbc_gb300.GpuSolver(ccase, storage)
+            cs.set_state(cst)
+            cs.run(a.warmup)
+            barrier(pg)
+            cms = allmax(pg, cs.run_timed(a.cavity_steps))
+            cres[name] = (cms, cs.get_fields())
+            del cs
+        m = ccase.solid_mask == 0
+        r32, u32, v32 = cres["f32"][1]
+        r64, u64, v64 = cres["f64"][1]
+        err = float(np.sqrt(np.sum((u32[m] - u64[m]) ** 2 + (v32[m] - v64[m]) ** 2) /
+                            np.sum(u64[m] ** 2 + v64[m] ** 2)))
+        c32 = ws * ccase.nodes * a.cavity_steps / (cres["f32"][0] / 1e3) / 1e6
+        c64 = ws * ccase.nodes * a.cavity_steps / (cres["f64"][0] / 1e3) / 1e6
+        cavity = {"grid": "2048x2048", "steps": a.warmup + a.cavity_steps, "f32_mlups": round(c32, 1),
+                  "f32_frac_hbm": round(c32 * 1e6 * 72 / 1e9 / hbm, 4), "fp64_mlups": round(c64, 1),
+                  "ratio_f32_vs_fp64": round(c32 / c64, 2), "u_l2_rel_f32_vs_fp64": err,
+                  "mass_rel_f32_vs_fp64": float(np.sum(r32[m]) / np.sum(r64[m]) - 1.0),
+                  "note": "moving-wall bounce-back lid, u 0.1, Re 1000; one replica per rank"}
     # Serving: a seeded Poisson stream of channel / cylinder / liner requests
     # (steps scaled down so the bench stays short), continuous batching. With
     # several ranks the stream has N times the requests, partitioned by work;
@@ -416,6 +445,7 @@ def run_ours(a, ws, rank, pg):
         "accuracy_after_200_steps": acc,
         "e2e": e2e,
         "liner_batch": liners,
+        "cavity": cavity,
         "serving": serve_res,
         "gpu_launches": f32["launches"],
         "clocks": clocks,

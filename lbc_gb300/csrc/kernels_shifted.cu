@@ -482,22 +482,22 @@ __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepPar
 // each case's list padded to a multiple of 32 entries (padding: i = -1), so
 // that a warp holds one chunk of one case and the force partials are those of
 // the case alone.
-// Blocks from nsb on advance the batch's impedance walls for this step
-// (impedance_ahead): imp[b - nsb] = (wall, first node) of 128 nodes, walls[w]
-// = the wall's stage parameters for both directions and its velocity buffer.
-// That FP64 work depends only on the previous step's moments, so it runs here,
+// The first nimp blocks advance the batch's impedance walls for this step
+// (impedance_ahead): imp[b] = (wall, first node) of 128 nodes, walls[w] = the
+// wall's stage parameters for both directions and its velocity buffer. That
+// FP64 work depends only on the previous step's moments, so it runs here,
 // beside the latency-bound special nodes, instead of at the head of the edge
-// launch.
+// launch; its blocks come first so that the long FP64 updates start first.
 template <typename T, typename I, bool FORCE>
 __global__ void __launch_bounds__(128) k_step_batch_special_shifted(const FastStepParams *__restrict__ sp,
                                                                     const int *__restrict__ phase,
                                                                     const int4 *__restrict__ nodes, int n,
-                                                                    int sel, int nsb,
+                                                                    int sel, int nimp,
                                                                     const ImpWall *__restrict__ walls,
                                                                     const int2 *__restrict__ imp) {
     pdl_launch_dependents();
-    if ((int)blockIdx.x >= nsb) {
-        const int2 b = imp[blockIdx.x - nsb];
+    if ((int)blockIdx.x < nimp) {
+        const int2 b = imp[blockIdx.x];
         const ImpWall &w = walls[b.x];
         const StageParams &p = w.pair[sel ^ phase[w.entry]];
         const int t = b.y + (int)threadIdx.x;
@@ -505,7 +505,7 @@ __global__ void __launch_bounds__(128) k_step_batch_special_shifted(const FastSt
         pdl_wait();
         return;
     }
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = ((int)blockIdx.x - nimp) * (int)blockDim.x + (int)threadIdx.x;
     if (q < n) {  // n is a multiple of 32: whole warps
         const int4 e = nodes[q];
         const FastStepParams &fp = sp[2 * e.x + (sel ^ phase[e.x])];
@@ -812,13 +812,12 @@ template <typename T, bool FORCE>
 static cudaError_t special_batch_shifted_tf(const FastStepParams *sp, const int *phase, const int4 *nodes, int n,
                                             int sel, const ImpWall *walls, const int2 *imp, int nimp, bool wide,
                                             bool after_bulk, cudaStream_t s) {
-    const int nsb = (n + 127) / 128;
-    const dim3 g(nsb + nimp), b(128);
+    const dim3 g(nimp + (n + 127) / 128), b(128);
     if (wide)
         return launch_follower(after_bulk, k_step_batch_special_shifted<T, long long, FORCE>, g, b, s, sp, phase,
-                               nodes, n, sel, nsb, walls, imp);
+                               nodes, n, sel, nimp, walls, imp);
     return launch_follower(after_bulk, k_step_batch_special_shifted<T, int, FORCE>, g, b, s, sp, phase, nodes, n,
-                           sel, nsb, walls, imp);
+                           sel, nimp, walls, imp);
 }
 
 cudaError_t special_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *nodes, int n, int sel,

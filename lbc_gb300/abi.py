@@ -95,12 +95,28 @@ class LbcAbi:
 
     def step(self, case: Case, st: State, bnd=None, swap: bool = True):
         """One ``main_lbm`` call followed by the caller-side swap of
-        cases/nit/nit.c:309-311. Returns (L, D)."""
+        cases/nit/nit.c:309-311. Returns (L, D). A case with moving walls
+        (wall_u / wall_v, an extension with no counterpart in lbc) takes the
+        oracle's ext_main_lbm_moving, which only the oracle library has."""
         if bnd is None:
             bnd = self.boundaries(case.bcs)
         arr, _keep = bnd
         L = C.c_double(0.0)
         D = C.c_double(0.0)
+        if case.wall_u is not None or case.wall_v is not None:
+            fn = getattr(self.lib, self.prefix + "ext_main_lbm_moving")
+            zero = np.zeros((case.Ny, case.Nx))
+            uw = np.ascontiguousarray(case.wall_u if case.wall_u is not None else zero, dtype=np.float64)
+            vw = np.ascontiguousarray(case.wall_v if case.wall_v is not None else zero, dtype=np.float64)
+            fn.restype = None
+            fn(case.Nx, case.Ny, Q, dptr(st.f), dptr(st.f_new), dptr(st.rho), dptr(st.u), dptr(st.v),
+               iptr(case.cx), iptr(case.cy), dptr(case.w), iptr(case.opp), dptr(case.omega_eff),
+               iptr(case.solid_mask), C.cast(arr, C.c_void_p), len(case.bcs), case.isperiodic_x,
+               case.isperiodic_y, C.c_double(case.Fx), C.c_double(case.Fy), C.byref(L), C.byref(D),
+               dptr(uw), dptr(vw))
+            if swap:
+                st.f, st.f_new = st.f_new, st.f
+            return L.value, D.value
         self.main_lbm(case.Nx, case.Ny, Q, dptr(st.f), dptr(st.f_new), dptr(st.rho), dptr(st.u),
                       dptr(st.v), iptr(case.cx), iptr(case.cy), dptr(case.w), iptr(case.opp),
                       dptr(case.omega_eff), iptr(case.solid_mask), C.cast(arr, C.c_void_p),

@@ -157,8 +157,14 @@ def standard_cases():
     ]
 
 
+def extension_cases():
+    """(name, builder, steps) for extensions with no counterpart in lbc
+    (checked against the oracle's restatement, not against lbc's build)."""
+    return [("zoo_moving_lid", zoo_moving_lid, 60)]
+
+
 def build(name):
-    for n, b, s in standard_cases():
+    for n, b, s in standard_cases() + extension_cases():
         if n == name:
             return b(), s
     raise KeyError(name)

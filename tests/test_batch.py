@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 FIELDS = ("f", "f_new", "rho", "u", "v")
 MIX = ["zoo_ibb", "zoo_convective_chain", "zoo_zh_mixed", "taylor_green", "poiseuille",
        "zoo_periodic_late", "zoo_pressure_reg", "cylinder_wake_small", "zoo_open_edges", "liner",
-       "taylor_green_odd", "cylinder_odd"]
+       "taylor_green_odd", "cylinder_odd", "zoo_moving_lid"]
 
 
 def _build(n):

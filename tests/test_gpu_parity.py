@@ -97,7 +97,7 @@ def test_resident_run_matches_lbc(oracle, name):
 
 @pytest.mark.parametrize("storage", ["f64", "f32", "f16"])
 @pytest.mark.parametrize("name", ["zoo_ibb", "zoo_convective_chain", "taylor_green", "zoo_open_edges",
-                                  "taylor_green_odd", "cylinder_odd"])
+                                  "taylor_green_odd", "cylinder_odd", "zoo_moving_lid"])
 def test_chunked_runs_and_block_shapes_agree(name, storage):
     """run(a); run(b) == run(a + b) bit for bit, and the result does not
     depend on the thread-block shape (no races between nodes)."""
@@ -117,6 +117,25 @@ def test_chunked_runs_and_block_shapes_agree(name, storage):
         else:
             for fld in FIELDS:
                 assert same(getattr(out, fld), getattr(ref, fld)), (name, storage, bx, by, chunks, fld)
+
+
+def test_moving_wall_matches_oracle(oracle):
+    """Moving-wall bounce-back (an extension, the lid of the cavity
+    configuration): a resident FP64 run is bit-identical to the oracle's
+    restatement (ext_main_lbm_moving), forces to the link-sum tolerance."""
+    from lbc_gb300 import F64, GpuSolver
+    (case, st), steps = casezoo.build("zoo_moving_lid")
+    s = GpuSolver(case, F64)
+    s.enable_force_history(steps)
+    s.set_state(st)
+    s.run(steps)
+    out = s.get_state()
+    fo = oracle.run(case, st, steps, record_forces=True)
+    for fld in FIELDS:
+        assert same(getattr(out, fld), getattr(st, fld)), (fld, maxrel(getattr(out, fld), getattr(st, fld)))
+    h = s.force_history(steps)
+    mag = gross_force(case)
+    assert force_close(h[:, 0], fo[:, 1], scale=mag) and force_close(h[:, 1], fo[:, 0], scale=mag)
 
 
 def test_cylinder_golden_forces_on_gpu():

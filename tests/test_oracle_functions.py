@@ -1,6 +1,7 @@
 """Each of lbc's functions in the oracle against lbc's own build (oracle/_ref),
 one call on seeded inputs, bit for bit."""
 import ctypes as C
+import dataclasses
 
 import numpy as np
 import pytest
@@ -95,3 +96,28 @@ def test_sponge_matches_lbc(oracle, ref):
         lib.sponge_layer(60, 40, 0.5, 15.0, 10.0, 5.0, 12.0, 0.6, 3.0, 0.4, dptr(om))
         out.append(om)
     assert same(out[0], out[1])
+
+
+def test_moving_wall_step_reduces_to_lbc_with_still_walls(oracle, ref):
+    """The oracle's moving-wall step (an extension, ext_main_lbm_moving) with
+    zero wall velocity is lbc's own main_lbm step, bit for bit; with the lid
+    moving it changes only the reflected populations of lid-adjacent nodes."""
+    case, st = casezoo.zoo_moving_lid()
+    still = dataclasses.replace(case, wall_u=np.zeros((case.Ny, case.Nx)), wall_v=np.zeros((case.Ny, case.Nx)))
+    plain = dataclasses.replace(case, wall_u=None, wall_v=None)
+    a, b, m = st.copy(), st.copy(), st.copy()
+    fa = oracle.run(still, a, 5, record_forces=True)
+    fb = ref.run(plain, b, 5, record_forces=True)
+    for fld in ("f", "f_new", "rho", "u", "v"):
+        assert same(getattr(a, fld), getattr(b, fld)), fld
+    # forces: lbc sums the links with OpenMP atomics in no fixed order
+    m_ = case.solid_mask.astype(bool)
+    links = sum(int(np.sum(~m_ & np.roll(np.roll(m_, -int(case.cy[k]), 0), -int(case.cx[k]), 1)))
+                for k in range(1, 9))
+    assert np.max(np.abs(np.asarray(fa) - np.asarray(fb))) <= 1e-12 * 0.5 * links
+    s1 = st.copy()
+    oracle.run(case, m, 1)
+    oracle.run(still, s1, 1)
+    diff = np.any(m.f != s1.f, axis=-1)  # [Ny, Nx]: new populations after the swap
+    assert diff[case.Ny - 2].any()       # the fluid row under the lid
+    assert not diff[: case.Ny - 2].any() and not diff[case.Ny - 1].any()

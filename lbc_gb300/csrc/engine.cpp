@@ -942,6 +942,7 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
         sg.fin = f;
         sg.fs = d_force_slot_;
         sg.nfs = (gi == 0 && has_mem_) ? 1 : 0;
+        sg.warm = (long long)d_.Nx * d_.Ny < (1LL << 20) ? 1 : 0;
         CK(launch::stage_group(sg, d_.store, collide, gi == 0, s));
     }
     return true;
@@ -1397,7 +1398,7 @@ bool Batch::launch_batched(int sel) {
     }
     for (int s = 0; s < max_stages_; s++)
         CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], max_along_, store_, sel, d_force_,
-                               s == 0 ? nforce_ : 0, s == 0, stream_));
+                               s == 0 ? nforce_ : 0, s == 0, nodes_ < (1LL << 20), stream_));
     if (nforce_ && max_stages_ == 0) CK(launch::force_reduce(d_force_, nforce_, true, stream_));
     return true;
 }

@@ -96,6 +96,7 @@ struct StageGroup {
     FinishParams fin;
     const ForceSlot *fs;
     int nfs;
+    int warm;   // FP64: run the instruction-cache warm-up pass (small grids)
 };
 
 // An impedance wall of a batch advanced ahead of its stage: the entry's
@@ -139,8 +140,9 @@ cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 
 int step_batch_exact_grid();
 // One level of a batch's Boundary lists (n entries); nfs > 0 adds one block
 // row per force slot fs[0 .. nfs).
+// warm: FP64 only, run the edge threads' instruction-cache warm-up pass.
 cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int max_along, int store,
-                        int sel, const ForceSlot *fs, int nfs, bool after_bulk, cudaStream_t s);
+                        int sel, const ForceSlot *fs, int nfs, bool after_bulk, bool warm, cudaStream_t s);
 cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStream_t s);
 
 // shifted storage (kernels_shifted.cu)

@@ -176,14 +176,17 @@ __global__ void __launch_bounds__(256) k_step_batch_exact(const StepParams *__re
 template <typename T> struct BandAccessor {
     const StageParams &p;
     const StagePre &c;
+    bool live;  // false: no stores (instruction-cache warm-up pass)
     __device__ int slot(int i, int j) const {
         if (i == c.ij.x && j == c.ij.y) return c.slot;
         if (i == c.nij.x && j == c.nij.y) return c.nslot;
         return band_slot(p.colbase, p.rowbase, i, j);
     }
     __device__ bool nb(int i, int j) const { return i == c.nij.x && j == c.nij.y; }
-    __device__ double get(int i, int j, int k) const { return p.bandf[(size_t)k * p.nslots + slot(i, j)]; }
-    __device__ void set(int i, int j, int k, double v) const { p.bandf[(size_t)k * p.nslots + slot(i, j)] = v; }
+    __device__ double get(int i, int j, int k) const { return __ldcg(p.bandf + (size_t)k * p.nslots + slot(i, j)); }
+    __device__ void set(int i, int j, int k, double v) const {
+        if (live) p.bandf[(size_t)k * p.nslots + slot(i, j)] = v;
+    }
     __device__ double rho(int i, int j) const { return nb(i, j) ? c.nrho : p.bandm_prev[slot(i, j)]; }
     __device__ double ux(int i, int j) const {
         return nb(i, j) ? c.nux : p.bandm_prev[(size_t)p.nslots + slot(i, j)];
@@ -204,36 +207,78 @@ template <typename T> struct BandAccessor {
 // applied to the pre-collision f_new of the band nodes, after the preload c.
 // Entries in different launches see the writes of the earlier ones, as in lbc.
 template <typename T>
-__device__ __forceinline__ void stage_point(const StageParams &p, const StagePre &c, int t) {
-    BandAccessor<T> a{p, c};
-    if (c.imp) {
+__device__ __forceinline__ void stage_point(const StageParams &p, const StagePre &c, int t, int kind, bool live) {
+    BandAccessor<T> a{p, c, live};
+    if (kind == BC_VEL_BOT_REG && c.imp) {
         bc_regularized(a, p.w, t, p.index, t, p.index + 1, false, c.v1, c.v2);
         return;
     }
-    bc_apply(a, p.w, p.kind, p.Nx, p.Ny, p.index, t, c.v1, c.v2);
+    bc_apply(a, p.w, kind, p.Nx, p.Ny, p.index, t, c.v1, c.v2);
 }
 
 // Moments and collision of a node an edge BC wrote (band slot `slot`).
+// live = false: the same instructions without their stores (warm-up pass);
+// band populations are read at L2, never from a possibly stale L1 line.
 template <bool COLLIDE>
-__device__ __forceinline__ void finish_node_exact(const FinishParams &p, int2 ij, int slot) {
+__device__ __forceinline__ void finish_node_exact(const FinishParams &p, int2 ij, int slot, bool live) {
     double f[9];
 #pragma unroll
-    for (int k = 0; k < 9; k++) f[k] = p.bandf[(size_t)k * p.nslots + slot];
+    for (int k = 0; k < 9; k++) f[k] = __ldcg(p.bandf + (size_t)k * p.nslots + slot);
     double rho, ux, uy;
     moments_exact(f, p.hFx, p.hFy, rho, ux, uy);
     const size_t dn = (size_t)ij.y * p.Nx + ij.x;
-    if (p.write_macro) { p.rho[dn] = rho; p.ux[dn] = ux; p.uy[dn] = uy; }
-    p.bandm_next[slot] = rho;
-    p.bandm_next[(size_t)p.nslots + slot] = ux;
-    p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
+    if (live) {
+        if (p.write_macro) { p.rho[dn] = rho; p.ux[dn] = ux; p.uy[dn] = uy; }
+        p.bandm_next[slot] = rho;
+        p.bandm_next[(size_t)p.nslots + slot] = ux;
+        p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
+    }
     if (COLLIDE) {
         const double om = p.omega ? p.omega[dn] : p.omega0;
         collide_exact(f, p.w, rho, ux, uy, om, p.has_force != 0, p.Fx, p.Fy);
     }
     double *D = (double *)p.dst;
     const long long node = (long long)ij.y * p.pitch + ij.x;
+    if (live) {
 #pragma unroll
-    for (int k = 0; k < 9; k++) D[k * p.plane + node] = f[k];
+        for (int k = 0; k < 9; k++) D[k * p.plane + node] = f[k];
+    }
+}
+
+// One stage thread, specialised on the entry's kind; with warm set, a
+// store-free pass before the wait warms the instruction cache (as
+// stage_thread_s in kernels_shifted.cu). In FP64 that pass repeats the BC's
+// and the collision's FP64 work beside the FP64-bound bulk kernel, so the
+// host sets warm only for small grids, where the bulk kernel is short and the
+// fetch latency is exposed (measured: cylinder 512x128 36.0 -> 32.9 ms per
+// 1000 steps with it, 35.0 without; 2048x512 82.2 -> 83.5 with it, 81.8
+// without).
+template <typename T, bool COLLIDE, int KIND>
+__device__ __forceinline__ void stage_thread(const StageParams &p, const FinishParams &f, int t, int warm) {
+    const StagePre c = stage_preload(p, t, KIND);
+#pragma unroll 1
+    for (int pass = warm ? 0 : 1; pass < 2; pass++) {
+        const bool live = pass != 0;
+        if (live) pdl_wait();
+        stage_point<T>(p, c, t, KIND, live);
+        if (c.fin) finish_node_exact<COLLIDE>(f, c.ij, c.slot, live);
+    }
+}
+
+template <typename T, bool COLLIDE>
+__device__ __forceinline__ void stage_dispatch(const StageParams &p, const FinishParams &f, int t, int warm) {
+    switch (p.kind) {
+#define LBM_STAGE_KIND(K) \
+    case K: stage_thread<T, COLLIDE, K>(p, f, t, warm); break;
+    LBM_STAGE_KIND(BC_VEL_IN_ZH) LBM_STAGE_KIND(BC_VEL_OUT_ZH) LBM_STAGE_KIND(BC_VEL_TOP_ZH)
+    LBM_STAGE_KIND(BC_VEL_BOT_ZH) LBM_STAGE_KIND(BC_PRES_IN_ZH) LBM_STAGE_KIND(BC_PRES_OUT_ZH)
+    LBM_STAGE_KIND(BC_CONV_IN) LBM_STAGE_KIND(BC_CONV_OUT) LBM_STAGE_KIND(BC_PERIODIC_X)
+    LBM_STAGE_KIND(BC_PERIODIC_Y) LBM_STAGE_KIND(BC_VEL_IN_REG) LBM_STAGE_KIND(BC_VEL_OUT_REG)
+    LBM_STAGE_KIND(BC_VEL_TOP_REG) LBM_STAGE_KIND(BC_VEL_BOT_REG) LBM_STAGE_KIND(BC_PRES_IN_REG)
+    LBM_STAGE_KIND(BC_PRES_OUT_REG) LBM_STAGE_KIND(BC_PRES_TOP_REG) LBM_STAGE_KIND(BC_PRES_BOT_REG)
+#undef LBM_STAGE_KIND
+    default: pdl_wait(); break;
+    }
 }
 
 // One group of Boundary entries of a case (blockIdx.y = member); a member
@@ -251,10 +296,7 @@ __global__ void k_stage_group(const StageGroup g) {
     const StageParams &p = g.p[blockIdx.y];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
-    const StagePre c = stage_preload(p, t, p.kind);
-    pdl_wait();
-    stage_point<T>(p, c, t);
-    if (c.fin) finish_node_exact<COLLIDE>(g.fin, c.ij, c.slot);
+    stage_dispatch<T, COLLIDE>(p, g.fin, t, g.warm);
 }
 
 // Stage level of every case of a batch: blockIdx.y selects the case entry,
@@ -262,7 +304,7 @@ __global__ void k_stage_group(const StageGroup g) {
 // rows n.. reduce the force slots fs[].
 template <typename T>
 __global__ void k_stage_batch(const StageParams *__restrict__ list, const int *__restrict__ ephase,
-                              int sel, int n, const ForceSlot *__restrict__ fs) {
+                              int sel, int n, const ForceSlot *__restrict__ fs, int warm) {
     const int e = blockIdx.y;
     if (e >= n) {
         pdl_wait();
@@ -272,10 +314,7 @@ __global__ void k_stage_batch(const StageParams *__restrict__ list, const int *_
     const StageParams &p = list[2 * e + (sel ^ ephase[e])];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
-    const StagePre c = stage_preload(p, t, p.kind);
-    pdl_wait();
-    stage_point<T>(p, c, t);
-    if (c.fin) finish_node_exact<true>(*p.fin, c.ij, c.slot);
+    stage_dispatch<T, true>(p, *p.fin, t, warm);
 }
 
 // Per-case force of a step from its segment partials (one warp per case).
@@ -619,12 +658,13 @@ cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 
 int step_batch_exact_grid() { return 1 << 30; }
 
 cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int max_along, int store,
-                        int sel, const ForceSlot *fs, int nfs, bool after_bulk, cudaStream_t s) {
+                        int sel, const ForceSlot *fs, int nfs, bool after_bulk, bool warm, cudaStream_t s) {
     if (n + nfs == 0) return cudaSuccess;
     if (store != STORE_F64)
         return stage_batch_shifted(list, ephase, n, max_along, store, sel, fs, nfs, after_bulk, s);
     const dim3 g(std::max(1, (max_along + 31) / 32), n + nfs);
-    return launch_follower(after_bulk, k_stage_batch<double>, g, dim3(32), s, list, ephase, sel, n, fs);
+    return launch_follower(after_bulk, k_stage_batch<double>, g, dim3(32), s, list, ephase, sel, n, fs,
+                           warm ? 1 : 0);
 }
 
 cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStream_t s) {

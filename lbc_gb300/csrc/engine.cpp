@@ -334,6 +334,22 @@ bool Solver::build_geometry() {
         if (!dalloc(&d_flags_, flags.size())) return false;
         CK(cudaMemcpyAsync(d_flags_, flags.data(), flags.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, stream_));
     }
+    if (has_flags_) {
+        // Clean 64-node row segments (every pair (2m, 2m + 1) in it exists and
+        // is not special): the geometry kernels skip their flag words.
+        const uint16_t slow = NF_SPECIAL_MASK | NF_SOLID | NF_BAND | NF_BCW | NF_LINKS;
+        const int nseg = (Nx + 63) / 64;
+        seg_words_ = (nseg + 31) / 32;
+        std::vector<uint32_t> bits((size_t)seg_words_ * Ny, 0);
+        for (int j = 0; j < Ny; j++)
+            for (int sg = 0; sg < nseg; sg++) {
+                bool clean = 64 * sg + 64 <= Nx;
+                for (int i = 64 * sg; clean && i < 64 * sg + 64; i++) clean = !(flags[(size_t)j * pitch_ + i] & slow);
+                if (clean) bits[(size_t)j * seg_words_ + sg / 32] |= 1u << (sg % 32);
+            }
+        if (!dalloc(&d_seg_clean_, bits.size())) return false;
+        CK(cudaMemcpyAsync(d_seg_clean_, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_));
+    }
     if (nspecial_) {
         if (!dalloc(&d_special_, special_host_.size())) return false;
         CK(cudaMemcpyAsync(d_special_, special_host_.data(), special_host_.size() * sizeof(int2), cudaMemcpyHostToDevice, stream_));
@@ -708,6 +724,7 @@ StepParams Solver::step_params(int src, int dst, bool write_macro, int bparity) 
     p.px = d_.px; p.py = d_.py;
     p.src = buf_[src]; p.dst = buf_[dst];
     p.flags = d_flags_; p.link_off = d_link_off_; p.links = d_links_;
+    p.seg_clean = d_seg_clean_; p.seg_words = seg_words_;
     p.omega = d_omega_; p.omega0 = omega0_;
     p.has_force = (d_.Fx != 0.0 || d_.Fy != 0.0);
     p.Fx = d_.Fx; p.Fy = d_.Fy; p.hFx = 0.5 * d_.Fx; p.hFy = 0.5 * d_.Fy;

@@ -243,6 +243,8 @@ class Solver {
     std::string vtk_err_;
     int *d_seg_slot_ = nullptr;     // per 32-node row segment (FP64) or 32-entry special-list chunk: force slot or -1
     std::vector<int2> special_host_;
+    uint32_t *d_seg_clean_ = nullptr;
+    int seg_words_ = 0;
     int2 *d_special_ = nullptr;
     int nspecial_ = 0;
     int nlink_segs_ = 0;

@@ -405,6 +405,8 @@ struct StepParams {
     const void *src;          // post-collision populations of step n (planes)
     void *dst;                // output populations (also holds the stale slots)
     const uint16_t *flags;    // [Ny * pitch] or null (fully periodic, no solids, no BCs)
+    const uint32_t *seg_clean; // bit per 64-node row segment whose 32 pairs are all clean; words per row: seg_words
+    int seg_words;
     const int *link_off;      // [Ny * pitch]
     const Link *links;
     const double *omega;      // [Ny * Nx] per-node omega, or null -> omega0

@@ -366,8 +366,7 @@ def run_ours(a, ws, rank, pg):
         fields[name] = s.get_fields()
         rates[name] = math.log(e_half / energy(fields[name])) / (E - E // 2)
         del s
-    nu = (0.56 - 0.5) / 3.0
-    rate_exact = 2.0 * nu * 2.0 * (2.0 * math.pi / n) ** 2
+    rate_exact = 2.0 * cases.taylor_green_decay_rate(n, n, 0.56)   # energy: twice the amplitude's rate
     r64, u64, v64 = fields["f64"]
     m0 = float(np.sum(st.rho))
     acc = {}

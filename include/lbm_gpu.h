@@ -35,8 +35,7 @@ typedef struct lbm_gpu_solver lbm_gpu_solver;
 
 /* The inputs of main_lbm that describe a case (lbc include/lbm_core.h:6-31),
  * plus optional moving walls and the storage mode. Arrays are read during
- * lbm_gpu_create only, except Boundary val1/val2, which are read again by
- * lbm_gpu_set_bc_values. */
+ * lbm_gpu_create only (new Boundary values go through lbm_gpu_set_bc_values). */
 typedef struct {
     int Nx, Ny;
     const int *cx, *cy, *opp;      /* must be lbc's D2Q9 ordering */
@@ -85,7 +84,9 @@ int lbm_gpu_set_state(lbm_gpu_solver *s, const double *f, const double *f_new, c
 int lbm_gpu_get_state(lbm_gpu_solver *s, double *f, double *f_new, double *rho, double *u,
                       double *v);
 int lbm_gpu_get_fields(lbm_gpu_solver *s, double *rho, double *u, double *v);
-/* Re-read val1/val2 (length Ny or Nx) of Boundary entry `entry`. */
+/* Copy new val1/val2 (length Ny or Nx; NULL keeps the current values) of
+ * Boundary entry `entry` to the device; later steps use them. The arrays are
+ * not kept. LBM_GPU_ERR_ARG for an entry outside the Boundary list. */
 int lbm_gpu_set_bc_values(lbm_gpu_solver *s, int entry, const double *val1, const double *val2);
 
 int lbm_gpu_run(lbm_gpu_solver *s, int nsteps);

@@ -648,6 +648,10 @@ int lbm_gpu_get_fields(lbm_gpu_solver *s, double *rho, double *u, double *v) {
 
 int lbm_gpu_set_bc_values(lbm_gpu_solver *s, int entry, const double *val1, const double *val2) {
     SOLVER_OR_FAIL(s);
+    if (entry < 0 || entry >= s->s->bc_count()) {
+        set_error("lbm_gpu_set_bc_values: no Boundary entry " + std::to_string(entry));
+        return LBM_GPU_ERR_ARG;
+    }
     return s->s->set_bc_values(entry, val1, val2) ? LBM_GPU_OK : LBM_GPU_ERR_CUDA;
 }
 

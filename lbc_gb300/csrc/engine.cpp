@@ -557,10 +557,6 @@ bool Solver::set_bc_values(int entry, const double *val1, const double *val2) {
         if (st.d_val1 && val1) CK(cudaMemcpyAsync(st.d_val1, val1, st.along * sizeof(double), cudaMemcpyHostToDevice, stream_));
         if (st.d_val2 && val2) CK(cudaMemcpyAsync(st.d_val2, val2, st.along * sizeof(double), cudaMemcpyHostToDevice, stream_));
     }
-    if (entry >= 0 && entry < (int)d_.bcs.size()) {
-        d_.bcs[entry].val1 = val1;
-        d_.bcs[entry].val2 = val2;
-    }
     return true;
 }
 

@@ -81,8 +81,11 @@ class Solver {
     // Whether the old content of f_new can reach the results (solid nodes, or
     // populations pulled from off a non-periodic edge).
     bool needs_old_dst() const { return needs_old_dst_; }
+    // Copies val1/val2 of Boundary entry `entry` to the device (null keeps the
+    // current values); the caller's arrays are not kept.
     bool set_bc_values(int entry, const double *val1, const double *val2);
     bool upload_all_bc_values();
+    int bc_count() const { return (int)d_.bcs.size(); }
     // n time steps, each equivalent to one main_lbm call plus the caller's swap.
     bool run(int nsteps);
     bool forces(double *Fx, double *Fy);  // MEM force of the last step

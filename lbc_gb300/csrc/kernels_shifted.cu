@@ -621,7 +621,6 @@ template <typename T> struct BandAccessorS {
         if (live) p.bandg[(size_t)k * p.nslots + slot(i, j)] = v;
     }
     __device__ float drho(int i, int j) const { return (float)((nb(i, j) ? c.nrho : m(0, i, j)) - 1.0); }
-    __device__ double rho64(int i, int j) const { return nb(i, j) ? c.nrho : m(0, i, j); }
     __device__ float ux(int i, int j) const { return (float)(nb(i, j) ? c.nux : m(1, i, j)); }
     __device__ float uy(int i, int j) const { return (float)(nb(i, j) ? c.nuy : m(2, i, j)); }
     __device__ float post(int i, int j, int k) const {

@@ -138,6 +138,42 @@ def test_moving_wall_matches_oracle(oracle):
     assert force_close(h[:, 0], fo[:, 1], scale=mag) and force_close(h[:, 1], fo[:, 0], scale=mag)
 
 
+@pytest.mark.parametrize("storage", ["f64", "f32"])
+def test_set_bc_values_between_runs(oracle, storage):
+    """lbm_gpu_set_bc_values between two resident runs acts from the next step,
+    as a case main that rewrites a Boundary entry's val1 between main_lbm calls
+    (cases/nit/nit.c:276-303 rewrites its wall values every step). FP64:
+    bit-identical to the oracle given the same values; FP32: within 1e-5 of
+    it, while the new inlet moves the flow far more than that."""
+    import dataclasses
+
+    from lbc_gb300 import STORAGE, GpuSolver
+    (case, st), _ = casezoo.build("cylinder_wake_small")
+    inlet = case.bcs[0]
+    case2 = dataclasses.replace(case, bcs=[dataclasses.replace(inlet, val1=inlet.val1 * 1.25)] + case.bcs[1:])
+    s = GpuSolver(case, STORAGE[storage])
+    s.set_state(st)
+    s.run(20)
+    s.set_bc_values(0, case2.bcs[0].val1)
+    s.run(30)
+    out = s.get_state()
+    with pytest.raises(RuntimeError):
+        s.set_bc_values(len(case.bcs), case2.bcs[0].val1)
+    s.close()
+    st_same = st.copy()
+    oracle.run(case, st, 20)
+    oracle.run(case2, st, 30)
+    oracle.run(case, st_same, 50)
+    if storage == "f64":
+        for fld in FIELDS:
+            assert same(getattr(out, fld), getattr(st, fld)), (fld, maxrel(getattr(out, fld), getattr(st, fld)))
+    else:
+        fluid = case.solid_mask == 0
+        err = max(float(np.max(np.abs(getattr(out, c)[fluid] - getattr(st, c)[fluid]))) for c in ("u", "v"))
+        moved = float(np.max(np.abs(st.u[fluid] - st_same.u[fluid])))
+        assert err < 1e-5 and moved > 100 * err, (err, moved)
+
+
 def test_cylinder_golden_forces_on_gpu():
     """lbc's shipped drag history (1000 x 400, IBB, Zou-He inlet, convective
     outlet, periodic y): the first 300 steps."""

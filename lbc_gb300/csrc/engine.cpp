@@ -329,7 +329,8 @@ bool Solver::build_geometry() {
         CK(cudaMemsetAsync(p, 0, (size_t)plane_ * 9 * esize_, stream_));
     }
     if (!dalloc(&d_rho_, N) || !dalloc(&d_ux_, N) || !dalloc(&d_uy_, N)) return false;
-    if (!dalloc(&d_stage_, N * 9)) return false;
+    stage_rows_ = staging_rows(Nx, Ny);
+    if (!dalloc(&d_stage_, (size_t)stage_rows_ * Nx * 9)) return false;
     if (has_flags_) {
         if (!dalloc(&d_flags_, flags.size())) return false;
         CK(cudaMemcpyAsync(d_flags_, flags.data(), flags.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, stream_));
@@ -571,8 +572,13 @@ bool Solver::set_state(const double *f, const double *f_new, const double *rho, 
         // The drop-in skips f_new when its old content cannot reach the
         // results (no solid nodes, no off-grid pull sources).
         if (b == 1 && !fnew_needed) continue;
-        CK(cudaMemcpyAsync(d_stage_, src[b], N * 9 * sizeof(double), cudaMemcpyHostToDevice, stream_));
-        CK(launch::aos_to_soa(d_stage_, buf_[b], d_.store, Nx, Ny, pitch_, plane_, d_.w, stream_));
+        for (int j0 = 0; j0 < Ny; j0 += stage_rows_) {
+            const int rows = std::min(stage_rows_, Ny - j0);
+            CK(cudaMemcpyAsync(d_stage_, src[b] + (size_t)j0 * Nx * 9, (size_t)rows * Nx * 9 * sizeof(double),
+                               cudaMemcpyHostToDevice, stream_));
+            CK(launch::aos_to_soa(d_stage_, (char *)buf_[b] + (size_t)j0 * pitch_ * esize_, d_.store, Nx, rows,
+                                  pitch_, plane_, d_.w, stream_));
+        }
     }
     CK(cudaMemcpyAsync(d_rho_, rho, N * sizeof(double), cudaMemcpyHostToDevice, stream_));
     CK(cudaMemcpyAsync(d_ux_, u, N * sizeof(double), cudaMemcpyHostToDevice, stream_));
@@ -585,13 +591,17 @@ bool Solver::set_state(const double *f, const double *f_new, const double *rho, 
 
 bool Solver::get_state(double *f, double *f_new, double *rho, double *u, double *v) {
     const int Nx = d_.Nx, Ny = d_.Ny;
-    const size_t N = (size_t)Nx * Ny;
     double *dst[2] = {f, f_new};
     const int which[2] = {cur_, 1 - cur_};
     for (int b = 0; b < 2; b++) {
         if (!dst[b]) continue;
-        CK(launch::soa_to_aos(buf_[which[b]], d_stage_, d_.store, Nx, Ny, pitch_, plane_, d_.w, stream_));
-        CK(cudaMemcpyAsync(dst[b], d_stage_, N * 9 * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+        for (int j0 = 0; j0 < Ny; j0 += stage_rows_) {
+            const int rows = std::min(stage_rows_, Ny - j0);
+            CK(launch::soa_to_aos((const char *)buf_[which[b]] + (size_t)j0 * pitch_ * esize_, d_stage_, d_.store,
+                                  Nx, rows, pitch_, plane_, d_.w, stream_));
+            CK(cudaMemcpyAsync(dst[b] + (size_t)j0 * Nx * 9, d_stage_, (size_t)rows * Nx * 9 * sizeof(double),
+                               cudaMemcpyDeviceToHost, stream_));
+        }
     }
     if (!get_fields(rho, u, v)) return false;
     CK(cudaStreamSynchronize(stream_));

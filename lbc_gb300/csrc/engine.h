@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <map>
 #include <string>
@@ -20,6 +21,15 @@ bool check_cuda(cudaError_t e, const char *what);
 // retain freed memory), freed with cudaFreeAsync on the owner's stream.
 bool device_alloc(void **q, size_t bytes, cudaStream_t s);
 void use_retaining_pool();
+
+// Rows of lbc's FP64 AoS arrays (72 B per node) that set_state / get_state
+// convert per chunk: 64 MiB of staging at most (one row when a row is larger),
+// so that staging costs no per-node device memory.
+inline int staging_rows(int Nx, int Ny) {
+    const long long row = 72LL * Nx;
+    const long long r = (64LL << 20) / row;
+    return (int)std::max(1LL, std::min<long long>(Ny, r));
+}
 
 // One entry of the Boundary list, resolved to a device BC kind.
 struct BCEntry {
@@ -218,7 +228,8 @@ class Solver {
     double *d_hist_ = nullptr;
     int hist_cap_ = 0;
     unsigned long long *hist_count_ptr_ = nullptr;
-    double *d_stage_ = nullptr;  // AoS staging (FP64, 72 N bytes)
+    double *d_stage_ = nullptr;  // AoS staging: staging_rows() rows of FP64 AoS
+    int stage_rows_ = 1;
     std::vector<Stage> stages_;
     std::vector<std::vector<int>> groups_;
     template <class Solid>

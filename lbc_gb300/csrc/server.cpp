@@ -78,8 +78,8 @@ size_t estimate_bytes(const Request &r) {
     const size_t N = (size_t)r.Nx * r.Ny;
     const size_t pitchN = (size_t)((r.Nx + 63) / 64 * 64) * r.Ny;
     const size_t es = r.storage == LBM_GPU_F64 ? 8 : (r.storage == LBM_GPU_F32_SHIFTED ? 4 : 2);
-    return 2 * 9 * es * pitchN + 72 * N + 24 * N + 2 * pitchN + (r.use_ibb ? 4 * pitchN : 0) +
-           8 * N + (1u << 20);
+    return 2 * 9 * es * pitchN + (size_t)staging_rows(r.Nx, r.Ny) * r.Nx * 72 + 24 * N + 2 * pitchN +
+           (r.use_ibb ? 4 * pitchN : 0) + 8 * N + (1u << 20);
 }
 
 }  // namespace

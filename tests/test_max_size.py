@@ -67,3 +67,22 @@ def test_64bit_offsets_match_the_tiled_small_grid(storage):
     for name, a, b in zip(("rho", "u", "v"), got, want):
         tiles = a.reshape(RY, TY, RX, TX)
         assert np.array_equal(tiles, np.broadcast_to(b[None, :, None, :], tiles.shape)), name
+
+
+def test_state_round_trip_over_several_staging_chunks():
+    """set_state / get_state convert lbc's FP64 AoS arrays through a staging
+    buffer of at most 64 MiB, a chunk of rows at a time: a 1024 x 1536 grid
+    (113 MB per array, two chunks) comes back bit for bit in FP64 storage."""
+    from lbc_gb300 import F64, GpuSolver
+    Nx, Ny = 1024, 1536
+    small, _ = cases.taylor_green(64, 48, 0.04, 0.56)
+    big = dataclasses.replace(small, name="round_trip", Nx=Nx, Ny=Ny, solid_mask=np.zeros((Ny, Nx), np.int32),
+                              omega_eff=np.full((Ny, Nx), small.omega_eff[0, 0]), phi=np.zeros((Ny, Nx)))
+    rng = np.random.default_rng(7)
+    st = State(rng.random((Ny, Nx, 9)), rng.random((Ny, Nx, 9)), rng.random((Ny, Nx)),
+               rng.random((Ny, Nx)), rng.random((Ny, Nx)))
+    s = GpuSolver(big, F64)
+    s.set_state(st)
+    out = s.get_state()
+    s.close()
+    assert np.array_equal(out.f, st.f) and np.array_equal(out.f_new, st.f_new)

@@ -57,8 +57,11 @@ typedef struct {
     int has_geometry;              /* 0: fully periodic, no solids, no edge BCs */
     int edge_stages;               /* Boundary entries run as edge kernels */
     int launches_per_step;         /* kernel launches per time step in the loop: the bulk
-                                      step plus edge_launches (these also finish the
-                                      BC-written nodes and reduce the wall force) */
+                                      step; the special-node step (F32/F16 storage with
+                                      a flag word); edge_launches, which also finish the
+                                      BC-written nodes and reduce the wall force, or,
+                                      with wall links but no edge stages, one force
+                                      reduction */
     size_t device_bytes;
     long long steps_done;
     int edge_launches;             /* launches the edge stages take per step: consecutive

@@ -26,7 +26,7 @@ from typing import List
 
 import numpy as np
 
-from .cases import BC, Case, State, equilibrium_state
+from .cases import BC, Case, equilibrium_state
 
 CS = 1.0 / math.sqrt(3.0)
 

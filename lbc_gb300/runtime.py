@@ -11,7 +11,7 @@ from typing import Optional
 
 import numpy as np
 
-from .abi import Boundary, LbcAbi, dptr, iptr
+from .abi import LbcAbi, dptr, iptr
 from .cases import Case, State, Q
 
 HERE = os.path.dirname(os.path.abspath(__file__))

@@ -1,7 +1,6 @@
 """Batches: many uneven cases advanced by one persistent kernel per step must
 each end exactly as when run alone: populations, fields, impedance-wall state
 and the per-step force record bit for bit."""
-import numpy as np
 import pytest
 
 import casezoo

@@ -6,9 +6,8 @@ import os
 import sys
 
 import numpy as np
-import pytest
 
-from conftest import GOLDEN, ROOT
+from conftest import GOLDEN
 
 sys.path.insert(0, GOLDEN)
 import make_golden  # noqa: E402

@@ -115,7 +115,7 @@ struct lbm_gpu_server {
     std::string err;
 };
 
-static bool admit(lbm_gpu_server *S, Request *r) {
+static bool admit(Request *r) {
     CaseDesc d;
     d.Nx = r->Nx;
     d.Ny = r->Ny;
@@ -274,7 +274,7 @@ static int lane_round(lbm_gpu_server *S, Lane &L) {
     std::vector<Request *> joined;
     for (Request *r : taken) {
         const double ta = now_s();
-        const bool good = admit(S, r);
+        const bool good = admit(r);
         {
             std::lock_guard<std::mutex> lk(S->mu);
             r->t_admit = ta;

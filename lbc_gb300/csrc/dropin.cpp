@@ -203,10 +203,69 @@ static Solver *dropin_solver(const CaseDesc &d) {
 extern "C" {
 
 // ------------------------------------------------------------------ main_lbm
+// A Boundary list that holds a function of the caller's own (not one of lbc's
+// BC functions) cannot run on the device. main_lbm then runs lbc's sequence
+// (src/core/main_lbm.c:32-61) from this library's standalone functions, each
+// a device kernel over the caller's arrays, and calls every Boundary entry
+// through its pointer: lbc's BC functions of this library on the device, the
+// caller's own on the host arrays, in list order. The results are lbc's; the
+// speed is that of the standalone functions (the arrays cross the host link
+// once each way per function). The sequence stops at the first failure.
+static bool has_user_bc(const Boundary *bnd, int nb) {
+    for (int b = 0; b < nb && bnd; b++)
+        if (bnd[b].apply && bc_kind_of((const void *)bnd[b].apply) < 0) return true;
+    return false;
+}
+
+static void main_lbm_with_user_bcs(int Nx, int Ny, int Q, double *f, double *f_new, double *rho, double *u,
+                                   double *v, int cx[], int cy[], double w[], int opp[], double *omega_eff,
+                                   int *solid_mask, Boundary boundaries[], int num_boundaries, int isperiodic_x,
+                                   int isperiodic_y, double Fx, double Fy, double *L, double *D, double *phi,
+                                   int use_IBB) {
+    for (int b = 0; b < num_boundaries; b++)
+        if (!boundaries[b].apply) {
+            set_error("Boundary entry " + std::to_string(b) + ": apply is NULL");
+            return report("main_lbm");
+        }
+    if (use_IBB && !phi) {
+        set_error("use_IBB needs phi");
+        return report("main_lbm");
+    }
+    const std::string before = last_error();
+    set_error("");
+    auto failed = [] { return last_error()[0] != '\0'; };
+    double fx = 0.0, fy = 0.0;
+    collision(Nx, Ny, Q, f, rho, u, v, omega_eff, solid_mask, cx, cy, w, Fx, Fy);
+    if (failed()) return;
+    if (use_IBB)
+        interpolated_bounce_back(Nx, Ny, Q, f, f_new, solid_mask, phi, opp, cx, cy, isperiodic_x, isperiodic_y);
+    else
+        bounce_back(Nx, Ny, Q, f, f_new, solid_mask, cx, cy, opp, isperiodic_x, isperiodic_y);
+    if (failed()) return;
+    compute_force_mem(Nx, Ny, Q, f, f_new, solid_mask, isperiodic_x, isperiodic_y, cx, cy, opp, &fx, &fy);
+    if (failed()) return;
+    streaming(Nx, Ny, Q, f, f_new, solid_mask, cx, cy, isperiodic_x, isperiodic_y);
+    if (failed()) return;
+    for (int b = 0; b < num_boundaries; b++) {
+        boundaries[b].apply(Nx, Ny, Q, boundaries[b].index, boundaries[b].val1, boundaries[b].val2, f, f_new,
+                            rho, u, v, solid_mask, cx, cy, w);
+        if (failed()) return;
+    }
+    compute_macroscopic_fields(Nx, Ny, Q, f_new, solid_mask, cx, cy, rho, u, v, Fx, Fy);
+    if (failed()) return;
+    if (D) *D = fx;
+    if (L) *L = fy;
+    set_error(before);
+}
+
 void main_lbm(int Nx, int Ny, int Q, double *f, double *f_new, double *rho, double *u, double *v,
               int cx[], int cy[], double w[], int opp[], double *omega_eff, int *solid_mask,
               Boundary boundaries[], int num_boundaries, int isperiodic_x, int isperiodic_y,
               double Fx, double Fy, double *L, double *D, double *phi, int use_IBB) {
+    if (num_boundaries > 0 && has_user_bc(boundaries, num_boundaries))
+        return main_lbm_with_user_bcs(Nx, Ny, Q, f, f_new, rho, u, v, cx, cy, w, opp, omega_eff, solid_mask,
+                                      boundaries, num_boundaries, isperiodic_x, isperiodic_y, Fx, Fy, L, D, phi,
+                                      use_IBB);
     std::lock_guard<std::mutex> lk(g_mu);
     if (!check_lattice(Q, cx, cy, opp)) return report("main_lbm");
     CaseDesc d;

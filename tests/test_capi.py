@@ -84,3 +84,36 @@ def test_no_device_fails_loudly(lib):
     api.step(case, st, swap=False)
     assert np.array_equal(st.f, before.f) and np.array_equal(st.rho, before.rho)
     assert lbc_gb300.last_error() != ""
+
+
+def _host_outflow_bc(calls):
+    """A Boundary function of the caller's own (not one of lbc's): copies the
+    populations of column index - 1 into column index."""
+    BCFN = C.CFUNCTYPE(None, *([C.c_int] * 4 + [C.c_void_p] * 11))
+
+    def outflow(Nx, Ny, Q, index, val1, val2, f, f_new, rho, u, v, mask, cx, cy, w):
+        calls.append(index)
+        fn = np.ctypeslib.as_array(C.cast(f_new, C.POINTER(C.c_double)), shape=(Ny, Nx, Q))
+        fn[:, index, :] = fn[:, index - 1, :]
+
+    return BCFN(outflow)
+
+
+def test_user_bc_without_device_fails_loudly(lib):
+    """A main_lbm call whose Boundary list holds a function of the caller's own
+    fails before anything runs when there is no device: the caller's arrays
+    are untouched and the callback is never reached."""
+    import lbc_gb300
+    if lib.lbm_gpu_device_count() > 0:
+        pytest.skip("a GPU is visible; covered by the gpu tests")
+    from lbc_gb300 import cases
+    api = lbc_gb300.dropin()
+    case, st = cases.cylinder_wake(48, 16, D=4, xc=12, yc=8)
+    calls = []
+    cb = _host_outflow_bc(calls)
+    arr, keep = api.boundaries(case.bcs)
+    arr[1].apply = C.cast(cb, C.c_void_p).value
+    before = st.copy()
+    api.step(case, st, bnd=(arr, keep), swap=False)
+    assert np.array_equal(st.f, before.f) and np.array_equal(st.f_new, before.f_new)
+    assert calls == [] and lbc_gb300.last_error() != ""

@@ -290,3 +290,27 @@ def test_shifted_storage_on_edge_bcs(oracle, name):
     fl = case.solid_mask == 0
     assert np.max(np.abs(u[fl] - st.u[fl])) < 1e-5
     assert np.max(np.abs(rho[fl] - st.rho[fl])) < 1e-5
+
+
+def test_dropin_main_lbm_with_a_user_bc_matches_lbc(gpu, oracle):
+    """A Boundary list that holds a function of the caller's own: main_lbm runs
+    lbc's sequence from the standalone device functions and calls the
+    caller's function on the host arrays in its place in the list. Fields
+    bit-identical to the oracle's main_lbm with the same callback, forces to
+    the link-sum tolerance."""
+    from test_capi import _host_outflow_bc
+    (case, st), _ = casezoo.build("cylinder_wake_small")
+    calls = []
+    cb = _host_outflow_bc(calls)
+    outs = []
+    for lib in (gpu, oracle):
+        s = st.copy()
+        arr, keep = lib.boundaries(case.bcs)
+        arr[1].apply = C.cast(cb, C.c_void_p).value
+        forces = [lib.step(case, s, bnd=(arr, keep)) for _ in range(12)]
+        outs.append((s, np.array(forces)))
+    (a, fa), (b, fb) = outs
+    assert calls == [case.Nx - 1] * 24
+    for fld in FIELDS:
+        assert same(getattr(a, fld), getattr(b, fld)), (fld, maxrel(getattr(a, fld), getattr(b, fld)))
+    assert force_close(fa, fb, scale=gross_force(case))

@@ -281,6 +281,17 @@ void lbm_gpu_dropin_release(void);
  * reach them (lbm_gpu_host_access > 0) and stages them through copies
  * otherwise; staged = 1 forces the copies (both give identical results). */
 void lbm_gpu_dropin_set_staged(int staged);
+/* Lazy drop-in (off by default). lazy = 1: main_lbm leaves its results on the
+ * device and returns only *L and *D. The next main_lbm call continues there when
+ * the caller has swapped f and f_new and passes the same rho, u, v and case (lbc's
+ * case mains do, cases/nit/nit.c:309-311); any other call writes the results
+ * back first. So do every other lbc function of this library, lbm_gpu_dropin_sync,
+ * lbm_gpu_dropin_release and set_lazy itself. Until then the caller's arrays
+ * are stale and must be neither read nor written. Results are the same bits as
+ * with lazy = 0. */
+void lbm_gpu_dropin_set_lazy(int lazy);
+/* Writes a pending lazy main_lbm result to the caller's arrays. */
+int lbm_gpu_dropin_sync(void);
 
 #ifdef __cplusplus
 }

@@ -125,6 +125,8 @@ def _bind_ext(lib: C.CDLL) -> None:
         "lbm_gpu_host_free": (None, [vp]),
         "lbm_gpu_dropin_release": (None, []),
         "lbm_gpu_dropin_set_staged": (None, [C.c_int]),
+        "lbm_gpu_dropin_set_lazy": (None, [C.c_int]),
+        "lbm_gpu_dropin_sync": (C.c_int, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -314,3 +314,34 @@ def test_dropin_main_lbm_with_a_user_bc_matches_lbc(gpu, oracle):
     for fld in FIELDS:
         assert same(getattr(a, fld), getattr(b, fld)), (fld, maxrel(getattr(a, fld), getattr(b, fld)))
     assert force_close(fa, fb, scale=gross_force(case))
+
+
+@pytest.mark.parametrize("name", ["cylinder_wake_small", "zoo_convective_chain", "taylor_green_odd"])
+def test_lazy_dropin_matches_lbc(gpu, oracle, name):
+    """lbm_gpu_dropin_set_lazy(1): main_lbm calls that follow the caller's swap
+    continue on the device and leave the caller's arrays untouched; *L and *D
+    arrive every call. lbm_gpu_dropin_sync (and switching lazy off) writes what
+    lbc leaves, bit for bit, whereupon the calls go on as usual."""
+    import lbc_gb300
+    lib = lbc_gb300.load_library()
+    (case, st), steps = casezoo.build(name)
+    st_o = st.copy()
+    half = steps // 2
+    lib.lbm_gpu_dropin_release()
+    lib.lbm_gpu_dropin_set_lazy(1)
+    try:
+        rho0 = st.rho.copy()
+        fg1 = gpu.run(case, st, half, record_forces=True)
+        assert same(st.rho, rho0)                    # still on the device
+        assert lib.lbm_gpu_dropin_sync() == 0
+        fo1 = oracle.run(case, st_o, half, record_forces=True)
+        for fld in FIELDS:
+            assert same(getattr(st, fld), getattr(st_o, fld)), (name, fld)
+        fg2 = gpu.run(case, st, steps - half, record_forces=True)
+    finally:
+        lib.lbm_gpu_dropin_set_lazy(0)                # writes the pending result back
+    fo2 = oracle.run(case, st_o, steps - half, record_forces=True)
+    for fld in FIELDS:
+        assert same(getattr(st, fld), getattr(st_o, fld)), (name, fld)
+    mag = gross_force(case)
+    assert force_close(np.concatenate([fg1, fg2]), np.concatenate([fo1, fo2]), scale=mag)

@@ -123,6 +123,13 @@ int lbm_gpu_forces(lbm_gpu_solver *s, double *L, double *D);
 int lbm_gpu_enable_force_history(lbm_gpu_solver *s, int capacity);
 /* Copies up to max_steps records (x, y), oldest first; returns the count. */
 int lbm_gpu_force_history(lbm_gpu_solver *s, double *xy, int max_steps);
+/* lbc's force record file (cases/cylinder/cylinder.c:162-185): for each step n
+ * (counted from lbm_gpu_enable_force_history) not written yet, the doubles
+ * n * dt, L * cf, D * cf. append = 1 adds to the file, 0 starts it. Called at
+ * least every `capacity` steps, it streams the whole run. Returns the number
+ * of records written; LBM_GPU_ERR_ARG when steps left the ring unwritten (the
+ * ones still held are written), LBM_GPU_ERR_IO when the file fails. */
+long long lbm_gpu_write_force_records(lbm_gpu_solver *s, const char *path, double dt, double cf, int append);
 
 /* ---- Time-domain impedance wall (no counterpart in lbc's library; it
  * replaces the host-side ADE coupling of lbc's cases/nit/nit.c:276-303).

@@ -817,6 +817,13 @@ int lbm_gpu_forces(lbm_gpu_solver *s, double *L, double *D) {
     return s->s->forces(D, L) ? LBM_GPU_OK : LBM_GPU_ERR_CUDA;
 }
 
+long long lbm_gpu_write_force_records(lbm_gpu_solver *s, const char *path, double dt, double cf, int append) {
+    SOLVER_OR_FAIL(s);
+    if (!path) { set_error("null path"); return LBM_GPU_ERR_ARG; }
+    const long long n = s->s->write_force_records(path, dt, cf, append != 0);
+    return n >= 0 ? n : (n == -2 ? LBM_GPU_ERR_ARG : LBM_GPU_ERR_IO);
+}
+
 int lbm_gpu_enable_force_history(lbm_gpu_solver *s, int capacity) {
     SOLVER_OR_FAIL(s);
     return s->s->enable_force_history(capacity) ? LBM_GPU_OK : LBM_GPU_ERR_ARG;

@@ -706,6 +706,52 @@ int Solver::force_history(double *out, int max_steps) {
     return n;
 }
 
+// lbc's force record file (cases/cylinder/cylinder.c:162-185): per step n
+// (counted from lbm_gpu_enable_force_history) three doubles, n * dt, L * cf,
+// D * cf, in the host's byte order, written with one fwrite each as lbc does.
+long long Solver::write_force_records(const char *path, double dt, double cf, bool append) {
+    if (!d_hist_) {
+        set_error("force history is not enabled");
+        return -1;
+    }
+    unsigned long long cnt = 0;
+    std::vector<double> ring((size_t)hist_cap_ * 2);
+    if (!check_cuda(cudaMemcpyAsync(&cnt, hist_count_ptr_, sizeof cnt, cudaMemcpyDeviceToHost, stream_), "records") ||
+        !check_cuda(cudaMemcpyAsync(ring.data(), d_hist_, ring.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                    stream_), "records") ||
+        !check_cuda(cudaStreamSynchronize(stream_), "records"))
+        return -1;
+    FILE *fp = std::fopen(path, append ? "ab" : "wb");
+    if (!fp) {
+        set_error(std::string("cannot open ") + path);
+        return -1;
+    }
+    // Steps older than the ring's capacity are gone: write from the oldest held.
+    const unsigned long long first = std::max<unsigned long long>(
+        hist_written_, cnt > (unsigned long long)hist_cap_ ? cnt - hist_cap_ : 0);
+    const bool lost = first > hist_written_;
+    struct Record { double time, L, D; };
+    bool okk = true;
+    for (unsigned long long n = first; n < cnt && okk; n++) {
+        const size_t slot = (size_t)(n % (unsigned long long)hist_cap_);
+        const Record rec{(double)n * dt, ring[2 * slot + 1] * cf, ring[2 * slot] * cf};
+        okk = std::fwrite(&rec, sizeof rec, 1, fp) == 1;
+    }
+    okk = (std::fclose(fp) == 0) && okk;
+    if (!okk) {
+        set_error(std::string("write failed: ") + path);
+        return -1;
+    }
+    const unsigned long long missed = first - hist_written_;
+    hist_written_ = cnt;
+    if (lost) {
+        set_error("the force records of " + std::to_string(missed) +
+                  " steps left the ring before they were written (drain it at least every capacity steps)");
+        return -2;
+    }
+    return (long long)(cnt - first);
+}
+
 bool Solver::launch_collide(int b, cudaStream_t s) {
     if (!s) s = stream_;
     CollideParams c;

@@ -102,6 +102,9 @@ class Solver {
     // Per-step force record (lbm_gpu_force_history).
     bool enable_force_history(int capacity);
     int force_history(double *out, int max_steps);
+    // Appends (append) or writes the force records of the steps not written
+    // yet; returns their count, or -1. -2: some steps left the ring unwritten.
+    long long write_force_records(const char *path, double dt, double cf, bool append);
 
     int Nx() const { return d_.Nx; }
     int Ny() const { return d_.Ny; }
@@ -228,6 +231,7 @@ class Solver {
     double *d_hist_ = nullptr;
     int hist_cap_ = 0;
     unsigned long long *hist_count_ptr_ = nullptr;
+    unsigned long long hist_written_ = 0;  // steps whose force record is in a file
     double *d_stage_ = nullptr;  // AoS staging: staging_rows() rows of FP64 AoS
     int stage_rows_ = 1;
     std::vector<Stage> stages_;

@@ -80,6 +80,7 @@ def _bind_ext(lib: C.CDLL) -> None:
         "lbm_gpu_forces": (C.c_int, [vp, dp, dp]),
         "lbm_gpu_enable_force_history": (C.c_int, [vp, C.c_int]),
         "lbm_gpu_force_history": (C.c_int, [vp, dp, C.c_int]),
+        "lbm_gpu_write_force_records": (C.c_longlong, [vp, C.c_char_p, C.c_double, C.c_double, C.c_int]),
         "lbm_gpu_get_info": (C.c_int, [vp, C.POINTER(Info)]),
         "lbm_gpu_set_block": (C.c_int, [vp, C.c_int, C.c_int]),
         "lbm_gpu_get_block": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
@@ -282,6 +283,14 @@ class GpuSolver:
         if n < 0:
             raise RuntimeError(last_error())
         return out[:n]
+
+    def write_force_records(self, path: str, dt: float, cf: float = 1.0, append: bool = False) -> int:
+        """lbc's {t, L, D} force record file for the steps not written yet
+        (lbm_gpu_write_force_records); returns the number of records."""
+        n = self.lib.lbm_gpu_write_force_records(self.h, path.encode(), dt, cf, 1 if append else 0)
+        if n < 0:
+            raise RuntimeError(f"lbm_gpu_write_force_records failed ({n}): {last_error()}")
+        return n
 
     def set_impedance_wall(self, entry: int, R, m, K, omegas=(), rho_ref: float = 1.0, alpha: float = 0.0,
                            window: int = 0):

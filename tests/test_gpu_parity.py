@@ -190,6 +190,35 @@ def test_cylinder_golden_forces_on_gpu():
     assert np.max(np.abs(L - g[:, 1])) < 1e-9 * np.max(np.abs(g[:, 2]))
 
 
+def test_force_records_stream_lbc_format(tmp_path):
+    """lbm_gpu_write_force_records writes lbc's {t, L, D} record file
+    (cases/cylinder/cylinder.c:162-185) from the device's force ring, drained
+    twice during the run: times bit for bit and forces as lbc's shipped record
+    of the first 300 steps. A ring drained too late loses its oldest steps and
+    says so, after writing the ones it still holds."""
+    from lbc_gb300 import F64, GpuSolver
+    g = np.load(os.path.join(GOLDEN, "lbc_cylinder_forces_res20_first300.npy"))
+    case, st, cf = cases.cylinder_golden()
+    dt = float(g[1, 0])
+    path = str(tmp_path / "forces.bin")
+    s = GpuSolver(case, F64)
+    s.enable_force_history(200)
+    s.set_state(st)
+    s.run(120)
+    assert s.write_force_records(path, dt, cf) == 120
+    s.run(180)
+    assert s.write_force_records(path, dt, cf, append=True) == 180
+    rec = np.fromfile(path, dtype=np.float64).reshape(-1, 3)
+    assert rec.shape == (300, 3) and same(rec[:, 0], g[:, 0])
+    assert np.max(np.abs(rec[:, 2] - g[:, 2]) / np.abs(g[:, 2])) < 1e-13
+    assert np.max(np.abs(rec[:, 1] - g[:, 1])) < 1e-9 * np.max(np.abs(g[:, 2]))
+    s.run(250)
+    with pytest.raises(RuntimeError):
+        s.write_force_records(path, dt, cf, append=True)
+    rec = np.fromfile(path, dtype=np.float64).reshape(-1, 3)
+    assert rec.shape == (500, 3) and rec[300, 0] == 350 * dt
+
+
 def _bc_call(lib, case, st, b):
     arr, keep = lib.boundaries([b])
     getattr(lib, b.name)(case.Nx, case.Ny, Q, b.index, arr[0].val1, arr[0].val2, dptr(st.f),

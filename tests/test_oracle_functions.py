@@ -143,3 +143,54 @@ def test_taylor_green_decays_at_the_analytic_rate(oracle):
     rate = math.log(a0 / amplitude()) / 200
     exact = cases.taylor_green_decay_rate(Nx, Ny, tau)
     assert abs(rate / exact - 1.0) < 2e-3, (rate, exact)   # measured: 4.8e-4
+
+
+@pytest.mark.parametrize("tau", [0.6, 0.9])
+def test_standing_sound_wave_speed_and_damping(oracle, tau):
+    """The oracle's acoustic mode, the study of cases/wave/process.py:56-118:
+    a standing density wave of angular wavenumber K on a periodic line
+    oscillates at c_s K (c_s = 1/sqrt(3)) and decays at nu K^2, the linear
+    theory of BGK D2Q9, whose bulk viscosity equals nu in 2D. Measured over
+    600 steps of a 100-node line with five wavelengths: 0.02-0.5 % off."""
+    import math
+
+    from lbc_gb300.cases import BC, Case, equilibrium_state
+    Nx, Ny, m, A = 100, 2, 5, 2e-4
+    K = 2 * math.pi * m / Nx
+    x = np.arange(Nx)
+    rho = np.tile(1 + A * np.cos(K * x), (Ny, 1))
+    st = equilibrium_state(rho, np.zeros((Ny, Nx)), np.zeros((Ny, Nx)))
+    case = Case("standing_wave", Nx, Ny, np.zeros((Ny, Nx), np.int32), np.full((Ny, Nx), 1 / tau),
+                np.zeros((Ny, Nx)), [BC("periodic_x"), BC("periodic_y")])
+    amp = []
+    for _ in range(600):
+        oracle.run(case, st, 1)
+        amp.append(2 * np.mean((st.rho[0] - 1) * np.cos(K * x)))
+    amp = np.array(amp)
+    env = np.abs(amp)
+    peaks = [i for i in range(1, len(env) - 1) if env[i] >= env[i - 1] and env[i] >= env[i + 1]]
+    gamma = -np.polyfit(np.array(peaks, float), np.log(env[peaks]), 1)[0]
+    crossings = [i for i in range(len(amp) - 1) if amp[i] * amp[i + 1] < 0]
+    omega = math.pi / np.mean(np.diff(crossings))
+    nu = (tau - 0.5) / 3
+    assert abs(gamma / (nu * K * K) - 1) < 0.02, gamma
+    assert abs(omega / K * math.sqrt(3) - 1) < 0.01, omega
+
+
+def test_couette_flow_is_the_linear_profile(oracle):
+    """Couette flow as cases/couette/couette.c:47-80 sets it up (solid row
+    j = 0 with halfway bounce-back, Zou-He velocity_top lid at j = Ny - 1,
+    periodic x) settles on the linear profile of cases/couette/process.py:59-69,
+    u = U (y - 1/2) / (Ny - 3/2), to round-off (measured 3.6e-15 of U)."""
+    from lbc_gb300.cases import BC, Case, equilibrium_state
+    Nx, Ny, tau, U = 4, 17, 1.0, 0.05
+    mask = np.zeros((Ny, Nx), np.int32)
+    mask[0, :] = 1
+    st = equilibrium_state(np.ones((Ny, Nx)), np.zeros((Ny, Nx)), np.zeros((Ny, Nx)))
+    case = Case("couette", Nx, Ny, mask, np.full((Ny, Nx), 1 / tau), np.zeros((Ny, Nx)),
+                [BC("periodic_x"), BC("velocity_top", Ny - 1, np.full(Nx, U), np.zeros(Nx))])
+    oracle.run(case, st, 12000)        # 7.8 diffusion times H^2 / nu
+    y = np.arange(1, Ny)
+    uref = U * (y - 0.5) / (Ny - 1.5)
+    assert np.max(np.abs(st.u[1:, :] - uref[:, None])) < 1e-12 * U
+    assert np.max(np.abs(st.v[1:, :])) < 1e-12 * U

@@ -189,7 +189,7 @@ def test_couette_flow_is_the_linear_profile(oracle):
     st = equilibrium_state(np.ones((Ny, Nx)), np.zeros((Ny, Nx)), np.zeros((Ny, Nx)))
     case = Case("couette", Nx, Ny, mask, np.full((Ny, Nx), 1 / tau), np.zeros((Ny, Nx)),
                 [BC("periodic_x"), BC("velocity_top", Ny - 1, np.full(Nx, U), np.zeros(Nx))])
-    oracle.run(case, st, 12000)        # 7.8 diffusion times H^2 / nu
+    oracle.run(case, st, 12000)        # about 8 diffusion times H^2 / nu
     y = np.arange(1, Ny)
     uref = U * (y - 0.5) / (Ny - 1.5)
     assert np.max(np.abs(st.u[1:, :] - uref[:, None])) < 1e-12 * U

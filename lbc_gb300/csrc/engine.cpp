@@ -681,6 +681,7 @@ bool Solver::enable_force_history(int capacity) {
     CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), stream_));
     hist_cap_ = capacity;
     hist_count_ptr_ = cnt;
+    hist_written_ = 0;  // a new ring: its records count from its first step
     graph_valid_ = false;
     return upload_force_slot();
 }
@@ -743,13 +744,13 @@ long long Solver::write_force_records(const char *path, double dt, double cf, bo
         return -1;
     }
     const unsigned long long missed = first - hist_written_;
-    hist_written_ = cnt;
+    hist_written_ = std::max(hist_written_, cnt);
     if (lost) {
         set_error("the force records of " + std::to_string(missed) +
                   " steps left the ring before they were written (drain it at least every capacity steps)");
         return -2;
     }
-    return (long long)(cnt - first);
+    return first < cnt ? (long long)(cnt - first) : 0;
 }
 
 bool Solver::launch_collide(int b, cudaStream_t s) {

@@ -293,7 +293,7 @@ def test_mei_initialization_matches_lbc(gpu, oracle):
 @pytest.mark.parametrize("storage,tol", [("f32", 2e-6), ("f16", 2e-3)])
 def test_shifted_storage_error_vs_fp64(oracle, storage, tol):
     """Taylor-Green 128 x 128, u0 = 0.04, tau = 0.56, 200 steps: relative L2
-    error of u against the FP64 oracle (spec bound for FP32: 1e-5)."""
+    error of u against the FP64 oracle (the FP32 accuracy target is 1e-5)."""
     from lbc_gb300 import STORAGE, GpuSolver
     case, st = cases.taylor_green(128, 128, 0.04, 0.56)
     s = GpuSolver(case, STORAGE[storage])

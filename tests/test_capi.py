@@ -117,3 +117,20 @@ def test_user_bc_without_device_fails_loudly(lib):
     api.step(case, st, bnd=(arr, keep), swap=False)
     assert np.array_equal(st.f, before.f) and np.array_equal(st.f_new, before.f_new)
     assert calls == [] and lbc_gb300.last_error() != ""
+
+
+def test_entry_points_reject_bad_arguments_on_the_host(lib):
+    """Argument checks that need no device: a null solver or batch, a pending
+    lazy result that does not exist, an unknown Boundary entry."""
+    import lbc_gb300
+    api = lbc_gb300.load_library()       # the bound signatures
+    ERR_ARG = -1
+    assert api.lbm_gpu_write_force_records(None, b"forces.bin", 1.0, 1.0, 0) == ERR_ARG
+    assert "null solver" in lbc_gb300.last_error()
+    assert api.lbm_gpu_set_bc_values(None, 0, None, None) == ERR_ARG
+    assert api.lbm_gpu_run(None, 1) == ERR_ARG
+    assert api.lbm_gpu_batch_run(None, 1) == ERR_ARG
+    assert api.lbm_gpu_dropin_sync() == 0          # nothing pending: nothing to write
+    api.lbm_gpu_dropin_set_lazy(1)
+    api.lbm_gpu_dropin_set_lazy(0)
+    assert api.lbm_gpu_dropin_sync() == 0

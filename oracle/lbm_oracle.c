@@ -15,9 +15,16 @@
  * Exported names carry the prefix orc_ so this library can be loaded next to the
  * GPU drop-in (which exports the reference's own names).
  *
+ * Pinned: bit for bit against lbc's own src/ compiled by oracle/build_ref.sh
+ * (every function, 15 cases) and against fixtures made by lbc's build
+ * (tests/golden/), and to 1e-15 against lbc's shipped drag record
+ * cases/cylinder/sol/forces_IBB_res_20_Re_20.00_tau_0.90.bin.
+ *
  * Extensions without a counterpart in lbc (moving-wall bounce-back and the
  * per-wall-node mass-spring-damper impedance wall) are at the end of the file and
- * are marked as such.
+ * are marked as such. The moving wall reduces to lbc's step when the walls are
+ * still; the impedance wall's parity is unpinned against lbc (its eduction lives
+ * in an external toolkit that is not present).
  */
 #include <math.h>
 #include <stdio.h>

@@ -44,7 +44,8 @@ typedef struct {
     const int *solid_mask;         /* [Ny][Nx] */
     const double *phi;             /* [Ny][Nx] level set, used when use_IBB */
     int use_IBB;
-    const Boundary *boundaries;    /* apply = this library's BC functions */
+    const Boundary *boundaries;    /* apply = this library's BC functions (a function of
+                                      the caller's own runs only through main_lbm) */
     int num_boundaries;
     int isperiodic_x, isperiodic_y;
     double Fx, Fy;

@@ -7,15 +7,23 @@
 // that reserves memory up front), or a loop that must not stall the device
 // (cudaFree synchronizes it). Its only scratch, the per-block partial sums of
 // the deterministic reduction and the arrival counter, lives in the static
-// device array below: every GPU that loads this library holds it (1 MiB + 256 B)
-// until the process exits.
+// device array below (1 MiB + 256 B). The array belongs to this file's module,
+// which CUDA loads into a context the first time the context uses it (with
+// lazy module loading, the default since CUDA 12.2, that is this entry
+// point's first call there; with eager loading, when the library's modules
+// load). From then on the device holds it until the context is destroyed.
 //
-// On the first call on a device (with that device current) the array's device
-// address is looked up once with cudaGetSymbolAddress; that first call should
-// come before any stream capture. All calls share the array and it keeps the
-// last call's contents: each call clears the counter it needs, and calls
-// whose kernels overlap on the GPU race on the array, so order them (one
-// stream, or events).
+// The first call in a context (with its device current) looks the array's
+// device address up with cudaGetSymbolAddress; that first call should come
+// before any stream capture, and in a process whose pool reserves nearly all
+// device memory, before the pool does. The address is kept per device together
+// with the identity of the context it was looked up in, and looked up again
+// when the current context differs (after cudaDeviceReset, for instance, the
+// module is loaded again and the array may sit elsewhere). All calls share the
+// array and it keeps the last call's contents: each call clears the counter it
+// needs, and calls whose kernels overlap on the GPU race on the array, so order
+// them (one stream, or events).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -34,12 +42,48 @@ constexpr int kNoallocDoubles = 2 * kNoallocMaxBlocks + 32;
 static __device__ __align__(256) double g_noalloc_scratch[kNoallocDoubles];
 
 struct DeviceScratch {
+    unsigned long long ctx_id = 0;   // context the address was looked up in (0: none yet)
     double *partials = nullptr;
     unsigned int *ticket = nullptr;
 };
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
 DeviceScratch g_noalloc_dev[kMaxDevices];
+
+// The driver's cuCtxGetCurrent / cuCtxGetId through the runtime's entry-point
+// query (no link against libcuda). Context ids are unique for the life of the
+// process, so a context destroyed and made again gets a new one even when its
+// handle is reused.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
+std::once_flag g_ctx_once;
+
+void resolve_ctx_entry_points() {
+    void *a = nullptr, *b = nullptr;
+    cudaDriverEntryPointQueryResult qa, qb;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+        qa == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+        qb == cudaDriverEntryPointSuccess) {
+        g_ctx_current = (CtxGetCurrentFn)a;
+        g_ctx_id = (CtxGetIdFn)b;
+    }
+    cudaGetLastError();  // a failed query leaves no sticky error behind
+}
+
+// Id of the context current on this thread, 0 when there is none or the
+// driver cannot say (then the address is looked up on every call).
+unsigned long long current_ctx_id() {
+    std::call_once(g_ctx_once, resolve_ctx_entry_points);
+    if (!g_ctx_current || !g_ctx_id) return 0;
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_current(&c) != CUDA_SUCCESS || !c) return 0;
+    if (g_ctx_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 bool scratch_for_current_device(DeviceScratch &out) {
     int dev = 0;
@@ -50,12 +94,20 @@ bool scratch_for_current_device(DeviceScratch &out) {
     }
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     DeviceScratch &d = g_noalloc_dev[dev];
-    if (!d.partials) {
-        void *p = nullptr;
-        if (!lbm::check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress")) return false;
-        d.partials = (double *)p;
-        d.ticket = (unsigned int *)((double *)p + 2 * kNoallocMaxBlocks);
+    unsigned long long id = current_ctx_id();
+    if (id != 0 && id == d.ctx_id && d.partials) {
+        out = d;
+        return true;
     }
+    // First call in this context (or no context made current yet: the lookup
+    // below makes the device's primary context current, as every runtime call
+    // that needs one does).
+    void *p = nullptr;
+    if (!lbm::check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress")) return false;
+    if (id == 0) id = current_ctx_id();
+    d.ctx_id = id;
+    d.partials = (double *)p;
+    d.ticket = (unsigned int *)((double *)p + 2 * kNoallocMaxBlocks);
     out = d;
     return true;
 }
@@ -111,9 +163,9 @@ extern "C" int lbm_gpu_compute_force_mem_noalloc(int Nx, int Ny, int Q, const do
     }
     const dim3 block(64, 4);
     const dim3 grid((Nx + 63) / 64, (Ny + 3) / 4);
-    if ((long long)grid.x * grid.y > kNoallocMaxBlocks) {
+    if ((long long)grid.x * grid.y > kNoallocMaxBlocks || grid.y > 65535u) {
         lbm::set_error("force_mem_noalloc: grid too large for the fixed scratch (at most 65536 blocks "
-                       "of 64 x 4 nodes, e.g. 4096 x 4096)");
+                       "of 64 x 4 nodes, e.g. 4096 x 4096, and at most 262140 rows)");
         return LBM_GPU_ERR_ARG;
     }
     DeviceScratch sc;

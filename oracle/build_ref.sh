@@ -2,13 +2,19 @@
 # Compile lbc's own src/ (read in place, never copied) into oracle/_ref/libref_lbc.so.
 # Every public lbc function is renamed with a ref_ prefix by -D so the library can
 # be loaded next to the GPU drop-in. Test infrastructure only.
-#   usage: oracle/build_ref.sh [LBC_SOURCE_DIR]   (default: $LBC_REF or /root/reference)
+#   usage: oracle/build_ref.sh [LBC_SOURCE_DIR]
+# The source directory is the argument, else $LBC_REF, else the read-only lbc
+# checkout of the build container below (this recipe is the one place that
+# names it). Exit status 2: no lbc sources there (nothing is built). The
+# directory used is recorded in oracle/_ref/SOURCE for the tests that compile
+# lbc's case mains against this library's headers.
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
 src="${1:-${LBC_REF:-/root/reference}}"
 [ -d "$src/src/core" ] || { echo "lbc sources not found at $src" >&2; exit 2; }
 out="$here/_ref"
 mkdir -p "$out"
+printf '%s\n' "$src" > "$out/SOURCE"
 names="main_lbm collision streaming compute_macroscopic_fields compute_force_mem
  mei_initialization sponge_layer bounce_back interpolated_bounce_back
  convective_inlet convective_outlet convective_top convective_bottom

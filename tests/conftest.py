@@ -70,3 +70,27 @@ def maxrel(a, b):
     m = np.isfinite(b)
     den = np.max(np.abs(b[m])) if m.any() else 1.0
     return float(np.max(np.abs(a[m] - b[m])) / den) if m.any() else 0.0
+
+
+def force_close(a, b, rtol=1e-12, scale=None):
+    """|a - b| <= rtol * scale; scale defaults to the largest |b| (pass the
+    force magnitude for a component that is only round-off, like the lift of
+    a symmetric flow)."""
+    a, b = np.asarray(a), np.asarray(b)
+    if not b.size:
+        return True
+    if scale is None:
+        scale = float(np.max(np.abs(b)))
+    return float(np.max(np.abs(a - b))) <= rtol * max(scale, 1e-300)
+
+
+def gross_force(case):
+    """Sum of |c_k| (f_k + f_opp) over all wall links, bounded by 0.5 per link:
+    the scale of the round-off in a force summed over the links in another
+    order (the net lift of a symmetric flow is pure cancellation)."""
+    m = case.solid_mask.astype(bool)
+    n = 0
+    for k in range(1, 9):
+        nb = np.roll(np.roll(m, -int(case.cy[k]), axis=0), -int(case.cx[k]), axis=1)
+        n += int(np.sum(~m & nb))
+    return 0.5 * max(n, 1)

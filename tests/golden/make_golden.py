@@ -54,8 +54,10 @@ def write_vtk_fixture(lib):
 
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    src = args[0] if args else os.environ.get("LBC_REF", "/root/reference")
-    subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), src], check=True)
+    # lbc's sources: the argument, else what oracle/build_ref.sh finds.
+    subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")] + args[:1], check=True)
+    with open(os.path.join(ROOT, "oracle", "_ref", "SOURCE")) as fh:
+        src = fh.read().strip()
     lib = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libref_lbc.so"))
     write_vtk_fixture(lib)
     if "--vtk-only" in sys.argv:

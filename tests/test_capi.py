@@ -14,7 +14,18 @@ import pytest
 from conftest import ROOT
 
 INCLUDE = os.path.join(ROOT, "include")
-REF = os.environ.get("LBC_REF", "/root/reference")
+def _ref_source():
+    """lbc's source tree: $LBC_REF, else the one oracle/build_ref.sh built from."""
+    if os.environ.get("LBC_REF"):
+        return os.environ["LBC_REF"]
+    try:
+        with open(os.path.join(ROOT, "oracle", "_ref", "SOURCE")) as fh:
+            return fh.read().strip()
+    except OSError:
+        return ""
+
+
+REF = _ref_source()
 
 
 def declared_functions():

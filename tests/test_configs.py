@@ -41,3 +41,58 @@ def test_poiseuille_256x64_full_run(oracle):
     m = case.solid_mask == 0
     assert maxrel(u32[m], g.u[m]) <= 1e-5
     assert maxrel(r32[m], g.rho[m]) <= 1e-6
+
+
+# The large configurations at their full grid sizes, FP64 against the oracle
+# for a few steps each: the oracle (lbc's step restated, OpenMP) does about
+# 200 M node updates per second on 16 host cores, so each takes seconds.
+FULL_SIZE = {
+    # periodic Taylor-Green vortex 4096 x 4096, u0 0.04, tau 0.56
+    "taylor_green_4096x4096": (lambda: cases.taylor_green(4096, 4096, 0.04, 0.56), 5),
+    # cylinder wake 2048 x 512: D 64 at (512, 256), IBB, regularized
+    # parabolic inlet and constant-pressure outlet, solid top and bottom rows
+    "cylinder_wake_2048x512": (lambda: cases.cylinder_wake(2048, 512, 64.0, 512.0, 256.0, 0.05, 100.0), 50),
+    # lid-driven cavity 2048 x 2048, Re 1000: lbc's Zou-He velocity_top lid
+    "cavity_zouhe_2048x2048": (lambda: cases.cavity_zouhe(2048, 0.1, 1000.0), 20),
+    # the same cavity with the moving-wall bounce-back lid (extension)
+    "cavity_moving_wall_2048x2048": (lambda: cases.cavity_moving_wall(2048, 0.1, 1000.0), 20),
+}
+
+
+@pytest.mark.parametrize("name", sorted(FULL_SIZE))
+def test_full_size_fp64_matches_oracle(oracle, name):
+    """A resident FP64 run at the configured grid size leaves the oracle's
+    populations, rho, u and v bit for bit (pitch, plane offsets and the
+    edge band at full size); wall forces to the link-sum tolerance."""
+    from conftest import force_close, gross_force
+    from lbc_gb300 import F64, GpuSolver
+    build, steps = FULL_SIZE[name]
+    case, st = build()
+    s = GpuSolver(case, F64)
+    hist = bool(s.info().has_geometry) and bool(case.solid_mask.any())
+    if hist:
+        s.enable_force_history(steps)
+    s.set_state(st)
+    s.run(steps)
+    out = s.get_state()
+    h = s.force_history(steps) if hist else None
+    s.close()
+    fo = oracle.run(case, st, steps, record_forces=True)
+    for fld in ("f", "f_new", "rho", "u", "v"):
+        assert same(getattr(out, fld), getattr(st, fld)), (name, fld, maxrel(getattr(out, fld), getattr(st, fld)))
+    if hist:
+        mag = gross_force(case)
+        assert force_close(h[:, 0], fo[:, 1], scale=mag) and force_close(h[:, 1], fo[:, 0], scale=mag), name
+
+
+def test_full_size_dropin_main_lbm_matches_oracle(gpu, oracle):
+    """lbc's main_lbm through the C ABI with host arrays on the 4096 x 4096
+    Taylor-Green grid (the end-to-end path of the benchmark), 3 calls."""
+    case, st = cases.taylor_green(4096, 4096, 0.04, 0.56)
+    st_o = st.copy()
+    gpu.run(case, st, 3)
+    oracle.run(case, st_o, 3)
+    import lbc_gb300
+    lbc_gb300.load_library().lbm_gpu_dropin_release()
+    for fld in ("f", "f_new", "rho", "u", "v"):
+        assert same(getattr(st, fld), getattr(st_o, fld)), (fld, maxrel(getattr(st, fld), getattr(st_o, fld)))

@@ -220,8 +220,14 @@ int lbm_gpu_batch_destroy(lbm_gpu_batch *b);
  * chunk runs, then retires finished ones: their fields (and populations when
  * asked for) are copied to host memory and their device memory is returned to
  * the pool. Lanes run concurrently. Results are identical to running each
- * request alone (lbm_gpu_run). budget_bytes = 0: 85 % of the free device
- * memory. */
+ * request alone (lbm_gpu_run). Admission is by the device memory free at the
+ * time of the round (cudaMemGetInfo, plus what the pool holds unused from
+ * retired requests), less a reserve (5 % of the device by default,
+ * lbm_gpu_server_set_reserve) and less the requests taken but not set up yet:
+ * memory that anything else takes after the server starts holds admissions
+ * back. budget_bytes > 0 also caps the estimated bytes of the active requests
+ * (0: no cap). When nothing is active one request is let in regardless, so a
+ * request larger than the memory left runs alone or fails cleanly. */
 typedef struct lbm_gpu_server lbm_gpu_server;
 int lbm_gpu_server_create(size_t budget_bytes, int max_active, int chunk_steps, lbm_gpu_server **out);
 /* Returns the request id (> 0) or a negative code. f = f_new = NULL: the
@@ -248,6 +254,11 @@ int lbm_gpu_server_fetch(lbm_gpu_server *srv, int id, double *f, double *f_new, 
 int lbm_gpu_server_release(lbm_gpu_server *srv, int id);
 int lbm_gpu_server_stats(lbm_gpu_server *srv, long long *lups_done, double *busy_s, int *queued,
                          int *active, size_t *bytes_in_use);
+/* Device memory admissions leave free (default: 5 % of the device). */
+int lbm_gpu_server_set_reserve(lbm_gpu_server *srv, size_t reserve_bytes);
+/* The device memory a request could be admitted into now (free memory plus the
+ * pool's unused part, less the reserve and the requests being set up). */
+int lbm_gpu_server_available(lbm_gpu_server *srv, size_t *bytes);
 /* Host time per phase of the scheduling rounds so far: out[0] rounds, [1]
  * admission (solver setup and state upload), [2] batch construction, [3]
  * launching and waiting for the chunks, [4] retiring (results to host, device

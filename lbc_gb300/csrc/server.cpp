@@ -4,7 +4,8 @@
 // any thread into a lock-protected queue. Each storage type (FP64, FP32-, FP16-
 // shifted) has its own lane: a thread that repeats rounds of
 //   1. taking queued requests of its storage type in arrival order while the
-//      device-memory budget and the slot limit (over all lanes) allow;
+//      device's free memory (read live each round, less a reserve) and the
+//      slot limit (over all lanes) allow, and the optional budget;
 //   2. launching one chunk for its active requests: they form one Batch (one
 //      persistent kernel per step over all their tiles, graph-captured),
 //      reused from the previous round while the set of requests is the same;
@@ -101,7 +102,10 @@ struct lbm_gpu_server {
     std::deque<Request *> queue;
     Lane lanes[3];
     int n_active = 0;  // over all lanes
-    size_t budget = 0, in_use = 0;
+    size_t budget = 0;    // optional cap on the requests' estimated bytes (0: none)
+    size_t in_use = 0;    // estimated bytes of the active requests
+    size_t reserve = 0;   // device memory admissions leave free
+    size_t pending = 0;   // estimated bytes of requests taken but not set up yet
     int max_active = 64;
     int chunk = 1000;
     int next_id = 1;
@@ -200,18 +204,44 @@ static bool retire(Request *r) {
     return okk;
 }
 
+// Device memory a new request may take now: the device's free memory plus
+// what the stream-ordered pool holds unused (freed by retired requests and
+// kept for reuse), less the reserve. Read live, so memory taken by anything
+// else in or outside this process after the server started holds admissions
+// back.
+static size_t device_available(const lbm_gpu_server *S) {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    size_t slack = 0;
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        unsigned long long reserved = 0, used = 0;  // cuuint64_t
+        if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && reserved > used)
+            slack = (size_t)(reserved - used);
+    }
+    cudaGetLastError();
+    const size_t have = fr + slack;
+    return have > S->reserve ? have - S->reserve : 0;
+}
+
 // Queued requests of this lane's storage type, in arrival order, while the
-// slot limit and the device-memory budget allow (one request is always let in
-// when nothing at all is active, so a request larger than the budget still
-// runs alone).
-// Requests of this lane's storage type, in arrival order, while the slot
-// limit and the memory budget allow. The FP64 lane holds at most a quarter of
-// the slots while requests of another type are queued or running: FP64
-// requests step at GB300's FP64 rate, about 12x slower per node than FP32,
-// and without the cap they accumulate in the active set and leave the
-// shorter requests queued behind them.
+// slot limit, the device memory available now (less what requests taken by
+// any lane but not set up yet will take) and the optional budget allow. One
+// request is always let in when nothing at all is active, so a request larger
+// than the memory left still runs alone (or fails cleanly when it cannot
+// allocate). The FP64 lanes hold at most a quarter of the slots while
+// requests of another type are queued or running: FP64 requests step at
+// GB300's FP64 rate, 7-12x slower per node than FP32, and without the cap
+// they accumulate in the active set and leave the shorter requests queued
+// behind them.
 static std::vector<Request *> take_admissions(lbm_gpu_server *S, Lane &L) {
     std::vector<Request *> out;
+    const size_t avail = device_available(S);
     std::lock_guard<std::mutex> lk(S->mu);
     int cap = S->max_active;
     if (L.storage == STORE_F64) {
@@ -227,10 +257,13 @@ static std::vector<Request *> take_admissions(lbm_gpu_server *S, Lane &L) {
             continue;
         }
         if (S->n_active >= S->max_active || (int)(L.active.size() + out.size()) >= cap) break;
-        if (S->in_use + r->est_bytes > S->budget && S->n_active > 0) break;
+        const bool fits_live = S->pending + r->est_bytes <= avail;
+        const bool fits_cap = S->budget == 0 || S->in_use + r->est_bytes <= S->budget;
+        if (!(fits_live && fits_cap) && S->n_active > 0) break;
         it = S->queue.erase(it);
         out.push_back(r);
         S->in_use += r->est_bytes;
+        S->pending += r->est_bytes;
         S->n_active++;
     }
     return out;
@@ -278,6 +311,7 @@ static int lane_round(lbm_gpu_server *S, Lane &L) {
         {
             std::lock_guard<std::mutex> lk(S->mu);
             r->t_admit = ta;
+            S->pending -= r->est_bytes;   // allocated now (or failed): the live figure has it
             if (good) r->state = 2;
         }
         if (good) joined.push_back(r);
@@ -346,16 +380,11 @@ int lbm_gpu_server_create(size_t budget_bytes, int max_active, int chunk_steps, 
         set_error("bad arguments");
         return LBM_GPU_ERR_ARG;
     }
+    size_t fr = 0, tot = 0;
+    if (!check_cuda(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo")) return LBM_GPU_ERR_CUDA;
     lbm_gpu_server *S = new lbm_gpu_server();
-    if (budget_bytes == 0) {
-        size_t fr = 0, tot = 0;
-        if (!check_cuda(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo")) {
-            delete S;
-            return LBM_GPU_ERR_CUDA;
-        }
-        budget_bytes = (size_t)(0.85 * (double)fr);
-    }
     S->budget = budget_bytes;
+    S->reserve = tot / 20;
     S->max_active = max_active;
     S->chunk = chunk_steps;
     S->lanes[0].storage = LBM_GPU_F64;
@@ -544,6 +573,27 @@ int lbm_gpu_server_stats(lbm_gpu_server *S, long long *lups_done, double *busy_s
     if (queued) *queued = (int)S->queue.size();
     if (active) *active = S->n_active;
     if (bytes_in_use) *bytes_in_use = S->in_use;
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_server_set_reserve(lbm_gpu_server *S, size_t reserve_bytes) {
+    if (!S) {
+        set_error("bad arguments");
+        return LBM_GPU_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->reserve = reserve_bytes;
+    return LBM_GPU_OK;
+}
+
+int lbm_gpu_server_available(lbm_gpu_server *S, size_t *bytes) {
+    if (!S || !bytes) {
+        set_error("bad arguments");
+        return LBM_GPU_ERR_ARG;
+    }
+    const size_t a = device_available(S);
+    std::lock_guard<std::mutex> lk(S->mu);
+    *bytes = a > S->pending ? a - S->pending : 0;
     return LBM_GPU_OK;
 }
 

@@ -118,6 +118,8 @@ def _bind_ext(lib: C.CDLL) -> None:
         "lbm_gpu_server_stats": (C.c_int, [vp, C.POINTER(C.c_longlong), dp, C.POINTER(C.c_int),
                                            C.POINTER(C.c_int), C.POINTER(C.c_size_t)]),
         "lbm_gpu_server_profile": (C.c_int, [vp, dp, C.c_int]),
+        "lbm_gpu_server_set_reserve": (C.c_int, [vp, C.c_size_t]),
+        "lbm_gpu_server_available": (C.c_int, [vp, C.POINTER(C.c_size_t)]),
         "lbm_gpu_server_destroy": (C.c_int, [vp]),
         "lbm_gpu_compute_force_mem_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_int, C.c_int,
                                                         C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -461,6 +463,16 @@ class GpuServer:
         _check(self.lib.lbm_gpu_server_stats(self.h, C.byref(l), C.byref(b), C.byref(q), C.byref(a), C.byref(m)),
                "lbm_gpu_server_stats")
         return {"lups": l.value, "busy_s": b.value, "queued": q.value, "active": a.value, "bytes": m.value}
+
+    def set_reserve(self, reserve_bytes: int):
+        """Device memory admissions leave free (lbm_gpu_server_set_reserve)."""
+        _check(self.lib.lbm_gpu_server_set_reserve(self.h, int(reserve_bytes)), "lbm_gpu_server_set_reserve")
+
+    def available(self) -> int:
+        """Device memory a request could be admitted into now (lbm_gpu_server_available)."""
+        b = C.c_size_t()
+        _check(self.lib.lbm_gpu_server_available(self.h, C.byref(b)), "lbm_gpu_server_available")
+        return b.value
 
     def profile(self):
         """Host seconds per phase of the scheduling rounds (lbm_gpu_server_profile)."""

@@ -112,3 +112,60 @@ def test_requests_started_from_equilibrium():
             assert same(res["spectra"], spec)
         srv.release(rid)
     srv.close()
+
+
+def _max_active_run(srv, stream):
+    ids = []
+    for r in stream:
+        case, st, spec = serving.build_request(r)
+        ids.append(srv.submit(case, st, r.steps, r.storage, impedance=spec))
+    most = 0
+    while srv.poll() > 0:
+        most = max(most, srv.stats()["active"])
+    return ids, most
+
+
+def test_admission_follows_live_free_memory():
+    """Admission reads the device's free memory every round: a small
+    allocation made after the server started holds admissions back (fewer
+    requests active at once), no request fails, and every result is the one
+    the request gives alone. With the allocation freed, more run at once."""
+    torch = pytest.importorskip("torch")
+    from lbc_gb300 import GpuServer
+    stream = [Req("channel", 1024, 256, 120, 1, 0.0, 3000 + q) for q in range(6)]
+    srv = GpuServer(0, 64, 40)
+    # One request's estimated footprint (all six are alike).
+    case, st, _ = serving.build_request(stream[0])
+    rid = srv.submit(case, st, 40, stream[0].storage)
+    srv.poll()
+    est = srv.stats()["bytes"]
+    while srv.poll() > 0:
+        pass
+    srv.release(rid)
+    assert est > 0
+    # Leave room for 4.5 requests beyond the reserve, then take 2 of them
+    # with an allocation the server knows nothing about.
+    total = torch.cuda.mem_get_info()[1]
+    reserve0 = total // 20
+    avail0 = srv.available()
+    assert avail0 > 10 * est
+    srv.set_reserve(avail0 + reserve0 - int(4.5 * est))
+    extra = torch.empty(2 * est, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    assert srv.available() < 3 * est
+    ids, most_held = _max_active_run(srv, stream)
+    assert 1 <= most_held <= 2, most_held
+    for r, rid in zip(stream, ids):
+        assert srv.status(rid)[0] == 3, srv.status(rid)
+        res = srv.fetch(rid)
+        rho, u, v, _ = _alone(r)
+        assert same(res["rho"], rho) and same(res["u"], u) and same(res["v"], v)
+        srv.release(rid)
+    del extra
+    torch.cuda.empty_cache()
+    ids, most_free = _max_active_run(srv, stream)
+    assert most_free > most_held, (most_free, most_held)
+    for rid in ids:
+        assert srv.status(rid)[0] == 3
+        srv.release(rid)
+    srv.close()

@@ -28,8 +28,13 @@ extern "C" {
 #define LBM_GPU_ERR_IO (-4)
 
 /* Population storage. F64: lbc's arithmetic, bit for bit. F32/F16_SHIFTED:
- * populations stored as f_k - w_k in FP32 / FP16, collision in FP32. */
-enum { LBM_GPU_F64 = 0, LBM_GPU_F32_SHIFTED = 1, LBM_GPU_F16_SHIFTED = 2 };
+ * populations stored as f_k - w_k in FP32 / FP16, collision in FP32.
+ * F64_FMA: FP64 storage, the step's moments and collision with fused
+ * multiply-adds and the D2Q9 pair symmetry (74 FP64 instructions per node
+ * against 125, so 1.6-1.9x faster on a part whose FP64 rate bounds the step);
+ * lbc's results to rounding (1e-12 relative), not bit for bit. It needs lbc's
+ * weight symmetry (w1 = w2 = w3 = w4, w5 = w6 = w7 = w8). */
+enum { LBM_GPU_F64 = 0, LBM_GPU_F32_SHIFTED = 1, LBM_GPU_F16_SHIFTED = 2, LBM_GPU_F64_FMA = 3 };
 
 typedef struct lbm_gpu_solver lbm_gpu_solver;
 
@@ -50,7 +55,7 @@ typedef struct {
     int isperiodic_x, isperiodic_y;
     double Fx, Fy;
     const double *wall_u, *wall_v; /* [Ny][Nx] wall velocity of solid nodes, or NULL */
-    int storage;                   /* LBM_GPU_F64 / _F32_SHIFTED / _F16_SHIFTED */
+    int storage;                   /* LBM_GPU_F64 / _F32_SHIFTED / _F16_SHIFTED / _F64_FMA */
 } lbm_gpu_case;
 
 typedef struct {
@@ -71,6 +76,11 @@ typedef struct {
 
 const char *lbm_gpu_last_error(void);
 int lbm_gpu_device_count(void);
+/* The current device's FP64 fused multiply-add issue rate, measured (thread
+ * FMA instructions per second, the fastest of five timed launches of a kernel
+ * of independent DFMA chains): the ceiling of the FP64 step kernels, which are
+ * bound by FP64 issue on parts with a low FP64 rate such as GB300. */
+int lbm_gpu_fp64_rate(double *lane_ops_per_s);
 /* How kernels can reach host memory at p: 1 page-locked and mapped at the
  * same address, 2 any pageable memory (the device walks the host page tables,
  * e.g. over NVLink-C2C), 0 neither (copies only), -1 no device. */
@@ -263,8 +273,8 @@ int lbm_gpu_server_available(lbm_gpu_server *srv, size_t *bytes);
  * admission (solver setup and state upload), [2] batch construction, [3]
  * launching and waiting for the chunks, [4] retiring (results to host, device
  * memory freed), [5..7] wall time of the FP64, FP32 and FP16 lanes' rounds
- * that ran a chunk; seconds (phases summed over lanes). Writes min(n, 8)
- * values. */
+ * that ran a chunk; seconds (phases summed over lanes); [8] the same for the
+ * FP64-FMA lane. Writes min(n, 9) values. */
 int lbm_gpu_server_profile(lbm_gpu_server *srv, double *out, int n);
 int lbm_gpu_server_destroy(lbm_gpu_server *srv);
 

@@ -705,6 +705,39 @@ int lbm_gpu_host_access(const void *p) {
     return (pageable && via_tables) ? 2 : 0;
 }
 
+int lbm_gpu_fp64_rate(double *lane_ops_per_s) {
+    if (!lane_ops_per_s) { set_error("null argument"); return LBM_GPU_ERR_ARG; }
+    int dev = 0, sms = 0;
+    if (!check_cuda(cudaGetDevice(&dev), "cudaGetDevice") ||
+        !check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"))
+        return LBM_GPU_ERR_CUDA;
+    double *sink = nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const int blocks = 8 * sms, iters = 4096;
+    float best = 0.f;
+    bool okk = check_cuda(cudaMalloc(&sink, sizeof(double)), "cudaMalloc") &&
+               check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate") &&
+               check_cuda(cudaEventCreate(&e0), "cudaEventCreate") && check_cuda(cudaEventCreate(&e1), "cudaEventCreate");
+    // One warm-up launch, then the fastest of five.
+    for (int rep = 0; okk && rep < 6; rep++) {
+        float ms = 0.f;
+        okk = check_cuda(cudaEventRecord(e0, s), "cudaEventRecord") &&
+              check_cuda(launch::fp64_rate(blocks, iters, sink, s), "k_fp64_rate") &&
+              check_cuda(cudaEventRecord(e1, s), "cudaEventRecord") &&
+              check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize") &&
+              check_cuda(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+        if (okk && rep > 0 && (best == 0.f || ms < best)) best = ms;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+    if (sink) cudaFree(sink);
+    if (!okk || best <= 0.f) return LBM_GPU_ERR_CUDA;
+    *lane_ops_per_s = (double)blocks * 256.0 * 8.0 * iters / (best * 1e-3);
+    return LBM_GPU_OK;
+}
+
 int lbm_gpu_device_count(void) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
@@ -716,15 +749,14 @@ int lbm_gpu_create(const lbm_gpu_case *c, lbm_gpu_solver **out) {
     *out = nullptr;
     if (!check_lattice(9, c->cx, c->cy, c->opp)) return LBM_GPU_ERR_ARG;
     if (!c->w || !c->omega_eff) { set_error("w and omega_eff are required"); return LBM_GPU_ERR_ARG; }
-    if (c->storage < LBM_GPU_F64 || c->storage > LBM_GPU_F16_SHIFTED) { set_error("bad storage"); return LBM_GPU_ERR_ARG; }
     CaseDesc d;
+    if (!storage_to_desc(c->storage, d)) { set_error("bad storage"); return LBM_GPU_ERR_ARG; }
     if (!fill_desc(d, c->Nx, c->Ny, c->w, c->omega_eff, c->solid_mask, c->boundaries,
                    c->num_boundaries, c->isperiodic_x, c->isperiodic_y, c->Fx, c->Fy, c->phi,
                    c->use_IBB))
         return LBM_GPU_ERR_ARG;
     d.wall_u = c->wall_u;
     d.wall_v = c->wall_v;
-    d.store = c->storage;
     std::unique_ptr<Solver> s(new Solver(d));
     if (!s->ok()) return LBM_GPU_ERR_CUDA;
     *out = new lbm_gpu_solver{std::move(s)};
@@ -859,7 +891,7 @@ int lbm_gpu_get_info(lbm_gpu_solver *s, lbm_gpu_info *info) {
     info->Nx = s->s->Nx();
     info->Ny = s->s->Ny();
     info->pitch = s->s->pitch();
-    info->storage = s->s->store();
+    info->storage = s->s->storage_code();
     info->has_geometry = s->s->has_flags() ? 1 : 0;
     info->edge_stages = s->s->nstages();
     info->launches_per_step = s->s->launches_per_step();

@@ -79,6 +79,14 @@ Solver::Solver(const CaseDesc &d) : d_(d) {
         set_error("grid must be at least 2 x 2");
         return;
     }
+    if (d_.fma64) {
+        const double *w = d_.w;
+        if (d_.store != STORE_F64 || !(w[1] == w[2] && w[1] == w[3] && w[1] == w[4] && w[5] == w[6] &&
+                                       w[5] == w[7] && w[5] == w[8])) {
+            set_error("FP64 FMA storage needs FP64 storage and lbc's weight symmetry (w1..w4 equal, w5..w8 equal)");
+            return;
+        }
+    }
     esize_ = d_.store == STORE_F64 ? 8 : (d_.store == STORE_F32 ? 4 : 2);
     pitch_ = (d_.Nx + 63) / 64 * 64;
     plane_ = (long long)pitch_ * d_.Ny;
@@ -765,6 +773,7 @@ bool Solver::launch_collide(int b, cudaStream_t s) {
     c.Fx = d_.Fx; c.Fy = d_.Fy;
     for (int k = 0; k < 9; k++) c.w[k] = d_.w[k];
     c.from_pops = fields_are_moments_ ? 1 : 0;
+    c.fma = d_.fma64 ? 1 : 0;
     if (d_.store == STORE_F64) CK(launch::collide_exact(c, s));
     else CK(launch::collide_shifted(c, d_.store, s));
     return true;
@@ -985,7 +994,7 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
     if (!s) s = stream_;
     const StepParams p = step_params(src, dst, write_macro, bparity);
     if (d_.store == STORE_F64) {
-        CK(launch::step_exact(p, has_flags_, collide, block_, s));
+        CK(launch::step_exact(p, has_flags_, collide, block_, s, d_.fma64));
     } else {
         const FastStepParams fp = fast_params(p);
         // The clean pairs, then the special nodes overlapping their last wave
@@ -1084,7 +1093,7 @@ const std::vector<int4> &Solver::tiles(int tws) const {
 }
 
 std::string Solver::tune_key() const {
-    return device_tag() + "/step/s" + std::to_string(d_.store) + "/" + std::to_string(d_.Nx) + "x" +
+    return device_tag() + "/step/s" + std::to_string(storage_code()) + "/" + std::to_string(d_.Nx) + "x" +
            std::to_string(d_.Ny) + (has_flags_ ? "/geo" : "/plain") + (has_mem_ ? "/mem" : "");
 }
 
@@ -1196,7 +1205,7 @@ Batch::Batch(const std::vector<Solver *> &cases) : cases_(cases) {
             set_error("batch: invalid case");
             return;
         }
-        if (c->store() != store_) {
+        if (c->store() != store_ || c->fma64() != cases_[0]->fma64()) {
             set_error("batch: all cases must use the same storage");
             return;
         }
@@ -1457,7 +1466,7 @@ bool Batch::build() {
 bool Batch::launch_batched(int sel) {
     if (store_ == STORE_F64) {
         CK(launch::step_batch_exact((const StepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
-                                    grid_, stream_));
+                                    grid_, stream_, cases_[0]->fma64()));
     } else {
         // the clean pairs, then the special nodes overlapping their tail
         CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,

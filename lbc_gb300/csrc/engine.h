@@ -51,7 +51,20 @@ struct CaseDesc {
     double Fx = 0.0, Fy = 0.0;
     std::vector<BCEntry> bcs;
     int store = STORE_F64;
+    // FP64 storage only: step with the fused multiply-add arithmetic
+    // (moments_fma / collide_fma), lbc's results to rounding instead of bit
+    // for bit; needs lbc's weight symmetry (w1..w4 equal, w5..w8 equal).
+    bool fma64 = false;
 };
+
+// The public storage codes (lbm_gpu.h): LBM_GPU_F64_FMA is FP64 storage with
+// the fused multiply-add step. False for an unknown code.
+inline bool storage_to_desc(int storage, CaseDesc &d) {
+    if (storage < 0 || storage > 3) return false;
+    d.store = storage == 3 ? STORE_F64 : storage;
+    d.fma64 = storage == 3;
+    return true;
+}
 
 struct Stage {
     int kind, index, along;
@@ -109,6 +122,9 @@ class Solver {
     int Nx() const { return d_.Nx; }
     int Ny() const { return d_.Ny; }
     int store() const { return d_.store; }
+    bool fma64() const { return d_.fma64; }
+    // The public storage code (lbm_gpu.h), LBM_GPU_F64_FMA included.
+    int storage_code() const { return d_.fma64 ? 3 : d_.store; }
     cudaStream_t stream() const { return stream_; }
     size_t device_bytes() const { return dev_bytes_; }
     bool has_flags() const { return has_flags_; }

@@ -25,6 +25,9 @@ struct CollideParams {
     // populations (state left by a previous run), so recompute them from the
     // populations in the fused step's own arithmetic.
     int from_pops;
+    // FP64 storage: collide as the fused multiply-add step does (collide_fma
+    // off the BC-written nodes), so that run(a) + run(b) = run(a + b).
+    int fma;
 };
 
 // Collision that reads lbc's AoS populations where they are (host memory the
@@ -110,8 +113,10 @@ struct ImpWall {
 };
 
 namespace launch {
-// exact FP64 (kernels_exact.cu)
-cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block, cudaStream_t s);
+// FP64 (kernels_exact.cu): lbc's rounding sequence, or with fma set the
+// fused multiply-add arithmetic (moments_fma / collide_fma)
+cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block, cudaStream_t s,
+                       bool fma = false);
 // collide: the finish of fused members applies the collision (false only in
 // the final step of a run, which leaves pre-collision populations).
 // after_bulk (here, stage_batch and force_reduce): the previous launch in s is
@@ -132,11 +137,13 @@ cudaError_t aos_bc(const AosArgs &a, int kind, int index, int along, const doubl
                    const double *val2, cudaStream_t s);
 cudaError_t mei_init(const AosArgs &a, double rho0, cudaStream_t s);
 cudaError_t mei_iter(const AosArgs &a, double rho0, unsigned long long *maxbits, cudaStream_t s);
+// blocks x 256 threads, each 8 x iters dependent DFMA (lbm_gpu_fp64_rate)
+cudaError_t fp64_rate(int blocks, int iters, double *sink, cudaStream_t s);
 
 // batches of cases (tile list = int4 {case, x0, y0, case has wall links})
 // Tiles of 2^tws x 2^(8 - tws) nodes, tws in [5, 8].
 cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 *tiles, int ntiles,
-                             int sel, int tws, int grid, cudaStream_t s);
+                             int sel, int tws, int grid, cudaStream_t s, bool fma = false);
 int step_batch_exact_grid();
 // One level of a batch's Boundary lists (n entries); nfs > 0 adds one block
 // row per force slot fs[0 .. nfs).

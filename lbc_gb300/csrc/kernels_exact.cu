@@ -37,7 +37,9 @@ namespace lbm {
 // its momentum-exchange terms (src/core/compute_force_mem.c:51-58), computes
 // moments (src/core/compute_macroscopic_fields.c:23-46) and, unless it is written
 // by an edge BC, collides (src/core/collision.c:22-38) and stores.
-template <bool FLAGS, bool COLLIDE>
+// FMA: moments_fma / collide_fma instead of lbc's rounding sequence (the same
+// step to rounding, in 74 FP64 instructions per node instead of 125).
+template <bool FLAGS, bool COLLIDE, bool FMA = false>
 __device__ __forceinline__ void step_node_exact(const StepParams &p, int i, int j, double &mfx,
                                                 double &mfy, bool &link) {
     {
@@ -111,7 +113,8 @@ __device__ __forceinline__ void step_node_exact(const StepParams &p, int i, int 
             }
             if (!(FLAGS && (fl & NF_BCW))) {
                 double rho, ux, uy;
-                moments_exact(f, p.hFx, p.hFy, rho, ux, uy);
+                if (FMA) moments_fma(f, p.hFx, p.hFy, p.has_force != 0, rho, ux, uy);
+                else moments_exact(f, p.hFx, p.hFy, rho, ux, uy);
                 if (p.write_macro) { p.rho[dn] = rho; p.ux[dn] = ux; p.uy[dn] = uy; }
                 if (slot >= 0) {
                     p.bandm_next[slot] = rho;
@@ -120,7 +123,8 @@ __device__ __forceinline__ void step_node_exact(const StepParams &p, int i, int 
                 }
                 if (COLLIDE) {
                     const double om = p.omega ? p.omega[dn] : p.omega0;
-                    collide_exact(f, p.w, rho, ux, uy, om, p.has_force != 0, p.Fx, p.Fy);
+                    if (FMA) collide_fma(f, p.w[0], p.w[1], p.w[5], rho, ux, uy, om, p.has_force != 0, p.Fx, p.Fy);
+                    else collide_exact(f, p.w, rho, ux, uy, om, p.has_force != 0, p.Fx, p.Fy);
                 }
 #pragma unroll
                 for (int k = 0; k < 9; k++) Dst[k * pl + node] = f[k];
@@ -129,14 +133,14 @@ __device__ __forceinline__ void step_node_exact(const StepParams &p, int i, int 
     }
 }
 
-template <bool FLAGS, bool COLLIDE>
+template <bool FLAGS, bool COLLIDE, bool FMA>
 __global__ void __launch_bounds__(256) k_step_exact(const StepParams p) {
     pdl_launch_dependents();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     double mfx = 0.0, mfy = 0.0;
     bool link = false;
-    if (i < p.Nx && j < p.Ny) step_node_exact<FLAGS, COLLIDE>(p, i, j, mfx, mfy, link);
+    if (i < p.Nx && j < p.Ny) step_node_exact<FLAGS, COLLIDE, FMA>(p, i, j, mfx, mfy, link);
     if (FLAGS && p.mem_partials) segment_reduce2_store(mfx, mfy, link, i, j, p.Nx, p.seg_slot, p.mem_partials);
 }
 
@@ -147,6 +151,7 @@ __global__ void __launch_bounds__(256) k_step_exact(const StepParams p) {
 // grids and different geometries share the launch. Force partials go to each
 // case's own segment slots (td.w != 0: the tile contains wall links), reduced
 // per case by k_force_reduce exactly as when the case runs alone.
+template <bool FMA>
 __global__ void __launch_bounds__(256) k_step_batch_exact(const StepParams *__restrict__ sp,
                                                           const int *__restrict__ phase,
                                                           const int4 *__restrict__ tiles, int ntiles,
@@ -161,9 +166,9 @@ __global__ void __launch_bounds__(256) k_step_batch_exact(const StepParams *__re
         bool link = false;
         const bool in = i < p.Nx && j < p.Ny;
         if (p.flags) {
-            if (in) step_node_exact<true, true>(p, i, j, mfx, mfy, link);
+            if (in) step_node_exact<true, true, FMA>(p, i, j, mfx, mfy, link);
         } else {
-            if (in) step_node_exact<false, true>(p, i, j, mfx, mfy, link);
+            if (in) step_node_exact<false, true, FMA>(p, i, j, mfx, mfy, link);
         }
         if (td.w) segment_reduce2_store(mfx, mfy, link, i, j, p.Nx, p.seg_slot, p.mem_partials);
     }
@@ -332,13 +337,19 @@ __global__ void k_collide_exact(const CollideParams p) {
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= p.Nx || j >= p.Ny) return;
     const long long node = (long long)j * p.pitch + i;
-    if (p.flags && (p.flags[node] & NF_SOLID)) return;
+    const uint16_t fl = p.flags ? p.flags[node] : (uint16_t)0;
+    if (fl & NF_SOLID) return;
     const size_t dn = (size_t)j * p.Nx + i;
     double f[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) f[k] = p.f[k * p.plane + node];
     const double om = p.omega ? p.omega[dn] : p.omega0;
-    collide_exact(f, p.w, p.rho[dn], p.ux[dn], p.uy[dn], om, p.has_force != 0, p.Fx, p.Fy);
+    // In the fused FMA step the nodes an edge BC writes are collided by the
+    // stage launch's finish in lbc's arithmetic, the others in the FMA form:
+    // the same split here, so that run(a) + run(b) = run(a + b) bit for bit.
+    if (p.fma && !(fl & NF_BCW))
+        collide_fma(f, p.w[0], p.w[1], p.w[5], p.rho[dn], p.ux[dn], p.uy[dn], om, p.has_force != 0, p.Fx, p.Fy);
+    else collide_exact(f, p.w, p.rho[dn], p.ux[dn], p.uy[dn], om, p.has_force != 0, p.Fx, p.Fy);
 #pragma unroll
     for (int k = 0; k < 9; k++) p.f[k * p.plane + node] = f[k];
 }
@@ -615,21 +626,52 @@ __global__ void k_mei_iter(AosArgs a, double rho0, unsigned long long *maxbits) 
         atomicMax(maxbits, (unsigned long long)__double_as_longlong(d));
 }
 
+// ---------------------------------------------------------------- FP64 rate
+
+// The device's FP64 FMA issue rate, the ceiling of the FP64 step kernels: each
+// thread runs eight independent dependency chains of DFMA (enough in flight
+// per warp to cover the pipe's latency). x <- a x + b with a < 1 stays bounded.
+__global__ void __launch_bounds__(256) k_fp64_rate(double *sink, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) x[q] = (threadIdx.x + q) * 1e-3;
+#pragma unroll 1
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) x[q] = fma(x[q], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) s += x[q];
+    if (s == -1.0) sink[0] = s;  // never true; keeps the chains live
+}
+
 // ---------------------------------------------------------------- launchers
 
 namespace launch {
 
+cudaError_t fp64_rate(int blocks, int iters, double *sink, cudaStream_t s) {
+    k_fp64_rate<<<blocks, 256, 0, s>>>(sink, iters, 0.9999999, 1e-9);
+    return cudaGetLastError();
+}
+
 static dim3 grid2(int Nx, int Ny, dim3 b) { return dim3((Nx + b.x - 1) / b.x, (Ny + b.y - 1) / b.y); }
 
-cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block, cudaStream_t s) {
-    const dim3 g = grid2(p.Nx, p.Ny, block);
+template <bool FMA>
+static void step_exact_t(const StepParams &p, bool flags, bool collide, dim3 g, dim3 block, cudaStream_t s) {
     if (flags) {
-        if (collide) k_step_exact<true, true><<<g, block, 0, s>>>(p);
-        else k_step_exact<true, false><<<g, block, 0, s>>>(p);
+        if (collide) k_step_exact<true, true, FMA><<<g, block, 0, s>>>(p);
+        else k_step_exact<true, false, FMA><<<g, block, 0, s>>>(p);
     } else {
-        if (collide) k_step_exact<false, true><<<g, block, 0, s>>>(p);
-        else k_step_exact<false, false><<<g, block, 0, s>>>(p);
+        if (collide) k_step_exact<false, true, FMA><<<g, block, 0, s>>>(p);
+        else k_step_exact<false, false, FMA><<<g, block, 0, s>>>(p);
     }
+}
+
+cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block, cudaStream_t s, bool fma) {
+    const dim3 g = grid2(p.Nx, p.Ny, block);
+    if (fma) step_exact_t<true>(p, flags, collide, g, block, s);
+    else step_exact_t<false>(p, flags, collide, g, block, s);
     return cudaGetLastError();
 }
 
@@ -643,10 +685,11 @@ cudaError_t stage_group(const StageGroup &g, int store, bool collide, bool after
 }
 
 cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 *tiles, int ntiles,
-                             int sel, int tws, int grid, cudaStream_t s) {
+                             int sel, int tws, int grid, cudaStream_t s, bool fma) {
     if (ntiles == 0) return cudaSuccess;
     if (tws < 5 || tws > 8) return cudaErrorInvalidValue;
-    k_step_batch_exact<<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+    if (fma) k_step_batch_exact<true><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+    else k_step_batch_exact<false><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
     return cudaGetLastError();
 }
 

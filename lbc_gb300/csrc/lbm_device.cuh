@@ -164,6 +164,110 @@ __device__ __forceinline__ void collide_exact(double f[9], const double w[9], do
 }
 
 // ---------------------------------------------------------------------------
+// FP64 with fused multiply-adds and the D2Q9 pair symmetry: the same physics
+// as moments_exact / collide_exact (src/core/compute_macroscopic_fields.c:23-46,
+// src/core/collision.c:24-38) in fewer FP64 instructions, rounded
+// differently, so it agrees with lbc to rounding, not bit for bit. Over the
+// 20,000 steps of the 256 x 64 channel both stay within 1e-12 of the same
+// step in extended precision (lbc's own rounding: 3e-13 in u) and within about
+// 1e-12 of each other in u and 1e-14 in rho. GB300 issues FP64 at about two
+// lane operations per clock per SM, so on this part the FP64 step is bound by
+// its FP64 instruction count, not by memory. Written with explicit fma()
+// calls, which --fmad=false leaves alone.
+//
+// Needs lbc's weight symmetry: w1 = w2 = w3 = w4 (axes) and w5 = ... = w8
+// (diagonals); the host checks it before choosing this arithmetic.
+
+#ifdef __CUDACC__  // device-only: the host translation units see none of it
+// 1/x by Newton-Raphson from the hardware's FP64 reciprocal seed (rcp.approx,
+// relative error below 2^-20), finished with the third-order step
+// r (1 + e + e^2), e = 1 - x r, whose error is about e^3: a result within an
+// ulp or two of 1/x for the positive densities the step sees.
+__device__ __forceinline__ double recip_fma(double x) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    const double e = fma(-x, r, 1.0);
+    return fma(r, fma(e, e, e), r);
+}
+
+// rho, (j + F / 2) / rho with shared partial sums: 14 additions for the three
+// moments, one reciprocal, two multiplies.
+__device__ __forceinline__ void moments_fma(const double f[9], double hFx, double hFy, bool force,
+                                            double &rho, double &ux, double &uy) {
+    const double a = (f[1] + f[5]) + f[8];   // c_x = +1
+    const double b = (f[3] + f[6]) + f[7];   // c_x = -1
+    const double c = (f[2] + f[5]) + f[6];   // c_y = +1
+    const double d = (f[4] + f[7]) + f[8];   // c_y = -1
+    double s = (((f[0] + f[2]) + f[4]) + a) + b;
+    double jx = a - b, jy = c - d;
+    if (force) { jx += hFx; jy += hFy; }
+    // lbc's floor (compute_macroscopic_fields.c:27), compared on the bit
+    // pattern: for doubles of either sign x < 1e-16 iff bits(x) < bits(1e-16)
+    // as signed integers, which spares an FP64 compare.
+    if (__double_as_longlong(s) < __double_as_longlong(1e-16)) s = 1e-16;
+    rho = s;
+    const double r = recip_fma(s);
+    ux = jx * r;
+    uy = jy * r;
+}
+
+// BGK collision, and with a body force Guo's term (1 - omega/2) w_k (3 c.F +
+// 9 (c.u)(c.F) - 3 u.F), in lbc's relaxation form f' = f + (omega (f_eq - f)
+// + G_k): f_eq - f is exact for populations near equilibrium (Sterbenz), so
+// the only rounding at the populations' scale is the final addition, as in
+// lbc (src/core/collision.c:36-37). That keeps the step's mass drift the one
+// lbc's own FP64 run has (from the weights' FP64 sum), which a form
+// (1 - omega) f + omega f_eq would change. f_eq of an opposite pair
+// (k, opp k), cu = c_k . u, is E +- O: even part E = w rho (1 - 1.5 u.u +
+// 4.5 cu^2), odd part O = 3 w rho cu; the forcing term splits the same way
+// into g w (9 cu cF - 3 u.F) and 3 g w cF.
+__device__ __forceinline__ void collide_fma(double f[9], double w0, double wa, double wd, double rho,
+                                            double ux, double uy, double om, bool force, double Fx,
+                                            double Fy) {
+    const double base = fma(-1.5, fma(ux, ux, uy * uy), 1.0);
+    const double wra = wa * rho, wrd = wd * rho;
+    const double Ba = wra * base, Bd = wrd * base;      // even part, constant term
+    const double Ca = 4.5 * wra, Cd = 4.5 * wrd;        // even part, c.u squared
+    const double Da = 3.0 * wra, Dd = 3.0 * wrd;        // odd part
+    const double B0 = (w0 * rho) * base;
+    const double u5 = ux + uy, u6 = uy - ux;
+    if (!force) {
+        auto pair = [&](double &fp, double &fm, double cu, double B, double C, double D) {
+            const double E = fma(C * cu, cu, B);
+            const double O = D * cu;
+            fp = fma(om, (E + O) - fp, fp);
+            fm = fma(om, (E - O) - fm, fm);
+        };
+        f[0] = fma(om, B0 - f[0], f[0]);
+        pair(f[1], f[3], ux, Ba, Ca, Da);
+        pair(f[2], f[4], uy, Ba, Ca, Da);
+        pair(f[5], f[7], u5, Bd, Cd, Dd);
+        pair(f[6], f[8], u6, Bd, Cd, Dd);
+        return;
+    }
+    const double g = fma(-0.5, om, 1.0);
+    const double ga = g * wa, gd = g * wd;
+    const double uF = fma(ux, Fx, uy * Fy);
+    const double ga9 = 9.0 * ga, gd9 = 9.0 * gd, ga3 = 3.0 * ga, gd3 = 3.0 * gd;
+    const double Ga = -ga3 * uF, Gd = -gd3 * uF;        // even forcing, constant term
+    f[0] = f[0] + fma(om, B0 - f[0], (-3.0 * (g * w0)) * uF);
+    const double F5 = Fx + Fy, F6 = Fy - Fx;
+    auto pair = [&](double &fp, double &fm, double cu, double P, double Qo, double B, double C, double D,
+                    double G) {
+        const double E = fma(C * cu, cu, B);
+        const double O = D * cu;
+        const double GE = fma(P, cu, G);
+        fp = fp + fma(om, (E + O) - fp, GE + Qo);
+        fm = fm + fma(om, (E - O) - fm, GE - Qo);
+    };
+    pair(f[1], f[3], ux, ga9 * Fx, ga3 * Fx, Ba, Ca, Da, Ga);
+    pair(f[2], f[4], uy, ga9 * Fy, ga3 * Fy, Ba, Ca, Da, Ga);
+    pair(f[5], f[7], u5, gd9 * F5, gd3 * F5, Bd, Cd, Dd, Gd);
+    pair(f[6], f[8], u6, gd9 * F6, gd3 * F6, Bd, Cd, Dd, Gd);
+}
+#endif  // __CUDACC__
+
+// ---------------------------------------------------------------------------
 // Edge BCs, generic over an accessor that reads/writes the current f_new of a
 // node, the previous-step moments and (periodic only) the post-collision f.
 // Accessor interface:

@@ -78,7 +78,8 @@ struct Request {
 size_t estimate_bytes(const Request &r) {
     const size_t N = (size_t)r.Nx * r.Ny;
     const size_t pitchN = (size_t)((r.Nx + 63) / 64 * 64) * r.Ny;
-    const size_t es = r.storage == LBM_GPU_F64 ? 8 : (r.storage == LBM_GPU_F32_SHIFTED ? 4 : 2);
+    const size_t es = (r.storage == LBM_GPU_F64 || r.storage == LBM_GPU_F64_FMA)
+                          ? 8 : (r.storage == LBM_GPU_F32_SHIFTED ? 4 : 2);
     return 2 * 9 * es * pitchN + (size_t)staging_rows(r.Nx, r.Ny) * r.Nx * 72 + 24 * N + 2 * pitchN +
            (r.use_ibb ? 4 * pitchN : 0) + 8 * N + (1u << 20);
 }
@@ -100,7 +101,7 @@ struct lbm_gpu_server {
     std::mutex mu;
     std::map<int, std::unique_ptr<Request>> reqs;
     std::deque<Request *> queue;
-    Lane lanes[3];
+    Lane lanes[4];
     int n_active = 0;  // over all lanes
     size_t budget = 0;    // optional cap on the requests' estimated bytes (0: none)
     size_t in_use = 0;    // estimated bytes of the active requests
@@ -139,7 +140,7 @@ static bool admit(Request *r) {
         d.bcs[e].val1 = r->bc_vals[2 * e].empty() ? nullptr : r->bc_vals[2 * e].data();
         d.bcs[e].val2 = r->bc_vals[2 * e + 1].empty() ? nullptr : r->bc_vals[2 * e + 1].data();
     }
-    d.store = r->storage;
+    storage_to_desc(r->storage, d);
     std::unique_ptr<Solver> s(new Solver(d));
     if (!s->ok()) {
         r->error = last_error();
@@ -244,7 +245,7 @@ static std::vector<Request *> take_admissions(lbm_gpu_server *S, Lane &L) {
     const size_t avail = device_available(S);
     std::lock_guard<std::mutex> lk(S->mu);
     int cap = S->max_active;
-    if (L.storage == STORE_F64) {
+    if (L.storage == LBM_GPU_F64 || L.storage == LBM_GPU_F64_FMA) {
         bool others = S->n_active > (int)L.active.size();
         for (const Request *r : S->queue)
             if (r->storage != L.storage) { others = true; break; }
@@ -390,6 +391,7 @@ int lbm_gpu_server_create(size_t budget_bytes, int max_active, int chunk_steps, 
     S->lanes[0].storage = LBM_GPU_F64;
     S->lanes[1].storage = LBM_GPU_F32_SHIFTED;
     S->lanes[2].storage = LBM_GPU_F16_SHIFTED;
+    S->lanes[3].storage = LBM_GPU_F64_FMA;
     *out = S;
     return LBM_GPU_OK;
 }
@@ -399,6 +401,11 @@ int lbm_gpu_server_prepare(lbm_gpu_server *S, const lbm_gpu_case *c, const doubl
                            int nsteps, int keep_populations) {
     if (!S || !c || !rho || !u || !v || nsteps < 1 || (!f) != (!f_new)) {
         set_error("bad arguments");
+        return LBM_GPU_ERR_ARG;
+    }
+    CaseDesc probe;
+    if (!storage_to_desc(c->storage, probe)) {
+        set_error("bad storage");
         return LBM_GPU_ERR_ARG;
     }
     std::unique_ptr<Request> r(new Request());
@@ -603,9 +610,9 @@ int lbm_gpu_server_profile(lbm_gpu_server *S, double *out, int n) {
         return LBM_GPU_ERR_ARG;
     }
     std::lock_guard<std::mutex> lk(S->mu);
-    const double v[8] = {(double)S->rounds, S->t_admit, S->t_build, S->t_run, S->t_retire,
-                         S->lanes[0].busy_s, S->lanes[1].busy_s, S->lanes[2].busy_s};
-    for (int q = 0; q < n && q < 8; q++) out[q] = v[q];
+    const double v[9] = {(double)S->rounds, S->t_admit, S->t_build, S->t_run, S->t_retire,
+                         S->lanes[0].busy_s, S->lanes[1].busy_s, S->lanes[2].busy_s, S->lanes[3].busy_s};
+    for (int q = 0; q < n && q < 9; q++) out[q] = v[q];
     return LBM_GPU_OK;
 }
 

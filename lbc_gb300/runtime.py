@@ -17,9 +17,9 @@ from .cases import Case, State, Q
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liblbm_gpu.so")
 
-F64, F32_SHIFTED, F16_SHIFTED = 0, 1, 2
-STORAGE = {"f64": F64, "f32": F32_SHIFTED, "f16": F16_SHIFTED}
-BYTES_PER_POP = {F64: 8, F32_SHIFTED: 4, F16_SHIFTED: 2}
+F64, F32_SHIFTED, F16_SHIFTED, F64_FMA = 0, 1, 2, 3
+STORAGE = {"f64": F64, "f32": F32_SHIFTED, "f16": F16_SHIFTED, "f64fma": F64_FMA}
+BYTES_PER_POP = {F64: 8, F32_SHIFTED: 4, F16_SHIFTED: 2, F64_FMA: 8}
 
 _lib: Optional[C.CDLL] = None
 
@@ -67,6 +67,7 @@ def _bind_ext(lib: C.CDLL) -> None:
     sig = {
         "lbm_gpu_last_error": (C.c_char_p, []),
         "lbm_gpu_device_count": (C.c_int, []),
+        "lbm_gpu_fp64_rate": (C.c_int, [dp]),
         "lbm_gpu_host_access": (C.c_int, [vp]),
         "lbm_gpu_create": (C.c_int, [C.POINTER(CaseDesc), C.POINTER(vp)]),
         "lbm_gpu_destroy": (C.c_int, [vp]),
@@ -476,10 +477,10 @@ class GpuServer:
 
     def profile(self):
         """Host seconds per phase of the scheduling rounds (lbm_gpu_server_profile)."""
-        out = np.zeros(8)
-        _check(self.lib.lbm_gpu_server_profile(self.h, dptr(out), 8), "lbm_gpu_server_profile")
+        out = np.zeros(9)
+        _check(self.lib.lbm_gpu_server_profile(self.h, dptr(out), 9), "lbm_gpu_server_profile")
         return {"rounds": int(out[0]), "admit_s": out[1], "build_s": out[2], "run_s": out[3], "retire_s": out[4],
-                "lane_f64_s": out[5], "lane_f32_s": out[6], "lane_f16_s": out[7]}
+                "lane_f64_s": out[5], "lane_f32_s": out[6], "lane_f16_s": out[7], "lane_f64fma_s": out[8]}
 
     def close(self):
         if getattr(self, "h", None):

@@ -142,6 +142,17 @@ int lbm_gpu_force_history(lbm_gpu_solver *s, double *xy, int max_steps);
  * ones still held are written), LBM_GPU_ERR_IO when the file fails. */
 long long lbm_gpu_write_force_records(lbm_gpu_solver *s, const char *path, double dt, double cf, int append);
 
+/* ---- Probes (no counterpart in lbc): density and velocity at n chosen nodes
+ * (i[q], j[q]) after every step, from the populations the step leaves, in a
+ * device ring of `capacity` steps; one small launch per step while set (in a
+ * batch, one launch for all of its cases; set probes before the batch is
+ * made). n = 0 removes them. At most 4096 probes. Probes are not saved in
+ * checkpoints. */
+int lbm_gpu_set_probes(lbm_gpu_solver *s, int n, const int *i, const int *j, int capacity);
+/* Copies up to max_steps records, oldest first: out[(t * n + q) * 3 + {0, 1, 2}]
+ * = rho, ux, uy of probe q at the t-th step held. Returns the count. */
+int lbm_gpu_probe_history(lbm_gpu_solver *s, double *out, int max_steps);
+
 /* ---- Time-domain impedance wall (no counterpart in lbc's library; it
  * replaces the host-side ADE coupling of lbc's cases/nit/nit.c:276-303).
  * Boundary entry `entry` must be velocity_bottom_regularized. Each of its
@@ -163,6 +174,20 @@ int lbm_gpu_set_impedance_wall(lbm_gpu_solver *s, int entry, const double *R, co
 /* spectra[(i * nf + f) * 4 + q]: q = 0,1 sum p' e^{-i w n} (re, im); q = 2,3 the
  * same for v. state[2 i + {0,1}] = (x, v). Either pointer may be NULL. */
 int lbm_gpu_impedance_readback(lbm_gpu_solver *s, int entry, double *spectra, double *state);
+/* The wall's per-step trace, streamed from a device ring of `capacity` steps:
+ * the mean over its active nodes of the pressure fluctuation p' it was driven
+ * with and of the velocity v it imposed (lbc's nit case traces the same pair
+ * for its one global impedance model, cases/nit/nit.c:262-273). */
+int lbm_gpu_enable_impedance_trace(lbm_gpu_solver *s, int entry, int capacity);
+/* Writes the trace as lbc's text file does: one "%lf %lf %lf" line per step,
+ * time, pressure, velocity, where the line of step n holds the values of step
+ * n - 1 (a first line of zeros starts the file): lines n dt, p' cp, v cu. Lines
+ * not written yet are appended (append = 1) or start the file (append = 0);
+ * called at least every `capacity` steps it streams the whole run. Returns the
+ * lines written; LBM_GPU_ERR_ARG when steps left the ring unwritten (the ones
+ * still held are written), LBM_GPU_ERR_IO when the file fails. */
+long long lbm_gpu_write_impedance_trace(lbm_gpu_solver *s, int entry, const char *path, double dt, double cp,
+                                        double cu, int append);
 /* The per-step update the wall uses: (x, v) <- A (x, v) + b p' is the exact
  * solution of m v' + R v + K x = p' over one step with p' held constant.
  * A row-major 2x2, b 2. Returns 0, or LBM_GPU_ERR_ARG unless m, K > 0, R >= 0. */

@@ -856,6 +856,32 @@ long long lbm_gpu_write_force_records(lbm_gpu_solver *s, const char *path, doubl
     return n >= 0 ? n : (n == -2 ? LBM_GPU_ERR_ARG : LBM_GPU_ERR_IO);
 }
 
+int lbm_gpu_set_probes(lbm_gpu_solver *s, int n, const int *i, const int *j, int capacity) {
+    SOLVER_OR_FAIL(s);
+    return s->s->set_probes(n, i, j, capacity) ? LBM_GPU_OK : LBM_GPU_ERR_ARG;
+}
+
+int lbm_gpu_probe_history(lbm_gpu_solver *s, double *out, int max_steps) {
+    SOLVER_OR_FAIL(s);
+    if (!out || max_steps < 0) { set_error("bad arguments"); return LBM_GPU_ERR_ARG; }
+    const int n = s->s->probe_history(out, max_steps);
+    return n < 0 ? LBM_GPU_ERR_CUDA : n;
+}
+
+int lbm_gpu_enable_impedance_trace(lbm_gpu_solver *s, int entry, int capacity) {
+    SOLVER_OR_FAIL(s);
+    return s->s->enable_impedance_trace(entry, capacity) ? LBM_GPU_OK : LBM_GPU_ERR_ARG;
+}
+
+long long lbm_gpu_write_impedance_trace(lbm_gpu_solver *s, int entry, const char *path, double dt, double cp,
+                                        double cu, int append) {
+    SOLVER_OR_FAIL(s);
+    if (!path) { set_error("null path"); return LBM_GPU_ERR_ARG; }
+    const long long n = s->s->write_impedance_trace(entry, path, dt, cp, cu, append != 0);
+    if (n == -2) return LBM_GPU_ERR_ARG;
+    return n < 0 ? LBM_GPU_ERR_IO : n;
+}
+
 int lbm_gpu_enable_force_history(lbm_gpu_solver *s, int capacity) {
     SOLVER_OR_FAIL(s);
     return s->s->enable_force_history(capacity) ? LBM_GPU_OK : LBM_GPU_ERR_ARG;

@@ -936,7 +936,8 @@ bool Solver::set_impedance(int entry, const double *R, const double *m, const do
         st->imp_sin[f] = std::sin(omegas[f]);
     }
     graph_valid_ = false;
-    return true;
+    // a wall trace reads this array: its record task follows a new allocation
+    return st->d_trace ? upload_records() : true;
 }
 
 bool Solver::impedance_readback(int entry, double *out, double *state) {
@@ -989,8 +990,8 @@ FinishParams Solver::finish_params(int dst, bool write_macro, int bparity) const
 
 // One time step src -> dst: fused bulk kernel, then the Boundary list in order,
 // one launch per stage group, whose threads finish the BC-written nodes.
-bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int bparity,
-                         cudaStream_t s) {
+bool Solver::launch_step_kernels(int src, int dst, bool collide, bool write_macro, int bparity,
+                                 cudaStream_t s) {
     if (!s) s = stream_;
     const StepParams p = step_params(src, dst, write_macro, bparity);
     if (d_.store == STORE_F64) {
@@ -1025,6 +1026,182 @@ bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int b
         CK(launch::stage_group(sg, d_.store, collide, gi == 0, s));
     }
     return true;
+}
+
+// One step (launch_step_kernels), then its records when probes or wall
+// traces are set: they read what the step's kernels left, so they follow them.
+bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int bparity, cudaStream_t s) {
+    if (!launch_step_kernels(src, dst, collide, write_macro, bparity, s)) return false;
+    if (!rec_host_.empty())
+        CK(launch::record(d_rec_, (int)rec_host_.size(), d_.store, buf_[dst], nullptr, 0, nullptr, 0, collide,
+                          s ? s : stream_));
+    return true;
+}
+
+bool Solver::upload_records() {
+    rec_host_.clear();
+    if (nprobes_ > 0) {
+        RecordTask r;
+        std::memset(&r, 0, sizeof r);
+        r.kind = REC_PROBES;
+        r.n = nprobes_;
+        r.cs = -1;
+        r.cap = probe_cap_;
+        r.nodes = d_probe_nodes_;
+        r.plane = plane_;
+        r.ring = d_probe_ring_;
+        r.count = probe_count_;
+        for (int k = 0; k < 9; k++) r.w[k] = d_.w[k];
+        r.hFx = 0.5 * d_.Fx;
+        r.hFy = 0.5 * d_.Fy;
+        rec_host_.push_back(r);
+    }
+    for (const Stage &st : stages_) {
+        if (!st.d_trace || !st.d_imp) continue;
+        RecordTask r;
+        std::memset(&r, 0, sizeof r);
+        r.kind = REC_WALL;
+        r.n = st.along;
+        r.cs = -1;
+        r.cap = st.trace_cap;
+        r.imp = st.d_imp;
+        r.ring = st.d_trace;
+        r.count = st.trace_count;
+        rec_host_.push_back(r);
+    }
+    graph_valid_ = false;
+    if (rec_host_.empty()) return true;
+    if ((int)rec_host_.size() > rec_cap_) {
+        if (!dalloc(&d_rec_, rec_host_.size())) return false;
+        rec_cap_ = (int)rec_host_.size();
+    }
+    CK(cudaMemcpyAsync(d_rec_, rec_host_.data(), rec_host_.size() * sizeof(RecordTask), cudaMemcpyHostToDevice,
+                       stream_));
+    CK(cudaStreamSynchronize(stream_));
+    return true;
+}
+
+bool Solver::set_probes(int n, const int *pi, const int *pj, int capacity) {
+    if (n < 0 || n > kMaxProbes || (n > 0 && (!pi || !pj || capacity <= 0))) {
+        set_error("probes: need 0 <= n <= " + std::to_string(kMaxProbes) + ", node arrays and capacity > 0");
+        return false;
+    }
+    std::vector<long long> off((size_t)n);
+    for (int q = 0; q < n; q++) {
+        if (pi[q] < 0 || pi[q] >= d_.Nx || pj[q] < 0 || pj[q] >= d_.Ny) {
+            set_error("probes: node " + std::to_string(q) + " is outside the grid");
+            return false;
+        }
+        off[q] = (long long)pj[q] * pitch_ + pi[q];
+    }
+    nprobes_ = 0;
+    if (n > 0) {
+        if (!dalloc(&d_probe_nodes_, (size_t)n) || !dalloc(&d_probe_ring_, (size_t)capacity * n * 3) ||
+            !dalloc(&probe_count_, 1))
+            return false;
+        CK(cudaMemcpyAsync(d_probe_nodes_, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice,
+                           stream_));
+        CK(cudaMemsetAsync(probe_count_, 0, sizeof(unsigned long long), stream_));
+        nprobes_ = n;
+        probe_cap_ = capacity;
+    }
+    return upload_records();
+}
+
+int Solver::probe_history(double *out, int max_steps) {
+    if (nprobes_ == 0) return 0;
+    unsigned long long cnt = 0;
+    std::vector<double> ring((size_t)probe_cap_ * nprobes_ * 3);
+    if (!check_cuda(cudaMemcpyAsync(&cnt, probe_count_, sizeof cnt, cudaMemcpyDeviceToHost, stream_), "probes") ||
+        !check_cuda(cudaMemcpyAsync(ring.data(), d_probe_ring_, ring.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                    stream_), "probes") ||
+        !check_cuda(cudaStreamSynchronize(stream_), "probes"))
+        return -1;
+    const long long avail = std::min<long long>((long long)cnt, probe_cap_);
+    const int n = (int)std::min<long long>(avail, max_steps);
+    const long long first = (long long)cnt - n;
+    const size_t rec = (size_t)nprobes_ * 3;
+    for (int t = 0; t < n; t++) {
+        const size_t slot = (size_t)((first + t) % probe_cap_);
+        std::memcpy(out + (size_t)t * rec, ring.data() + slot * rec, rec * sizeof(double));
+    }
+    return n;
+}
+
+bool Solver::enable_impedance_trace(int entry, int capacity) {
+    Stage *st = nullptr;
+    for (Stage &x : stages_)
+        if (x.entry == entry) st = &x;
+    if (!st || !st->d_imp) {
+        set_error("impedance trace: no impedance wall on this entry");
+        return false;
+    }
+    if (capacity <= 0) {
+        set_error("impedance trace: capacity must be positive");
+        return false;
+    }
+    if (!dalloc(&st->d_trace, (size_t)capacity * 2) || !dalloc(&st->trace_count, 1)) return false;
+    CK(cudaMemsetAsync(st->trace_count, 0, sizeof(unsigned long long), stream_));
+    st->trace_cap = capacity;
+    st->trace_written = 0;
+    return upload_records();
+}
+
+// lbc's trace of its impedance BC (cases/nit/nit.c:262-273): a text line
+// "%lf %lf %lf\n" per iteration, time, surface-averaged pressure fluctuation
+// and acoustic velocity, where the line of iteration n holds the values
+// computed in iteration n - 1 (the file starts with a line of zeros). Here the
+// values of step n are the wall's mean p' and v over its active nodes
+// (scaled by cp and cu to physical units), the time (n + 1) dt. Lines not
+// written yet are appended (append) or the file is started.
+long long Solver::write_impedance_trace(int entry, const char *path, double dt, double cp, double cu,
+                                        bool append) {
+    Stage *st = nullptr;
+    for (Stage &x : stages_)
+        if (x.entry == entry) st = &x;
+    if (!st || !st->d_trace) {
+        set_error("impedance trace: not enabled on this entry");
+        return -1;
+    }
+    unsigned long long cnt = 0;
+    std::vector<double> ring((size_t)st->trace_cap * 2);
+    if (!check_cuda(cudaMemcpyAsync(&cnt, st->trace_count, sizeof cnt, cudaMemcpyDeviceToHost, stream_), "trace") ||
+        !check_cuda(cudaMemcpyAsync(ring.data(), st->d_trace, ring.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                    stream_), "trace") ||
+        !check_cuda(cudaStreamSynchronize(stream_), "trace"))
+        return -1;
+    FILE *fp = std::fopen(path, append ? "a" : "w");
+    if (!fp) {
+        set_error(std::string("cannot open ") + path);
+        return -1;
+    }
+    const unsigned long long first = std::max<unsigned long long>(
+        st->trace_written, cnt > (unsigned long long)st->trace_cap ? cnt - st->trace_cap : 0);
+    const bool lost = first > st->trace_written;
+    bool okk = true;
+    long long lines = 0;
+    if (st->trace_written == 0 && !append) {
+        okk = std::fprintf(fp, "%lf %lf %lf\n", 0.0, 0.0, 0.0) > 0;
+        lines++;
+    }
+    for (unsigned long long n = first; n < cnt && okk; n++) {
+        const size_t slot = (size_t)(n % (unsigned long long)st->trace_cap);
+        okk = std::fprintf(fp, "%lf %lf %lf\n", (double)(n + 1) * dt, ring[2 * slot] * cp, ring[2 * slot + 1] * cu) > 0;
+        lines++;
+    }
+    okk = (std::fclose(fp) == 0) && okk;
+    if (!okk) {
+        set_error(std::string("write failed: ") + path);
+        return -1;
+    }
+    const unsigned long long missed = first - st->trace_written;
+    st->trace_written = std::max(st->trace_written, cnt);
+    if (lost) {
+        set_error("the trace of " + std::to_string(missed) +
+                  " steps left the ring before it was written (drain it at least every capacity steps)");
+        return -2;
+    }
+    return lines;
 }
 
 bool Solver::begin_steps(cudaStream_t s) { return launch_collide(cur_, s); }
@@ -1457,8 +1634,21 @@ bool Batch::build() {
             walls_host_ = walls;
         }
     }
+    // Every case's probes and wall traces: one record launch per step.
+    std::vector<RecordTask> rec;
+    for (int c = 0; c < nc; c++)
+        for (RecordTask r : cases_[c]->record_tasks()) {
+            r.cs = c;
+            rec.push_back(r);
+        }
+    nrec_ = (int)rec.size();
+    if (nrec_) {
+        if (!balloc(allocs_, &d_rec_, rec.size(), stream_)) return false;
+        CK(cudaMemcpyAsync(d_rec_, rec.data(), rec.size() * sizeof(RecordTask), cudaMemcpyHostToDevice, stream_));
+    }
     // The force reductions ride in the first stage level's launch.
-    launches_per_step_ = 1 + (nspecial_ || nimp_ ? 1 : 0) + max_stages_ + (nforce_ && max_stages_ == 0 ? 1 : 0);
+    launches_per_step_ = 1 + (nspecial_ || nimp_ ? 1 : 0) + max_stages_ + (nforce_ && max_stages_ == 0 ? 1 : 0) +
+                         (nrec_ ? 1 : 0);
     CK(cudaStreamSynchronize(stream_));
     return true;
 }
@@ -1479,6 +1669,11 @@ bool Batch::launch_batched(int sel) {
         CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], max_along_, store_, sel, d_force_,
                                s == 0 ? nforce_ : 0, s == 0, nodes_ < (1LL << 20), stream_));
     if (nforce_ && max_stages_ == 0) CK(launch::force_reduce(d_force_, nforce_, true, stream_));
+    if (nrec_) {
+        const int psize = store_ == STORE_F64 ? (int)sizeof(StepParams) : (int)sizeof(FastStepParams);
+        CK(launch::record(d_rec_, nrec_, store_, nullptr, (const char *)d_sp_, psize, d_phase_, sel, true,
+                          stream_));
+    }
     return true;
 }
 

@@ -79,7 +79,15 @@ struct Stage {
     double imp_wcos = 1.0, imp_wsin = 0.0;
     int imp_windowed = 0;
     double imp_cos[8] = {1, 1, 1, 1, 1, 1, 1, 1}, imp_sin[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // the wall's per-step trace (mean p', v), when enabled
+    double *d_trace = nullptr;
+    unsigned long long *trace_count = nullptr;
+    int trace_cap = 0;
+    unsigned long long trace_written = 0;
 };
+
+// Most probes a solver records (one block of a record launch walks them).
+constexpr int kMaxProbes = 4096;
 
 // Zero-order-hold update of m v' + R v + K x = p over one lattice step:
 // (x, v) <- A (x, v) + b p. Returns false unless m > 0 and K > 0.
@@ -137,8 +145,9 @@ class Solver {
     // Kernel launches per time step inside the loop (for launch counting).
     int launches_per_step() const {
         const int bulk = 1 + (special_launch() ? 1 : 0);
-        if (groups_.empty()) return bulk + (has_mem_ ? 1 : 0);
-        return bulk + (int)groups_.size();
+        const int rec = rec_host_.empty() ? 0 : 1;
+        if (groups_.empty()) return bulk + (has_mem_ ? 1 : 0) + rec;
+        return bulk + (int)groups_.size() + rec;
     }
     // Shifted storage: the nodes the clean-pair kernels leave to the
     // special-node kernel (row-major; both nodes of a pair with a special
@@ -199,6 +208,16 @@ class Solver {
     // thread while the solver keeps stepping; finished by vtk_wait().
     bool write_vtk(const char *path, double dx, double cu, double crho);
     bool vtk_wait();
+    // Probes: density and velocity (rho, ux, uy) at n nodes after every step,
+    // in a device ring of `capacity` steps (n = 0 removes them).
+    bool set_probes(int n, const int *i, const int *j, int capacity);
+    // Copies up to max_steps records, oldest first: out[(t n + q) 3 + {0,1,2}].
+    int probe_history(double *out, int max_steps);
+    // The impedance wall's per-step trace on Boundary entry `entry`.
+    bool enable_impedance_trace(int entry, int capacity);
+    long long write_impedance_trace(int entry, const char *path, double dt, double cp, double cu, bool append);
+    // The record tasks of this solver (probes, wall traces) for a batch.
+    const std::vector<RecordTask> &record_tasks() const { return rec_host_; }
     bool begin_steps(cudaStream_t s);
     bool end_steps(cudaStream_t s);
     void advance(int nsteps);
@@ -209,6 +228,15 @@ class Solver {
     bool alloc();
     bool launch_step(int src, int dst, bool collide, bool write_macro, int bparity,
                      cudaStream_t s = nullptr);
+    bool launch_step_kernels(int src, int dst, bool collide, bool write_macro, int bparity, cudaStream_t s);
+    bool upload_records();
+    std::vector<RecordTask> rec_host_;
+    RecordTask *d_rec_ = nullptr;
+    int rec_cap_ = 0;
+    long long *d_probe_nodes_ = nullptr;
+    double *d_probe_ring_ = nullptr;
+    unsigned long long *probe_count_ = nullptr;
+    int nprobes_ = 0, probe_cap_ = 0;
     bool launch_collide(int b, cudaStream_t s = nullptr);
     bool capture_pair();
     bool trial_step();
@@ -353,6 +381,8 @@ class Batch {
     // impedance walls advanced in the special-node launch (shifted storage)
     ImpWall *d_walls_ = nullptr;
     int2 *d_imp_ = nullptr;         // (wall, first node) per 128-node block
+    RecordTask *d_rec_ = nullptr;   // every case's probes and wall traces (case index set)
+    int nrec_ = 0;
     int nimp_ = 0;
     std::vector<ImpWall> walls_host_;
     std::vector<int2> wall_at_;     // (level, entry) of each wall's stage

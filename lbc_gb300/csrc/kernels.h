@@ -112,7 +112,35 @@ struct ImpWall {
     double *vn;
 };
 
+// Per-step records, one block per task, launched after a step's last kernel:
+// probes (density and velocity at chosen nodes, from the populations the step
+// left) and impedance-wall traces (the wall's mean p' and v over its active
+// nodes, the per-step record lbc's nit case writes, cases/nit/nit.c:262-273).
+// Each task's ring holds `cap` steps; *count counts the steps recorded.
+enum : int { REC_PROBES = 0, REC_WALL = 1 };
+struct RecordTask {
+    int kind;
+    int n;                       // probes: number of nodes; wall: nodes along the wall
+    int cs;                      // batch case index (its step parameters), -1 alone
+    int cap;
+    const long long *nodes;      // probes: plane offsets
+    long long plane;
+    const double *imp;           // wall: impedance state [fields][n]
+    double *ring;                // probes: [cap][n][3] (rho, ux, uy); wall: [cap][2] (p', v)
+    unsigned long long *count;
+    double w[9];                 // shifted storage: f = g + w
+    double hFx, hFy;             // half the body force: lbc's u = (j + F / 2) / rho
+};
+
 namespace launch {
+// Records of one step: tasks[0 .. n). Alone: the step's populations are at
+// dst. In a batch (spbase set): case cs's are the dst of its step parameters
+// for this direction, spbase + (2 cs + (sel ^ phase[cs])) * spstride bytes.
+// collided: the step ended with a collision (Guo's forcing then added F to the
+// momentum, so u = (j - F / 2) / rho); a run's last step leaves pre-collision
+// populations (u = (j + F / 2) / rho, as lbc's moments).
+cudaError_t record(const RecordTask *tasks, int n, int store, const void *dst, const char *spbase, int spstride,
+                   const int *phase, int sel, bool collided, cudaStream_t s);
 // FP64 (kernels_exact.cu): lbc's rounding sequence, or with fma set the
 // fused multiply-add arithmetic (moments_fma / collide_fma)
 cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block, cudaStream_t s,

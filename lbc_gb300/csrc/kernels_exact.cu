@@ -626,6 +626,73 @@ __global__ void k_mei_iter(AosArgs a, double rho0, unsigned long long *maxbits) 
         atomicMax(maxbits, (unsigned long long)__double_as_longlong(d));
 }
 
+// ---------------------------------------------------------------- records
+
+// One block per task. Every thread reads the step count before the barrier at
+// the end, after which thread 0 advances it, so all of a task's values of a
+// step land in the same ring slot.
+template <typename T>
+__global__ void __launch_bounds__(256) k_record(const RecordTask *__restrict__ tasks, const void *dst,
+                                                const char *spbase, int spstride, const int *phase, int sel,
+                                                int collided) {
+    __shared__ double sp_[256], sv_[256];
+    __shared__ int sn_[256];
+    const RecordTask &r = tasks[blockIdx.x];
+    const unsigned long long k = *r.count;
+    const size_t slot = (size_t)(k % (unsigned long long)r.cap);
+    if (r.kind == REC_PROBES) {
+        const void *buf = dst;
+        if (spbase)
+            buf = ((const StepParams *)(spbase + (size_t)(2 * r.cs + (sel ^ phase[r.cs])) * spstride))->dst;
+        const T *f = (const T *)buf;
+        for (int q = threadIdx.x; q < r.n; q += blockDim.x) {
+            const long long o = r.nodes[q];
+            double rho = 0.0, jx = 0.0, jy = 0.0;
+#pragma unroll
+            for (int kk = 0; kk < 9; kk++) {
+                const double fk = Store<T>::to_f64(f[kk * r.plane + o], r.w[kk]);
+                rho += fk;
+                jx += cxk(kk) * fk;
+                jy += cyk(kk) * fk;
+            }
+            double *out = r.ring + (slot * r.n + q) * 3;
+            out[0] = rho;
+            out[1] = (collided ? jx - r.hFx : jx + r.hFx) / rho;
+            out[2] = (collided ? jy - r.hFy : jy + r.hFy) / rho;
+        }
+    } else {
+        // Mean p' and v over the active nodes, summed in a fixed order (a
+        // strided partial per thread, then a tree over the block).
+        double a = 0.0, b = 0.0;
+        int na = 0;
+        for (int t = threadIdx.x; t < r.n; t += blockDim.x) {
+            if (r.imp[(size_t)IMP_ACTIVE * r.n + t] == 0.0) continue;
+            a += r.imp[(size_t)IMP_P * r.n + t];
+            b += r.imp[(size_t)IMP_V * r.n + t];
+            na++;
+        }
+        sp_[threadIdx.x] = a;
+        sv_[threadIdx.x] = b;
+        sn_[threadIdx.x] = na;
+        __syncthreads();
+        for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+            if ((int)threadIdx.x < h) {
+                sp_[threadIdx.x] += sp_[threadIdx.x + h];
+                sv_[threadIdx.x] += sv_[threadIdx.x + h];
+                sn_[threadIdx.x] += sn_[threadIdx.x + h];
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            const double cnt = sn_[0] > 0 ? (double)sn_[0] : 1.0;
+            r.ring[slot * 2] = sp_[0] / cnt;
+            r.ring[slot * 2 + 1] = sv_[0] / cnt;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *r.count = k + 1ull;
+}
+
 // ---------------------------------------------------------------- FP64 rate
 
 // The device's FP64 FMA issue rate, the ceiling of the FP64 step kernels: each
@@ -649,6 +716,16 @@ __global__ void __launch_bounds__(256) k_fp64_rate(double *sink, int iters, doub
 // ---------------------------------------------------------------- launchers
 
 namespace launch {
+
+cudaError_t record(const RecordTask *tasks, int n, int store, const void *dst, const char *spbase, int spstride,
+                   const int *phase, int sel, bool collided, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int c = collided ? 1 : 0;
+    if (store == STORE_F64) k_record<double><<<n, 256, 0, s>>>(tasks, dst, spbase, spstride, phase, sel, c);
+    else if (store == STORE_F32) k_record<float><<<n, 256, 0, s>>>(tasks, dst, spbase, spstride, phase, sel, c);
+    else k_record<__half><<<n, 256, 0, s>>>(tasks, dst, spbase, spstride, phase, sel, c);
+    return cudaGetLastError();
+}
 
 cudaError_t fp64_rate(int blocks, int iters, double *sink, cudaStream_t s) {
     k_fp64_rate<<<blocks, 256, 0, s>>>(sink, iters, 0.9999999, 1e-9);

@@ -64,6 +64,7 @@ enum BCKind : int {
 enum : int {
     IMP_ACTIVE = 0, IMP_A11, IMP_A12, IMP_A21, IMP_A22, IMP_B1, IMP_B2, IMP_X, IMP_V, IMP_RHOBAR,
     IMP_WC, IMP_WS,  // window phasor (cos, sin of 2 pi n / window length)
+    IMP_P,           // the pressure fluctuation p' of the last update (for the wall's trace)
     IMP_FIELDS
 };
 // per frequency f: phasor (re, im), sum p' e^{-i w n} (re, im), sum v e^{-i w n} (re, im)
@@ -355,6 +356,7 @@ __device__ __forceinline__ double impedance_step(double *imp, int along, int nf,
         IMP(IMP_WS) = ws0 * wcos + wc0 * wsin;
     }
     IMP(IMP_RHOBAR) = rb + alpha * (rho_n - rb);
+    IMP(IMP_P) = p;
     const double xn = a11 * x + a12 * v + b1 * p;
     const double vn = a21 * x + a22 * v + b2 * p;
     IMP(IMP_X) = xn;

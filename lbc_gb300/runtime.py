@@ -82,6 +82,11 @@ def _bind_ext(lib: C.CDLL) -> None:
         "lbm_gpu_enable_force_history": (C.c_int, [vp, C.c_int]),
         "lbm_gpu_force_history": (C.c_int, [vp, dp, C.c_int]),
         "lbm_gpu_write_force_records": (C.c_longlong, [vp, C.c_char_p, C.c_double, C.c_double, C.c_int]),
+        "lbm_gpu_set_probes": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]),
+        "lbm_gpu_probe_history": (C.c_int, [vp, dp, C.c_int]),
+        "lbm_gpu_enable_impedance_trace": (C.c_int, [vp, C.c_int, C.c_int]),
+        "lbm_gpu_write_impedance_trace": (C.c_longlong, [vp, C.c_int, C.c_char_p, C.c_double, C.c_double,
+                                                         C.c_double, C.c_int]),
         "lbm_gpu_get_info": (C.c_int, [vp, C.POINTER(Info)]),
         "lbm_gpu_set_block": (C.c_int, [vp, C.c_int, C.c_int]),
         "lbm_gpu_get_block": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
@@ -286,6 +291,36 @@ class GpuSolver:
         if n < 0:
             raise RuntimeError(last_error())
         return out[:n]
+
+    def set_probes(self, nodes, capacity: int):
+        """Record (rho, ux, uy) at nodes [(i, j), ...] after every step
+        (lbm_gpu_set_probes); an empty list removes the probes."""
+        nodes = list(nodes)
+        ii = np.ascontiguousarray([int(n[0]) for n in nodes], dtype=np.int32)
+        jj = np.ascontiguousarray([int(n[1]) for n in nodes], dtype=np.int32)
+        self._nprobes = len(nodes)
+        _check(self.lib.lbm_gpu_set_probes(self.h, len(nodes), iptr(ii), iptr(jj), capacity), "lbm_gpu_set_probes")
+
+    def probe_history(self, max_steps: int) -> np.ndarray:
+        """[steps, probes, 3] (rho, ux, uy), oldest first (lbm_gpu_probe_history)."""
+        n = getattr(self, "_nprobes", 0)
+        out = np.empty((max_steps, max(n, 1), 3))
+        k = self.lib.lbm_gpu_probe_history(self.h, dptr(out), max_steps)
+        if k < 0:
+            raise RuntimeError(last_error())
+        return out[:k, :n]
+
+    def enable_impedance_trace(self, entry: int, capacity: int):
+        _check(self.lib.lbm_gpu_enable_impedance_trace(self.h, entry, capacity), "lbm_gpu_enable_impedance_trace")
+
+    def write_impedance_trace(self, entry: int, path: str, dt: float = 1.0, cp: float = 1.0, cu: float = 1.0,
+                              append: bool = False) -> int:
+        """lbc's TDIBC text trace for the steps not written yet
+        (lbm_gpu_write_impedance_trace); returns the number of lines."""
+        n = self.lib.lbm_gpu_write_impedance_trace(self.h, entry, path.encode(), dt, cp, cu, 1 if append else 0)
+        if n < 0:
+            raise RuntimeError(f"lbm_gpu_write_impedance_trace failed ({n}): {last_error()}")
+        return n
 
     def write_force_records(self, path: str, dt: float, cf: float = 1.0, append: bool = False) -> int:
         """lbc's {t, L, D} force record file for the steps not written yet

@@ -49,7 +49,7 @@ void mei_initialization(int Nx, int Ny, int Q, LBM_POP(f), LBM_POP(f_new), LBM_F
                         int isperiodic_y, int init_iter_max, double tol_rho,
                         LBM_MASK(solid_mask));
 
-/* lbc include/lbm_core.h:117-128, src/core/sponge_layer.c (host setup) */
+/* lbc include/lbm_core.h:117-128, src/core/sponge_layer.c (filled on the device) */
 void sponge_layer(int Nx, int Ny, double dx, double xc, double yc, double r_inner,
                   double r_outer, double tau_base, double incr_tau, double exp_coeff,
                   LBM_FLD(omega_eff));

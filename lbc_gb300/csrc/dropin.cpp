@@ -609,22 +609,20 @@ void mei_initialization(int Nx, int Ny, int Q, double *f, double *f_new, double 
 // ------------------------------------------------------------------ host utilities
 
 // src/core/sponge_layer.c:3-45: per-node omega = 1/tau with a radial exponential
-// ramp of tau between r_inner and r_outer. One-shot setup, done on the host.
+// ramp of tau between r_inner and r_outer, filled on the device (k_sponge) and
+// written to the caller's array.
 void sponge_layer(int Nx, int Ny, double dx, double xc, double yc, double r_inner, double r_outer,
                   double tau_base, double incr_tau, double exp_coeff, double *omega_eff) {
-    const double span = std::exp(exp_coeff * (r_outer - r_inner)) - 1;
-    for (int j = 0; j < Ny; j++) {
-        const double y = j * dx - yc;
-        for (int i = 0; i < Nx; i++) {
-            const double x = i * dx - xc;
-            const double r = std::sqrt(x * x + y * y);
-            double tau;
-            if (r <= r_inner) tau = tau_base;
-            else if (r <= r_outer) tau = tau_base + (incr_tau - 1) * tau_base * (std::exp(exp_coeff * (r - r_inner)) - 1) / span;
-            else tau = tau_base * incr_tau;
-            omega_eff[(size_t)j * Nx + i] = 1.0 / tau;
-        }
-    }
+    EntryLock lk;
+    AosArgs a;
+    const size_t N = (size_t)Nx * Ny;
+    if (!omega_eff || !aos_begin(a, Nx, Ny, 0, 0)) return report("sponge_layer");
+    double *d = (double *)g_scr.get(SL_OMEGA, N * 8);
+    const bool okk = d &&
+                     check_cuda(launch::sponge(Nx, Ny, dx, xc, yc, r_inner, r_outer, tau_base, incr_tau, exp_coeff,
+                                               d, g_scr.s), "sponge_layer") &&
+                     down(omega_eff, d, N * 8) && check_cuda(cudaStreamSynchronize(g_scr.s), "sponge_layer");
+    if (!okk) report("sponge_layer");
 }
 
 // src/utils/filesystem.c:38-57 (POSIX branch).

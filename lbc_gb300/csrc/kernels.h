@@ -165,6 +165,9 @@ cudaError_t aos_bc(const AosArgs &a, int kind, int index, int along, const doubl
                    const double *val2, cudaStream_t s);
 cudaError_t mei_init(const AosArgs &a, double rho0, cudaStream_t s);
 cudaError_t mei_iter(const AosArgs &a, double rho0, unsigned long long *maxbits, cudaStream_t s);
+// lbc's sponge_layer omega field, [Ny][Nx] into omega (device or device-reachable memory)
+cudaError_t sponge(int Nx, int Ny, double dx, double xc, double yc, double r_inner, double r_outer,
+                   double tau_base, double incr_tau, double exp_coeff, double *omega, cudaStream_t s);
 // blocks x 256 threads, each 8 x iters dependent DFMA (lbm_gpu_fp64_rate)
 cudaError_t fp64_rate(int blocks, int iters, double *sink, cudaStream_t s);
 

@@ -626,6 +626,30 @@ __global__ void k_mei_iter(AosArgs a, double rho0, unsigned long long *maxbits) 
         atomicMax(maxbits, (unsigned long long)__double_as_longlong(d));
 }
 
+// ---------------------------------------------------------------- sponge
+
+// src/core/sponge_layer.c:21-43 on the device, one thread per node: omega =
+// 1 / tau with tau ramped exponentially in the radius between r_inner and
+// r_outer, in lbc's operation order (--fmad=false, correctly rounded sqrt and
+// division). exp is CUDA's (within 1 ulp of the exact value, not libm's bits),
+// so ramp nodes can differ from lbc in the last bits; the rest are identical.
+__global__ void k_sponge(int Nx, int Ny, double dx, double xc, double yc, double r_inner, double r_outer,
+                         double tau_base, double incr_tau, double exp_coeff, double *omega) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= Nx || j >= Ny) return;
+    const double y = j * dx - yc;
+    const double x = i * dx - xc;
+    const double r = sqrt(x * x + y * y);
+    double tau;
+    if (r <= r_inner) tau = tau_base;
+    else if (r <= r_outer)
+        tau = tau_base + (incr_tau - 1) * tau_base * (exp(exp_coeff * (r - r_inner)) - 1) /
+                             (exp(exp_coeff * (r_outer - r_inner)) - 1);
+    else tau = tau_base * incr_tau;
+    omega[(size_t)j * Nx + i] = 1.0 / tau;
+}
+
 // ---------------------------------------------------------------- records
 
 // One block per task. Every thread reads the step count before the barrier at
@@ -724,6 +748,14 @@ cudaError_t record(const RecordTask *tasks, int n, int store, const void *dst, c
     if (store == STORE_F64) k_record<double><<<n, 256, 0, s>>>(tasks, dst, spbase, spstride, phase, sel, c);
     else if (store == STORE_F32) k_record<float><<<n, 256, 0, s>>>(tasks, dst, spbase, spstride, phase, sel, c);
     else k_record<__half><<<n, 256, 0, s>>>(tasks, dst, spbase, spstride, phase, sel, c);
+    return cudaGetLastError();
+}
+
+cudaError_t sponge(int Nx, int Ny, double dx, double xc, double yc, double r_inner, double r_outer,
+                   double tau_base, double incr_tau, double exp_coeff, double *omega, cudaStream_t s) {
+    const dim3 b(64, 4);
+    const dim3 g((Nx + b.x - 1) / b.x, (Ny + b.y - 1) / b.y);
+    k_sponge<<<g, b, 0, s>>>(Nx, Ny, dx, xc, yc, r_inner, r_outer, tau_base, incr_tau, exp_coeff, omega);
     return cudaGetLastError();
 }
 

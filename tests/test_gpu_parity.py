@@ -374,3 +374,24 @@ def test_lazy_dropin_matches_lbc(gpu, oracle, name):
         assert same(getattr(st, fld), getattr(st_o, fld)), (name, fld)
     mag = gross_force(case)
     assert force_close(np.concatenate([fg1, fg2]), np.concatenate([fo1, fo2]), scale=mag)
+
+
+@pytest.mark.parametrize("args", [(60, 40, 0.5, 15.0, 10.0, 5.0, 12.0, 0.6, 3.0, 0.4),
+                                  (2048, 512, 1.0, 512.0, 256.0, 300.0, 700.0, 0.55, 5.0, 0.01)])
+def test_sponge_layer_on_the_device(gpu, oracle, args):
+    """lbc's sponge_layer (src/core/sponge_layer.c:3-45) filled by a device
+    kernel: nodes inside r_inner and outside r_outer are lbc's bits; the ramp
+    between uses CUDA's exp, so it agrees to 1e-14 relative, well inside the
+    1e-12 the FP64 path is held to."""
+    Nx, Ny = args[0], args[1]
+    dx, xc, yc, ri, ro = args[2:7]
+    got = np.full((Ny, Nx), np.nan)
+    want = np.zeros((Ny, Nx))
+    gpu.sponge_layer(*args, dptr(got))
+    oracle.sponge_layer(*args, dptr(want))
+    j, i = np.mgrid[0:Ny, 0:Nx]
+    r = np.sqrt((i * dx - xc) ** 2 + (j * dx - yc) ** 2)
+    flat = (r <= ri) | (r > ro)
+    assert same(got[flat], want[flat])
+    assert np.max(np.abs(got - want) / np.abs(want)) <= 1e-14
+    assert (~flat).sum() > 100

@@ -156,3 +156,83 @@ def test_liner_batch_eduction():
     print(r)
     assert r["finite"]
     assert max(r["eduction_err_median"]) < 5e-2
+
+
+# ---------------------------------------------------------------------------
+# Eduction from the lattice's acoustic field (probes), which tests the wall's
+# coupling to the lattice rather than the wall's own ODE.
+
+def test_two_microphone_recovers_a_known_reflection():
+    """Synthetic plane-wave spectra p(y) = A (e^{iky} + G e^{-iky}) with
+    attenuation: the transfer-function method returns G and Z to round-off."""
+    om = np.array([0.03, 0.07, 0.11, 0.2])
+    nu = 0.04
+    k = imp.wavenumber(om, imp.CS, nu)
+    G = np.array([0.3 - 0.2j, -0.5 + 0.1j, 0.0 + 0.6j, 0.9 + 0.0j])
+    A = np.array([1.0, 0.3 + 0.2j, 2.0j, 0.1])
+    y1, y2 = 3.0, 7.0
+    P = lambda y: A * (np.exp(1j * k * y) + G * np.exp(-1j * k * y))  # noqa: E731
+    G2, Z = imp.two_microphone(P(y1), P(y2), y1, y2, om, imp.CS, nu)
+    assert np.allclose(G2, G, rtol=0, atol=1e-12)
+    assert np.allclose(Z, imp.CS * (1 + G) / (1 - G), rtol=1e-12)
+
+
+def test_insitu_extrapolates_quadratic_fields_exactly():
+    y = np.array([1.0, 2.0, 3.0])
+    p = 0.3 - 0.2 * y + 0.05 * y ** 2
+    u = -0.1 + 0.04 * y - 0.01 * y ** 2
+    assert abs(imp.insitu(p, u) - 0.3 / 0.1) < 1e-12
+
+
+def test_two_microphone_sees_a_rigid_wall_in_the_oracle(oracle):
+    """The method itself on lbc's step: a tube closed by a solid row (halfway
+    bounce-back, wall at y = 1/2) reflects everything, G = 1 at the wall
+    plane, to 1 % (the window holds the incident pulse and its reflection
+    only)."""
+    from lbc_gb300.cases import BC, Case, equilibrium_state
+    Nx, Ny, tau = 4, 512, 0.6
+    mask = np.zeros((Ny, Nx), np.int32)
+    mask[0, :] = 1
+    mask[Ny - 1, :] = 1
+    case = Case("rigid_tube", Nx, Ny, mask, np.full((Ny, Nx), 1 / tau), np.zeros((Ny, Nx)), [BC("periodic_x")])
+    tp = imp.TubeParams(1.0, 1e-3, 0.05, ny=Ny, tau=tau)
+    y = np.arange(Ny, dtype=float)[:, None] * np.ones((1, Nx))
+    drho = 1e-3 * np.exp(-(y - tp.y0) ** 2 / (2 * tp.width ** 2))
+    st = equilibrium_state(1 + drho, np.zeros((Ny, Nx)), -imp.CS * drho)
+    y1, y2 = tp.mics
+    steps = tp.gate()
+    bnd = oracle.boundaries(case.bcs)
+    rec = np.zeros((steps, 2))
+    for n in range(steps):
+        oracle.step(case, st, bnd)
+        rec[n] = (st.rho[y1, 0] - 1) / 3, (st.rho[y2, 0] - 1) / 3
+    P = imp.spectra(rec, imp.EDUCTION_OMEGAS)
+    G, _ = imp.two_microphone(P[:, 0], P[:, 1], y1 - 0.5, y2 - 0.5, imp.EDUCTION_OMEGAS, imp.CS, tp.nu)
+    assert np.all(np.abs(G - 1.0) < 1e-2), G
+
+
+TUBES = [(2.0, 4e-3, 0.03), (0.5, 4e-3, 0.03), (1.0, 1e-2, 0.016), (3.0, 1e-3, 0.1), (1.0, 2e-1, 0.02)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("R,m,f_res", TUBES)
+@pytest.mark.parametrize("storage", [0, 1])
+def test_impedance_tube_field_eduction(R, m, f_res, storage):
+    """A normal-incidence impedance tube on the device: the impedance educed
+    from the lattice's field by the two-microphone method and in situ (probes
+    at rows 1..3) matches the imposed R + i (w m - K / w). The resistance to 3 %
+    up to w = 0.1; the whole Z to 1.5 w rho c + 0.01 rho c (two-microphone) and
+    2.5 w rho c + 0.01 rho c (in situ), the first-order error of the coupling
+    (the wall is driven by the pressure one cell into the fluid, one step
+    before the velocity it imposes). A coupling with the wrong sign, a wrong
+    population or no velocity at all gives a resistance off by far more
+    (|G| > 1, or G = 1)."""
+    tp = imp.TubeParams(R * imp.CS, m, f_res)
+    r = imp.run_impedance_tube(tp, storage)
+    w = r["omegas"]
+    Zm, Z2, Zi = r["model"], r["two_mic"], r["insitu"]
+    print("model", Zm, "two-mic", Z2, "in situ", Zi)
+    low = w <= 0.1
+    assert np.all(np.abs(Z2.real[low] - Zm.real[low]) <= 0.03 * Zm.real[low])
+    assert np.all(np.abs(Z2 - Zm) <= (1.5 * w + 0.01) * imp.CS)
+    assert np.all(np.abs(Zi - Zm) <= (2.5 * w + 0.01) * imp.CS)

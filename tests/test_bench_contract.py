@@ -18,6 +18,9 @@ def test_reference_arm_prints_the_contract_line():
     assert line["impl"] == "reference" and line["unit"] == "MLUPS" and line["value"] > 0
     assert line["higher_is_better"] is True and line["n_gpus"] == 1 and line["steps"] == 1
     assert line["config"]["workload"] == "taylor_green_4096x4096"
+    # the same config dict as the GPU arm's line (bench.workload_config)
+    import bench
+    assert line["config"] == bench.workload_config(4096)
     cpu = line["cpu_baseline"]
     assert cpu["kind"] in ("reference", "port") and cpu["cores"] >= 1 and cpu["value"] == line["value"]
     e2e = line["e2e"]

@@ -841,6 +841,7 @@ StageParams Solver::stage_params(const Stage &st, int src, int bparity) const {
     s.imp_wcos = st.imp_wcos;
     s.imp_wsin = st.imp_wsin;
     s.imp_windowed = st.imp_windowed;
+    s.imp_slot = bparity;
     for (int f = 0; f < 8; f++) {
         s.imp_cos[f] = st.imp_cos[f];
         s.imp_sin[f] = st.imp_sin[f];
@@ -900,8 +901,14 @@ bool Solver::set_impedance(int entry, const double *R, const double *m, const do
         return false;
     }
     const int n = st->along;
-    const int nfield = IMP_FIELDS + 6 * nf;
-    std::vector<double> h((size_t)nfield * n, 0.0);
+    std::vector<double> h(imp_doubles(nf, n), 0.0);
+    // Both slots of the phasor table start at n = 0: window phasor (1, 0),
+    // e^{-i w 0} = (1, 0) per frequency.
+    for (int slot = 0; slot < 2; slot++) {
+        double *tab = h.data() + imp_tab_offset(nf, n, slot);
+        tab[0] = 1.0;
+        for (int f = 0; f < nf; f++) tab[2 + 2 * f] = 1.0;
+    }
     for (int t = 0; t < n; t++) {
         if (!(m[t] > 0.0)) continue;
         double A[4], b[2];
@@ -917,8 +924,6 @@ bool Solver::set_impedance(int entry, const double *R, const double *m, const do
         h[(size_t)IMP_B1 * n + t] = b[0];
         h[(size_t)IMP_B2 * n + t] = b[1];
         h[(size_t)IMP_RHOBAR * n + t] = rho_ref;
-        h[(size_t)IMP_WC * n + t] = 1.0;
-        for (int f = 0; f < nf; f++) h[(size_t)imp_field(f, 0) * n + t] = 1.0;
     }
     if (!st->d_vn && !dalloc(&st->d_vn, (size_t)n)) return false;
     if (!st->d_imp || st->imp_nf != nf) {
@@ -949,7 +954,7 @@ bool Solver::impedance_readback(int entry, double *out, double *state) {
         return false;
     }
     const int n = st->along, nf = st->imp_nf;
-    std::vector<double> h((size_t)(IMP_FIELDS + 6 * nf) * n);
+    std::vector<double> h((size_t)(IMP_FIELDS + 4 * nf) * n);
     CK(cudaStreamSynchronize(stream_));
     CK(cudaMemcpy(h.data(), st->d_imp, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
     for (int t = 0; t < n; t++) {
@@ -959,7 +964,7 @@ bool Solver::impedance_readback(int entry, double *out, double *state) {
         }
         if (out)
             for (int f = 0; f < nf; f++)
-                for (int q = 0; q < 4; q++) out[((size_t)t * nf + f) * 4 + q] = h[(size_t)imp_field(f, 2 + q) * n + t];
+                for (int q = 0; q < 4; q++) out[((size_t)t * nf + f) * 4 + q] = h[(size_t)imp_field(f, q) * n + t];
     }
     return true;
 }
@@ -1634,6 +1639,15 @@ bool Batch::build() {
             walls_host_ = walls;
         }
     }
+    // Shifted storage with special nodes or walls: the persistent clean-pair
+    // grid may leave block slots free on every SM, so that the special-node
+    // launch (programmatic, right behind it) runs beside it instead of after
+    // its last wave (LBM_GPU_BULK_RESERVE: slots per SM left free).
+    bulk_reserve_ = 0;
+    if (store_ != STORE_F64 && (nspecial_ || nimp_)) {
+        const char *e = std::getenv("LBM_GPU_BULK_RESERVE");
+        bulk_reserve_ = e ? std::max(0, std::atoi(e)) : kBulkReserve;
+    }
     // Every case's probes and wall traces: one record launch per step.
     std::vector<RecordTask> rec;
     for (int c = 0; c < nc; c++)
@@ -1660,7 +1674,7 @@ bool Batch::launch_batched(int sel) {
     } else {
         // the clean pairs, then the special nodes overlapping their tail
         CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
-                                      store_, wide_, any_force_, all_flags_, grid_, stream_));
+                                      store_, wide_, any_force_, all_flags_, bulk_grid(), stream_));
         if (nspecial_ || nimp_)
             CK(launch::special_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_special_, nspecial_, sel,
                                              d_walls_, d_imp_, nimp_, store_, wide_, any_force_, true, stream_));

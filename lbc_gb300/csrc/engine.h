@@ -383,6 +383,14 @@ class Batch {
     int2 *d_imp_ = nullptr;         // (wall, first node) per 128-node block
     RecordTask *d_rec_ = nullptr;   // every case's probes and wall traces (case index set)
     int nrec_ = 0;
+    int bulk_reserve_ = 0;          // block slots per SM the clean-pair grid leaves to the special launch
+    static constexpr int kBulkReserve = 0;
+    int bulk_grid() const {
+        if (!bulk_reserve_) return grid_;
+        const int per_sm = launch::step_batch_shifted_grid(store_) / launch::sm_count();
+        const int keep = std::max(1, per_sm - bulk_reserve_);
+        return std::min(grid_, keep * launch::sm_count());
+    }
     int nimp_ = 0;
     std::vector<ImpWall> walls_host_;
     std::vector<int2> wall_at_;     // (level, entry) of each wall's stage

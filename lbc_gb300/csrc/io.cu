@@ -115,7 +115,7 @@ bool Solver::checkpoint_save(const char *path) {
     for (const Stage &st : stages_) {
         if (!okk) break;
         const size_t vb = st.d_val1 ? (size_t)st.along * 8 : 0;
-        const size_t ib = st.d_imp ? (size_t)(IMP_FIELDS + 6 * st.imp_nf) * st.along * 8 : 0;
+        const size_t ib = st.d_imp ? imp_doubles(st.imp_nf, st.along) * 8 : 0;
         okk = put_blob(f, st.d_val1, vb, tmp) && put_blob(f, st.d_val2, vb, tmp) && put_blob(f, st.d_imp, ib, tmp);
     }
     okk = okk && put_blob(f, d_mem_out_, d_mem_out_ ? 16 : 0, tmp) &&
@@ -160,7 +160,7 @@ bool Solver::checkpoint_load(const char *path) {
     for (Stage &st : stages_) {
         if (!okk) break;
         const size_t vb = st.d_val1 ? (size_t)st.along * 8 : 0;
-        const size_t ib = st.d_imp ? (size_t)(IMP_FIELDS + 6 * st.imp_nf) * st.along * 8 : 0;
+        const size_t ib = st.d_imp ? imp_doubles(st.imp_nf, st.along) * 8 : 0;
         okk = get_blob(f, st.d_val1, vb, tmp, "BC values") && get_blob(f, st.d_val2, vb, tmp, "BC values") &&
               get_blob(f, st.d_imp, ib, tmp, "impedance wall (set the same wall up before loading)");
     }

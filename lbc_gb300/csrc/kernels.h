@@ -209,6 +209,7 @@ cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const
                                int ntiles, int sel, int tws, int store, bool wide, bool force, bool all_flags,
                                int grid, cudaStream_t s);
 int step_batch_shifted_grid(int store);
+int sm_count();
 }  // namespace launch
 
 }  // namespace lbm

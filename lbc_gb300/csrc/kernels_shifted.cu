@@ -879,6 +879,13 @@ cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const
                                                 after_special, s);
 }
 
+int sm_count() {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    return nsm > 0 ? nsm : 1;
+}
+
 int step_batch_shifted_grid(int store) {
     int nb = 0, dev = 0, nsm = 0;
     cudaGetDevice(&dev);

@@ -60,15 +60,26 @@ enum BCKind : int {
 // regularized entry, a mass-spring-damper m v' + R v + K x = p' advanced once
 // per step with the exact zero-order-hold update of the 2x2 system, plus
 // running DFTs of p' and v at nf frequencies for eduction. Layout: field-major
-// [IMP_FIELDS + 6 nf][along] doubles.
+// [IMP_FIELDS + 4 nf][along] doubles, then the wall's phasor table: two slots
+// (the step's band parity selects the one read; the other is written for the
+// next step) of imp_tab_stride(nf) doubles: the window phasor (cos, sin of
+// 2 pi n / window length), then e^{-i w_f n} (re, im) per frequency. Every
+// node of a wall rotates the same phasors from the same start, so one copy
+// per wall serves them all (and spares each node the rotations' FP64 work).
 enum : int {
     IMP_ACTIVE = 0, IMP_A11, IMP_A12, IMP_A21, IMP_A22, IMP_B1, IMP_B2, IMP_X, IMP_V, IMP_RHOBAR,
-    IMP_WC, IMP_WS,  // window phasor (cos, sin of 2 pi n / window length)
     IMP_P,           // the pressure fluctuation p' of the last update (for the wall's trace)
     IMP_FIELDS
 };
-// per frequency f: phasor (re, im), sum p' e^{-i w n} (re, im), sum v e^{-i w n} (re, im)
-__host__ __device__ inline int imp_field(int f, int q) { return IMP_FIELDS + 6 * f + q; }
+// per frequency f: sum p' e^{-i w n} (re, im), sum v e^{-i w n} (re, im)
+__host__ __device__ inline int imp_field(int f, int q) { return IMP_FIELDS + 4 * f + q; }
+__host__ __device__ inline int imp_tab_stride(int nf) { return 2 + 2 * nf; }
+// Offset of the phasor table's slot `slot` in a wall's array; imp_doubles is
+// the array's size.
+__host__ __device__ inline size_t imp_tab_offset(int nf, int along, int slot) {
+    return (size_t)(IMP_FIELDS + 4 * nf) * (size_t)along + (size_t)slot * imp_tab_stride(nf);
+}
+__host__ __device__ inline size_t imp_doubles(int nf, int along) { return imp_tab_offset(nf, along, 2); }
 
 __host__ __device__ inline bool bc_is_column(int kind) {
     return kind == BC_VEL_IN_ZH || kind == BC_VEL_OUT_ZH || kind == BC_PRES_IN_ZH ||
@@ -320,41 +331,36 @@ __device__ __forceinline__ void bc_regularized(A &a, const double w[9], int ib, 
 // and the wall-normal velocity into the liner returned (the BC imposes
 // u_y = -v).
 // The DFT sums are weighted by a Hann window over the eduction length
-// (weight 0.5 (1 - cos(2 pi n / L)), from a rotating phasor; no window when
-// the wall was set up without a length: wcos = 1, wsin = 0 keeps weight 1).
-__device__ __forceinline__ double impedance_step(double *imp, int along, int nf, int t,
-                                                 double rho_n, double alpha,
-                                                 const double *cw, const double *sw,
-                                                 double wcos, double wsin, int windowed) {
+// (weight 0.5 (1 - cos(2 pi n / L)) from the window phasor; no window when
+// the wall was set up without a length). tab: this step's slot of the wall's
+// phasor table.
+__device__ __forceinline__ double impedance_step(double *imp, int along, int nf, int t, double rho_n,
+                                                 double alpha, const double *tab, int windowed) {
 #define IMP(f) imp[(size_t)(f) * along + t]
     // The fields share one array, so the compiler cannot move a load above an
     // earlier store to it: all loads of a group are issued before its stores
     // (the node's state, then the DFT in groups of four frequencies), which
     // keeps the chain to a few memory latencies. The arithmetic is the same
     // sequence as a field-by-field update.
-    const double rb = IMP(IMP_RHOBAR), wc0 = IMP(IMP_WC), ws0 = IMP(IMP_WS);
+    const double rb = IMP(IMP_RHOBAR);
     const double x = IMP(IMP_X), v = IMP(IMP_V);
     const double a11 = IMP(IMP_A11), a12 = IMP(IMP_A12), b1 = IMP(IMP_B1);
     const double a21 = IMP(IMP_A21), a22 = IMP(IMP_A22), b2 = IMP(IMP_B2);
+    const double wc0 = tab[0];
     double cr[4], ci[4], ac[4][4];
     auto load_group = [&](int f0) {
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             if (f0 + q >= nf) break;
-            cr[q] = IMP(imp_field(f0 + q, 0));
-            ci[q] = IMP(imp_field(f0 + q, 1));
+            cr[q] = tab[2 + 2 * (f0 + q)];
+            ci[q] = tab[3 + 2 * (f0 + q)];
 #pragma unroll
-            for (int m = 0; m < 4; m++) ac[q][m] = IMP(imp_field(f0 + q, 2 + m));
+            for (int m = 0; m < 4; m++) ac[q][m] = IMP(imp_field(f0 + q, m));
         }
     };
     load_group(0);
     const double p = (rho_n - rb) / 3.0;
-    double win = 1.0;
-    if (windowed) {
-        win = 0.5 * (1.0 - wc0);
-        IMP(IMP_WC) = wc0 * wcos - ws0 * wsin;
-        IMP(IMP_WS) = ws0 * wcos + wc0 * wsin;
-    }
+    const double win = windowed ? 0.5 * (1.0 - wc0) : 1.0;
     IMP(IMP_RHOBAR) = rb + alpha * (rho_n - rb);
     IMP(IMP_P) = p;
     const double xn = a11 * x + a12 * v + b1 * p;
@@ -368,17 +374,34 @@ __device__ __forceinline__ double impedance_step(double *imp, int along, int nf,
         for (int q = 0; q < 4; q++) {
             const int f = f0 + q;
             if (f >= nf) break;
-            IMP(imp_field(f, 2)) = ac[q][0] + wp * cr[q];
-            IMP(imp_field(f, 3)) = ac[q][1] + wp * ci[q];
-            IMP(imp_field(f, 4)) = ac[q][2] + wv * cr[q];
-            IMP(imp_field(f, 5)) = ac[q][3] + wv * ci[q];
-            // advance the phasor e^{-i w n} by one step
-            IMP(imp_field(f, 0)) = cr[q] * cw[f] + ci[q] * sw[f];
-            IMP(imp_field(f, 1)) = ci[q] * cw[f] - cr[q] * sw[f];
+            IMP(imp_field(f, 0)) = ac[q][0] + wp * cr[q];
+            IMP(imp_field(f, 1)) = ac[q][1] + wp * ci[q];
+            IMP(imp_field(f, 2)) = ac[q][2] + wv * cr[q];
+            IMP(imp_field(f, 3)) = ac[q][3] + wv * ci[q];
         }
     }
     return vn;
 #undef IMP
+}
+
+// The wall's phasors one step on: from this step's slot `cur` into the other
+// slot `next` (window phasor rotated by 2 pi / length, e^{-i w_f n} by
+// e^{-i w_f}). One thread per wall per step.
+__device__ __forceinline__ void impedance_advance(const double *cur, double *next, int nf, const double *cw,
+                                                  const double *sw, double wcos, double wsin, int windowed) {
+    const double wc0 = cur[0], ws0 = cur[1];
+    if (windowed) {
+        next[0] = wc0 * wcos - ws0 * wsin;
+        next[1] = ws0 * wcos + wc0 * wsin;
+    } else {
+        next[0] = wc0;
+        next[1] = ws0;
+    }
+    for (int f = 0; f < nf; f++) {
+        const double cr = cur[2 + 2 * f], ci = cur[3 + 2 * f];
+        next[2 + 2 * f] = cr * cw[f] + ci * sw[f];
+        next[3 + 2 * f] = ci * cw[f] - cr * sw[f];
+    }
 }
 
 template <class A>
@@ -555,6 +578,7 @@ struct StageParams {
     double imp_alpha;
     double imp_wcos, imp_wsin;     // window phasor rotation (2 pi / length)
     int imp_windowed;
+    int imp_slot;                  // the phasor table slot this step reads (the step's band parity)
     double imp_cos[8], imp_sin[8];  // e^{-i w_f} per frequency
     const uint16_t *flags;
     const int *colbase, *rowbase;
@@ -656,13 +680,17 @@ __device__ __forceinline__ StagePre stage_preload(const StageParams &p, int t, i
     c.v2 = p.val2 ? p.val2[t] : 0.0;
     c.fin = !c.solid && p.last[c.slot] == p.entry;
     c.imp = false;
+    if (kind == BC_VEL_BOT_REG && p.imp && !p.vn && t == 0)
+        impedance_advance(p.imp + imp_tab_offset(p.imp_nf, p.along, p.imp_slot),
+                          p.imp + imp_tab_offset(p.imp_nf, p.along, p.imp_slot ^ 1), p.imp_nf, p.imp_cos, p.imp_sin,
+                          p.imp_wcos, p.imp_wsin, p.imp_windowed);
     if (kind == BC_VEL_BOT_REG && p.imp && p.imp[(size_t)IMP_ACTIVE * p.along + t] != 0.0 && !c.solid) {
         // Impedance wall on this node: the regularized bottom BC with the
         // normal velocity from the node's mass-spring-damper (computed ahead
         // when p.vn is set: the caller reads it after its wait).
         if (!p.vn)
-            c.v2 = -impedance_step(p.imp, p.along, p.imp_nf, t, c.nrho, p.imp_alpha, p.imp_cos, p.imp_sin,
-                                   p.imp_wcos, p.imp_wsin, p.imp_windowed);
+            c.v2 = -impedance_step(p.imp, p.along, p.imp_nf, t, c.nrho, p.imp_alpha,
+                                   p.imp + imp_tab_offset(p.imp_nf, p.along, p.imp_slot), p.imp_windowed);
         c.imp = true;
     }
     return c;
@@ -671,11 +699,15 @@ __device__ __forceinline__ StagePre stage_preload(const StageParams &p, int t, i
 // The impedance wall's update of node t ahead of its stage (what
 // stage_preload does when p.vn is null), storing the wall velocity in vn[t].
 __device__ __forceinline__ void impedance_ahead(const StageParams &p, double *vn, int t) {
+    if (t == 0)
+        impedance_advance(p.imp + imp_tab_offset(p.imp_nf, p.along, p.imp_slot),
+                          p.imp + imp_tab_offset(p.imp_nf, p.along, p.imp_slot ^ 1), p.imp_nf, p.imp_cos, p.imp_sin,
+                          p.imp_wcos, p.imp_wsin, p.imp_windowed);
     if (p.imp[(size_t)IMP_ACTIVE * p.along + t] == 0.0) return;
     if (p.flags[(long long)p.index * p.pitch + t] & NF_SOLID) return;
     const int nslot = band_slot(p.colbase, p.rowbase, t, p.index + 1);
-    vn[t] = impedance_step(p.imp, p.along, p.imp_nf, t, p.bandm_prev[nslot], p.imp_alpha, p.imp_cos, p.imp_sin,
-                           p.imp_wcos, p.imp_wsin, p.imp_windowed);
+    vn[t] = impedance_step(p.imp, p.along, p.imp_nf, t, p.bandm_prev[nslot], p.imp_alpha,
+                           p.imp + imp_tab_offset(p.imp_nf, p.along, p.imp_slot), p.imp_windowed);
 }
 
 }  // namespace lbm

@@ -155,6 +155,7 @@ bool Solver::build_geometry() {
             const int flag = b.kind == BC_PERIODIC_X ? d_.px : d_.py;
             if (flag && !nonperiodic_seen) continue;
             Stage st{b.kind, 0, b.kind == BC_PERIODIC_X ? 2 * Ny : 2 * Nx, (int)e};
+            st.open.assign(st.along, 1);
             stages_.push_back(st);
             continue;
         }
@@ -166,6 +167,8 @@ bool Solver::build_geometry() {
             return false;
         }
         Stage st{b.kind, b.index, col ? Ny : Nx, (int)e};
+        st.open.resize(st.along);
+        for (int t = 0; t < st.along; t++) st.open[t] = col ? !solid(b.index, t) : !solid(t, b.index);
         stages_.push_back(st);
     }
 
@@ -1563,11 +1566,10 @@ bool Batch::build() {
         if (9LL * s->plane() >= (1LL << 31)) wide_ = true;
         if (s->has_force()) any_force_ = true;
         if (!s->has_flags()) all_flags_ = false;
+        if (s->has_links()) any_links_ = true;
         if (s->has_mem()) force.push_back(s->force_slot());
         max_stages_ = std::max(max_stages_, (int)s->stage_groups().size());
-        for (const Stage &st : s->stages()) max_along_ = std::max(max_along_, st.along);
     }
-    if (!build_tiles(tws_)) return false;
     // Shifted storage: every case's special nodes, each case's list padded to
     // a multiple of 32 so that a warp steps one force chunk of one case.
     std::vector<int4> special;
@@ -1579,6 +1581,7 @@ bool Batch::build() {
                 special.push_back(q < n ? make_int4(c, sl[q].x, sl[q].y, q >> 5) : make_int4(c, -1, -1, q >> 5));
         }
     nspecial_ = (int)special.size();
+    if (!build_tiles(tws_)) return false;
     nforce_ = (int)force.size();
     const size_t psize = store_ == STORE_F64 ? sizeof(StepParams) : sizeof(FastStepParams);
     void *sp = nullptr;
@@ -1609,8 +1612,43 @@ bool Batch::build() {
         d_stage_lists_.push_back(d);
         stage_counts_.push_back(cnt);
     }
+    // The blocks of each level's launch: every run of kStageBatchPoints points
+    // of an entry with a fluid node, and every entry's first run, whose point
+    // 0 advances an impedance wall's window phasor (entries numbered as run()
+    // fills the lists); then, on the first level, one block per force slot.
+    // (A grid of entries x the longest entry launched 4 to 6 times as many
+    // blocks on seeded liner ducts, most of them empty or on the solid wall.)
+    {
+        const int bs = store_ == STORE_F64 ? launch::kStageBatchPointsF64 : launch::kStageBatchPoints;
+        std::vector<int> next(max_stages_, 0);
+        std::vector<std::vector<int2>> blocks(max_stages_);
+        for (Solver *c : cases_)
+            for (size_t l = 0; l < c->stage_groups().size(); l++)
+                for (int k : c->stage_groups()[l]) {
+                    const Stage &st = c->stages()[k];
+                    const int e = next[l]++;
+                    for (int t0 = 0; t0 < st.along; t0 += bs) {
+                        bool any = t0 == 0;
+                        for (int t = t0; t < std::min(st.along, t0 + bs) && !any; t++) any = st.open[t] != 0;
+                        if (any) blocks[l].push_back(make_int2(e, t0));
+                    }
+                }
+        if (max_stages_ > 0)
+            for (int f = 0; f < nforce_; f++) blocks[0].push_back(make_int2(level_cnt[0] + f, 0));
+        for (int l = 0; l < max_stages_; l++) {
+            int2 *d = nullptr;
+            if (!blocks[l].empty()) {
+                if (!balloc(allocs_, &d, blocks[l].size(), stream_)) return false;
+                CK(cudaMemcpyAsync(d, blocks[l].data(), blocks[l].size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                   stream_));
+            }
+            d_stage_blocks_.push_back(d);
+            stage_nblocks_.push_back((int)blocks[l].size());
+        }
+    }
     // Shifted storage: impedance walls are advanced ahead of their stage, in
-    // the special-node launch (entries numbered as run() fills the lists).
+    // a launch beside the special nodes (entries numbered as run() fills the
+    // lists).
     if (store_ != STORE_F64) {
         std::vector<ImpWall> walls;
         std::vector<int2> imp;
@@ -1626,7 +1664,13 @@ bool Batch::build() {
                     w.pair = d_stage_lists_[l] + 2 * e;
                     w.entry = e;
                     w.vn = st.d_vn;
-                    for (int t0 = 0; t0 < st.along; t0 += 128) imp.push_back(make_int2((int)walls.size(), t0));
+                    // blocks of 128 nodes with a fluid node, and the first
+                    // (its node 0 advances the wall's phasors)
+                    for (int t0 = 0; t0 < st.along; t0 += 128) {
+                        bool any = t0 == 0;
+                        for (int t = t0; t < std::min(st.along, t0 + 128) && !any; t++) any = st.open[t] != 0;
+                        if (any) imp.push_back(make_int2((int)walls.size(), t0));
+                    }
                     walls.push_back(w);
                     wall_at_.push_back(make_int2((int)l, e));
                 }
@@ -1638,15 +1682,6 @@ bool Batch::build() {
             CK(cudaMemcpyAsync(d_imp_, imp.data(), imp.size() * sizeof(int2), cudaMemcpyHostToDevice, stream_));
             walls_host_ = walls;
         }
-    }
-    // Shifted storage with special nodes or walls: the persistent clean-pair
-    // grid may leave block slots free on every SM, so that the special-node
-    // launch (programmatic, right behind it) runs beside it instead of after
-    // its last wave (LBM_GPU_BULK_RESERVE: slots per SM left free).
-    bulk_reserve_ = 0;
-    if (store_ != STORE_F64 && (nspecial_ || nimp_)) {
-        const char *e = std::getenv("LBM_GPU_BULK_RESERVE");
-        bulk_reserve_ = e ? std::max(0, std::atoi(e)) : kBulkReserve;
     }
     // Every case's probes and wall traces: one record launch per step.
     std::vector<RecordTask> rec;
@@ -1661,8 +1696,10 @@ bool Batch::build() {
         CK(cudaMemcpyAsync(d_rec_, rec.data(), rec.size() * sizeof(RecordTask), cudaMemcpyHostToDevice, stream_));
     }
     // The force reductions ride in the first stage level's launch.
-    launches_per_step_ = 1 + (nspecial_ || nimp_ ? 1 : 0) + max_stages_ + (nforce_ && max_stages_ == 0 ? 1 : 0) +
-                         (nrec_ ? 1 : 0);
+    int stage_launches = 0;
+    for (int nb : stage_nblocks_) stage_launches += nb > 0 ? 1 : 0;
+    launches_per_step_ = 1 + (nspecial_ ? 1 : 0) + (nimp_ ? 1 : 0) + stage_launches +
+                         (nforce_ && max_stages_ == 0 ? 1 : 0) + (nrec_ ? 1 : 0);
     CK(cudaStreamSynchronize(stream_));
     return true;
 }
@@ -1672,16 +1709,21 @@ bool Batch::launch_batched(int sel) {
         CK(launch::step_batch_exact((const StepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
                                     grid_, stream_, cases_[0]->fma64()));
     } else {
-        // the clean pairs, then the special nodes overlapping their tail
+        // the clean pairs, then the impedance walls and the special nodes
+        // overlapping their tail
         CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
-                                      store_, wide_, any_force_, all_flags_, bulk_grid(), stream_));
-        if (nspecial_ || nimp_)
-            CK(launch::special_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_special_, nspecial_, sel,
-                                             d_walls_, d_imp_, nimp_, store_, wide_, any_force_, true, stream_));
+                                      store_, wide_, any_force_, all_flags_, grid_, stream_));
+        CK(launch::impedance_batch(d_phase_, sel, d_walls_, d_imp_, nimp_, true, stream_));
+        CK(launch::special_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_special_, nspecial_, sel, store_,
+                                         wide_, any_force_, any_links_, true, stream_));
     }
-    for (int s = 0; s < max_stages_; s++)
-        CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], max_along_, store_, sel, d_force_,
-                               s == 0 ? nforce_ : 0, s == 0, nodes_ < (1LL << 20), stream_));
+    bool first = true;
+    for (int s = 0; s < max_stages_; s++) {
+        if (!stage_nblocks_[s]) continue;
+        CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], d_stage_blocks_[s], stage_nblocks_[s],
+                               store_, sel, d_force_, first, nodes_ < (1LL << 20), stream_));
+        first = false;
+    }
     if (nforce_ && max_stages_ == 0) CK(launch::force_reduce(d_force_, nforce_, true, stream_));
     if (nrec_) {
         const int psize = store_ == STORE_F64 ? (int)sizeof(StepParams) : (int)sizeof(FastStepParams);

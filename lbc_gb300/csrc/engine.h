@@ -69,6 +69,10 @@ inline bool storage_to_desc(int storage, CaseDesc &d) {
 struct Stage {
     int kind, index, along;
     int entry;                  // position in the Boundary list
+    // per point t: the BC's node is fluid (every point of a periodic entry);
+    // a solid node's point writes nothing, so batches launch no block whose
+    // points are all solid
+    std::vector<uint8_t> open;
     double *d_val1 = nullptr, *d_val2 = nullptr;
     // impedance wall (bottom regularized entries only)
     double *d_imp = nullptr;
@@ -176,6 +180,7 @@ class Solver {
     // Consecutive stages that share one launch (indices into stages()).
     const std::vector<std::vector<int>> &stage_groups() const { return groups_; }
     bool has_mem() const { return has_mem_; }
+    bool has_links() const { return has_links_; }
     bool has_force() const { return d_.Fx != 0.0 || d_.Fy != 0.0; }
     // 1 for fluid nodes with at least one solid pull source (wall link), [Ny][Nx].
     const std::vector<uint8_t> &link_nodes() const { return link_node_; }
@@ -363,34 +368,31 @@ class Batch {
     bool ok_ = false;
     cudaStream_t stream_ = nullptr;
     long long nodes_ = 0;
-    int ntiles_ = 0, grid_ = 0, max_stages_ = 0, max_along_ = 0, nforce_ = 0;
+    int ntiles_ = 0, grid_ = 0, max_stages_ = 0, nforce_ = 0;
     int tws_ = 6;
     bool wide_ = false;  // some case needs 64-bit element offsets
     bool any_force_ = false;  // some case has a body force
     bool all_flags_ = true;   // every case has a flag word
+    bool any_links_ = false;  // some case has cut-link records
     int launches_per_step_ = 0;
     void *d_sp_ = nullptr;         // StepParams or FastStepParams [2 * ncases]
     int *d_phase_ = nullptr;       // [ncases] (and stage entries)
     int4 *d_tiles_ = nullptr;
     std::vector<StageParams *> d_stage_lists_;
     std::vector<int> stage_counts_;
+    // per level: the launch's blocks, (entry, first point) or (count + force
+    // slot, 0) on the first level
+    std::vector<int2 *> d_stage_blocks_;
+    std::vector<int> stage_nblocks_;
     FinishParams *d_fin_ = nullptr;
     ForceSlot *d_force_ = nullptr;
     int4 *d_special_ = nullptr;    // (case, i, j, chunk), shifted storage
     int nspecial_ = 0;
-    // impedance walls advanced in the special-node launch (shifted storage)
+    // impedance walls advanced ahead of their stage (shifted storage)
     ImpWall *d_walls_ = nullptr;
     int2 *d_imp_ = nullptr;         // (wall, first node) per 128-node block
     RecordTask *d_rec_ = nullptr;   // every case's probes and wall traces (case index set)
     int nrec_ = 0;
-    int bulk_reserve_ = 0;          // block slots per SM the clean-pair grid leaves to the special launch
-    static constexpr int kBulkReserve = 0;
-    int bulk_grid() const {
-        if (!bulk_reserve_) return grid_;
-        const int per_sm = launch::step_batch_shifted_grid(store_) / launch::sm_count();
-        const int keep = std::max(1, per_sm - bulk_reserve_);
-        return std::min(grid_, keep * launch::sm_count());
-    }
     int nimp_ = 0;
     std::vector<ImpWall> walls_host_;
     std::vector<int2> wall_at_;     // (level, entry) of each wall's stage

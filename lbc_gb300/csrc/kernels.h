@@ -176,11 +176,13 @@ cudaError_t fp64_rate(int blocks, int iters, double *sink, cudaStream_t s);
 cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 *tiles, int ntiles,
                              int sel, int tws, int grid, cudaStream_t s, bool fma = false);
 int step_batch_exact_grid();
-// One level of a batch's Boundary lists (n entries); nfs > 0 adds one block
-// row per force slot fs[0 .. nfs).
+// One level of a batch's Boundary lists (n entries): block b steps points
+// blocks[b].y .. + kStageBatchPoints(F64) - 1 of entry blocks[b].x, or, for
+// blocks[b].x >= n, reduces force slot fs[blocks[b].x - n].
 // warm: FP64 only, run the edge threads' instruction-cache warm-up pass.
-cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int max_along, int store,
-                        int sel, const ForceSlot *fs, int nfs, bool after_bulk, bool warm, cudaStream_t s);
+constexpr int kStageBatchPoints = 64, kStageBatchPointsF64 = 32;
+cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, const int2 *blocks, int nblocks,
+                        int store, int sel, const ForceSlot *fs, bool after_bulk, bool warm, cudaStream_t s);
 cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStream_t s);
 
 // shifted storage (kernels_shifted.cu)
@@ -192,15 +194,18 @@ cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool co
 cudaError_t special_shifted(const FastStepParams &p, const int2 *nodes, int n, int store, bool flags, bool collide,
                             bool after_bulk, cudaStream_t s);
 // The special nodes of a batch: nodes[q] = (case, i, j, chunk), n a multiple
-// of 32 (each case's list padded to 32 entries, i = -1); then nimp blocks of
-// impedance-wall updates, imp[b] = (wall, first of 128 nodes).
+// of 32 (each case's list padded to 32 entries, i = -1); links: some case has
+// cut-link records.
 cudaError_t special_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *nodes, int n, int sel,
-                                  const ImpWall *walls, const int2 *imp, int nimp, int store, bool wide, bool force,
-                                  bool after_bulk, cudaStream_t s);
+                                  int store, bool wide, bool force, bool links, bool after, cudaStream_t s);
+// The impedance-wall updates of a batch for one step, nimp blocks of 128
+// nodes, imp[b] = (wall, first node).
+cudaError_t impedance_batch(const int *phase, int sel, const ImpWall *walls, const int2 *imp, int nimp, bool after,
+                            cudaStream_t s);
 // Edge BCs of shifted storage in FP32 (launch::stage_group / stage_batch dispatch here).
 cudaError_t stage_group_shifted(const StageGroup &g, int store, bool collide, bool after_bulk, cudaStream_t s);
-cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, int max_along, int store,
-                                int sel, const ForceSlot *fs, int nfs, bool after_bulk, cudaStream_t s);
+cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, const int2 *blocks, int nblocks,
+                                int store, int sel, const ForceSlot *fs, bool after_bulk, cudaStream_t s);
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s);
 // wide: some case has 9 * plane >= 2^31 elements (64-bit element offsets).
 // force: some case has a body force (the forced kernel form serves all cases).

@@ -304,20 +304,22 @@ __global__ void k_stage_group(const StageGroup g) {
     stage_dispatch<T, COLLIDE>(p, g.fin, t, g.warm);
 }
 
-// Stage level of every case of a batch: blockIdx.y selects the case entry,
-// list[2 * e + (sel ^ phase)] its parameters for this ping-pong direction;
-// rows n.. reduce the force slots fs[].
+// Stage level of every case of a batch: block b steps points blk[b].y ..
+// of entry e = blk[b].x, list[2 * e + (sel ^ phase)] its parameters for this
+// ping-pong direction; e >= n: reduce force slot fs[e - n].
 template <typename T>
 __global__ void k_stage_batch(const StageParams *__restrict__ list, const int *__restrict__ ephase,
-                              int sel, int n, const ForceSlot *__restrict__ fs, int warm) {
-    const int e = blockIdx.y;
+                              const int2 *__restrict__ blk, int sel, int n, const ForceSlot *__restrict__ fs,
+                              int warm) {
+    const int2 b = blk[blockIdx.x];
+    const int e = b.x;
     if (e >= n) {
         pdl_wait();
-        if (blockIdx.x == 0 && threadIdx.x < 32) force_reduce_warp(fs[e - n], (int)threadIdx.x);
+        if (threadIdx.x < 32) force_reduce_warp(fs[e - n], (int)threadIdx.x);
         return;
     }
     const StageParams &p = list[2 * e + (sel ^ ephase[e])];
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = b.y + (int)threadIdx.x;
     if (t >= p.along) return;
     stage_dispatch<T, true>(p, *p.fin, t, warm);
 }
@@ -809,14 +811,12 @@ cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 
 // free up. Measured on 64 liner ducts: 4.03 GLUPS persistent, 4.10 per tile.
 int step_batch_exact_grid() { return 1 << 30; }
 
-cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, int max_along, int store,
-                        int sel, const ForceSlot *fs, int nfs, bool after_bulk, bool warm, cudaStream_t s) {
-    if (n + nfs == 0) return cudaSuccess;
-    if (store != STORE_F64)
-        return stage_batch_shifted(list, ephase, n, max_along, store, sel, fs, nfs, after_bulk, s);
-    const dim3 g(std::max(1, (max_along + 31) / 32), n + nfs);
-    return launch_follower(after_bulk, k_stage_batch<double>, g, dim3(32), s, list, ephase, sel, n, fs,
-                           warm ? 1 : 0);
+cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, const int2 *blocks, int nblocks,
+                        int store, int sel, const ForceSlot *fs, bool after_bulk, bool warm, cudaStream_t s) {
+    if (nblocks == 0) return cudaSuccess;
+    if (store != STORE_F64) return stage_batch_shifted(list, ephase, n, blocks, nblocks, store, sel, fs, after_bulk, s);
+    return launch_follower(after_bulk, k_stage_batch<double>, dim3(nblocks), dim3(kStageBatchPointsF64), s, list,
+                           ephase, blocks, sel, n, fs, warm ? 1 : 0);
 }
 
 cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStream_t s) {

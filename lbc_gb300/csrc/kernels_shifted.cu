@@ -214,8 +214,11 @@ __device__ __noinline__ float2 omega_pair(const double *omega, size_t dn) {
 // One node of the fused step in shifted storage (solids, bounce-back links,
 // stale slots, edge-BC band: everything). I is the element-offset type: int
 // whenever all nine planes fit in 2^31 elements (fewer address instructions),
-// long long otherwise.
-template <typename T, typename I, bool FLAGS, bool COLLIDE, bool FORCE>
+// long long otherwise. LINKS = false: no case of the launch has cut-link
+// records (plain bounce-back on every solid link), and the record path is
+// left out (measured: 116 -> 64 registers for the batched special-node
+// kernel, twice the resident warps).
+template <typename T, typename I, bool FLAGS, bool COLLIDE, bool FORCE, bool LINKS = true>
 __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int i, int j,
                                                   float &mfx, float &mfy, bool &link) {
     const StepParams &p = fp.s;
@@ -249,14 +252,14 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
     if (FLAGS) {
 #pragma unroll
         for (int k = 1; k < 9; k++) own[k] = SV<T>::ld(S + (I)oppk(k) * pl + node);
-        if (p.link_off) lo = p.link_off[node];
+        if (LINKS && p.link_off) lo = p.link_off[node];
     }
     if (FLAGS && (fl & NF_SOLID)) {
         solid_node_outputs<T>(p, i, j, (long long)node, dn, fl);
         return;
     }
     if (FLAGS && (fl & NF_SPECIAL_MASK)) {
-        const bool has_links = (fl & NF_LINKS) != 0;
+        const bool has_links = LINKS && (fl & NF_LINKS) != 0;
         bool off[9];
         Link L[9];
         int m = 0;
@@ -440,7 +443,7 @@ __global__ void __launch_bounds__(256, 5) k_step_shifted_geo(const FastStepParam
 // that kernel only at its end, so that what follows sees both. (Launched the
 // other way round, the clean-pair blocks must each wait at their end and hold
 // their SMs: measured slower.)
-template <typename T, typename I, bool FLAGS, bool COLLIDE, bool FORCE>
+template <typename T, typename I, bool FLAGS, bool COLLIDE, bool FORCE, bool LINKS>
 __global__ void __launch_bounds__(128) k_step_special_shifted(const FastStepParams fp,
                                                               const int2 *__restrict__ nodes, int n) {
     pdl_launch_dependents();
@@ -449,7 +452,7 @@ __global__ void __launch_bounds__(128) k_step_special_shifted(const FastStepPara
     bool link = false;
     if (q < n) {
         const int2 ij = nodes[q];
-        step_node_shifted<T, I, FLAGS, COLLIDE, FORCE>(fp, ij.x, ij.y, mx, my, link);
+        step_node_shifted<T, I, FLAGS, COLLIDE, FORCE, LINKS>(fp, ij.x, ij.y, mx, my, link);
     }
     if (fp.s.mem_partials)
         chunk_reduce2_store((double)mx, (double)my, link, q >> 5, fp.s.chunk_slot, fp.s.mem_partials);
@@ -458,10 +461,11 @@ __global__ void __launch_bounds__(128) k_step_special_shifted(const FastStepPara
 
 // Batched form (see k_step_batch_exact in kernels_exact.cu): tiles of
 // 2^(tws + 1) x 2^(8 - tws) nodes, two adjacent nodes per thread, clean pairs
-// only (the special nodes of all cases are k_step_batch_special_shifted's).
-// Blocks stride through the tile list, so the tiles in flight at any moment
-// are neighbours in memory (sequential DRAM streams, halo rows shared through
-// L2).
+// only (the special nodes of all cases are k_step_batch_special_shifted's:
+// blocks of them spread through this kernel's tile list, on 64 liner ducts
+// without cut links, measured 57.4 vs 67.7 GLUPS). Blocks stride through the
+// tile list, so the tiles in flight at any moment are neighbours in memory
+// (sequential DRAM streams, halo rows shared through L2).
 template <typename T, typename I, bool FORCE, bool ALLFLAGS>
 __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepParams *__restrict__ sp,
                                                             const int *__restrict__ phase,
@@ -488,43 +492,45 @@ __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepPar
 // The special nodes of every case of a batch: nodes[q] = (case, i, j, chunk),
 // each case's list padded to a multiple of 32 entries (padding: i = -1), so
 // that a warp holds one chunk of one case and the force partials are those of
-// the case alone.
-// The first nimp blocks advance the batch's impedance walls for this step
-// (impedance_ahead): imp[b] = (wall, first node) of 128 nodes, walls[w] = the
-// wall's stage parameters for both directions and its velocity buffer. That
-// FP64 work depends only on the previous step's moments, so it runs here,
-// beside the latency-bound special nodes, instead of at the head of the edge
-// launch; its blocks come first so that the long FP64 updates start first.
-template <typename T, typename I, bool FORCE>
+// the case alone. LINKS: some case of the batch has cut-link records.
+template <typename T, typename I, bool FORCE, bool LINKS>
 __global__ void __launch_bounds__(128) k_step_batch_special_shifted(const FastStepParams *__restrict__ sp,
                                                                     const int *__restrict__ phase,
                                                                     const int4 *__restrict__ nodes, int n,
-                                                                    int sel, int nimp,
-                                                                    const ImpWall *__restrict__ walls,
-                                                                    const int2 *__restrict__ imp) {
+                                                                    int sel) {
     pdl_launch_dependents();
-    if ((int)blockIdx.x < nimp) {
-        const int2 b = imp[blockIdx.x];
-        const ImpWall &w = walls[b.x];
-        const StageParams &p = w.pair[sel ^ phase[w.entry]];
-        const int t = b.y + (int)threadIdx.x;
-        if (t < p.along) impedance_ahead(p, w.vn, t);
-        pdl_wait();
-        return;
-    }
-    const int q = ((int)blockIdx.x - nimp) * (int)blockDim.x + (int)threadIdx.x;
+    const int q = (int)blockIdx.x * (int)blockDim.x + (int)threadIdx.x;
     if (q < n) {  // n is a multiple of 32: whole warps
         const int4 e = nodes[q];
         const FastStepParams &fp = sp[2 * e.x + (sel ^ phase[e.x])];
         float mx = 0.f, my = 0.f;
         bool link = false;
         if (e.y >= 0) {
-            if (fp.s.flags) step_node_shifted<T, I, true, true, FORCE>(fp, e.y, e.z, mx, my, link);
-            else step_node_shifted<T, I, false, true, FORCE>(fp, e.y, e.z, mx, my, link);
+            if (fp.s.flags) step_node_shifted<T, I, true, true, FORCE, LINKS>(fp, e.y, e.z, mx, my, link);
+            else step_node_shifted<T, I, false, true, FORCE, LINKS>(fp, e.y, e.z, mx, my, link);
         }
         if (fp.s.mem_partials)
             chunk_reduce2_store((double)mx, (double)my, link, e.w, fp.s.chunk_slot, fp.s.mem_partials);
     }
+    pdl_wait();
+}
+
+// The impedance walls of a batch, advanced for this step (impedance_ahead):
+// imp[b] = (wall, first node) of 128 nodes, walls[w] = the wall's stage
+// parameters for both directions and its velocity buffer. That FP64 work
+// depends only on the previous step's moments, so it runs beside the
+// latency-bound special nodes, behind the clean pairs, instead of at the head
+// of the edge launch. Its own launch (first of the two) keeps its FP64
+// registers off the special-node kernel.
+__global__ void __launch_bounds__(128) k_impedance_batch(const int *__restrict__ phase, int sel,
+                                                         const ImpWall *__restrict__ walls,
+                                                         const int2 *__restrict__ imp) {
+    pdl_launch_dependents();
+    const int2 b = imp[blockIdx.x];
+    const ImpWall &w = walls[b.x];
+    const StageParams &p = w.pair[sel ^ phase[w.entry]];
+    const int t = b.y + (int)threadIdx.x;
+    if (t < p.along) impedance_ahead(p, w.vn, t);
     pdl_wait();
 }
 
@@ -703,15 +709,17 @@ __global__ void k_stage_group_shifted(const StageGroup g) {
 
 template <typename T>
 __global__ void k_stage_batch_shifted(const StageParams *__restrict__ list, const int *__restrict__ ephase,
-                                      int sel, int n, const ForceSlot *__restrict__ fs) {
-    const int e = blockIdx.y;
+                                      const int2 *__restrict__ blk, int sel, int n,
+                                      const ForceSlot *__restrict__ fs) {
+    const int2 b = blk[blockIdx.x];
+    const int e = b.x;
     if (e >= n) {
         pdl_wait();
-        if (blockIdx.x == 0 && threadIdx.x < 32) force_reduce_warp(fs[e - n], (int)threadIdx.x);
+        if (threadIdx.x < 32) force_reduce_warp(fs[e - n], (int)threadIdx.x);
         return;
     }
     const StageParams &p = list[2 * e + (sel ^ ephase[e])];
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = b.y + (int)threadIdx.x;
     if (t >= p.along) return;
     stage_dispatch_s<T, true>(p, *p.fin, t);
 }
@@ -728,13 +736,13 @@ cudaError_t stage_group_shifted(const StageGroup &g, int store, bool collide, bo
     return launch_follower(after_bulk, k_stage_group_shifted<__half, false>, grid, b, s, g);
 }
 
-cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, int max_along, int store,
-                                int sel, const ForceSlot *fs, int nfs, bool after_bulk, cudaStream_t s) {
-    if (n + nfs == 0) return cudaSuccess;
-    const dim3 g(std::max(1, (max_along + 63) / 64), n + nfs), b(64);
+cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, const int2 *blocks, int nblocks,
+                                int store, int sel, const ForceSlot *fs, bool after_bulk, cudaStream_t s) {
+    if (nblocks == 0) return cudaSuccess;
+    const dim3 g(nblocks), b(kStageBatchPoints);
     if (store == STORE_F32)
-        return launch_follower(after_bulk, k_stage_batch_shifted<float>, g, b, s, list, ephase, sel, n, fs);
-    return launch_follower(after_bulk, k_stage_batch_shifted<__half>, g, b, s, list, ephase, sel, n, fs);
+        return launch_follower(after_bulk, k_stage_batch_shifted<float>, g, b, s, list, ephase, blocks, sel, n, fs);
+    return launch_follower(after_bulk, k_stage_batch_shifted<__half>, g, b, s, list, ephase, blocks, sel, n, fs);
 }
 
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s) {
@@ -783,16 +791,28 @@ cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool co
     return step_shifted_t<__half>(p, flags, collide, false, g, block, s);
 }
 
+template <typename T, typename I, bool FORCE, bool LINKS>
+static cudaError_t special_shifted_tifl(const FastStepParams &p, const int2 *nodes, int n, bool flags, bool collide,
+                                        bool after_bulk, cudaStream_t s) {
+    const dim3 g((n + 127) / 128), b(128);
+    if (flags) {
+        if (collide)
+            return launch_follower(after_bulk, k_step_special_shifted<T, I, true, true, FORCE, LINKS>, g, b, s, p,
+                                   nodes, n);
+        return launch_follower(after_bulk, k_step_special_shifted<T, I, true, false, FORCE, LINKS>, g, b, s, p, nodes,
+                               n);
+    }
+    if (collide)
+        return launch_follower(after_bulk, k_step_special_shifted<T, I, false, true, FORCE, LINKS>, g, b, s, p, nodes,
+                               n);
+    return launch_follower(after_bulk, k_step_special_shifted<T, I, false, false, FORCE, LINKS>, g, b, s, p, nodes, n);
+}
+
 template <typename T, typename I, bool FORCE>
 static cudaError_t special_shifted_tif(const FastStepParams &p, const int2 *nodes, int n, bool flags, bool collide,
                                        bool after_bulk, cudaStream_t s) {
-    const dim3 g((n + 127) / 128), b(128);
-    if (flags) {
-        if (collide) return launch_follower(after_bulk, k_step_special_shifted<T, I, true, true, FORCE>, g, b, s, p, nodes, n);
-        return launch_follower(after_bulk, k_step_special_shifted<T, I, true, false, FORCE>, g, b, s, p, nodes, n);
-    }
-    if (collide) return launch_follower(after_bulk, k_step_special_shifted<T, I, false, true, FORCE>, g, b, s, p, nodes, n);
-    return launch_follower(after_bulk, k_step_special_shifted<T, I, false, false, FORCE>, g, b, s, p, nodes, n);
+    if (p.s.links) return special_shifted_tifl<T, I, FORCE, true>(p, nodes, n, flags, collide, after_bulk, s);
+    return special_shifted_tifl<T, I, FORCE, false>(p, nodes, n, flags, collide, after_bulk, s);
 }
 
 template <typename T>
@@ -814,31 +834,40 @@ cudaError_t special_shifted(const FastStepParams &p, const int2 *nodes, int n, i
     return special_shifted_t<__half>(p, nodes, n, flags, collide, after_bulk, s);
 }
 
-template <typename T, bool FORCE>
-static cudaError_t special_batch_shifted_tf(const FastStepParams *sp, const int *phase, const int4 *nodes, int n,
-                                            int sel, const ImpWall *walls, const int2 *imp, int nimp, bool wide,
-                                            bool after_bulk, cudaStream_t s) {
-    const dim3 g(nimp + (n + 127) / 128), b(128);
+template <typename T, bool FORCE, bool LINKS>
+static cudaError_t special_batch_shifted_tfl(const FastStepParams *sp, const int *phase, const int4 *nodes, int n,
+                                             int sel, bool wide, bool after, cudaStream_t s) {
+    const dim3 g((n + 127) / 128), b(128);
     if (wide)
-        return launch_follower(after_bulk, k_step_batch_special_shifted<T, long long, FORCE>, g, b, s, sp, phase,
-                               nodes, n, sel, nimp, walls, imp);
-    return launch_follower(after_bulk, k_step_batch_special_shifted<T, int, FORCE>, g, b, s, sp, phase, nodes, n,
-                           sel, nimp, walls, imp);
+        return launch_follower(after, k_step_batch_special_shifted<T, long long, FORCE, LINKS>, g, b, s, sp, phase,
+                               nodes, n, sel);
+    return launch_follower(after, k_step_batch_special_shifted<T, int, FORCE, LINKS>, g, b, s, sp, phase, nodes, n,
+                           sel);
+}
+
+template <typename T>
+static cudaError_t special_batch_shifted_t(const FastStepParams *sp, const int *phase, const int4 *nodes, int n,
+                                           int sel, bool wide, bool force, bool links, bool after, cudaStream_t s) {
+    if (force) {
+        if (links) return special_batch_shifted_tfl<T, true, true>(sp, phase, nodes, n, sel, wide, after, s);
+        return special_batch_shifted_tfl<T, true, false>(sp, phase, nodes, n, sel, wide, after, s);
+    }
+    if (links) return special_batch_shifted_tfl<T, false, true>(sp, phase, nodes, n, sel, wide, after, s);
+    return special_batch_shifted_tfl<T, false, false>(sp, phase, nodes, n, sel, wide, after, s);
 }
 
 cudaError_t special_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *nodes, int n, int sel,
-                                  const ImpWall *walls, const int2 *imp, int nimp, int store, bool wide, bool force,
-                                  bool after_bulk, cudaStream_t s) {
-    if (n + nimp == 0) return cudaSuccess;
+                                  int store, bool wide, bool force, bool links, bool after, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
     if (n % 32) return cudaErrorInvalidValue;
-    if (store == STORE_F32) {
-        if (force)
-            return special_batch_shifted_tf<float, true>(sp, phase, nodes, n, sel, walls, imp, nimp, wide, after_bulk, s);
-        return special_batch_shifted_tf<float, false>(sp, phase, nodes, n, sel, walls, imp, nimp, wide, after_bulk, s);
-    }
-    if (force)
-        return special_batch_shifted_tf<__half, true>(sp, phase, nodes, n, sel, walls, imp, nimp, wide, after_bulk, s);
-    return special_batch_shifted_tf<__half, false>(sp, phase, nodes, n, sel, walls, imp, nimp, wide, after_bulk, s);
+    if (store == STORE_F32) return special_batch_shifted_t<float>(sp, phase, nodes, n, sel, wide, force, links, after, s);
+    return special_batch_shifted_t<__half>(sp, phase, nodes, n, sel, wide, force, links, after, s);
+}
+
+cudaError_t impedance_batch(const int *phase, int sel, const ImpWall *walls, const int2 *imp, int nimp, bool after,
+                            cudaStream_t s) {
+    if (nimp == 0) return cudaSuccess;
+    return launch_follower(after, k_impedance_batch, dim3(nimp), dim3(128), s, phase, sel, walls, imp);
 }
 
 template <typename T, bool FORCE, bool ALLFLAGS>

@@ -310,18 +310,25 @@ bool Solver::build_geometry() {
     has_flags_ = any_special || !stages_.empty() || !d_.px || !d_.py;
     // Shifted storage: the nodes the clean-pair kernels leave out (both nodes
     // of every pair (2m, 2m + 1) of a row with a special node, and the last
-    // column of an odd-width grid), in row-major order.
+    // column of an odd-width grid), in row-major order. Solid nodes off the
+    // edge band are marked (kSpecialSolid in x): their step only writes NaN
+    // moments on steps that write the fields, with no load but the entry.
     special_host_.clear();
     if (d_.store != STORE_F64) {
         const uint16_t slow = NF_SPECIAL_MASK | NF_SOLID | NF_BAND | NF_BCW | NF_LINKS;
+        auto entry = [&](int i, int j) {
+            const uint16_t f = flags[(size_t)j * pitch_ + i];
+            const bool mark = (f & NF_SOLID) && !(f & NF_BAND) && Nx <= kSpecialSolid;
+            return make_int2(mark ? (i | kSpecialSolid) : i, j);
+        };
         for (int j = 0; j < Ny; j++)
             for (int i0 = 0; i0 < Nx; i0 += 2) {
                 const bool two = i0 + 1 < Nx;
                 const size_t n0 = (size_t)j * pitch_ + i0;
                 const bool sp = !two || (flags[n0] & slow) || (flags[n0 + 1] & slow);
                 if (!sp) continue;
-                special_host_.push_back(make_int2(i0, j));
-                if (two) special_host_.push_back(make_int2(i0 + 1, j));
+                special_host_.push_back(entry(i0, j));
+                if (two) special_host_.push_back(entry(i0 + 1, j));
             }
     }
     nspecial_ = (int)special_host_.size();
@@ -515,7 +522,7 @@ bool Solver::compute_segment_slots() {
             bool any = false;
             for (int q = 32 * c; q < std::min(nspecial_, 32 * c + 32); q++) {
                 const int2 ij = special_host_[q];
-                if (link_node_[(size_t)ij.y * Nx + ij.x]) { any = true; break; }
+                if (link_node_[(size_t)ij.y * Nx + (ij.x & ~kSpecialSolid)]) { any = true; break; }
             }
             if (any) slot[c] = n++;
         }

@@ -171,13 +171,12 @@ __device__ __forceinline__ void moments_shifted(const float g[9], float hFx, flo
 // Rare per-node outputs, kept out of line so the compiler cannot hoist their
 // FP64 conversions into every thread's path (FP64 issue is slow on GB300).
 template <typename T>
-__device__ __noinline__ void solid_node_outputs(const StepParams &p, int i, int j, long long node,
-                                                size_t dn, uint16_t fl) {
+__device__ __noinline__ void solid_node_outputs(const StepParams &p, int slot, long long node, size_t dn,
+                                                uint16_t fl) {
     if (p.write_macro) { p.rho[dn] = NAN; p.ux[dn] = NAN; p.uy[dn] = NAN; }
     if (fl & NF_BAND) {
         // A BC may read a solid neighbour: lbc sees the untouched buffer
         // content and NaN moments there.
-        const int slot = band_slot(p.colbase, p.rowbase, i, j);
         const T *Dst = (const T *)p.dst;
 #pragma unroll
         for (int k = 0; k < 9; k++) p.bandg[(size_t)k * p.nslots + slot] = SV<T>::ld_plain(Dst + k * p.plane + node);
@@ -187,6 +186,16 @@ __device__ __noinline__ void solid_node_outputs(const StepParams &p, int i, int 
     }
 }
 
+
+// A solid node off the edge band (kSpecialSolid entries): NaN moments on steps
+// that write the fields, as solid_node_outputs writes them.
+__device__ __forceinline__ void solid_nan(const StepParams &p, int i, int j) {
+    if (!p.write_macro) return;
+    const size_t dn = (size_t)j * (size_t)p.Nx + (size_t)i;
+    p.rho[dn] = NAN;
+    p.ux[dn] = NAN;
+    p.uy[dn] = NAN;
+}
 
 __device__ __noinline__ void macro_store(const StepParams &p, size_t dn, int slot, float dr, float ux,
                                          float uy) {
@@ -229,13 +238,14 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
     const I pl = (I)p.plane;
     // The loads come in three waves of independent loads, not one chain: (1)
     // the flag word, the nine pulled populations, the node's eight own
-    // opposite populations and its cut-link offset; (2) the cut-link records
-    // of its flagged directions; (3) the populations behind interpolated
-    // links and the stale slots of off-grid sources. Source neighbours are
-    // wrapped on periodic axes and clamped otherwise, so that every load of
-    // wave 1 is in bounds whatever the flags say. (Measured: the own
-    // populations loaded in wave 2, for flagged directions only, cost the
-    // channel and the cylinder 2-4 %.)
+    // opposite populations, its cut-link offset, its band bases and (without
+    // cut-link records) the stale slots of off-grid sources, which the
+    // position alone decides; (2) the cut-link records of its flagged
+    // directions; (3) the populations behind interpolated links (and the
+    // stale slots, with records). Source neighbours are wrapped on periodic axes and
+    // clamped otherwise, so that every load of wave 1 is in bounds whatever
+    // the flags say. (Measured: the own populations loaded in wave 2, for
+    // flagged directions only, cost the channel and the cylinder 2-4 %.)
     int im = i - 1, ip = i + 1, jm = j - 1, jp = j + 1;
     if (p.px) { if (im < 0) im += p.Nx; if (ip >= p.Nx) ip -= p.Nx; }
     else { im = max(im, 0); ip = min(ip, p.Nx - 1); }
@@ -247,26 +257,44 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
     float g[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) g[k] = SV<T>::ld(S + (I)k * pl + so[k]);
-    int lo = 0;
+    int lo = 0, cb = -1, rb = -1;
     float own[9];
+    bool off[9];
     if (FLAGS) {
 #pragma unroll
         for (int k = 1; k < 9; k++) own[k] = SV<T>::ld(S + (I)oppk(k) * pl + node);
         if (LINKS && p.link_off) lo = p.link_off[node];
+        // Without cut-link records, also the band bases and the stale slots
+        // of off-grid sources (this node's own destination slots, written by
+        // no other thread). With records they stay in the later waves: their
+        // registers (96 -> 116 for the per-case kernel) cost more than the
+        // latency saved.
+        if (!LINKS && p.colbase) { cb = p.colbase[i]; rb = p.rowbase[j]; }
+        if (!LINKS) {
+#pragma unroll
+            for (int k = 1; k < 9; k++) {
+                const int si = i - cxk(k), sj = j - cyk(k);
+                off[k] = (!p.px && (si < 0 || si >= p.Nx)) || (!p.py && (sj < 0 || sj >= p.Ny));
+                if (off[k]) g[k] = SV<T>::ld_plain(Dst + (I)k * pl + node);
+            }
+        }
     }
+    int slot = -1;
+    if (FLAGS && (fl & NF_BAND)) slot = LINKS ? band_slot(p.colbase, p.rowbase, i, j) : (cb >= 0 ? cb + j : rb + i);
     if (FLAGS && (fl & NF_SOLID)) {
-        solid_node_outputs<T>(p, i, j, (long long)node, dn, fl);
+        solid_node_outputs<T>(p, slot, (long long)node, dn, fl);
         return;
     }
     if (FLAGS && (fl & NF_SPECIAL_MASK)) {
         const bool has_links = LINKS && (fl & NF_LINKS) != 0;
-        bool off[9];
         Link L[9];
         int m = 0;
 #pragma unroll
         for (int k = 1; k < 9; k++) {
-            const int si = i - cxk(k), sj = j - cyk(k);
-            off[k] = (!p.px && (si < 0 || si >= p.Nx)) || (!p.py && (sj < 0 || sj >= p.Ny));
+            if (LINKS) {
+                const int si = i - cxk(k), sj = j - cyk(k);
+                off[k] = (!p.px && (si < 0 || si >= p.Nx)) || (!p.py && (sj < 0 || sj >= p.Ny));
+            }
             // link records in direction order, one per flagged on-grid direction
             if ((fl & (1u << k)) && !off[k] && has_links) L[k] = p.links[lo + m++];
         }
@@ -276,7 +304,7 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
             behind[k] = 0.f;
             if (!(fl & (1u << k))) continue;
             if (off[k]) {
-                g[k] = SV<T>::ld_plain(Dst + (I)k * pl + node);
+                if (LINKS) g[k] = SV<T>::ld_plain(Dst + (I)k * pl + node);
             } else if (has_links) {
                 if (L[k].mode == LINK_IBB_LO) behind[k] = SV<T>::ld(S + (I)oppk(k) * pl + (I)L[k].behind);
                 else if (L[k].mode == LINK_IBB_HI) behind[k] = SV<T>::ld(S + (I)k * pl + (I)L[k].behind);
@@ -300,9 +328,7 @@ __device__ __forceinline__ void step_node_shifted(const FastStepParams &fp, int 
             link = true;
         }
     }
-    int slot = -1;
     if (FLAGS && (fl & NF_BAND)) {
-        slot = band_slot(p.colbase, p.rowbase, i, j);
 #pragma unroll
         for (int k = 0; k < 9; k++) p.bandg[(size_t)k * p.nslots + slot] = g[k];
     }
@@ -452,7 +478,8 @@ __global__ void __launch_bounds__(128) k_step_special_shifted(const FastStepPara
     bool link = false;
     if (q < n) {
         const int2 ij = nodes[q];
-        step_node_shifted<T, I, FLAGS, COLLIDE, FORCE, LINKS>(fp, ij.x, ij.y, mx, my, link);
+        if (ij.x & kSpecialSolid) solid_nan(fp.s, ij.x & ~kSpecialSolid, ij.y);
+        else step_node_shifted<T, I, FLAGS, COLLIDE, FORCE, LINKS>(fp, ij.x, ij.y, mx, my, link);
     }
     if (fp.s.mem_partials)
         chunk_reduce2_store((double)mx, (double)my, link, q >> 5, fp.s.chunk_slot, fp.s.mem_partials);
@@ -505,7 +532,8 @@ __global__ void __launch_bounds__(128) k_step_batch_special_shifted(const FastSt
         const FastStepParams &fp = sp[2 * e.x + (sel ^ phase[e.x])];
         float mx = 0.f, my = 0.f;
         bool link = false;
-        if (e.y >= 0) {
+        if (e.y & kSpecialSolid) solid_nan(fp.s, e.y & ~kSpecialSolid, e.z);
+        else if (e.y >= 0) {
             if (fp.s.flags) step_node_shifted<T, I, true, true, FORCE, LINKS>(fp, e.y, e.z, mx, my, link);
             else step_node_shifted<T, I, false, true, FORCE, LINKS>(fp, e.y, e.z, mx, my, link);
         }

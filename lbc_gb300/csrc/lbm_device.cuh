@@ -622,9 +622,16 @@ struct FinishParams {
     float omega0f, Fxf, Fyf, hFxf, hFyf;
 };
 
+// Special-node list entries (shifted storage): bit 30 of the column marks a
+// solid node off the edge band, whose step only writes NaN moments on steps
+// that write the fields (grids narrower than 2^30 columns).
+constexpr int kSpecialSolid = 1 << 30;
+
+// Both bases are loaded at once (rowbase[j] is in bounds whatever colbase[i]
+// holds): one memory latency, not two dependent ones.
 __device__ __forceinline__ int band_slot(const int *colbase, const int *rowbase, int i, int j) {
-    const int c = colbase[i];
-    return c >= 0 ? c + j : rowbase[j] + i;
+    const int c = colbase[i], r = rowbase[j];
+    return c >= 0 ? c + j : r + i;
 }
 
 // The node that thread t of a Boundary entry works on (bc_apply's mapping:

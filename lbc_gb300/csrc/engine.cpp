@@ -935,7 +935,6 @@ bool Solver::set_impedance(int entry, const double *R, const double *m, const do
         h[(size_t)IMP_B2 * n + t] = b[1];
         h[(size_t)IMP_RHOBAR * n + t] = rho_ref;
     }
-    if (!st->d_vn && !dalloc(&st->d_vn, (size_t)n)) return false;
     if (!st->d_imp || st->imp_nf != nf) {
         if (!dalloc(&st->d_imp, h.size())) return false;
     }
@@ -1653,43 +1652,6 @@ bool Batch::build() {
             stage_nblocks_.push_back((int)blocks[l].size());
         }
     }
-    // Shifted storage: impedance walls are advanced ahead of their stage, in
-    // a launch beside the special nodes (entries numbered as run() fills the
-    // lists).
-    if (store_ != STORE_F64) {
-        std::vector<ImpWall> walls;
-        std::vector<int2> imp;
-        std::vector<int> next(max_stages_, 0);
-        for (Solver *c : cases_)
-            for (size_t l = 0; l < c->stage_groups().size(); l++)
-                for (int k : c->stage_groups()[l]) {
-                    const Stage &st = c->stages()[k];
-                    const int e = next[l]++;
-                    if (!st.d_imp || !st.d_vn || st.kind != BC_VEL_BOT_REG) continue;
-                    ImpWall w;
-                    std::memset(&w, 0, sizeof w);
-                    w.pair = d_stage_lists_[l] + 2 * e;
-                    w.entry = e;
-                    w.vn = st.d_vn;
-                    // blocks of 128 nodes with a fluid node, and the first
-                    // (its node 0 advances the wall's phasors)
-                    for (int t0 = 0; t0 < st.along; t0 += 128) {
-                        bool any = t0 == 0;
-                        for (int t = t0; t < std::min(st.along, t0 + 128) && !any; t++) any = st.open[t] != 0;
-                        if (any) imp.push_back(make_int2((int)walls.size(), t0));
-                    }
-                    walls.push_back(w);
-                    wall_at_.push_back(make_int2((int)l, e));
-                }
-        nimp_ = (int)imp.size();
-        if (nimp_) {
-            if (!balloc(allocs_, &d_walls_, walls.size(), stream_) || !balloc(allocs_, &d_imp_, imp.size(), stream_))
-                return false;
-            CK(cudaMemcpyAsync(d_walls_, walls.data(), walls.size() * sizeof(ImpWall), cudaMemcpyHostToDevice, stream_));
-            CK(cudaMemcpyAsync(d_imp_, imp.data(), imp.size() * sizeof(int2), cudaMemcpyHostToDevice, stream_));
-            walls_host_ = walls;
-        }
-    }
     // Every case's probes and wall traces: one record launch per step.
     std::vector<RecordTask> rec;
     for (int c = 0; c < nc; c++)
@@ -1705,7 +1667,7 @@ bool Batch::build() {
     // The force reductions ride in the first stage level's launch.
     int stage_launches = 0;
     for (int nb : stage_nblocks_) stage_launches += nb > 0 ? 1 : 0;
-    launches_per_step_ = 1 + (nspecial_ ? 1 : 0) + (nimp_ ? 1 : 0) + stage_launches +
+    launches_per_step_ = 1 + (nspecial_ ? 1 : 0) + stage_launches +
                          (nforce_ && max_stages_ == 0 ? 1 : 0) + (nrec_ ? 1 : 0);
     CK(cudaStreamSynchronize(stream_));
     return true;
@@ -1716,11 +1678,9 @@ bool Batch::launch_batched(int sel) {
         CK(launch::step_batch_exact((const StepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
                                     grid_, stream_, cases_[0]->fma64()));
     } else {
-        // the clean pairs, then the impedance walls and the special nodes
-        // overlapping their tail
+        // the clean pairs, then the special nodes overlapping their tail
         CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
                                       store_, wide_, any_force_, all_flags_, grid_, stream_));
-        CK(launch::impedance_batch(d_phase_, sel, d_walls_, d_imp_, nimp_, true, stream_));
         CK(launch::special_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_special_, nspecial_, sel, store_,
                                          wide_, any_force_, any_links_, true, stream_));
     }
@@ -1801,12 +1761,6 @@ bool Batch::run(int nsteps) {
                     lists[l].push_back(s->stage_params(s->stages()[k], 1 - cur, par ^ 1));
                     lists[l].back().fin = d_fin_ + 2 * c + 1;
                 }
-        }
-        // Walls advanced ahead: their stages read the velocities.
-        for (size_t w = 0; w < wall_at_.size(); w++) {
-            const int2 le = wall_at_[w];
-            lists[le.x][2 * le.y].vn = walls_host_[w].vn;
-            lists[le.x][2 * le.y + 1].vn = walls_host_[w].vn;
         }
         if (store_ == STORE_F64)
             okk = okk && check_cuda(cudaMemcpyAsync(d_sp_, sp.data(), sp.size() * sizeof(StepParams), cudaMemcpyHostToDevice, stream_), "H2D");

@@ -76,7 +76,6 @@ struct Stage {
     double *d_val1 = nullptr, *d_val2 = nullptr;
     // impedance wall (bottom regularized entries only)
     double *d_imp = nullptr;
-    double *d_vn = nullptr;     // wall velocity of the current step, when a batch computes it ahead
 
     int imp_nf = 0;
     double imp_alpha = 0.0;
@@ -388,14 +387,8 @@ class Batch {
     ForceSlot *d_force_ = nullptr;
     int4 *d_special_ = nullptr;    // (case, i, j, chunk), shifted storage
     int nspecial_ = 0;
-    // impedance walls advanced ahead of their stage (shifted storage)
-    ImpWall *d_walls_ = nullptr;
-    int2 *d_imp_ = nullptr;         // (wall, first node) per 128-node block
     RecordTask *d_rec_ = nullptr;   // every case's probes and wall traces (case index set)
     int nrec_ = 0;
-    int nimp_ = 0;
-    std::vector<ImpWall> walls_host_;
-    std::vector<int2> wall_at_;     // (level, entry) of each wall's stage
     cudaGraphExec_t pair_exec_ = nullptr;
     std::vector<void *> allocs_;
     // host copies of the per-run parameters (kept until their uploads ran)

@@ -102,16 +102,6 @@ struct StageGroup {
     int warm;   // FP64: run the instruction-cache warm-up pass (small grids)
 };
 
-// An impedance wall of a batch advanced ahead of its stage: the entry's
-// stage parameters for both directions (pair[sel ^ phase[entry]]) and the
-// buffer the stage reads the wall velocities from.
-struct ImpWall {
-    const StageParams *pair;
-    int entry;
-    int pad;
-    double *vn;
-};
-
 // Per-step records, one block per task, launched after a step's last kernel:
 // probes (density and velocity at chosen nodes, from the populations the step
 // left) and impedance-wall traces (the wall's mean p' and v over its active
@@ -198,10 +188,6 @@ cudaError_t special_shifted(const FastStepParams &p, const int2 *nodes, int n, i
 // cut-link records.
 cudaError_t special_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *nodes, int n, int sel,
                                   int store, bool wide, bool force, bool links, bool after, cudaStream_t s);
-// The impedance-wall updates of a batch for one step, nimp blocks of 128
-// nodes, imp[b] = (wall, first node).
-cudaError_t impedance_batch(const int *phase, int sel, const ImpWall *walls, const int2 *imp, int nimp, bool after,
-                            cudaStream_t s);
 // Edge BCs of shifted storage in FP32 (launch::stage_group / stage_batch dispatch here).
 cudaError_t stage_group_shifted(const StageGroup &g, int store, bool collide, bool after_bulk, cudaStream_t s);
 cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, const int2 *blocks, int nblocks,

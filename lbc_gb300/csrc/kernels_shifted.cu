@@ -543,25 +543,6 @@ __global__ void __launch_bounds__(128) k_step_batch_special_shifted(const FastSt
     pdl_wait();
 }
 
-// The impedance walls of a batch, advanced for this step (impedance_ahead):
-// imp[b] = (wall, first node) of 128 nodes, walls[w] = the wall's stage
-// parameters for both directions and its velocity buffer. That FP64 work
-// depends only on the previous step's moments, so it runs beside the
-// latency-bound special nodes, behind the clean pairs, instead of at the head
-// of the edge launch. Its own launch (first of the two) keeps its FP64
-// registers off the special-node kernel.
-__global__ void __launch_bounds__(128) k_impedance_batch(const int *__restrict__ phase, int sel,
-                                                         const ImpWall *__restrict__ walls,
-                                                         const int2 *__restrict__ imp) {
-    pdl_launch_dependents();
-    const int2 b = imp[blockIdx.x];
-    const ImpWall &w = walls[b.x];
-    const StageParams &p = w.pair[sel ^ phase[w.entry]];
-    const int t = b.y + (int)threadIdx.x;
-    if (t < p.along) impedance_ahead(p, w.vn, t);
-    pdl_wait();
-}
-
 // live = false: the same instructions without their stores (the stage
 // threads' instruction-cache warm-up, stage_thread_s). Band populations are
 // read at L2 (__ldcg), never from a possibly stale L1 line.
@@ -695,11 +676,7 @@ __device__ __forceinline__ void stage_thread_s(const StageParams &p, const Finis
 #pragma unroll 1
     for (int pass = 0; pass < 2; pass++) {
         const bool live = pass != 0;
-        if (live) {
-            pdl_wait();
-            // impedance wall advanced ahead (batches): its velocity is ready now
-            if (KIND == BC_VEL_BOT_REG && c.imp && p.vn) c.v2 = -__ldcg(p.vn + t);
-        }
+        if (live) pdl_wait();
         stage_point_s<T>(p, c, t, KIND, live);
         if (c.fin) finish_node_shifted<T, COLLIDE>(f, c.ij, c.slot, live);
     }
@@ -890,12 +867,6 @@ cudaError_t special_batch_shifted(const FastStepParams *sp, const int *phase, co
     if (n % 32) return cudaErrorInvalidValue;
     if (store == STORE_F32) return special_batch_shifted_t<float>(sp, phase, nodes, n, sel, wide, force, links, after, s);
     return special_batch_shifted_t<__half>(sp, phase, nodes, n, sel, wide, force, links, after, s);
-}
-
-cudaError_t impedance_batch(const int *phase, int sel, const ImpWall *walls, const int2 *imp, int nimp, bool after,
-                            cudaStream_t s) {
-    if (nimp == 0) return cudaSuccess;
-    return launch_follower(after, k_impedance_batch, dim3(nimp), dim3(128), s, phase, sel, walls, imp);
 }
 
 template <typename T, bool FORCE, bool ALLFLAGS>

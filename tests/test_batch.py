@@ -84,10 +84,10 @@ def test_batch_info_counts_launches():
     assert nodes == sum(c.nodes for _, c, _, _ in mixed)
     levels = max(s.info().edge_launches for _, _, _, s in mixed)
     assert 1 <= levels <= max(s.info().edge_stages for _, _, _, s in mixed)
-    # clean pairs + the liner's impedance wall + special nodes + one launch
-    # per stage level; the levels also finish the BC-written nodes and reduce
+    # special nodes + clean pairs + one launch per stage level; the levels
+    # also advance the impedance walls, finish the BC-written nodes and reduce
     # the wall forces
-    assert "liner" in MIX and lps == 3 + levels
+    assert lps == 2 + levels
     for _, _, _, s in mixed:
         i = s.info()
         bulk = 2 if i.has_geometry else 1  # flag-free grids: one plain kernel

@@ -1047,7 +1047,7 @@ bool Solver::launch_step_kernels(int src, int dst, bool collide, bool write_macr
 bool Solver::launch_step(int src, int dst, bool collide, bool write_macro, int bparity, cudaStream_t s) {
     if (!launch_step_kernels(src, dst, collide, write_macro, bparity, s)) return false;
     if (!rec_host_.empty())
-        CK(launch::record(d_rec_, (int)rec_host_.size(), d_.store, buf_[dst], nullptr, 0, nullptr, 0, collide,
+        CK(launch::record(d_rec_, (int)rec_host_.size(), d_.store, buf_[dst], nullptr, 0, 0, collide,
                           s ? s : stream_));
     return true;
 }
@@ -1598,13 +1598,7 @@ bool Batch::build() {
     std::vector<int> level_cnt(max_stages_, 0);
     for (Solver *c : cases_)
         for (size_t l = 0; l < c->stage_groups().size(); l++) level_cnt[l] += (int)c->stage_groups()[l].size();
-    // d_phase_ is indexed by case (bulk, finish) and by level entry (stages).
-    int nphase = nc;
-    for (int cnt : level_cnt) nphase = std::max(nphase, cnt);
-    if (!balloc(allocs_, &d_phase_, nphase, stream_) || !balloc(allocs_, &d_fin_, 2 * nc, stream_) ||
-        !balloc(allocs_, &d_force_, force.size(), stream_))
-        return false;
-    CK(cudaMemsetAsync(d_phase_, 0, nphase * sizeof(int), stream_));
+    if (!balloc(allocs_, &d_fin_, 2 * nc, stream_) || !balloc(allocs_, &d_force_, force.size(), stream_)) return false;
     if (nforce_) CK(cudaMemcpyAsync(d_force_, force.data(), force.size() * sizeof(ForceSlot), cudaMemcpyHostToDevice, stream_));
     if (nspecial_) {
         if (!balloc(allocs_, &d_special_, special.size(), stream_)) return false;
@@ -1675,26 +1669,26 @@ bool Batch::build() {
 
 bool Batch::launch_batched(int sel) {
     if (store_ == STORE_F64) {
-        CK(launch::step_batch_exact((const StepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
+        CK(launch::step_batch_exact((const StepParams *)d_sp_, d_tiles_, ntiles_, sel, tws_,
                                     grid_, stream_, cases_[0]->fma64()));
     } else {
         // the clean pairs, then the special nodes overlapping their tail
-        CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_tiles_, ntiles_, sel, tws_,
+        CK(launch::step_batch_shifted((const FastStepParams *)d_sp_, d_tiles_, ntiles_, sel, tws_,
                                       store_, wide_, any_force_, all_flags_, grid_, stream_));
-        CK(launch::special_batch_shifted((const FastStepParams *)d_sp_, d_phase_, d_special_, nspecial_, sel, store_,
+        CK(launch::special_batch_shifted((const FastStepParams *)d_sp_, d_special_, nspecial_, sel, store_,
                                          wide_, any_force_, any_links_, true, stream_));
     }
     bool first = true;
     for (int s = 0; s < max_stages_; s++) {
         if (!stage_nblocks_[s]) continue;
-        CK(launch::stage_batch(d_stage_lists_[s], d_phase_, stage_counts_[s], d_stage_blocks_[s], stage_nblocks_[s],
+        CK(launch::stage_batch(d_stage_lists_[s], stage_counts_[s], d_stage_blocks_[s], stage_nblocks_[s],
                                store_, sel, d_force_, first, nodes_ < (1LL << 20), stream_));
         first = false;
     }
     if (nforce_ && max_stages_ == 0) CK(launch::force_reduce(d_force_, nforce_, true, stream_));
     if (nrec_) {
         const int psize = store_ == STORE_F64 ? (int)sizeof(StepParams) : (int)sizeof(FastStepParams);
-        CK(launch::record(d_rec_, nrec_, store_, nullptr, (const char *)d_sp_, psize, d_phase_, sel, true,
+        CK(launch::record(d_rec_, nrec_, store_, nullptr, (const char *)d_sp_, psize, sel, true,
                           stream_));
     }
     return true;

@@ -375,7 +375,6 @@ class Batch {
     bool any_links_ = false;  // some case has cut-link records
     int launches_per_step_ = 0;
     void *d_sp_ = nullptr;         // StepParams or FastStepParams [2 * ncases]
-    int *d_phase_ = nullptr;       // [ncases] (and stage entries)
     int4 *d_tiles_ = nullptr;
     std::vector<StageParams *> d_stage_lists_;
     std::vector<int> stage_counts_;

@@ -125,12 +125,12 @@ struct RecordTask {
 namespace launch {
 // Records of one step: tasks[0 .. n). Alone: the step's populations are at
 // dst. In a batch (spbase set): case cs's are the dst of its step parameters
-// for this direction, spbase + (2 cs + (sel ^ phase[cs])) * spstride bytes.
+// for this direction, spbase + (2 cs + sel) * spstride bytes.
 // collided: the step ended with a collision (Guo's forcing then added F to the
 // momentum, so u = (j - F / 2) / rho); a run's last step leaves pre-collision
 // populations (u = (j + F / 2) / rho, as lbc's moments).
 cudaError_t record(const RecordTask *tasks, int n, int store, const void *dst, const char *spbase, int spstride,
-                   const int *phase, int sel, bool collided, cudaStream_t s);
+                   int sel, bool collided, cudaStream_t s);
 // FP64 (kernels_exact.cu): lbc's rounding sequence, or with fma set the
 // fused multiply-add arithmetic (moments_fma / collide_fma)
 cudaError_t step_exact(const StepParams &p, bool flags, bool collide, dim3 block, cudaStream_t s,
@@ -163,7 +163,7 @@ cudaError_t fp64_rate(int blocks, int iters, double *sink, cudaStream_t s);
 
 // batches of cases (tile list = int4 {case, x0, y0, case has wall links})
 // Tiles of 2^tws x 2^(8 - tws) nodes, tws in [5, 8].
-cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 *tiles, int ntiles,
+cudaError_t step_batch_exact(const StepParams *sp, const int4 *tiles, int ntiles,
                              int sel, int tws, int grid, cudaStream_t s, bool fma = false);
 int step_batch_exact_grid();
 // One level of a batch's Boundary lists (n entries): block b steps points
@@ -171,7 +171,7 @@ int step_batch_exact_grid();
 // blocks[b].x >= n, reduces force slot fs[blocks[b].x - n].
 // warm: FP64 only, run the edge threads' instruction-cache warm-up pass.
 constexpr int kStageBatchPoints = 64, kStageBatchPointsF64 = 32;
-cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, const int2 *blocks, int nblocks,
+cudaError_t stage_batch(const StageParams *list, int n, const int2 *blocks, int nblocks,
                         int store, int sel, const ForceSlot *fs, bool after_bulk, bool warm, cudaStream_t s);
 cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStream_t s);
 
@@ -186,17 +186,17 @@ cudaError_t special_shifted(const FastStepParams &p, const int2 *nodes, int n, i
 // The special nodes of a batch: nodes[q] = (case, i, j, chunk), n a multiple
 // of 32 (each case's list padded to 32 entries, i = -1); links: some case has
 // cut-link records.
-cudaError_t special_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *nodes, int n, int sel,
+cudaError_t special_batch_shifted(const FastStepParams *sp, const int4 *nodes, int n, int sel,
                                   int store, bool wide, bool force, bool links, bool after, cudaStream_t s);
 // Edge BCs of shifted storage in FP32 (launch::stage_group / stage_batch dispatch here).
 cudaError_t stage_group_shifted(const StageGroup &g, int store, bool collide, bool after_bulk, cudaStream_t s);
-cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, const int2 *blocks, int nblocks,
+cudaError_t stage_batch_shifted(const StageParams *list, int n, const int2 *blocks, int nblocks,
                                 int store, int sel, const ForceSlot *fs, bool after_bulk, cudaStream_t s);
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s);
 // wide: some case has 9 * plane >= 2^31 elements (64-bit element offsets).
 // force: some case has a body force (the forced kernel form serves all cases).
 // all_flags: every case has a flag word (the flag-free pair form is left out).
-cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
+cudaError_t step_batch_shifted(const FastStepParams *sp, const int4 *tiles,
                                int ntiles, int sel, int tws, int store, bool wide, bool force, bool all_flags,
                                int grid, cudaStream_t s);
 int step_batch_shifted_grid(int store);

@@ -147,20 +147,19 @@ __global__ void __launch_bounds__(256) k_step_exact(const StepParams p) {
 // Many cases in one launch: a persistent loop over a flattened list of
 // 2D tiles (one tile = one thread block's worth of nodes of one case: 256
 // threads as 2^tws x 2^(8 - tws) nodes). Each case brings its own parameters
-// (sp[2 * c + (sel ^ phase[c])]: the two ping-pong directions), so uneven
+// (sp[2 * c + sel]: the two ping-pong directions), so uneven
 // grids and different geometries share the launch. Force partials go to each
 // case's own segment slots (td.w != 0: the tile contains wall links), reduced
 // per case by k_force_reduce exactly as when the case runs alone.
 template <bool FMA>
 __global__ void __launch_bounds__(256) k_step_batch_exact(const StepParams *__restrict__ sp,
-                                                          const int *__restrict__ phase,
                                                           const int4 *__restrict__ tiles, int ntiles,
                                                           int sel, int tws) {
     pdl_launch_dependents();
     const int tx = threadIdx.x & ((1 << tws) - 1), ty = threadIdx.x >> tws;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int4 td = tiles[t];
-        const StepParams &p = sp[2 * td.x + (sel ^ phase[td.x])];
+        const StepParams &p = sp[2 * td.x + sel];
         const int i = td.y + tx, j = td.z + ty;
         double mfx = 0.0, mfy = 0.0;
         bool link = false;
@@ -305,10 +304,10 @@ __global__ void k_stage_group(const StageGroup g) {
 }
 
 // Stage level of every case of a batch: block b steps points blk[b].y ..
-// of entry e = blk[b].x, list[2 * e + (sel ^ phase)] its parameters for this
+// of entry e = blk[b].x, list[2 * e + sel] its parameters for this
 // ping-pong direction; e >= n: reduce force slot fs[e - n].
 template <typename T>
-__global__ void k_stage_batch(const StageParams *__restrict__ list, const int *__restrict__ ephase,
+__global__ void k_stage_batch(const StageParams *__restrict__ list,
                               const int2 *__restrict__ blk, int sel, int n, const ForceSlot *__restrict__ fs,
                               int warm) {
     const int2 b = blk[blockIdx.x];
@@ -318,7 +317,7 @@ __global__ void k_stage_batch(const StageParams *__restrict__ list, const int *_
         if (threadIdx.x < 32) force_reduce_warp(fs[e - n], (int)threadIdx.x);
         return;
     }
-    const StageParams &p = list[2 * e + (sel ^ ephase[e])];
+    const StageParams &p = list[2 * e + sel];
     const int t = b.y + (int)threadIdx.x;
     if (t >= p.along) return;
     stage_dispatch<T, true>(p, *p.fin, t, warm);
@@ -659,7 +658,7 @@ __global__ void k_sponge(int Nx, int Ny, double dx, double xc, double yc, double
 // step land in the same ring slot.
 template <typename T>
 __global__ void __launch_bounds__(256) k_record(const RecordTask *__restrict__ tasks, const void *dst,
-                                                const char *spbase, int spstride, const int *phase, int sel,
+                                                const char *spbase, int spstride, int sel,
                                                 int collided) {
     __shared__ double sp_[256], sv_[256];
     __shared__ int sn_[256];
@@ -669,7 +668,7 @@ __global__ void __launch_bounds__(256) k_record(const RecordTask *__restrict__ t
     if (r.kind == REC_PROBES) {
         const void *buf = dst;
         if (spbase)
-            buf = ((const StepParams *)(spbase + (size_t)(2 * r.cs + (sel ^ phase[r.cs])) * spstride))->dst;
+            buf = ((const StepParams *)(spbase + (size_t)(2 * r.cs + sel) * spstride))->dst;
         const T *f = (const T *)buf;
         for (int q = threadIdx.x; q < r.n; q += blockDim.x) {
             const long long o = r.nodes[q];
@@ -744,12 +743,12 @@ __global__ void __launch_bounds__(256) k_fp64_rate(double *sink, int iters, doub
 namespace launch {
 
 cudaError_t record(const RecordTask *tasks, int n, int store, const void *dst, const char *spbase, int spstride,
-                   const int *phase, int sel, bool collided, cudaStream_t s) {
+                   int sel, bool collided, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     const int c = collided ? 1 : 0;
-    if (store == STORE_F64) k_record<double><<<n, 256, 0, s>>>(tasks, dst, spbase, spstride, phase, sel, c);
-    else if (store == STORE_F32) k_record<float><<<n, 256, 0, s>>>(tasks, dst, spbase, spstride, phase, sel, c);
-    else k_record<__half><<<n, 256, 0, s>>>(tasks, dst, spbase, spstride, phase, sel, c);
+    if (store == STORE_F64) k_record<double><<<n, 256, 0, s>>>(tasks, dst, spbase, spstride, sel, c);
+    else if (store == STORE_F32) k_record<float><<<n, 256, 0, s>>>(tasks, dst, spbase, spstride, sel, c);
+    else k_record<__half><<<n, 256, 0, s>>>(tasks, dst, spbase, spstride, sel, c);
     return cudaGetLastError();
 }
 
@@ -795,12 +794,12 @@ cudaError_t stage_group(const StageGroup &g, int store, bool collide, bool after
     return launch_follower(after_bulk, k_stage_group<double, false>, grid, dim3(32), s, g);
 }
 
-cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 *tiles, int ntiles,
+cudaError_t step_batch_exact(const StepParams *sp, const int4 *tiles, int ntiles,
                              int sel, int tws, int grid, cudaStream_t s, bool fma) {
     if (ntiles == 0) return cudaSuccess;
     if (tws < 5 || tws > 8) return cudaErrorInvalidValue;
-    if (fma) k_step_batch_exact<true><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
-    else k_step_batch_exact<false><<<grid, 256, 0, s>>>(sp, phase, tiles, ntiles, sel, tws);
+    if (fma) k_step_batch_exact<true><<<grid, 256, 0, s>>>(sp, tiles, ntiles, sel, tws);
+    else k_step_batch_exact<false><<<grid, 256, 0, s>>>(sp, tiles, ntiles, sel, tws);
     return cudaGetLastError();
 }
 
@@ -811,12 +810,12 @@ cudaError_t step_batch_exact(const StepParams *sp, const int *phase, const int4 
 // free up. Measured on 64 liner ducts: 4.03 GLUPS persistent, 4.10 per tile.
 int step_batch_exact_grid() { return 1 << 30; }
 
-cudaError_t stage_batch(const StageParams *list, const int *ephase, int n, const int2 *blocks, int nblocks,
+cudaError_t stage_batch(const StageParams *list, int n, const int2 *blocks, int nblocks,
                         int store, int sel, const ForceSlot *fs, bool after_bulk, bool warm, cudaStream_t s) {
     if (nblocks == 0) return cudaSuccess;
-    if (store != STORE_F64) return stage_batch_shifted(list, ephase, n, blocks, nblocks, store, sel, fs, after_bulk, s);
+    if (store != STORE_F64) return stage_batch_shifted(list, n, blocks, nblocks, store, sel, fs, after_bulk, s);
     return launch_follower(after_bulk, k_stage_batch<double>, dim3(nblocks), dim3(kStageBatchPointsF64), s, list,
-                           ephase, blocks, sel, n, fs, warm ? 1 : 0);
+                           blocks, sel, n, fs, warm ? 1 : 0);
 }
 
 cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStream_t s) {

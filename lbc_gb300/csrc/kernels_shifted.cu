@@ -495,14 +495,13 @@ __global__ void __launch_bounds__(128) k_step_special_shifted(const FastStepPara
 // (sequential DRAM streams, halo rows shared through L2).
 template <typename T, typename I, bool FORCE, bool ALLFLAGS>
 __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepParams *__restrict__ sp,
-                                                            const int *__restrict__ phase,
                                                             const int4 *__restrict__ tiles,
                                                             int ntiles, int sel, int tws) {
     pdl_launch_dependents();
     const int tx = threadIdx.x & ((1 << tws) - 1), ty = threadIdx.x >> tws;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int4 td = tiles[t];
-        const FastStepParams &fp = sp[2 * td.x + (sel ^ phase[td.x])];
+        const FastStepParams &fp = sp[2 * td.x + sel];
         const int i0 = td.y + 2 * tx, j = td.z + ty;
         // FORCE: some case of the batch has a body force; force-free cases
         // still take their own (force-free) arithmetic per case (collide_v).
@@ -522,14 +521,13 @@ __global__ void __launch_bounds__(256, 4) k_step_batch_shifted(const FastStepPar
 // the case alone. LINKS: some case of the batch has cut-link records.
 template <typename T, typename I, bool FORCE, bool LINKS>
 __global__ void __launch_bounds__(128) k_step_batch_special_shifted(const FastStepParams *__restrict__ sp,
-                                                                    const int *__restrict__ phase,
                                                                     const int4 *__restrict__ nodes, int n,
                                                                     int sel) {
     pdl_launch_dependents();
     const int q = (int)blockIdx.x * (int)blockDim.x + (int)threadIdx.x;
     if (q < n) {  // n is a multiple of 32: whole warps
         const int4 e = nodes[q];
-        const FastStepParams &fp = sp[2 * e.x + (sel ^ phase[e.x])];
+        const FastStepParams &fp = sp[2 * e.x + sel];
         float mx = 0.f, my = 0.f;
         bool link = false;
         if (e.y & kSpecialSolid) solid_nan(fp.s, e.y & ~kSpecialSolid, e.z);
@@ -713,7 +711,7 @@ __global__ void k_stage_group_shifted(const StageGroup g) {
 }
 
 template <typename T>
-__global__ void k_stage_batch_shifted(const StageParams *__restrict__ list, const int *__restrict__ ephase,
+__global__ void k_stage_batch_shifted(const StageParams *__restrict__ list,
                                       const int2 *__restrict__ blk, int sel, int n,
                                       const ForceSlot *__restrict__ fs) {
     const int2 b = blk[blockIdx.x];
@@ -723,7 +721,7 @@ __global__ void k_stage_batch_shifted(const StageParams *__restrict__ list, cons
         if (threadIdx.x < 32) force_reduce_warp(fs[e - n], (int)threadIdx.x);
         return;
     }
-    const StageParams &p = list[2 * e + (sel ^ ephase[e])];
+    const StageParams &p = list[2 * e + sel];
     const int t = b.y + (int)threadIdx.x;
     if (t >= p.along) return;
     stage_dispatch_s<T, true>(p, *p.fin, t);
@@ -741,13 +739,13 @@ cudaError_t stage_group_shifted(const StageGroup &g, int store, bool collide, bo
     return launch_follower(after_bulk, k_stage_group_shifted<__half, false>, grid, b, s, g);
 }
 
-cudaError_t stage_batch_shifted(const StageParams *list, const int *ephase, int n, const int2 *blocks, int nblocks,
+cudaError_t stage_batch_shifted(const StageParams *list, int n, const int2 *blocks, int nblocks,
                                 int store, int sel, const ForceSlot *fs, bool after_bulk, cudaStream_t s) {
     if (nblocks == 0) return cudaSuccess;
     const dim3 g(nblocks), b(kStageBatchPoints);
     if (store == STORE_F32)
-        return launch_follower(after_bulk, k_stage_batch_shifted<float>, g, b, s, list, ephase, blocks, sel, n, fs);
-    return launch_follower(after_bulk, k_stage_batch_shifted<__half>, g, b, s, list, ephase, blocks, sel, n, fs);
+        return launch_follower(after_bulk, k_stage_batch_shifted<float>, g, b, s, list, blocks, sel, n, fs);
+    return launch_follower(after_bulk, k_stage_batch_shifted<__half>, g, b, s, list, blocks, sel, n, fs);
 }
 
 cudaError_t collide_shifted(const CollideParams &p, int store, cudaStream_t s) {
@@ -840,54 +838,53 @@ cudaError_t special_shifted(const FastStepParams &p, const int2 *nodes, int n, i
 }
 
 template <typename T, bool FORCE, bool LINKS>
-static cudaError_t special_batch_shifted_tfl(const FastStepParams *sp, const int *phase, const int4 *nodes, int n,
+static cudaError_t special_batch_shifted_tfl(const FastStepParams *sp, const int4 *nodes, int n,
                                              int sel, bool wide, bool after, cudaStream_t s) {
     const dim3 g((n + 127) / 128), b(128);
     if (wide)
-        return launch_follower(after, k_step_batch_special_shifted<T, long long, FORCE, LINKS>, g, b, s, sp, phase,
-                               nodes, n, sel);
-    return launch_follower(after, k_step_batch_special_shifted<T, int, FORCE, LINKS>, g, b, s, sp, phase, nodes, n,
-                           sel);
+        return launch_follower(after, k_step_batch_special_shifted<T, long long, FORCE, LINKS>, g, b, s, sp, nodes,
+                               n, sel);
+    return launch_follower(after, k_step_batch_special_shifted<T, int, FORCE, LINKS>, g, b, s, sp, nodes, n, sel);
 }
 
 template <typename T>
-static cudaError_t special_batch_shifted_t(const FastStepParams *sp, const int *phase, const int4 *nodes, int n,
+static cudaError_t special_batch_shifted_t(const FastStepParams *sp, const int4 *nodes, int n,
                                            int sel, bool wide, bool force, bool links, bool after, cudaStream_t s) {
     if (force) {
-        if (links) return special_batch_shifted_tfl<T, true, true>(sp, phase, nodes, n, sel, wide, after, s);
-        return special_batch_shifted_tfl<T, true, false>(sp, phase, nodes, n, sel, wide, after, s);
+        if (links) return special_batch_shifted_tfl<T, true, true>(sp, nodes, n, sel, wide, after, s);
+        return special_batch_shifted_tfl<T, true, false>(sp, nodes, n, sel, wide, after, s);
     }
-    if (links) return special_batch_shifted_tfl<T, false, true>(sp, phase, nodes, n, sel, wide, after, s);
-    return special_batch_shifted_tfl<T, false, false>(sp, phase, nodes, n, sel, wide, after, s);
+    if (links) return special_batch_shifted_tfl<T, false, true>(sp, nodes, n, sel, wide, after, s);
+    return special_batch_shifted_tfl<T, false, false>(sp, nodes, n, sel, wide, after, s);
 }
 
-cudaError_t special_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *nodes, int n, int sel,
+cudaError_t special_batch_shifted(const FastStepParams *sp, const int4 *nodes, int n, int sel,
                                   int store, bool wide, bool force, bool links, bool after, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     if (n % 32) return cudaErrorInvalidValue;
-    if (store == STORE_F32) return special_batch_shifted_t<float>(sp, phase, nodes, n, sel, wide, force, links, after, s);
-    return special_batch_shifted_t<__half>(sp, phase, nodes, n, sel, wide, force, links, after, s);
+    if (store == STORE_F32) return special_batch_shifted_t<float>(sp, nodes, n, sel, wide, force, links, after, s);
+    return special_batch_shifted_t<__half>(sp, nodes, n, sel, wide, force, links, after, s);
 }
 
 template <typename T, bool FORCE, bool ALLFLAGS>
-static cudaError_t step_batch_shifted_tfa(const FastStepParams *sp, const int *phase, const int4 *tiles, int ntiles,
+static cudaError_t step_batch_shifted_tfa(const FastStepParams *sp, const int4 *tiles, int ntiles,
                                           int sel, int tws, bool wide, int grid, bool after, cudaStream_t s) {
     if (wide)
         return launch_follower(after, k_step_batch_shifted<T, long long, FORCE, ALLFLAGS>, dim3(grid), dim3(256), s,
-                               sp, phase, tiles, ntiles, sel, tws);
-    return launch_follower(after, k_step_batch_shifted<T, int, FORCE, ALLFLAGS>, dim3(grid), dim3(256), s, sp, phase,
-                           tiles, ntiles, sel, tws);
+                               sp, tiles, ntiles, sel, tws);
+    return launch_follower(after, k_step_batch_shifted<T, int, FORCE, ALLFLAGS>, dim3(grid), dim3(256), s, sp, tiles,
+                           ntiles, sel, tws);
 }
 
 template <typename T, bool FORCE>
-static cudaError_t step_batch_shifted_tf(const FastStepParams *sp, const int *phase, const int4 *tiles, int ntiles,
+static cudaError_t step_batch_shifted_tf(const FastStepParams *sp, const int4 *tiles, int ntiles,
                                          int sel, int tws, bool wide, bool all_flags, int grid, bool after,
                                          cudaStream_t s) {
-    if (all_flags) return step_batch_shifted_tfa<T, FORCE, true>(sp, phase, tiles, ntiles, sel, tws, wide, grid, after, s);
-    return step_batch_shifted_tfa<T, FORCE, false>(sp, phase, tiles, ntiles, sel, tws, wide, grid, after, s);
+    if (all_flags) return step_batch_shifted_tfa<T, FORCE, true>(sp, tiles, ntiles, sel, tws, wide, grid, after, s);
+    return step_batch_shifted_tfa<T, FORCE, false>(sp, tiles, ntiles, sel, tws, wide, grid, after, s);
 }
 
-cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const int4 *tiles,
+cudaError_t step_batch_shifted(const FastStepParams *sp, const int4 *tiles,
                                int ntiles, int sel, int tws, int store, bool wide, bool force, bool all_flags,
                                int grid, cudaStream_t s) {
     const bool after_special = false;  // an ordinary launch
@@ -895,15 +892,15 @@ cudaError_t step_batch_shifted(const FastStepParams *sp, const int *phase, const
     if (tws < 5 || tws > 8) return cudaErrorInvalidValue;
     if (store == STORE_F32) {
         if (force)
-            return step_batch_shifted_tf<float, true>(sp, phase, tiles, ntiles, sel, tws, wide, all_flags, grid,
+            return step_batch_shifted_tf<float, true>(sp, tiles, ntiles, sel, tws, wide, all_flags, grid,
                                                       after_special, s);
-        return step_batch_shifted_tf<float, false>(sp, phase, tiles, ntiles, sel, tws, wide, all_flags, grid,
+        return step_batch_shifted_tf<float, false>(sp, tiles, ntiles, sel, tws, wide, all_flags, grid,
                                                    after_special, s);
     }
     if (force)
-        return step_batch_shifted_tf<__half, true>(sp, phase, tiles, ntiles, sel, tws, wide, all_flags, grid,
+        return step_batch_shifted_tf<__half, true>(sp, tiles, ntiles, sel, tws, wide, all_flags, grid,
                                                    after_special, s);
-    return step_batch_shifted_tf<__half, false>(sp, phase, tiles, ntiles, sel, tws, wide, all_flags, grid,
+    return step_batch_shifted_tf<__half, false>(sp, tiles, ntiles, sel, tws, wide, all_flags, grid,
                                                 after_special, s);
 }
 

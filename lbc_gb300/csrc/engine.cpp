@@ -310,15 +310,37 @@ bool Solver::build_geometry() {
     has_flags_ = any_special || !stages_.empty() || !d_.px || !d_.py;
     // Shifted storage: the nodes the clean-pair kernels leave out (both nodes
     // of every pair (2m, 2m + 1) of a row with a special node, and the last
-    // column of an odd-width grid), in row-major order. Solid nodes off the
-    // edge band are marked (kSpecialSolid in x): their step only writes NaN
-    // moments on steps that write the fields, with no load but the entry.
+    // column of an odd-width grid), in row-major order. Solid nodes whose band
+    // values no BC reads (off the band, or on it but the neighbour of no fluid
+    // BC node: a BC reads only its node and that neighbour) are marked
+    // (kSpecialSolid in x): their step only writes NaN moments on steps that
+    // write the fields, with no load but the entry.
     special_host_.clear();
     if (d_.store != STORE_F64) {
         const uint16_t slow = NF_SPECIAL_MASK | NF_SOLID | NF_BAND | NF_BCW | NF_LINKS;
+        std::vector<uint8_t> read_solid((size_t)std::max(nslots_, 1), 0);
+        for (const Stage &st : stages_) {
+            if (st.kind == BC_PERIODIC_X || st.kind == BC_PERIODIC_Y) continue;
+            const bool col = bc_is_column(st.kind);
+            for (int t = 0; t < st.along; t++) {
+                const int i = col ? st.index : t, j = col ? t : st.index;
+                if (solid(i, j)) continue;
+                int ni = i, nj = j;
+                switch (st.kind) {
+                case BC_PRES_IN_ZH: case BC_CONV_IN: case BC_VEL_IN_REG: case BC_PRES_IN_REG: ni = i + 1; break;
+                case BC_PRES_OUT_ZH: case BC_CONV_OUT: case BC_VEL_OUT_REG: case BC_PRES_OUT_REG: ni = i - 1; break;
+                case BC_VEL_BOT_REG: case BC_PRES_BOT_REG: nj = j + 1; break;
+                case BC_VEL_TOP_REG: case BC_PRES_TOP_REG: nj = j - 1; break;
+                default: continue;
+                }
+                if (ni < 0 || ni >= Nx || nj < 0 || nj >= Ny || !solid(ni, nj)) continue;
+                read_solid[(size_t)slot_of(ni, nj)] = 1;
+            }
+        }
         auto entry = [&](int i, int j) {
             const uint16_t f = flags[(size_t)j * pitch_ + i];
-            const bool mark = (f & NF_SOLID) && !(f & NF_BAND) && Nx <= kSpecialSolid;
+            const bool unread = !(f & NF_BAND) || !read_solid[(size_t)slot_of(i, j)];
+            const bool mark = (f & NF_SOLID) && unread && Nx <= kSpecialSolid;
             return make_int2(mark ? (i | kSpecialSolid) : i, j);
         };
         for (int j = 0; j < Ny; j++)

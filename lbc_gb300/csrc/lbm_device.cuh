@@ -619,8 +619,8 @@ struct FinishParams {
 };
 
 // Special-node list entries (shifted storage): bit 30 of the column marks a
-// solid node off the edge band, whose step only writes NaN moments on steps
-// that write the fields (grids narrower than 2^30 columns).
+// solid node whose band values no BC reads, whose step only writes NaN
+// moments on steps that write the fields (grids narrower than 2^30 columns).
 constexpr int kSpecialSolid = 1 << 30;
 
 // Both bases are loaded at once (rowbase[j] is in bounds whatever colbase[i]

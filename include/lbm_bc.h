@@ -81,6 +81,14 @@ void pressure_top_regularized(LBM_BC_PARAMS);
 /* lbc include/lbm_bc.h:339-355, src/bc/pressure_bottom_regularized.c */
 void pressure_bottom_regularized(LBM_BC_PARAMS);
 
+/* Extension (no counterpart in lbc): velocity_bottom with the Zou-He closure
+ * for population 6, f6 = f8 + (f1 - f3)/2 - rho U/2 + rho V/6. lbc's
+ * velocity_bottom (src/bc/velocity_bottom.c:39) writes that value to
+ * population 7 a second time and leaves 6 as streamed; velocity_bottom keeps
+ * lbc's behaviour for drop-in parity, and a case opts into the corrected
+ * closure by putting this function in its Boundary list. */
+void velocity_bottom_corrected(LBM_BC_PARAMS);
+
 
 #ifdef __cplusplus
 }

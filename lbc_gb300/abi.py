@@ -44,6 +44,8 @@ _BC_NAMES = (
     "pressure_inlet_regularized", "pressure_outlet_regularized",
     "pressure_top_regularized", "pressure_bottom_regularized",
 )
+# Extensions with no counterpart in lbc (its own build does not export them).
+_BC_EXT_NAMES = ("velocity_bottom_corrected",)
 
 
 class LbcAbi:
@@ -67,6 +69,9 @@ class LbcAbi:
         g("sponge_layer", None, [C.c_int, C.c_int] + [C.c_double] * 8 + [_dp])
         for n in _BC_NAMES:
             g(n, None, _BC_ARGS)
+        for n in _BC_EXT_NAMES:
+            if hasattr(self.lib, self.prefix + n):
+                g(n, None, _BC_ARGS)
 
     def _fn(self, name, restype, argtypes):
         fn = getattr(self.lib, self.prefix + name)

@@ -35,7 +35,7 @@ BC_COLUMN = (
     "convective_inlet", "convective_outlet",
 )
 BC_ROW = (
-    "velocity_top", "velocity_bottom",
+    "velocity_top", "velocity_bottom", "velocity_bottom_corrected",
     "velocity_top_regularized", "velocity_bottom_regularized",
     "pressure_top_regularized", "pressure_bottom_regularized",
 )
@@ -132,6 +132,19 @@ def poiseuille(Nx: int = 256, Ny: int = 64, tau: float = 0.8, Fx: float = 1e-6):
     f = np.empty((Ny, Nx, Q))
     f[:] = W  # f = w rho0 (cases/poiseuille/poiseuille.c:100-105)
     return case, State(f, f.copy(), rho, zero, zero.copy())
+
+
+def couette_zh(Nx: int = 16, Ny: int = 12, tau: float = 0.8, U: float = 0.05,
+               bottom: str = "velocity_bottom_corrected"):
+    """Plane Couette flow between Zou-He walls, periodic in x: the bottom row
+    moves at U (`bottom`: velocity_bottom_corrected or lbc's velocity_bottom),
+    the top row is at rest (velocity_top). The steady profile is linear between
+    the wall nodes, u(j) = U (1 - j / (Ny - 1))."""
+    mask = np.zeros((Ny, Nx), dtype=np.int32)
+    bcs = [BC("periodic_x"), BC(bottom, 0, np.full(Nx, U), np.zeros(Nx)),
+           BC("velocity_top", Ny - 1, np.zeros(Nx), np.zeros(Nx))]
+    case = Case("couette_zh", Nx, Ny, mask, _uniform(Ny, Nx, 1.0 / tau), _uniform(Ny, Nx, 0.0), bcs)
+    return case, equilibrium_state(_uniform(Ny, Nx, 1.0), _uniform(Ny, Nx, 0.0), _uniform(Ny, Nx, 0.0))
 
 
 def poiseuille_analytic(Ny: int, tau: float, Fx: float) -> np.ndarray:

@@ -132,14 +132,15 @@ __device__ __forceinline__ void bc_apply_s(A &a, const float w[9], int kind, int
         a.set(ib, jb, 7, g5 + 0.5f * (g1 - g3) - 0.5f * r * U - c16 * r * V);
         a.set(ib, jb, 8, g6 - 0.5f * (g1 - g3) + 0.5f * r * U - c16 * r * V);
     } break;
-    case BC_VEL_BOT_ZH: {  // src/bc/velocity_bottom.c:25-39 (second write to 7 kept, :39)
+    case BC_VEL_BOT_ZH:      // src/bc/velocity_bottom.c:25-39 (second write to 7 kept, :39)
+    case BC_VEL_BOT_ZH_FIX: {  // the same, the last line written to 6
         const float U = (float)v1, V = (float)v2;
         const float g0 = a.get(ib, jb, 0), g1 = a.get(ib, jb, 1), g3 = a.get(ib, jb, 3),
                     g4 = a.get(ib, jb, 4), g7 = a.get(ib, jb, 7), g8 = a.get(ib, jb, 8);
         const float r = (1.0f + (g0 + g1 + g3 + 2.0f * (g4 + g7 + g8))) / (1.0f - V);
         a.set(ib, jb, 2, g4 + c23 * r * V);
         a.set(ib, jb, 5, g7 - 0.5f * (g1 - g3) + 0.5f * r * U + c16 * r * V);
-        a.set(ib, jb, 7, g8 + 0.5f * (g1 - g3) - 0.5f * r * U + c16 * r * V);
+        a.set(ib, jb, kind == BC_VEL_BOT_ZH_FIX ? 6 : 7, g8 + 0.5f * (g1 - g3) - 0.5f * r * U + c16 * r * V);
     } break;
     case BC_PRES_IN_ZH: {  // src/bc/pressure_inlet.c:25-39
         const float R = (float)v1, dR = (float)(v1 - 1.0);

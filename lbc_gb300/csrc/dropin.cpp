@@ -168,6 +168,7 @@ int lbm::bc_kind_of(const void *fn) {
         {(const void *)&pressure_outlet_regularized, BC_PRES_OUT_REG, "pressure_outlet_regularized"},
         {(const void *)&pressure_top_regularized, BC_PRES_TOP_REG, "pressure_top_regularized"},
         {(const void *)&pressure_bottom_regularized, BC_PRES_BOT_REG, "pressure_bottom_regularized"},
+        {(const void *)&velocity_bottom_corrected, BC_VEL_BOT_ZH_FIX, "velocity_bottom_corrected"},
     };
     for (const auto &t : tab)
         if (t.p == fn) return t.kind;
@@ -498,7 +499,7 @@ static void run_bc(const char *name, int kind, int Nx, int Ny, int Q, int index,
     okk = okk && up(SL_MASK, solid_mask, N * 4, &p); a.mask = (int *)p;
     if (per) { okk = okk && up(SL_F, f, N * 9 * 8, &p); a.f = (double *)p; }
     const bool needs_fields = !per && kind != BC_VEL_IN_ZH && kind != BC_VEL_OUT_ZH &&
-                              kind != BC_VEL_TOP_ZH && kind != BC_VEL_BOT_ZH &&
+                              kind != BC_VEL_TOP_ZH && kind != BC_VEL_BOT_ZH && kind != BC_VEL_BOT_ZH_FIX &&
                               kind != BC_CONV_IN && kind != BC_CONV_OUT;
     if (needs_fields) {
         okk = okk && up(SL_RHO, rho, N * 8, &p); a.rho = (double *)p;
@@ -544,6 +545,8 @@ LBM_DEFINE_BC(pressure_inlet_regularized, BC_PRES_IN_REG)
 LBM_DEFINE_BC(pressure_outlet_regularized, BC_PRES_OUT_REG)
 LBM_DEFINE_BC(pressure_top_regularized, BC_PRES_TOP_REG)
 LBM_DEFINE_BC(pressure_bottom_regularized, BC_PRES_BOT_REG)
+// extension: the corrected Zou-He bottom closure (lbm_bc.h)
+LBM_DEFINE_BC(velocity_bottom_corrected, BC_VEL_BOT_ZH_FIX)
 
 extern "C" {
 

@@ -192,7 +192,7 @@ bool Solver::build_geometry() {
         case BC_PERIODIC_X: okk = need(true, 0, true) && need(true, Nx - 1, true); break;
         case BC_PERIODIC_Y: okk = need(false, 0, true) && need(false, Ny - 1, true); break;
         case BC_VEL_IN_ZH: case BC_VEL_OUT_ZH: okk = need(true, x, true); break;
-        case BC_VEL_TOP_ZH: case BC_VEL_BOT_ZH: okk = need(false, x, true); break;
+        case BC_VEL_TOP_ZH: case BC_VEL_BOT_ZH: case BC_VEL_BOT_ZH_FIX: okk = need(false, x, true); break;
         case BC_PRES_IN_ZH: case BC_CONV_IN: case BC_VEL_IN_REG: case BC_PRES_IN_REG:
             okk = need(true, x, true) && need(true, x + 1, false); break;
         case BC_PRES_OUT_ZH: case BC_CONV_OUT: case BC_VEL_OUT_REG: case BC_PRES_OUT_REG:
@@ -484,7 +484,7 @@ bool Solver::group_stages(const Solid &solid, const std::vector<int> &colbase, c
         case BC_PERIODIC_X: line(true, 0, 0, 0, false); line(true, Nx - 1, 0, 0, false); r.clear(); break;
         case BC_PERIODIC_Y: line(false, 0, 0, 0, false); line(false, Ny - 1, 0, 0, false); r.clear(); break;
         case BC_VEL_IN_ZH: case BC_VEL_OUT_ZH: case BC_PRES_IN_ZH: case BC_PRES_OUT_ZH: line(true, x, 0, 0, false); break;
-        case BC_VEL_TOP_ZH: case BC_VEL_BOT_ZH: line(false, x, 0, 0, false); break;
+        case BC_VEL_TOP_ZH: case BC_VEL_BOT_ZH: case BC_VEL_BOT_ZH_FIX: line(false, x, 0, 0, false); break;
         case BC_CONV_IN: case BC_VEL_IN_REG: case BC_PRES_IN_REG: line(true, x, 1, 0, true); break;
         case BC_CONV_OUT: case BC_VEL_OUT_REG: case BC_PRES_OUT_REG: line(true, x, -1, 0, true); break;
         case BC_VEL_BOT_REG: case BC_PRES_BOT_REG: line(false, x, 0, 1, true); break;

@@ -280,6 +280,7 @@ __device__ __forceinline__ void stage_dispatch(const StageParams &p, const Finis
     LBM_STAGE_KIND(BC_PERIODIC_Y) LBM_STAGE_KIND(BC_VEL_IN_REG) LBM_STAGE_KIND(BC_VEL_OUT_REG)
     LBM_STAGE_KIND(BC_VEL_TOP_REG) LBM_STAGE_KIND(BC_VEL_BOT_REG) LBM_STAGE_KIND(BC_PRES_IN_REG)
     LBM_STAGE_KIND(BC_PRES_OUT_REG) LBM_STAGE_KIND(BC_PRES_TOP_REG) LBM_STAGE_KIND(BC_PRES_BOT_REG)
+    LBM_STAGE_KIND(BC_VEL_BOT_ZH_FIX)
 #undef LBM_STAGE_KIND
     default: pdl_wait(); break;
     }

@@ -45,7 +45,8 @@ struct Link {
 };
 static_assert(sizeof(Link) == 32, "Link layout");
 
-// Edge-BC kinds (lbc's 18 BC functions that act on populations).
+// Edge-BC kinds (lbc's 18 BC functions that act on populations, then the
+// extensions this library adds).
 enum BCKind : int {
     BC_VEL_IN_ZH = 0, BC_VEL_OUT_ZH, BC_VEL_TOP_ZH, BC_VEL_BOT_ZH,
     BC_PRES_IN_ZH, BC_PRES_OUT_ZH,
@@ -53,6 +54,10 @@ enum BCKind : int {
     BC_PERIODIC_X, BC_PERIODIC_Y,
     BC_VEL_IN_REG, BC_VEL_OUT_REG, BC_VEL_TOP_REG, BC_VEL_BOT_REG,
     BC_PRES_IN_REG, BC_PRES_OUT_REG, BC_PRES_TOP_REG, BC_PRES_BOT_REG,
+    // velocity_bottom with the Zou-He closure written to population 6 (lbc's
+    // src/bc/velocity_bottom.c:39 writes 7 a second time and leaves 6 as
+    // streamed); an extension, opt-in by function (velocity_bottom_corrected)
+    BC_VEL_BOT_ZH_FIX,
     BC_KIND_COUNT
 };
 
@@ -475,14 +480,15 @@ __device__ __forceinline__ void bc_apply(A &a, const double w[9], int kind, int 
         a.set(ib, jb, 7, f5 + (f1 - f3) / 2.0 - 0.5 * r * U - 1.0 / 6.0 * r * V);
         a.set(ib, jb, 8, f6 - (f1 - f3) / 2.0 + 0.5 * r * U - 1.0 / 6.0 * r * V);
     } break;
-    case BC_VEL_BOT_ZH: {  // src/bc/velocity_bottom.c:25-39 (second write to 7 kept, :39)
+    case BC_VEL_BOT_ZH:      // src/bc/velocity_bottom.c:25-39 (second write to 7 kept, :39)
+    case BC_VEL_BOT_ZH_FIX: {  // the same, the last line written to 6
         const double U = v1, V = v2;
         const double f0 = a.get(ib, jb, 0), f1 = a.get(ib, jb, 1), f3 = a.get(ib, jb, 3),
                      f4 = a.get(ib, jb, 4), f7 = a.get(ib, jb, 7), f8 = a.get(ib, jb, 8);
         const double r = (f0 + f1 + f3 + 2 * (f4 + f7 + f8)) / (1 - V);
         a.set(ib, jb, 2, f4 + 2.0 / 3.0 * r * V);
         a.set(ib, jb, 5, f7 - (f1 - f3) / 2.0 + 0.5 * r * U + 1.0 / 6.0 * r * V);
-        a.set(ib, jb, 7, f8 + (f1 - f3) / 2.0 - 0.5 * r * U + 1.0 / 6.0 * r * V);
+        a.set(ib, jb, kind == BC_VEL_BOT_ZH_FIX ? 6 : 7, f8 + (f1 - f3) / 2.0 - 0.5 * r * U + 1.0 / 6.0 * r * V);
     } break;
     case BC_PRES_IN_ZH: {  // src/bc/pressure_inlet.c:25-39
         const double R = v1;

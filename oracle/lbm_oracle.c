@@ -393,6 +393,24 @@ void orc_velocity_bottom(ORC_BC_ARGS) {
     }
 }
 
+/* Extension (no counterpart in lbc): velocity_bottom with the last Zou-He line
+ * written to population 6, as the closure for a bottom wall has it (the mirror
+ * of src/bc/velocity_top.c:37-39 in y). */
+void orc_velocity_bottom_corrected(ORC_BC_ARGS) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < Nx; i++) {
+        size_t b = nid(Nx, index, i);
+        if (solid_mask[b]) continue;
+        double *p = f_new + b * (size_t)Q;
+        double U = val1[i], V = val2[i];
+        double f1 = p[1], f3 = p[3], f4 = p[4], f7 = p[7], f8 = p[8];
+        double rh = (p[0] + f1 + f3 + 2 * (f4 + f7 + f8)) / (1 - V);
+        p[2] = f4 + 2.0 / 3.0 * rh * V;
+        p[5] = f7 - (f1 - f3) / 2.0 + 0.5 * rh * U + 1.0 / 6.0 * rh * V;
+        p[6] = f8 + (f1 - f3) / 2.0 - 0.5 * rh * U + 1.0 / 6.0 * rh * V;
+    }
+}
+
 /* src/bc/pressure_inlet.c:17-41. Transverse velocity from the previous-step v at
  * i+1 (:35). */
 void orc_pressure_inlet(ORC_BC_ARGS) {

@@ -134,6 +134,21 @@ def zoo_moving_lid(seed=18):
     return case, cases.random_state(case, seed, amp=0.01)
 
 
+def zoo_zh_corrected(seed=19):
+    """The corrected Zou-He bottom closure (extension; not in lbc) beside
+    lbc's Zou-He top, a convective outlet, a velocity inlet and an obstacle."""
+    rng = np.random.default_rng(seed)
+    Nx, Ny = 44, 20
+    mask = np.zeros((Ny, Nx), np.int32)
+    _obstacle(mask, 18, 8, 4, 4)
+    bcs = [BC("velocity_inlet", 0, 0.02 + _rng_vals(rng, Ny, 1e-3), _rng_vals(rng, Ny, 1e-3)),
+           BC("convective_outlet", Nx - 1, None, None),
+           BC("velocity_bottom_corrected", 0, 0.03 + _rng_vals(rng, Nx, 1e-3), _rng_vals(rng, Nx, 1e-3)),
+           BC("velocity_top", Ny - 1, _rng_vals(rng, Nx, 1e-3), _rng_vals(rng, Nx, 1e-3))]
+    case = Case("zoo_zh_corrected", Nx, Ny, mask, np.full((Ny, Nx), 1.0 / 0.7), np.zeros((Ny, Nx)), bcs)
+    return case, cases.random_state(case, seed)
+
+
 def standard_cases():
     """(name, builder, steps) for lbc-semantics parity tests."""
     return [
@@ -160,7 +175,7 @@ def standard_cases():
 def extension_cases():
     """(name, builder, steps) for extensions with no counterpart in lbc
     (checked against the oracle's restatement, not against lbc's build)."""
-    return [("zoo_moving_lid", zoo_moving_lid, 60)]
+    return [("zoo_moving_lid", zoo_moving_lid, 60), ("zoo_zh_corrected", zoo_zh_corrected, 60)]
 
 
 def build(name):

@@ -138,6 +138,56 @@ def test_moving_wall_matches_oracle(oracle):
     assert force_close(h[:, 0], fo[:, 1], scale=mag) and force_close(h[:, 1], fo[:, 0], scale=mag)
 
 
+@pytest.mark.parametrize("storage", ["f64", "f32", "f64fma"])
+def test_corrected_bottom_zou_he_matches_oracle(oracle, storage):
+    """velocity_bottom_corrected (an extension: the Zou-He bottom closure
+    written to population 6) beside lbc's BCs and an obstacle: FP64 resident
+    runs bit-identical to the oracle's restatement, forces to the link-sum
+    tolerance; the FMA form within 1e-12; FP32-shifted within 1e-5."""
+    from lbc_gb300 import STORAGE, GpuSolver
+    (case, st), steps = casezoo.build("zoo_zh_corrected")
+    s = GpuSolver(case, STORAGE[storage])
+    s.enable_force_history(steps)
+    s.set_state(st)
+    s.run(steps)
+    out = s.get_state()
+    h = s.force_history(steps)
+    fo = oracle.run(case, st, steps, record_forces=True)
+    fl = case.solid_mask == 0
+    mag = gross_force(case)
+    if storage == "f64":
+        for fld in FIELDS:
+            assert same(getattr(out, fld), getattr(st, fld)), (fld, maxrel(getattr(out, fld), getattr(st, fld)))
+        assert force_close(h[:, 0], fo[:, 1], scale=mag) and force_close(h[:, 1], fo[:, 0], scale=mag)
+    elif storage == "f64fma":
+        for fld in ("rho", "u", "v"):
+            a, b = getattr(out, fld)[fl], getattr(st, fld)[fl]
+            assert np.max(np.abs(a - b)) <= 1e-12 * max(np.max(np.abs(b)), 1e-3), fld
+        assert force_close(h[:, 0], fo[:, 1], rtol=1e-12, scale=mag)
+    else:
+        assert np.max(np.abs(out.u[fl] - st.u[fl])) < 1e-5
+        assert np.max(np.abs(out.rho[fl] - st.rho[fl])) < 1e-5
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32"])
+def test_corrected_bottom_zou_he_couette_on_the_device(storage):
+    """The corrected closure on the device settles plane Couette flow on the
+    linear profile (FP64 to round-off, FP32-shifted to its storage
+    precision) and keeps the density at 1."""
+    from lbc_gb300 import STORAGE, GpuSolver
+    from lbc_gb300 import cases as lc
+    U, Ny = 0.05, 12
+    case, st = lc.couette_zh(16, Ny, 0.8, U)
+    s = GpuSolver(case, STORAGE[storage])
+    s.set_state(st)
+    s.run(4000)
+    rho, u, v = s.get_fields()
+    lin = U * (1.0 - np.arange(Ny) / (Ny - 1))
+    tol = 1e-10 if storage == "f64" else 1e-5
+    assert np.max(np.abs(u - lin[:, None])) <= tol * U * (1 if storage == "f64" else 20)
+    assert np.max(np.abs(rho - 1.0)) <= (1e-9 if storage == "f64" else 1e-5)
+
+
 @pytest.mark.parametrize("storage", ["f64", "f32"])
 def test_set_bc_values_between_runs(oracle, storage):
     """lbm_gpu_set_bc_values between two resident runs acts from the next step,

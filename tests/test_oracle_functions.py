@@ -212,3 +212,24 @@ def test_poiseuille_flow_is_the_parabola(oracle):
         ua = cases.poiseuille_analytic(18, tau, 1e-6)
         err = np.max(np.abs(st.u[1:-1, :] - ua[1:-1, None])) / np.nanmax(ua)
         assert err < tol, (tau, err)
+
+
+def test_corrected_bottom_zou_he_holds_couette_flow(oracle):
+    """velocity_bottom_corrected (an extension) closes the bottom wall's
+    unknown populations 2, 5 and 6: a plane Couette flow between a moving
+    bottom and a still Zou-He top settles on the linear profile to round-off
+    and keeps its density. lbc's velocity_bottom (src/bc/velocity_bottom.c:39
+    writes 7 a second time and leaves 6 as streamed) gains mass and misses
+    the profile by more than 1 %: the drop-in keeps that behaviour under its
+    own name."""
+    from lbc_gb300 import cases
+    U, Ny = 0.05, 12
+    lin = U * (1.0 - np.arange(Ny) / (Ny - 1))
+    case, st = cases.couette_zh(16, Ny, 0.8, U, "velocity_bottom_corrected")
+    oracle.run(case, st, 4000)
+    assert np.max(np.abs(st.u - lin[:, None])) <= 1e-10 * U
+    assert np.max(np.abs(st.v)) <= 1e-12 and np.max(np.abs(st.rho - 1.0)) <= 1e-9
+    case, st = cases.couette_zh(16, Ny, 0.8, U, "velocity_bottom")
+    oracle.run(case, st, 4000)
+    assert np.max(np.abs(st.u - lin[:, None])) > 1e-2 * U
+    assert np.min(st.rho) > 1.01

@@ -670,7 +670,7 @@ __device__ __forceinline__ void stage_point_s(const StageParams &p, const StageP
 // that counts, after the wait, runs from a warm cache.
 template <typename T, bool COLLIDE, int KIND>
 __device__ __forceinline__ void stage_thread_s(const StageParams &p, const FinishParams &f, int t) {
-    StagePre c = stage_preload(p, t, KIND);
+    StagePre c = stage_preload<true>(p, t, KIND);
 #pragma unroll 1
     for (int pass = 0; pass < 2; pass++) {
         const bool live = pass != 0;

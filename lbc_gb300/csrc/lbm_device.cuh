@@ -5,6 +5,7 @@
 // velocity set is the canonical one (cases/nit/nit.c:195-202):
 //   c = (0,0) (1,0) (0,1) (-1,0) (0,-1) (1,1) (-1,1) (-1,-1) (1,-1), opp = 0 3 4 1 2 7 8 5 6.
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
@@ -339,6 +340,11 @@ __device__ __forceinline__ void bc_regularized(A &a, const double w[9], int ib, 
 // (weight 0.5 (1 - cos(2 pi n / L)) from the window phasor; no window when
 // the wall was set up without a length). tab: this step's slot of the wall's
 // phasor table.
+// FMA: the update with fused multiply-adds and p' = (rho - rho_bar) * (1/3)
+// (about half the FP64 instructions: shifted storage, whose populations are
+// FP32 or FP16 anyway); otherwise the oracle's sequence, bit for bit (FP64
+// storage).
+template <bool FMA = false>
 __device__ __forceinline__ double impedance_step(double *imp, int along, int nf, int t, double rho_n,
                                                  double alpha, const double *tab, int windowed) {
 #define IMP(f) imp[(size_t)(f) * along + t]
@@ -364,12 +370,13 @@ __device__ __forceinline__ double impedance_step(double *imp, int along, int nf,
         }
     };
     load_group(0);
-    const double p = (rho_n - rb) / 3.0;
+    const double d = rho_n - rb;
+    const double p = FMA ? d * (1.0 / 3.0) : d / 3.0;
     const double win = windowed ? 0.5 * (1.0 - wc0) : 1.0;
-    IMP(IMP_RHOBAR) = rb + alpha * (rho_n - rb);
+    IMP(IMP_RHOBAR) = FMA ? fma(alpha, d, rb) : rb + alpha * d;
     IMP(IMP_P) = p;
-    const double xn = a11 * x + a12 * v + b1 * p;
-    const double vn = a21 * x + a22 * v + b2 * p;
+    const double xn = FMA ? fma(a11, x, fma(a12, v, b1 * p)) : a11 * x + a12 * v + b1 * p;
+    const double vn = FMA ? fma(a21, x, fma(a22, v, b2 * p)) : a21 * x + a22 * v + b2 * p;
     IMP(IMP_X) = xn;
     IMP(IMP_V) = vn;
     const double wp = win * p, wv = win * vn;
@@ -379,10 +386,10 @@ __device__ __forceinline__ double impedance_step(double *imp, int along, int nf,
         for (int q = 0; q < 4; q++) {
             const int f = f0 + q;
             if (f >= nf) break;
-            IMP(imp_field(f, 0)) = ac[q][0] + wp * cr[q];
-            IMP(imp_field(f, 1)) = ac[q][1] + wp * ci[q];
-            IMP(imp_field(f, 2)) = ac[q][2] + wv * cr[q];
-            IMP(imp_field(f, 3)) = ac[q][3] + wv * ci[q];
+            IMP(imp_field(f, 0)) = FMA ? fma(wp, cr[q], ac[q][0]) : ac[q][0] + wp * cr[q];
+            IMP(imp_field(f, 1)) = FMA ? fma(wp, ci[q], ac[q][1]) : ac[q][1] + wp * ci[q];
+            IMP(imp_field(f, 2)) = FMA ? fma(wv, cr[q], ac[q][2]) : ac[q][2] + wv * cr[q];
+            IMP(imp_field(f, 3)) = FMA ? fma(wv, ci[q], ac[q][3]) : ac[q][3] + wv * ci[q];
         }
     }
     return vn;
@@ -671,6 +678,7 @@ struct StagePre {
     double v1, v2;   // v2 = -(wall velocity) on impedance nodes (imp)
 };
 
+template <bool FMA = false>
 __device__ __forceinline__ StagePre stage_preload(const StageParams &p, int t, int kind) {
     StagePre c;
     c.ij = stage_node(kind, p.Nx, p.Ny, p.index, t);
@@ -700,7 +708,7 @@ __device__ __forceinline__ StagePre stage_preload(const StageParams &p, int t, i
         // previous step's moments). Batches did it once in a launch of its
         // own ahead of the special nodes: measured on 64 liner ducts, 195.4
         // vs 192.5 us per step here.
-        c.v2 = -impedance_step(p.imp, p.along, p.imp_nf, t, c.nrho, p.imp_alpha,
+        c.v2 = -impedance_step<FMA>(p.imp, p.along, p.imp_nf, t, c.nrho, p.imp_alpha,
                                p.imp + imp_tab_offset(p.imp_nf, p.along, p.imp_slot), p.imp_windowed);
         c.imp = true;
     }

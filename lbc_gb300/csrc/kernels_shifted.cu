@@ -668,11 +668,16 @@ __device__ __forceinline__ void stage_point_s(const StageParams &p, const StageP
 // first runs it once without stores (pass 0, while the bulk kernel still
 // runs: the band values it reads are stale and discarded), so that the pass
 // that counts, after the wait, runs from a warm cache.
-template <typename T, bool COLLIDE, int KIND>
+// WARM = false (batches): no warm-up pass. A batch's edge launch has several
+// blocks on every SM and starts only as the special-node kernel drains, so
+// the pass mostly lengthens the path after the wait (measured on 64 liner
+// ducts: 186.3 -> 184.7 us per step without it; the solo cylinder 2048x512
+// keeps it: 19.6 vs 20.6 us).
+template <typename T, bool COLLIDE, int KIND, bool WARM>
 __device__ __forceinline__ void stage_thread_s(const StageParams &p, const FinishParams &f, int t) {
     StagePre c = stage_preload<true>(p, t, KIND);
 #pragma unroll 1
-    for (int pass = 0; pass < 2; pass++) {
+    for (int pass = WARM ? 0 : 1; pass < 2; pass++) {
         const bool live = pass != 0;
         if (live) pdl_wait();
         stage_point_s<T>(p, c, t, KIND, live);
@@ -680,11 +685,11 @@ __device__ __forceinline__ void stage_thread_s(const StageParams &p, const Finis
     }
 }
 
-template <typename T, bool COLLIDE>
+template <typename T, bool COLLIDE, bool WARM>
 __device__ __forceinline__ void stage_dispatch_s(const StageParams &p, const FinishParams &f, int t) {
     switch (p.kind) {
 #define LBM_STAGE_KIND(K) \
-    case K: stage_thread_s<T, COLLIDE, K>(p, f, t); break;
+    case K: stage_thread_s<T, COLLIDE, K, WARM>(p, f, t); break;
     LBM_STAGE_KIND(BC_VEL_IN_ZH) LBM_STAGE_KIND(BC_VEL_OUT_ZH) LBM_STAGE_KIND(BC_VEL_TOP_ZH)
     LBM_STAGE_KIND(BC_VEL_BOT_ZH) LBM_STAGE_KIND(BC_PRES_IN_ZH) LBM_STAGE_KIND(BC_PRES_OUT_ZH)
     LBM_STAGE_KIND(BC_CONV_IN) LBM_STAGE_KIND(BC_CONV_OUT) LBM_STAGE_KIND(BC_PERIODIC_X)
@@ -708,7 +713,7 @@ __global__ void k_stage_group_shifted(const StageGroup g) {
     const StageParams &p = g.p[blockIdx.y];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
-    stage_dispatch_s<T, COLLIDE>(p, g.fin, t);
+    stage_dispatch_s<T, COLLIDE, true>(p, g.fin, t);
 }
 
 template <typename T>
@@ -725,7 +730,7 @@ __global__ void k_stage_batch_shifted(const StageParams *__restrict__ list,
     const StageParams &p = list[2 * e + sel];
     const int t = b.y + (int)threadIdx.x;
     if (t >= p.along) return;
-    stage_dispatch_s<T, true>(p, *p.fin, t);
+    stage_dispatch_s<T, true, false>(p, *p.fin, t);
 }
 
 namespace launch {

@@ -1702,12 +1702,14 @@ bool Batch::launch_batched(int sel) {
     }
     bool first = true;
     for (int s = 0; s < max_stages_; s++) {
-        if (!stage_nblocks_[s]) continue;
-        CK(launch::stage_batch(d_stage_lists_[s], stage_counts_[s], d_stage_blocks_[s], stage_nblocks_[s],
-                               store_, sel, d_force_, first, nodes_ < (1LL << 20), stream_));
+        // the first level's force blocks come last in its list
+        const int nb = stage_nblocks_[s] - (s == 0 && !forces_ ? nforce_ : 0);
+        if (nb <= 0) continue;
+        CK(launch::stage_batch(d_stage_lists_[s], stage_counts_[s], d_stage_blocks_[s], nb, store_, sel, d_force_,
+                               first, nodes_ < (1LL << 20), stream_));
         first = false;
     }
-    if (nforce_ && max_stages_ == 0) CK(launch::force_reduce(d_force_, nforce_, true, stream_));
+    if (forces_ && nforce_ && max_stages_ == 0) CK(launch::force_reduce(d_force_, nforce_, true, stream_));
     if (nrec_) {
         const int psize = store_ == STORE_F64 ? (int)sizeof(StepParams) : (int)sizeof(FastStepParams);
         CK(launch::record(d_rec_, nrec_, store_, nullptr, (const char *)d_sp_, psize, sel, true,
@@ -1759,11 +1761,24 @@ bool Batch::run(int nsteps) {
         fsp.assign(store_ == STORE_F64 ? 0 : 2 * nc, FastStepParams());
         fin.assign(2 * nc, FinishParams());
         lists.assign(max_stages_, std::vector<StageParams>());
+        // The wall force of the batched steps is needed only by cases that
+        // record it every step (force history): the run's last step, which
+        // gives lbm_gpu_forces its value, is each case's own. Without a
+        // history the batched steps store no force partials and reduce none
+        // (measured on 64 liner ducts: see launch_batched).
+        bool forces = false;
+        for (Solver *c : cases_) forces = forces || c->hist_cap() > 0;
+        if (forces != forces_ && pair_exec_) {
+            cudaGraphExecDestroy(pair_exec_);
+            pair_exec_ = nullptr;
+        }
+        forces_ = forces;
         for (int c = 0; c < nc; c++) {
             Solver *s = cases_[c];
             const int cur = s->current(), par = s->parity();
             sp[2 * c] = s->step_params(cur, 1 - cur, false, par);
             sp[2 * c + 1] = s->step_params(1 - cur, cur, false, par ^ 1);
+            if (!forces) sp[2 * c].mem_partials = sp[2 * c + 1].mem_partials = nullptr;
             if (!fsp.empty()) {
                 fsp[2 * c] = s->fast_params(sp[2 * c]);
                 fsp[2 * c + 1] = s->fast_params(sp[2 * c + 1]);

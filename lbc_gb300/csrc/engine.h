@@ -373,6 +373,7 @@ class Batch {
     bool any_force_ = false;  // some case has a body force
     bool all_flags_ = true;   // every case has a flag word
     bool any_links_ = false;  // some case has cut-link records
+    bool forces_ = true;      // the batched steps reduce wall forces (some case records them)
     int launches_per_step_ = 0;
     void *d_sp_ = nullptr;         // StepParams or FastStepParams [2 * ncases]
     int4 *d_tiles_ = nullptr;

@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(256) k_step_batch_exact(const StepParams *__re
         } else {
             if (in) step_node_exact<false, true, FMA>(p, i, j, mfx, mfy, link);
         }
-        if (td.w) segment_reduce2_store(mfx, mfy, link, i, j, p.Nx, p.seg_slot, p.mem_partials);
+        if (td.w && p.mem_partials) segment_reduce2_store(mfx, mfy, link, i, j, p.Nx, p.seg_slot, p.mem_partials);
     }
 }
 

@@ -1,6 +1,7 @@
 """Batches: many uneven cases advanced by one persistent kernel per step must
 each end exactly as when run alone: populations, fields, impedance-wall state
 and the per-step force record bit for bit."""
+import numpy as np
 import pytest
 
 import casezoo
@@ -74,6 +75,41 @@ def test_batch_equals_alone(storage, chunks, mix):
         ha, hb = sa.force_history(total), sb.force_history(total)
         assert ha.shape == hb.shape
         assert same(ha, hb), (storage, n, "force history")
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32"])
+@pytest.mark.parametrize("mix", ["links", "plain"])
+def test_batch_without_force_history(storage, mix):
+    """Without a force history the batched steps store and reduce no wall
+    force; populations, fields and the force of the run's last step (each
+    case's own step, which lbm_gpu_forces reports) are still exactly those of
+    the case alone."""
+    from lbc_gb300 import STORAGE, GpuBatch, GpuSolver
+    names = MIX if mix == "links" else MIX_PLAIN
+
+    def plain(n):
+        (case, st), lp = _build(n)
+        s = GpuSolver(case, STORAGE[storage])
+        if lp is not None:
+            from lbc_gb300 import impedance as imp
+            s.set_impedance_wall(imp.LINER_ENTRY, *imp.liner_arrays(lp), imp.TRACKED_OMEGAS, 1.0, imp.MEAN_RATE, 37)
+        s.set_state(st)
+        return s
+
+    alone = [plain(n) for n in names]
+    for s in alone:
+        s.run(20)
+        s.run(17)
+    mixed = [plain(n) for n in names]
+    b = GpuBatch(mixed)
+    b.run(20)
+    b.run(17)
+    for n, sa, sb in zip(names, alone, mixed):
+        a, m = sa.get_state(), sb.get_state()
+        for fld in FIELDS:
+            assert same(getattr(a, fld), getattr(m, fld)), (storage, n, fld)
+        assert same(np.array(sa.forces()), np.array(sb.forces())), (storage, n)
+    b.close()
 
 
 def test_batch_info_counts_launches():

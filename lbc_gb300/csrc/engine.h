@@ -387,6 +387,8 @@ class Batch {
     ForceSlot *d_force_ = nullptr;
     int4 *d_special_ = nullptr;    // (case, i, j, chunk), shifted storage
     int nspecial_ = 0;
+    int4 *d_special_nf_ = nullptr; // the same without marked solids (runs that reduce no force)
+    int nspecial_nf_ = 0;
     RecordTask *d_rec_ = nullptr;   // every case's probes and wall traces (case index set)
     int nrec_ = 0;
     cudaGraphExec_t pair_exec_ = nullptr;

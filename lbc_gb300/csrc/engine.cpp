@@ -1029,7 +1029,12 @@ FinishParams Solver::finish_params(int dst, bool write_macro, int bparity) const
 bool Solver::launch_step_kernels(int src, int dst, bool collide, bool write_macro, int bparity,
                                  cudaStream_t s) {
     if (!s) s = stream_;
-    const StepParams p = step_params(src, dst, write_macro, bparity);
+    // The wall force is needed on a step that writes the fields (a run's
+    // last step: lbm_gpu_forces reports it) and on every step of a force
+    // history; other steps store no force partials and reduce none.
+    const bool forces = has_mem_ && (write_macro || hist_cap_ > 0);
+    StepParams p = step_params(src, dst, write_macro, bparity);
+    if (!forces) p.mem_partials = nullptr;
     if (d_.store == STORE_F64) {
         CK(launch::step_exact(p, has_flags_, collide, block_, s, d_.fma64));
     } else {
@@ -1040,7 +1045,7 @@ bool Solver::launch_step_kernels(int src, int dst, bool collide, bool write_macr
         if (special_launch()) CK(launch::special_shifted(fp, d_special_, nspecial_, d_.store, true, collide, true, s));
     }
     if (groups_.empty()) {
-        if (has_mem_) CK(launch::force_reduce(d_force_slot_, 1, true, s));
+        if (forces) CK(launch::force_reduce(d_force_slot_, 1, true, s));
         return true;
     }
     // The force (from the bulk kernel's partials) rides in the first stage
@@ -1057,7 +1062,7 @@ bool Solver::launch_step_kernels(int src, int dst, bool collide, bool write_macr
         }
         sg.fin = f;
         sg.fs = d_force_slot_;
-        sg.nfs = (gi == 0 && has_mem_) ? 1 : 0;
+        sg.nfs = (gi == 0 && forces) ? 1 : 0;
         sg.warm = (long long)d_.Nx * d_.Ny < (1LL << 20) ? 1 : 0;
         CK(launch::stage_group(sg, d_.store, collide, gi == 0, s));
     }

@@ -149,7 +149,8 @@ class Solver {
     int launches_per_step() const {
         const int bulk = 1 + (special_launch() ? 1 : 0);
         const int rec = rec_host_.empty() ? 0 : 1;
-        if (groups_.empty()) return bulk + (has_mem_ ? 1 : 0) + rec;
+        // (the loop's steps reduce the wall force only for a force history)
+        if (groups_.empty()) return bulk + (has_mem_ && hist_cap_ > 0 ? 1 : 0) + rec;
         return bulk + (int)groups_.size() + rec;
     }
     // Shifted storage: the nodes the clean-pair kernels leave to the

@@ -1039,13 +1039,17 @@ bool Solver::launch_step_kernels(int src, int dst, bool collide, bool write_macr
         CK(launch::step_exact(p, has_flags_, collide, block_, s, d_.fma64));
     } else {
         const FastStepParams fp = fast_params(p);
-        // The clean pairs, then the special nodes overlapping their last wave
+        // The special nodes first, as an ordinary launch, then the clean pairs
+        // as its programmatic follower: the grid of clean-pair blocks fills the
+        // SMs around the special nodes' latency-bound blocks from the start
         // (the plain kernel of a flag-free grid steps its own odd column).
-        CK(launch::step_shifted(fp, d_.store, has_flags_, collide, block_, s));
-        if (special_launch()) CK(launch::special_shifted(fp, d_special_, nspecial_, d_.store, true, collide, true, s));
+        // What follows is an ordinary launch, so it sees both.
+        if (special_launch()) CK(launch::special_shifted(fp, d_special_, nspecial_, d_.store, true, collide, false, s));
+        CK(launch::step_shifted(fp, d_.store, has_flags_, collide, block_, s, special_launch()));
     }
+    const bool after_bulk = d_.store == STORE_F64;
     if (groups_.empty()) {
-        if (forces) CK(launch::force_reduce(d_force_slot_, 1, true, s));
+        if (forces) CK(launch::force_reduce(d_force_slot_, 1, after_bulk, s));
         return true;
     }
     // The force (from the bulk kernel's partials) rides in the first stage
@@ -1064,7 +1068,7 @@ bool Solver::launch_step_kernels(int src, int dst, bool collide, bool write_macr
         sg.fs = d_force_slot_;
         sg.nfs = (gi == 0 && forces) ? 1 : 0;
         sg.warm = (long long)d_.Nx * d_.Ny < (1LL << 20) ? 1 : 0;
-        CK(launch::stage_group(sg, d_.store, collide, gi == 0, s));
+        CK(launch::stage_group(sg, d_.store, collide, gi == 0 && after_bulk, s));
     }
     return true;
 }

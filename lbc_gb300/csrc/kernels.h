@@ -177,7 +177,7 @@ cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStr
 
 // shifted storage (kernels_shifted.cu)
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
-                         cudaStream_t s);
+                         cudaStream_t s, bool after = false);
 // The special nodes of a case (nodes[0 .. n)) on the per-node path; flags: the
 // case has a flag word. Launched right after the case's clean-pair kernel
 // (after_bulk), it overlaps that kernel's last wave and completes after it.

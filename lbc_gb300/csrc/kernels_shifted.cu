@@ -792,12 +792,13 @@ static cudaError_t step_shifted_t(const FastStepParams &p, bool flags, bool coll
 }
 
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
-                         cudaStream_t s) {
-    // Two nodes per thread along x; an ordinary launch (what follows it is
-    // launched as its programmatic follower).
+                         cudaStream_t s, bool after) {
+    // Two nodes per thread along x. after: the programmatic follower of the
+    // special-node kernel launched just before it (the two touch disjoint
+    // nodes, so it needs no wait).
     const dim3 g((p.s.Nx + 2 * block.x - 1) / (2 * block.x), (p.s.Ny + block.y - 1) / block.y);
-    if (store == STORE_F32) return step_shifted_t<float>(p, flags, collide, false, g, block, s);
-    return step_shifted_t<__half>(p, flags, collide, false, g, block, s);
+    if (store == STORE_F32) return step_shifted_t<float>(p, flags, collide, after, g, block, s);
+    return step_shifted_t<__half>(p, flags, collide, after, g, block, s);
 }
 
 template <typename T, typename I, bool FORCE, bool LINKS>

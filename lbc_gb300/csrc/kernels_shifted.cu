@@ -541,11 +541,10 @@ __global__ void __launch_bounds__(128) k_step_batch_special_shifted(const FastSt
     pdl_wait();
 }
 
-// live = false: the same instructions without their stores (the stage
-// threads' instruction-cache warm-up, stage_thread_s). Band populations are
-// read at L2 (__ldcg), never from a possibly stale L1 line.
+// Band populations are read at L2 (__ldcg), never from a possibly stale L1
+// line.
 template <typename T, bool COLLIDE>
-__device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 ij, int slot, bool live = true) {
+__device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 ij, int slot) {
     float g[9], wf[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) {
@@ -555,12 +554,10 @@ __device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 
     float dr, rho, ux, uy, Jx, Jy, jx, jy;
     moments_shifted(g, p.hFxf, p.hFyf, dr, rho, ux, uy, Jx, Jy, jx, jy);
     const size_t dn = (size_t)ij.y * p.Nx + ij.x;
-    if (live && p.write_macro) { p.rho[dn] = 1.0 + (double)dr; p.ux[dn] = ux; p.uy[dn] = uy; }
-    if (live) {
-        p.bandm_next[slot] = 1.0 + (double)dr;
-        p.bandm_next[(size_t)p.nslots + slot] = ux;
-        p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
-    }
+    if (p.write_macro) { p.rho[dn] = 1.0 + (double)dr; p.ux[dn] = ux; p.uy[dn] = uy; }
+    p.bandm_next[slot] = 1.0 + (double)dr;
+    p.bandm_next[(size_t)p.nslots + slot] = ux;
+    p.bandm_next[2 * (size_t)p.nslots + slot] = uy;
     if (COLLIDE) {
         const float om = p.omega ? (float)p.omega[dn] : p.omega0f;
         float h1, h5;
@@ -570,10 +567,8 @@ __device__ __forceinline__ void finish_node_shifted(const FinishParams &p, int2 
     }
     T *D = (T *)p.dst;
     const long long node = (long long)ij.y * p.pitch + ij.x;
-    if (live) {
 #pragma unroll
-        for (int k = 0; k < 9; k++) SV<T>::st(D + k * p.plane + node, g[k]);
-    }
+    for (int k = 0; k < 9; k++) SV<T>::st(D + k * p.plane + node, g[k]);
 }
 
 // In-place collision of shifted populations with the stored (FP64) rho/u/v:
@@ -621,7 +616,6 @@ __global__ void k_collide_shifted(const CollideParams p) {
 template <typename T> struct BandAccessorS {
     const StageParams &p;
     const StagePre &c;
-    bool live;  // false: no stores (instruction-cache warm-up pass)
     __device__ int slot(int i, int j) const {
         if (i == c.ij.x && j == c.ij.y) return c.slot;
         if (i == c.nij.x && j == c.nij.y) return c.nslot;
@@ -631,7 +625,7 @@ template <typename T> struct BandAccessorS {
     __device__ double m(int q, int i, int j) const { return p.bandm_prev[(size_t)q * p.nslots + slot(i, j)]; }
     __device__ float get(int i, int j, int k) const { return __ldcg(p.bandg + (size_t)k * p.nslots + slot(i, j)); }
     __device__ void set(int i, int j, int k, float v) const {
-        if (live) p.bandg[(size_t)k * p.nslots + slot(i, j)] = v;
+        p.bandg[(size_t)k * p.nslots + slot(i, j)] = v;
     }
     __device__ float drho(int i, int j) const { return (float)((nb(i, j) ? c.nrho : m(0, i, j)) - 1.0); }
     __device__ float ux(int i, int j) const { return (float)(nb(i, j) ? c.nux : m(1, i, j)); }
@@ -648,9 +642,8 @@ template <typename T> struct BandAccessorS {
 // One point of one Boundary entry (src/core/main_lbm.c:49-58) after its
 // preload, as stage_point in kernels_exact.cu.
 template <typename T>
-__device__ __forceinline__ void stage_point_s(const StageParams &p, const StagePre &c, int t, int kind,
-                                              bool live) {
-    BandAccessorS<T> a{p, c, live};
+__device__ __forceinline__ void stage_point_s(const StageParams &p, const StagePre &c, int t, int kind) {
+    BandAccessorS<T> a{p, c};
     float w[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) w[k] = p.wf[k];
@@ -661,35 +654,27 @@ __device__ __forceinline__ void stage_point_s(const StageParams &p, const StageP
     bc_apply_s(a, w, kind, p.Nx, p.Ny, p.index, t, c.v1, c.v2);
 }
 
-// One stage thread, specialised on the entry's kind: preload, wait for the
-// bulk kernel, the BC, the finish. The edge launch runs a few warps per SM
-// on a cold instruction cache, and instruction fetch, not arithmetic, sets
-// its duration; so each kind is one short region of code, and the thread
-// first runs it once without stores (pass 0, while the bulk kernel still
-// runs: the band values it reads are stale and discarded), so that the pass
-// that counts, after the wait, runs from a warm cache.
-// WARM = false (batches): no warm-up pass. A batch's edge launch has several
-// blocks on every SM and starts only as the special-node kernel drains, so
-// the pass mostly lengthens the path after the wait (measured on 64 liner
-// ducts: 186.3 -> 184.7 us per step without it; the solo cylinder 2048x512
-// keeps it: 19.6 vs 20.6 us).
-template <typename T, bool COLLIDE, int KIND, bool WARM>
+// One stage thread, specialised on the entry's kind (each kind one short
+// region of code): preload, wait for the kernels before it, the BC, the
+// finish. (Alone, the edge launch is an ordinary launch behind the special
+// nodes and the clean pairs; in a batch it follows the special nodes.) An
+// instruction-cache warm-up pass before the wait, the same code without its
+// stores, paid off while the edge launch overlapped the clean pairs' last
+// wave; measured without it: cylinder 2048x512 17.96 -> 16.42 us per step
+// in the current order, 64 liner ducts 186.3 -> 184.7 us.
+template <typename T, bool COLLIDE, int KIND>
 __device__ __forceinline__ void stage_thread_s(const StageParams &p, const FinishParams &f, int t) {
     StagePre c = stage_preload<true>(p, t, KIND);
-#pragma unroll 1
-    for (int pass = WARM ? 0 : 1; pass < 2; pass++) {
-        const bool live = pass != 0;
-        if (live) pdl_wait();
-        stage_point_s<T>(p, c, t, KIND, live);
-        if (c.fin) finish_node_shifted<T, COLLIDE>(f, c.ij, c.slot, live);
-    }
+    pdl_wait();
+    stage_point_s<T>(p, c, t, KIND);
+    if (c.fin) finish_node_shifted<T, COLLIDE>(f, c.ij, c.slot);
 }
 
-template <typename T, bool COLLIDE, bool WARM>
+template <typename T, bool COLLIDE>
 __device__ __forceinline__ void stage_dispatch_s(const StageParams &p, const FinishParams &f, int t) {
     switch (p.kind) {
 #define LBM_STAGE_KIND(K) \
-    case K: stage_thread_s<T, COLLIDE, K, WARM>(p, f, t); break;
+    case K: stage_thread_s<T, COLLIDE, K>(p, f, t); break;
     LBM_STAGE_KIND(BC_VEL_IN_ZH) LBM_STAGE_KIND(BC_VEL_OUT_ZH) LBM_STAGE_KIND(BC_VEL_TOP_ZH)
     LBM_STAGE_KIND(BC_VEL_BOT_ZH) LBM_STAGE_KIND(BC_PRES_IN_ZH) LBM_STAGE_KIND(BC_PRES_OUT_ZH)
     LBM_STAGE_KIND(BC_CONV_IN) LBM_STAGE_KIND(BC_CONV_OUT) LBM_STAGE_KIND(BC_PERIODIC_X)
@@ -713,7 +698,7 @@ __global__ void k_stage_group_shifted(const StageGroup g) {
     const StageParams &p = g.p[blockIdx.y];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.along) return;
-    stage_dispatch_s<T, COLLIDE, true>(p, g.fin, t);
+    stage_dispatch_s<T, COLLIDE>(p, g.fin, t);
 }
 
 template <typename T>
@@ -730,7 +715,7 @@ __global__ void k_stage_batch_shifted(const StageParams *__restrict__ list,
     const StageParams &p = list[2 * e + sel];
     const int t = b.y + (int)threadIdx.x;
     if (t >= p.along) return;
-    stage_dispatch_s<T, true, false>(p, *p.fin, t);
+    stage_dispatch_s<T, true>(p, *p.fin, t);
 }
 
 namespace launch {

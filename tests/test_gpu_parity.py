@@ -95,6 +95,27 @@ def test_resident_run_matches_lbc(oracle, name):
         assert force_close(h[:, 0], fo[:, 1], scale=mag) and force_close(h[:, 1], fo[:, 0], scale=mag)
 
 
+@pytest.mark.parametrize("storage", ["f64", "f32"])
+@pytest.mark.parametrize("name", ["zoo_ibb", "cylinder_wake_small", "zoo_zh_mixed", "poiseuille"])
+def test_last_force_without_a_history(oracle, name, storage):
+    """Without a force history only a run's last step reduces the wall force:
+    lbm_gpu_forces after run(n) is the force of the n-th main_lbm call (FP64
+    to the link-sum tolerance, FP32-shifted within 1e-4 of the gross link sum)."""
+    from lbc_gb300 import STORAGE, GpuSolver
+    (case, st), steps = casezoo.build(name)
+    s = GpuSolver(case, STORAGE[storage])
+    s.set_state(st)
+    s.run(steps // 2)
+    s.run(steps - steps // 2)
+    L, D = s.forces()
+    fo = oracle.run(case, st, steps, record_forces=True)
+    mag = gross_force(case)
+    if storage == "f64":
+        assert force_close(np.array([D]), fo[-1:, 1], scale=mag) and force_close(np.array([L]), fo[-1:, 0], scale=mag)
+    else:
+        assert abs(D - fo[-1, 1]) <= 1e-4 * mag and abs(L - fo[-1, 0]) <= 1e-4 * mag, (D, L, fo[-1], mag)
+
+
 @pytest.mark.parametrize("storage", ["f64", "f32", "f16"])
 @pytest.mark.parametrize("name", ["zoo_ibb", "zoo_convective_chain", "taylor_green", "zoo_open_edges",
                                   "taylor_green_odd", "cylinder_odd", "zoo_moving_lid"])

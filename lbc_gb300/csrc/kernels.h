@@ -179,8 +179,9 @@ cudaError_t force_reduce(const ForceSlot *slots, int n, bool after_bulk, cudaStr
 cudaError_t step_shifted(const FastStepParams &p, int store, bool flags, bool collide, dim3 block,
                          cudaStream_t s, bool after = false);
 // The special nodes of a case (nodes[0 .. n)) on the per-node path; flags: the
-// case has a flag word. Launched right after the case's clean-pair kernel
-// (after_bulk), it overlaps that kernel's last wave and completes after it.
+// case has a flag word. after_bulk: the programmatic follower of the kernel
+// before it (a case alone launches it first, without the attribute, and the
+// clean pairs as its follower: step_shifted's after).
 cudaError_t special_shifted(const FastStepParams &p, const int2 *nodes, int n, int store, bool flags, bool collide,
                             bool after_bulk, cudaStream_t s);
 // The special nodes of a batch: nodes[q] = (case, i, j, chunk), n a multiple

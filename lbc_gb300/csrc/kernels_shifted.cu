@@ -464,11 +464,12 @@ __global__ void __launch_bounds__(256, 5) k_step_shifted_geo(const FastStepParam
 // The special nodes of a case, one per thread, on the per-node path (same
 // arithmetic as the pair path, so a node's bits do not depend on which path
 // steps it). Wall-link force terms are summed per 32-entry chunk of the list.
-// It reads and writes nothing the clean-pair kernel touches, so it is
-// launched right behind it and overlaps its last wave (pdl.cuh); it waits for
-// that kernel only at its end, so that what follows sees both. (Launched the
-// other way round, the clean-pair blocks must each wait at their end and hold
-// their SMs: measured slower.)
+// It reads and writes nothing the clean-pair kernel touches: a case alone
+// launches it first, as an ordinary launch, with the clean pairs as its
+// programmatic follower (pdl.cuh), so their blocks fill the SMs around its
+// latency-bound ones; the launch after both is ordinary. (The trigger at the
+// start lets the follower launch at once; the wait at the end is then a
+// no-op.)
 template <typename T, typename I, bool FLAGS, bool COLLIDE, bool FORCE, bool LINKS>
 __global__ void __launch_bounds__(128) k_step_special_shifted(const FastStepParams fp,
                                                               const int2 *__restrict__ nodes, int n) {

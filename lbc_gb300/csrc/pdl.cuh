@@ -1,15 +1,17 @@
-// pdl.cuh -- programmatic dependent launch between the bulk step and the
-// short launches that follow it in the same stream (edge stages, force
+// pdl.cuh -- programmatic dependent launch between consecutive kernels of a
+// step in the same stream (clean pairs, special nodes, edge stages, force
 // reduction).
 //
-// The bulk kernels signal at their start that the next kernel may be launched
+// A kernel signals at its start that the next kernel may be launched
 // (griddepcontrol.launch_dependents); a follower launched with programmatic
-// stream serialization is then scheduled once every bulk block has started,
-// so its launch latency hides behind the bulk kernel's last wave. The
-// follower calls pdl_wait() (griddepcontrol.wait: returns once the bulk grid
-// has completed and its writes are visible) before it reads or writes
-// anything the bulk kernel touches. A kernel launched without the attribute
-// passes through both instructions unaffected.
+// stream serialization is then scheduled once every block of the kernel
+// before it has started, so its launch latency hides behind that kernel's
+// last wave, or (a case alone: the special nodes, then the clean pairs) so
+// that the two run side by side. A follower calls pdl_wait()
+// (griddepcontrol.wait: returns once the kernel before it has completed and
+// its writes are visible) before it reads or writes anything that kernel
+// touches. A kernel launched without the attribute passes through both
+// instructions unaffected.
 #pragma once
 #include <cuda_runtime.h>
 

@@ -325,14 +325,8 @@ bool Solver::build_geometry() {
             for (int t = 0; t < st.along; t++) {
                 const int i = col ? st.index : t, j = col ? t : st.index;
                 if (solid(i, j)) continue;
-                int ni = i, nj = j;
-                switch (st.kind) {
-                case BC_PRES_IN_ZH: case BC_CONV_IN: case BC_VEL_IN_REG: case BC_PRES_IN_REG: ni = i + 1; break;
-                case BC_PRES_OUT_ZH: case BC_CONV_OUT: case BC_VEL_OUT_REG: case BC_PRES_OUT_REG: ni = i - 1; break;
-                case BC_VEL_BOT_REG: case BC_PRES_BOT_REG: nj = j + 1; break;
-                case BC_VEL_TOP_REG: case BC_PRES_TOP_REG: nj = j - 1; break;
-                default: continue;
-                }
+                const int2 nb = stage_neighbour(st.kind, make_int2(i, j));  // the node's own stage thread reads
+                const int ni = nb.x, nj = nb.y;
                 if (ni < 0 || ni >= Nx || nj < 0 || nj >= Ny || !solid(ni, nj)) continue;
                 read_solid[(size_t)slot_of(ni, nj)] = 1;
             }

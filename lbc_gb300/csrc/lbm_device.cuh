@@ -653,7 +653,7 @@ __device__ __forceinline__ int2 stage_node(int kind, int Nx, int Ny, int index, 
 
 // The interior neighbour whose populations or moments a Boundary entry reads
 // at node ij (the band's read lines), x = -1 for entries that read none.
-__device__ __forceinline__ int2 stage_neighbour(int kind, int2 ij) {
+__host__ __device__ __forceinline__ int2 stage_neighbour(int kind, int2 ij) {
     switch (kind) {
     case BC_PRES_IN_ZH: case BC_CONV_IN: case BC_VEL_IN_REG: case BC_PRES_IN_REG: return make_int2(ij.x + 1, ij.y);
     case BC_PRES_OUT_ZH: case BC_CONV_OUT: case BC_VEL_OUT_REG: case BC_PRES_OUT_REG: return make_int2(ij.x - 1, ij.y);

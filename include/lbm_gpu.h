@@ -67,7 +67,9 @@ typedef struct {
                                       a flag word); edge_launches, which also finish the
                                       BC-written nodes and reduce the wall force, or,
                                       with wall links but no edge stages, one force
-                                      reduction */
+                                      reduction when a force history is enabled (the
+                                      loop's steps reduce the force only then; a run's
+                                      last step always does, for lbm_gpu_forces) */
     size_t device_bytes;
     long long steps_done;
     int edge_launches;             /* launches the edge stages take per step: consecutive

@@ -154,7 +154,7 @@ bool Solver::build_geometry() {
             // when its flag is off or an earlier entry overwrote the edge.
             const int flag = b.kind == BC_PERIODIC_X ? d_.px : d_.py;
             if (flag && !nonperiodic_seen) continue;
-            Stage st{b.kind, 0, b.kind == BC_PERIODIC_X ? 2 * Ny : 2 * Nx, (int)e};
+            Stage st{b.kind, 0, b.kind == BC_PERIODIC_X ? 2 * Ny : 2 * Nx, (int)e, {}};
             st.open.assign(st.along, 1);
             stages_.push_back(st);
             continue;
@@ -166,7 +166,7 @@ bool Solver::build_geometry() {
             set_error("boundary entry " + std::to_string(e) + ": index out of range");
             return false;
         }
-        Stage st{b.kind, b.index, col ? Ny : Nx, (int)e};
+        Stage st{b.kind, b.index, col ? Ny : Nx, (int)e, {}};
         st.open.resize(st.along);
         for (int t = 0; t < st.along; t++) st.open[t] = col ? !solid(b.index, t) : !solid(t, b.index);
         stages_.push_back(st);
